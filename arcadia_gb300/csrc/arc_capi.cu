@@ -1,0 +1,507 @@
+// arc_capi.cu — context, pools and the C ABI of libarc_trace.so.
+//
+// The context owns the device copies of Arcadia's Group-0 pools (chunk roots, Node64 pool,
+// LeafBrick64 pool, 256-entry palette), the camera block, per-launch scratch and a status word
+// that device-side range checks write. Host-pointer entry points stage through context-owned device
+// buffers; *_dev entry points work on caller device pointers in stream order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "arc_ctx.h"
+
+using arc::Scratch;
+
+namespace {
+
+int set_err(arc_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_fail(arc_ctx* c, cudaError_t e, const char* what) {
+    return set_err(c, ARC_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define ARC_CK(ctx, expr)                                          \
+    do {                                                           \
+        cudaError_t e__ = (expr);                                  \
+        if (e__ != cudaSuccess) return cuda_fail((ctx), e__, #expr); \
+    } while (0)
+
+inline uint32_t popc64(uint32_t lo, uint32_t hi) { return (uint32_t)__builtin_popcount(lo) + (uint32_t)__builtin_popcount(hi); }
+
+// Range check of a node slice against the pool sizes it will live in.
+int validate_nodes(arc_ctx* c, const arc_node64* nodes, uint32_t n, uint32_t node_limit, uint32_t brick_limit, uint32_t first) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const arc_node64& nd = nodes[i];
+        if (nd.mask_low == 0 && nd.mask_high == 0) continue;
+        const uint32_t ptr = nd.child_ptr & ARC_PTR_INDEX_MASK;
+        if (nd.child_ptr & ARC_IS_LEAF_FLAG) {
+            if (!(nd.child_ptr & ARC_IS_UNIFORM_FLAG) && ptr >= brick_limit) {
+                char b[160];
+                snprintf(b, sizeof b, "node %u: brick index %u >= brick count %u", first + i, ptr, brick_limit);
+                return set_err(c, ARC_E_INVALID_POOL, b);
+            }
+        } else {
+            const uint64_t end = (uint64_t)ptr + popc64(nd.mask_low, nd.mask_high);
+            if (end > node_limit) {
+                char b[160];
+                snprintf(b, sizeof b, "node %u: child slice [%u, %llu) beyond node count %u", first + i, ptr,
+                         (unsigned long long)end, node_limit);
+                return set_err(c, ARC_E_INVALID_POOL, b);
+            }
+        }
+    }
+    return ARC_OK;
+}
+
+template <typename T>
+int ensure_device(arc_ctx* c, T** p, size_t* cap_bytes, size_t need_bytes) {
+    if (*cap_bytes >= need_bytes && *p) return ARC_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap_bytes = 0;
+    cudaError_t e = cudaMalloc((void**)p, need_bytes);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc");
+    *cap_bytes = need_bytes;
+    return ARC_OK;
+}
+
+}  // namespace
+
+arc::World arc_ctx::world() const {
+    arc::World w;
+    w.roots = d_roots;
+    w.nodes = reinterpret_cast<const uint4*>(d_nodes);
+    w.bricks = reinterpret_cast<const uint32_t*>(d_bricks);
+    w.palette = reinterpret_cast<const float4*>(d_palette);
+    w.n_nodes = n_nodes;
+    w.n_bricks = n_bricks;
+    w.n_roots = n_roots;
+    w.status = d_status;
+    return w;
+}
+
+int arc_ctx_check_ready(arc_ctx* c, bool need_cam) {
+    if (!c) return ARC_E_INVALID_ARG;
+    if (!c->have_world) return set_err(c, ARC_E_NO_WORLD, "no world uploaded");
+    if (need_cam && !c->have_cam) return set_err(c, ARC_E_NO_CAMERA, "no camera set");
+    return ARC_OK;
+}
+
+int arc_ctx_finish(arc_ctx* c) {
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamSynchronize");
+    uint32_t st = 0;
+    e = cudaMemcpy(&st, c->d_status, sizeof st, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "status readback");
+    c->last_status = st;
+    if (st) {
+        char b[128];
+        snprintf(b, sizeof b, "device range check failed (status 0x%x): pool index out of range", st);
+        cudaMemsetAsync(c->d_status, 0, sizeof(uint32_t), c->stream);
+        cudaStreamSynchronize(c->stream);
+        return set_err(c, ARC_E_DEVICE_CHECK, b);
+    }
+    return ARC_OK;
+}
+
+int arc_ctx_stage(arc_ctx* c, size_t bytes, void** out) {
+    int rc = ensure_device(c, reinterpret_cast<unsigned char**>(&c->d_stage), &c->stage_bytes, bytes);
+    if (rc) return rc;
+    *out = c->d_stage;
+    return ARC_OK;
+}
+
+extern "C" {
+
+int arc_create(int device, arc_ctx** out) {
+    if (!out) return ARC_E_INVALID_ARG;
+    *out = nullptr;
+    arc_ctx* c = new (std::nothrow) arc_ctx();
+    if (!c) return ARC_E_OUT_OF_MEMORY;
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { int rc = cuda_fail(c, e, "cudaSetDevice"); delete c; return rc; }
+    cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, device);
+    if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaMalloc((void**)&c->d_scratch, sizeof(Scratch))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&c->d_status, sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess) {
+        int rc = cuda_fail(c, e, "context setup");
+        arc_destroy(c);
+        return rc;
+    }
+    cudaMemset(c->d_scratch, 0, sizeof(Scratch));
+    cudaMemset(c->d_status, 0, sizeof(uint32_t));
+    c->cfg.variant = 1;
+    c->cfg.block_threads = 256;
+    c->cfg.blocks_per_sm = 0;
+    c->cfg.tile_w = 8;
+    c->cfg.tile_h = 4;
+    c->cfg.refill_threshold = 8;
+    *out = c;
+    return ARC_OK;
+}
+
+int arc_destroy(arc_ctx* c) {
+    if (!c) return ARC_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->d_roots);
+    cudaFree(c->d_nodes);
+    cudaFree(c->d_bricks);
+    cudaFree(c->d_palette);
+    cudaFree(c->d_scratch);
+    cudaFree(c->d_status);
+    cudaFree(c->d_stage);
+    cudaFree(c->d_sharc_keys);
+    cudaFree(c->d_sharc_accum);
+    cudaFree(c->d_sharc_resolved);
+    cudaFree(c->d_sharc_stage);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return ARC_OK;
+}
+
+int arc_last_error(const arc_ctx* c, char* buf, size_t n) {
+    if (!c || !buf || n == 0) return ARC_E_INVALID_ARG;
+    snprintf(buf, n, "%s", c->err.c_str());
+    return ARC_OK;
+}
+
+int arc_synchronize(arc_ctx* c) {
+    if (!c) return ARC_E_INVALID_ARG;
+    return arc_ctx_finish(c);
+}
+
+int arc_get_stream(arc_ctx* c, void** stream) {
+    if (!c || !stream) return ARC_E_INVALID_ARG;
+    *stream = (void*)c->stream;
+    return ARC_OK;
+}
+
+int arc_set_launch_config(arc_ctx* c, const arc_launch_config* cfg) {
+    if (!c || !cfg) return ARC_E_INVALID_ARG;
+    if (cfg->variant > 1u) return set_err(c, ARC_E_INVALID_ARG, "variant must be 0 or 1");
+    if (cfg->block_threads == 0 || cfg->block_threads % 32u || cfg->block_threads > 1024u)
+        return set_err(c, ARC_E_INVALID_ARG, "block_threads must be a multiple of 32 in [32, 1024]");
+    if (cfg->variant == 0u && cfg->block_threads % 8u) return set_err(c, ARC_E_INVALID_ARG, "plain variant needs block_threads % 8 == 0");
+    if (cfg->tile_w * cfg->tile_h != 32u) return set_err(c, ARC_E_INVALID_ARG, "tile_w * tile_h must be 32");
+    if (cfg->refill_threshold < 1u || cfg->refill_threshold > 32u) return set_err(c, ARC_E_INVALID_ARG, "refill_threshold in [1, 32]");
+    if (cfg->variant == 1u && cfg->block_threads > 256u) return set_err(c, ARC_E_INVALID_ARG, "persistent variant: block_threads <= 256");
+    c->cfg = *cfg;
+    return ARC_OK;
+}
+
+int arc_get_launch_config(const arc_ctx* c, arc_launch_config* cfg) {
+    if (!c || !cfg) return ARC_E_INVALID_ARG;
+    *cfg = c->cfg;
+    return ARC_OK;
+}
+
+int arc_get_stats(const arc_ctx* c, arc_stats* out) {
+    if (!c || !out) return ARC_E_INVALID_ARG;
+    out->last_kernel_ms = c->last_ms;
+    out->rays_traced = c->last_rays;
+    out->device_status = c->last_status;
+    out->n_sm = (uint32_t)c->n_sm;
+    return ARC_OK;
+}
+
+int arc_upload_world(arc_ctx* c, const uint32_t grid[3], const uint32_t* roots, uint32_t n_roots, const arc_node64* nodes,
+                     uint32_t n_nodes, const arc_brick64* bricks, uint32_t n_bricks, const arc_material* palette,
+                     uint32_t node_headroom, uint32_t brick_headroom) {
+    if (!c || !grid || !roots || !nodes || !palette || n_nodes == 0) return set_err(c, ARC_E_INVALID_ARG, "null pool or empty node pool");
+    if (n_bricks && !bricks) return set_err(c, ARC_E_INVALID_ARG, "null brick pool");
+    for (int i = 0; i < 3; ++i)
+        if (grid[i] == 0 || grid[i] > 1024u) return set_err(c, ARC_E_INVALID_ARG, "grid dims must be in [1, 1024]");
+    const uint64_t nch = (uint64_t)grid[0] * grid[1] * grid[2];
+    if (nch != n_roots) return set_err(c, ARC_E_INVALID_ARG, "n_roots != grid volume");
+    const uint64_t cap_nodes = (uint64_t)n_nodes + node_headroom, cap_bricks = (uint64_t)std::max<uint32_t>(n_bricks, 1u) + brick_headroom;
+    if (cap_nodes > ARC_PTR_INDEX_MASK || cap_bricks > ARC_PTR_INDEX_MASK) return set_err(c, ARC_E_CAPACITY, "pool beyond 30-bit index range");
+    for (uint32_t i = 0; i < n_roots; ++i)
+        if (roots[i] != ARC_EMPTY_CHUNK && roots[i] >= n_nodes) {
+            char b[128];
+            snprintf(b, sizeof b, "chunk %u: root %u >= node count %u", i, roots[i], n_nodes);
+            return set_err(c, ARC_E_INVALID_POOL, b);
+        }
+    int rc = validate_nodes(c, nodes, n_nodes, n_nodes, n_bricks, 0);
+    if (rc) return rc;
+    ARC_CK(c, cudaSetDevice(c->device));
+    ARC_CK(c, cudaStreamSynchronize(c->stream));
+    cudaFree(c->d_roots);
+    cudaFree(c->d_nodes);
+    cudaFree(c->d_bricks);
+    c->d_roots = nullptr;
+    c->d_nodes = nullptr;
+    c->d_bricks = nullptr;
+    c->have_world = false;
+    ARC_CK(c, cudaMalloc((void**)&c->d_roots, sizeof(uint32_t) * n_roots));
+    ARC_CK(c, cudaMalloc((void**)&c->d_nodes, sizeof(arc_node64) * cap_nodes));
+    ARC_CK(c, cudaMalloc((void**)&c->d_bricks, sizeof(arc_brick64) * cap_bricks));
+    if (!c->d_palette) ARC_CK(c, cudaMalloc((void**)&c->d_palette, sizeof(arc_material) * 256));
+    ARC_CK(c, cudaMemcpyAsync(c->d_roots, roots, sizeof(uint32_t) * n_roots, cudaMemcpyHostToDevice, c->stream));
+    ARC_CK(c, cudaMemcpyAsync(c->d_nodes, nodes, sizeof(arc_node64) * n_nodes, cudaMemcpyHostToDevice, c->stream));
+    if (n_bricks) ARC_CK(c, cudaMemcpyAsync(c->d_bricks, bricks, sizeof(arc_brick64) * n_bricks, cudaMemcpyHostToDevice, c->stream));
+    else ARC_CK(c, cudaMemsetAsync(c->d_bricks, 0, sizeof(arc_brick64), c->stream));
+    ARC_CK(c, cudaMemcpyAsync(c->d_palette, palette, sizeof(arc_material) * 256, cudaMemcpyHostToDevice, c->stream));
+    ARC_CK(c, cudaStreamSynchronize(c->stream));
+    c->grid[0] = grid[0];
+    c->grid[1] = grid[1];
+    c->grid[2] = grid[2];
+    c->n_roots = n_roots;
+    c->n_nodes = n_nodes;
+    c->cap_nodes = (uint32_t)cap_nodes;
+    c->n_bricks = std::max<uint32_t>(n_bricks, 1u);
+    c->cap_bricks = (uint32_t)cap_bricks;
+    c->have_world = true;
+    return ARC_OK;
+}
+
+int arc_apply_patch(arc_ctx* c, uint32_t chunk, uint32_t new_root, uint32_t node_offset, const arc_node64* nodes,
+                    uint32_t n_nodes, uint32_t brick_offset, const arc_brick64* bricks, uint32_t n_bricks) {
+    int rc = arc_ctx_check_ready(c, false);
+    if (rc) return rc;
+    if (chunk >= c->n_roots) return set_err(c, ARC_E_INVALID_ARG, "chunk index out of range");
+    if ((n_nodes && !nodes) || (n_bricks && !bricks)) return set_err(c, ARC_E_INVALID_ARG, "null patch slice");
+    if ((uint64_t)node_offset + n_nodes > c->cap_nodes || (uint64_t)brick_offset + n_bricks > c->cap_bricks)
+        return set_err(c, ARC_E_CAPACITY, "patch beyond pool capacity (re-upload with more headroom)");
+    const uint32_t node_limit = std::max<uint32_t>(c->n_nodes, node_offset + n_nodes);
+    const uint32_t brick_limit = std::max<uint32_t>(c->n_bricks, brick_offset + n_bricks);
+    if (new_root != ARC_EMPTY_CHUNK && new_root >= node_limit) return set_err(c, ARC_E_INVALID_POOL, "patch root out of range");
+    rc = validate_nodes(c, nodes, n_nodes, node_limit, brick_limit, node_offset);
+    if (rc) return rc;
+    if (n_nodes) ARC_CK(c, cudaMemcpyAsync(c->d_nodes + node_offset, nodes, sizeof(arc_node64) * n_nodes, cudaMemcpyHostToDevice, c->stream));
+    if (n_bricks) ARC_CK(c, cudaMemcpyAsync(c->d_bricks + brick_offset, bricks, sizeof(arc_brick64) * n_bricks, cudaMemcpyHostToDevice, c->stream));
+    ARC_CK(c, cudaMemcpyAsync(c->d_roots + chunk, &new_root, sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
+    ARC_CK(c, cudaStreamSynchronize(c->stream));
+    c->n_nodes = node_limit;
+    c->n_bricks = brick_limit;
+    return ARC_OK;
+}
+
+int arc_set_camera(arc_ctx* c, const arc_camera_uniforms* cam) {
+    if (!c || !cam) return ARC_E_INVALID_ARG;
+    const uint32_t w = cam->world_grid_dims[3] & 0xFFFFu, h = cam->world_grid_dims[3] >> 16;
+    if (c->have_world && (cam->world_grid_dims[0] != c->grid[0] || cam->world_grid_dims[1] != c->grid[1] ||
+                          cam->world_grid_dims[2] != c->grid[2]))
+        return set_err(c, ARC_E_INVALID_ARG, "camera world_grid_dims do not match the uploaded world");
+    (void)w;
+    (void)h;
+    c->cam = *cam;
+    c->have_cam = true;
+    return ARC_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Frame passes
+// ------------------------------------------------------------------------------------------------
+
+static int check_dims(arc_ctx* c, uint32_t width, uint32_t height) {
+    if (width == 0 || height == 0 || width > 0xFFFFu || height > 0xFFFFu) return set_err(c, ARC_E_INVALID_ARG, "bad frame size");
+    const uint32_t w = c->cam.world_grid_dims[3] & 0xFFFFu, h = c->cam.world_grid_dims[3] >> 16;
+    if (w != width || h != height) return set_err(c, ARC_E_INVALID_ARG, "frame size differs from camera world_grid_dims.w");
+    return ARC_OK;
+}
+
+static arc::FrameParams frame_params(arc_ctx* c, uint32_t width, uint32_t height) {
+    arc::FrameParams P;
+    memset(&P, 0, sizeof P);
+    P.world = c->world();
+    P.width = width;
+    P.height = height;
+    P.scratch = c->d_scratch;
+    P.tile_w = c->cfg.tile_w;
+    P.tile_h = c->cfg.tile_h;
+    P.tiles_x = (width + c->cfg.tile_w - 1u) / c->cfg.tile_w;
+    const uint32_t tiles_y = (height + c->cfg.tile_h - 1u) / c->cfg.tile_h;
+    P.queue_len = P.tiles_x * tiles_y * 32u;
+    P.refill_threshold = c->cfg.refill_threshold;
+    return P;
+}
+
+static int run_frame(arc_ctx* c, arc::FrameParams& P) {
+    ARC_CK(c, cudaMemsetAsync(c->d_scratch, 0, sizeof(Scratch), c->stream));
+    ARC_CK(c, cudaEventRecord(c->ev0, c->stream));
+    ARC_CK(c, arc::launch_frame(P, c->cam, c->cfg, c->n_sm, c->stream));
+    ARC_CK(c, cudaEventRecord(c->ev1, c->stream));
+    c->timing_pending = true;
+    return ARC_OK;
+}
+
+static int collect_frame(arc_ctx* c, uint64_t primary_rays, uint64_t* n_gi_host) {
+    Scratch s;
+    ARC_CK(c, cudaMemcpyAsync(&s, c->d_scratch, sizeof s, cudaMemcpyDeviceToHost, c->stream));
+    int rc = arc_ctx_finish(c);
+    if (rc) return rc;
+    float ms = 0.0f;
+    if (c->timing_pending && cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) c->last_ms = ms;
+    c->timing_pending = false;
+    c->last_rays = primary_rays + s.gi_rays;
+    if (n_gi_host) *n_gi_host = s.gi_rays;
+    return ARC_OK;
+}
+
+int arc_trace_frame_dev(arc_ctx* c, uint32_t width, uint32_t height, uint32_t* gdm, uint32_t* gnm, uint32_t* gaa,
+                        arc_hit_record* hits, arc_hit_record* gi_hits, uint64_t* n_gi_dev) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if ((rc = check_dims(c, width, height))) return rc;
+    if (!gdm || !gnm || !gaa) return set_err(c, ARC_E_INVALID_ARG, "null G-buffer");
+    arc::FrameParams P = frame_params(c, width, height);
+    P.gbuf_depth_mat = gdm;
+    P.gbuf_norm_motion = gnm;
+    P.gbuf_albedo_ao = gaa;
+    P.hits = hits;
+    P.gi_hits = gi_hits;
+    P.do_gi = 1;
+    if ((rc = run_frame(c, P))) return rc;
+    if (n_gi_dev) ARC_CK(c, cudaMemcpyAsync(n_gi_dev, &c->d_scratch->gi_rays, sizeof(uint64_t), cudaMemcpyDeviceToDevice, c->stream));
+    c->last_rays = (uint64_t)width * height;
+    return ARC_OK;
+}
+
+int arc_trace_primary_dev(arc_ctx* c, uint32_t width, uint32_t height, uint32_t* gdm, uint32_t* gnm, uint32_t* gaa,
+                          arc_hit_record* hits) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if ((rc = check_dims(c, width, height))) return rc;
+    if (!gdm || !gnm || !gaa) return set_err(c, ARC_E_INVALID_ARG, "null G-buffer");
+    arc::FrameParams P = frame_params(c, width, height);
+    P.gbuf_depth_mat = gdm;
+    P.gbuf_norm_motion = gnm;
+    P.gbuf_albedo_ao = gaa;
+    P.hits = hits;
+    P.do_gi = 0;
+    return run_frame(c, P);
+}
+
+int arc_trace_secondary_dev(arc_ctx* c, uint32_t width, uint32_t height, const uint32_t* gdm, const uint32_t* gnm,
+                            arc_hit_record* gi_hits) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if ((rc = check_dims(c, width, height))) return rc;
+    if (!gdm || !gnm || !gi_hits) return set_err(c, ARC_E_INVALID_ARG, "null buffer");
+    arc::FrameParams P = frame_params(c, width, height);
+    P.gbuf_depth_mat = const_cast<uint32_t*>(gdm);
+    P.gbuf_norm_motion = const_cast<uint32_t*>(gnm);
+    P.gi_hits = gi_hits;
+    ARC_CK(c, arc::launch_secondary(P, c->cam, c->stream));
+    return ARC_OK;
+}
+
+// Host-buffer variants: stage outputs in one context-owned device block.
+int arc_trace_frame(arc_ctx* c, uint32_t width, uint32_t height, uint32_t* gdm, uint32_t* gnm, uint32_t* gaa,
+                    arc_hit_record* hits, arc_hit_record* gi_hits, uint64_t* n_gi_out) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if ((rc = check_dims(c, width, height))) return rc;
+    if (!gdm || !gnm || !gaa) return set_err(c, ARC_E_INVALID_ARG, "null G-buffer");
+    const size_t np = (size_t)width * height;
+    const size_t b_g = np * 20, b_h = hits ? np * 20 : 0, b_gi = gi_hits ? np * 20 : 0;
+    void* stage;
+    if ((rc = arc_ctx_stage(c, b_g + b_h + b_gi, &stage))) return rc;
+    unsigned char* base = static_cast<unsigned char*>(stage);
+    arc::FrameParams P = frame_params(c, width, height);
+    P.gbuf_depth_mat = reinterpret_cast<uint32_t*>(base);
+    P.gbuf_norm_motion = reinterpret_cast<uint32_t*>(base + np * 8);
+    P.gbuf_albedo_ao = reinterpret_cast<uint32_t*>(base + np * 16);
+    P.hits = hits ? reinterpret_cast<arc_hit_record*>(base + b_g) : nullptr;
+    P.gi_hits = gi_hits ? reinterpret_cast<arc_hit_record*>(base + b_g + b_h) : nullptr;
+    P.do_gi = 1;
+    if ((rc = run_frame(c, P))) return rc;
+    ARC_CK(c, cudaMemcpyAsync(gdm, P.gbuf_depth_mat, np * 8, cudaMemcpyDeviceToHost, c->stream));
+    ARC_CK(c, cudaMemcpyAsync(gnm, P.gbuf_norm_motion, np * 8, cudaMemcpyDeviceToHost, c->stream));
+    ARC_CK(c, cudaMemcpyAsync(gaa, P.gbuf_albedo_ao, np * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (hits) ARC_CK(c, cudaMemcpyAsync(hits, P.hits, b_h, cudaMemcpyDeviceToHost, c->stream));
+    if (gi_hits) ARC_CK(c, cudaMemcpyAsync(gi_hits, P.gi_hits, b_gi, cudaMemcpyDeviceToHost, c->stream));
+    return collect_frame(c, np, n_gi_out);
+}
+
+int arc_trace_primary(arc_ctx* c, uint32_t width, uint32_t height, uint32_t* gdm, uint32_t* gnm, uint32_t* gaa,
+                      arc_hit_record* hits) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if ((rc = check_dims(c, width, height))) return rc;
+    if (!gdm || !gnm || !gaa) return set_err(c, ARC_E_INVALID_ARG, "null G-buffer");
+    const size_t np = (size_t)width * height;
+    const size_t b_g = np * 20, b_h = hits ? np * 20 : 0;
+    void* stage;
+    if ((rc = arc_ctx_stage(c, b_g + b_h, &stage))) return rc;
+    unsigned char* base = static_cast<unsigned char*>(stage);
+    uint32_t* d_gdm = reinterpret_cast<uint32_t*>(base);
+    uint32_t* d_gnm = reinterpret_cast<uint32_t*>(base + np * 8);
+    uint32_t* d_gaa = reinterpret_cast<uint32_t*>(base + np * 16);
+    arc_hit_record* d_hits = hits ? reinterpret_cast<arc_hit_record*>(base + b_g) : nullptr;
+    if ((rc = arc_trace_primary_dev(c, width, height, d_gdm, d_gnm, d_gaa, d_hits))) return rc;
+    ARC_CK(c, cudaMemcpyAsync(gdm, d_gdm, np * 8, cudaMemcpyDeviceToHost, c->stream));
+    ARC_CK(c, cudaMemcpyAsync(gnm, d_gnm, np * 8, cudaMemcpyDeviceToHost, c->stream));
+    ARC_CK(c, cudaMemcpyAsync(gaa, d_gaa, np * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (hits) ARC_CK(c, cudaMemcpyAsync(hits, d_hits, b_h, cudaMemcpyDeviceToHost, c->stream));
+    return collect_frame(c, np, nullptr);
+}
+
+int arc_trace_secondary(arc_ctx* c, uint32_t width, uint32_t height, const uint32_t* gdm, const uint32_t* gnm,
+                        arc_hit_record* gi_hits) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if ((rc = check_dims(c, width, height))) return rc;
+    if (!gdm || !gnm || !gi_hits) return set_err(c, ARC_E_INVALID_ARG, "null buffer");
+    const size_t np = (size_t)width * height;
+    void* stage;
+    if ((rc = arc_ctx_stage(c, np * 36, &stage))) return rc;
+    unsigned char* base = static_cast<unsigned char*>(stage);
+    uint32_t* d_gdm = reinterpret_cast<uint32_t*>(base);
+    uint32_t* d_gnm = reinterpret_cast<uint32_t*>(base + np * 8);
+    arc_hit_record* d_hits = reinterpret_cast<arc_hit_record*>(base + np * 16);
+    ARC_CK(c, cudaMemcpyAsync(d_gdm, gdm, np * 8, cudaMemcpyHostToDevice, c->stream));
+    ARC_CK(c, cudaMemcpyAsync(d_gnm, gnm, np * 8, cudaMemcpyHostToDevice, c->stream));
+    if ((rc = arc_trace_secondary_dev(c, width, height, d_gdm, d_gnm, d_hits))) return rc;
+    ARC_CK(c, cudaMemcpyAsync(gi_hits, d_hits, np * 20, cudaMemcpyDeviceToHost, c->stream));
+    return arc_ctx_finish(c);
+}
+
+int arc_trace_rays_dev(arc_ctx* c, const arc_ray* rays, uint32_t n, float max_dist_m, uint32_t lod_bias, int ignore_water,
+                       arc_hit_record* hits) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if (n && (!rays || !hits)) return set_err(c, ARC_E_INVALID_ARG, "null buffer");
+    if (lod_bias > 2u) return set_err(c, ARC_E_INVALID_ARG, "lod_bias must be 0, 1 or 2");
+    ARC_CK(c, arc::launch_rays(c->world(), c->cam, rays, n, max_dist_m, lod_bias, ignore_water, hits, c->stream));
+    return ARC_OK;
+}
+
+int arc_trace_rays(arc_ctx* c, const arc_ray* rays, uint32_t n, float max_dist_m, uint32_t lod_bias, int ignore_water,
+                   arc_hit_record* hits) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if (n == 0) return ARC_OK;
+    if (!rays || !hits) return set_err(c, ARC_E_INVALID_ARG, "null buffer");
+    void* stage;
+    if ((rc = arc_ctx_stage(c, (size_t)n * 44, &stage))) return rc;
+    arc_ray* d_rays = static_cast<arc_ray*>(stage);
+    arc_hit_record* d_hits = reinterpret_cast<arc_hit_record*>(static_cast<unsigned char*>(stage) + (size_t)n * 24);
+    ARC_CK(c, cudaMemcpyAsync(d_rays, rays, (size_t)n * 24, cudaMemcpyHostToDevice, c->stream));
+    if ((rc = arc_trace_rays_dev(c, d_rays, n, max_dist_m, lod_bias, ignore_water, d_hits))) return rc;
+    ARC_CK(c, cudaMemcpyAsync(hits, d_hits, (size_t)n * 20, cudaMemcpyDeviceToHost, c->stream));
+    return arc_ctx_finish(c);
+}
+
+int arc_shadow_rays_dev(arc_ctx* c, const arc_ray* rays, uint32_t n, float max_dist_m, float* vis) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if (n && (!rays || !vis)) return set_err(c, ARC_E_INVALID_ARG, "null buffer");
+    ARC_CK(c, arc::launch_shadow(c->world(), c->cam, rays, n, max_dist_m, vis, c->stream));
+    return ARC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,56 @@
+// arc_ctx.h — the opaque arc_ctx behind the C ABI (one device, one stream).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "arc_kernels.h"
+
+struct arc_ctx {
+    int device = 0;
+    int n_sm = 0;
+    cudaStream_t stream = nullptr;
+
+    // Group-0 pools (device copies of WorldMap's packed buffers)
+    uint32_t grid[3] = {0, 0, 0};
+    uint32_t n_roots = 0;
+    uint32_t* d_roots = nullptr;
+    arc_node64* d_nodes = nullptr;
+    uint32_t n_nodes = 0, cap_nodes = 0;
+    arc_brick64* d_bricks = nullptr;
+    uint32_t n_bricks = 0, cap_bricks = 0;
+    arc_material* d_palette = nullptr;
+    bool have_world = false;
+
+    arc_camera_uniforms cam{};
+    bool have_cam = false;
+
+    arc::Scratch* d_scratch = nullptr;
+    uint32_t* d_status = nullptr;
+    uint32_t last_status = 0;
+
+    // staging block of the host-buffer entry points
+    void* d_stage = nullptr;
+    size_t stage_bytes = 0;
+
+    // SHARC cache
+    uint32_t* d_sharc_keys = nullptr;
+    uint32_t* d_sharc_accum = nullptr;
+    arc_sharc_slot* d_sharc_resolved = nullptr;
+    void* d_sharc_stage = nullptr;
+    size_t sharc_stage_bytes = 0;
+
+    arc_launch_config cfg{};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool timing_pending = false;
+    float last_ms = 0.0f;
+    uint64_t last_rays = 0;
+    std::string err;
+
+    arc::World world() const;
+};
+
+int arc_ctx_check_ready(arc_ctx* c, bool need_cam);
+int arc_ctx_finish(arc_ctx* c);
+int arc_ctx_stage(arc_ctx* c, size_t bytes, void** out);

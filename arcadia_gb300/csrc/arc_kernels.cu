@@ -1,0 +1,381 @@
+// arc_kernels.cu — traversal kernels of libarc_trace.so (sm_103a).
+//
+//   frame_plain_kernel       one thread per pixel: primary ray (primary_raymarch,
+//                            shaders/primary_gbuffer.wgsl:93-312) then, for a hit, the GI secondary ray
+//                            (shaders/lighting_restir_gi.wgsl:195-209) in the same thread.
+//   frame_persistent_kernel  persistent warps pulling pixels from a global queue; a lane whose ray
+//                            finishes is refilled with the next pixel between DDA iterations, a primary
+//                            hit turns the lane into its GI ray, so uneven ray lengths do not idle lanes.
+//   secondary_kernel         GI ray per pixel from an existing G-buffer.
+//   rays_kernel / shadow_kernel  trace_world_64tree / trace_shadow_vis over a ray batch.
+//   sharc_*                  shaders/sharc_update.wgsl, sharc_resolve.wgsl, common/sharc_query.wgsl.
+//
+// Compiled with --fmad=false --prec-div=true --prec-sqrt=true (canonical arithmetic, arc_math.cuh).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "arc_kernels.h"
+#include "arc_traverse.cuh"
+
+namespace arc {
+
+// ------------------------------------------------------------------------------------------------
+// Outputs
+// ------------------------------------------------------------------------------------------------
+
+__device__ __forceinline__ void store_hit(arc_hit_record* p, const HitInfo& h, bool hit) {
+    uint32_t* q = reinterpret_cast<uint32_t*>(p);
+    if (hit) {
+        q[0] = h.vx;
+        q[1] = h.vy;
+        q[2] = h.vz;
+        q[3] = face_id(h.normal) | (h.mat << 8) | ((ARC_HIT_FLAG_HIT | ((h.shift >> 1) << 1)) << 16);
+    } else {
+        q[0] = q[1] = q[2] = 0xFFFFFFFFu;
+        q[3] = ARC_FACE_NONE;
+    }
+    q[4] = __float_as_uint(h.t_voxels * ARC_VOXEL_SIZE);
+}
+
+__device__ __forceinline__ void store_no_ray(arc_hit_record* p) {
+    uint32_t* q = reinterpret_cast<uint32_t*>(p);
+    q[0] = q[1] = q[2] = 0xFFFFFFFFu;
+    q[3] = ARC_FACE_NONE;
+    q[4] = 0u;
+}
+
+// G-buffer words of one pixel (primary_gbuffer.wgsl:138-143 miss, 145-311 hit; no rigid bodies and
+// no water / mirror / underwater shading branches). Returns the packed depth and normal words the
+// GI ray is generated from.
+__device__ __forceinline__ void primary_store(const FrameParams& P, const arc_camera_uniforms& cam, uint32_t x,
+                                              uint32_t y, f3 dir, bool hit, const HitInfo& h, uint32_t* depth_word,
+                                              uint32_t* normal_word) {
+    const size_t k = (size_t)y * P.width + x;
+    if (P.hits) store_hit(&P.hits[k], h, hit);
+    if (!hit) {
+        float ox, oy;
+        oct_encode(dir, &ox, &oy);
+        const uint32_t n0 = pack2x16snorm(ox, oy);
+        reinterpret_cast<uint2*>(P.gbuf_depth_mat)[k] = make_uint2(__float_as_uint(1e5f), 0u);
+        reinterpret_cast<uint2*>(P.gbuf_norm_motion)[k] = make_uint2(n0, pack2x16float(0.0f, 0.0f));
+        P.gbuf_albedo_ao[k] = pack4x8unorm(0.0f, 0.0f, 0.0f, 1.0f);
+        *depth_word = __float_as_uint(1e5f);
+        *normal_word = n0;
+        return;
+    }
+    const float hit_dist = h.t_voxels * ARC_VOXEL_SIZE;
+    const float4 alb_r = __ldg(&P.world.palette[2u * h.mat]);
+    const float4 em_m = __ldg(&P.world.palette[2u * h.mat + 1u]);
+    const float vrw = 1.0f - smoothstepf(18.0f, 48.0f, hit_dist);
+    const float vr = (__fdiv_rn((float)(h.voxel_hash & 0xFFu), 255.0f) * 2.0f - 1.0f) * vrw;
+    const float k_var = 1.0f + vr * em_m.w;
+    const float ar = clampf(alb_r.x * k_var, 0.01f, 1.0f);
+    const float ag = clampf(alb_r.y * k_var, 0.01f, 1.0f);
+    const float ab = clampf(alb_r.z * k_var, 0.01f, 1.0f);
+    // analytic motion vector (primary_gbuffer.wgsl:298-305), column-major prev_view_proj
+    const float pu = __fdiv_rn((float)x + 0.5f, (float)P.width);
+    const float pv = __fdiv_rn((float)y + 0.5f, (float)P.height);
+    const float* M = cam.prev_view_proj;
+    const f3 hp = h.hit_pos_m;
+    float clip[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) clip[r] = ((M[r] * hp.x + M[4 + r] * hp.y) + M[8 + r] * hp.z) + M[12 + r] * 1.0f;
+    float mx = -2.0f, my = -2.0f;
+    if (clip[3] > 0.001f) {
+        const float ndx = __fdiv_rn(clip[0], clip[3]), ndy = __fdiv_rn(clip[1], clip[3]);
+        mx = (ndx * 0.5f + 0.5f) - pu;
+        my = (0.5f - ndy * 0.5f) - pv;
+    }
+    float ox, oy;
+    oct_encode(h.normal, &ox, &oy);
+    const uint32_t n0 = pack2x16snorm(ox, oy);
+    reinterpret_cast<uint2*>(P.gbuf_depth_mat)[k] = make_uint2(__float_as_uint(hit_dist), h.mat & 0xFFFFu);
+    reinterpret_cast<uint2*>(P.gbuf_norm_motion)[k] = make_uint2(n0, pack2x16float(mx, my));
+    P.gbuf_albedo_ao[k] = pack4x8unorm(ar, ag, ab, clampf(h.contact_ao, 0.0f, 1.0f));
+    *depth_word = __float_as_uint(hit_dist);
+    *normal_word = n0;
+}
+
+// probe_emissive_macro_candidate (lighting_restir_gi.wgsl:20-54).
+__device__ __forceinline__ float probe_emissive(const World& w, const arc_camera_uniforms& cam, f3 pos, f3 d, float dist) {
+    const f3 vp = mul3s(add3(pos, mul3s(d, dist)), ARC_VOXELS_PER_METER);
+    const uint32_t gx = cam.world_grid_dims[0], gy = cam.world_grid_dims[1], gz = cam.world_grid_dims[2];
+    if (vp.x < 0.0f || vp.y < 0.0f || vp.z < 0.0f) return 0.0f;
+    if (vp.x >= (float)gx * ARC_CHUNK_DIM_F || vp.y >= (float)gy * ARC_CHUNK_DIM_F || vp.z >= (float)gz * ARC_CHUNK_DIM_F)
+        return 0.0f;
+    const uint32_t vx = f2u(vp.x), vy = f2u(vp.y), vz = f2u(vp.z);
+    const uint32_t root_idx = load_root(w, (vx >> 8) + (vy >> 8) * gx + (vz >> 8) * gx * gy);
+    if (root_idx == ARC_EMPTY_CHUNK) return 0.0f;
+    const uint32_t lx = vx & 255u, ly = vy & 255u, lz = vz & 255u;
+    const uint4 root = load_node(w, root_idx);
+    const uint32_t b0 = (((lz >> 6) & 3u) << 4) | (((ly >> 6) & 3u) << 2) | ((lx >> 6) & 3u);
+    if (!has_child(root.x, root.y, b0)) return 0.0f;
+    uint32_t m_id;
+    if (root.z & ARC_IS_LEAF_FLAG) {
+        m_id = (root.w >> 24) & 0xFFu;
+    } else {
+        const uint4 l1 = load_node(w, child_index(root, b0));
+        const uint32_t b1 = (((lz >> 4) & 3u) << 4) | (((ly >> 4) & 3u) << 2) | ((lx >> 4) & 3u);
+        if (!has_child(l1.x, l1.y, b1)) return 0.0f;
+        m_id = (l1.w >> 24) & 0xFFu;
+    }
+    const float4 em = __ldg(&w.palette[2u * m_id + 1u]);
+    return (em.x * 0.333f + em.y * 0.333f) + em.z * 0.333f;
+}
+
+// GI secondary ray of a hit pixel from its G-buffer words (lighting_restir_gi.wgsl:69-87, 195-209).
+__device__ __forceinline__ bool gi_setup(const World& w, const arc_camera_uniforms& cam, uint32_t x, uint32_t y,
+                                         uint32_t W, uint32_t H, uint32_t depth_word, uint32_t normal_word, f3* origin,
+                                         f3* dir) {
+    const float hit_dist = __uint_as_float(depth_word);
+    if (hit_dist >= 1e4f) return false;
+    const f3 rd = camera_dir(cam, x, y, W, H);
+    const f3 eye{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]};
+    const f3 hp = add3(eye, mul3s(rd, hit_dist));
+    float ox, oy;
+    unpack2x16snorm(normal_word, &ox, &oy);
+    const f3 n = oct_decode(ox, oy);
+    float u1, u2;
+    gradient_noise((float)x, (float)y, __float_as_uint(cam.cam_up_frame[3]), &u1, &u2);
+    const f3 sn = normalize3(f3{n.x + 0.0f, n.y + 0.22f, n.z + 0.0f});
+    f3 bt, bb;
+    make_basis(sn, &bt, &bb);
+    f3 bd = cosine_sample(u1, u2, sn, bt, bb);
+    const f3 cd = cosine_sample(fractf(u1 + 0.5f), fractf(u2 + 0.381966f), sn, bt, bb);
+    const float em_near = probe_emissive(w, cam, hp, cd, 1.25f);
+    const float em_mid = probe_emissive(w, cam, hp, cd, 3.0f);
+    if (fmaxf(em_near, em_mid) > 0.25f) bd = cd;
+    *origin = add3(hp, mul3s(n, 0.10f));
+    *dir = bd;
+    return true;
+}
+
+__device__ __forceinline__ void pixel_of(const FrameParams& P, uint32_t q, uint32_t* x, uint32_t* y) {
+    const uint32_t tile = q >> 5, within = q & 31u;
+    const uint32_t tx = tile % P.tiles_x, ty = tile / P.tiles_x;
+    *x = tx * P.tile_w + within % P.tile_w;
+    *y = ty * P.tile_h + within / P.tile_w;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Frame kernels
+// ------------------------------------------------------------------------------------------------
+
+__global__ void frame_plain_kernel(const FrameParams P, const __grid_constant__ arc_camera_uniforms cam) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.width || y >= P.height) return;
+    const World& w = P.world;
+    const f3 eye{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]};
+    const f3 dir = camera_dir(cam, x, y, P.width, P.height);
+    const bool underwater = (cam.point_light_count[1] & 0xFFFFu) != 0u;
+    RayState s;
+    HitInfo h;
+    StepResult r = kMiss;
+    if (ray_begin(s, cam, eye, dir, 0.0f, 250.0f, 0u, underwater)) {
+        do {
+            r = ray_advance(s, w, cam, h);
+        } while (r == kContinue);
+    }
+    if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
+    uint32_t dw, nw;
+    primary_store(P, cam, x, y, dir, r == kHit, h, &dw, &nw);
+    if (!P.do_gi) return;
+    const size_t k = (size_t)y * P.width + x;
+    f3 go, gd;
+    if (!gi_setup(w, cam, x, y, P.width, P.height, dw, nw, &go, &gd)) {
+        if (P.gi_hits) store_no_ray(&P.gi_hits[k]);
+        return;
+    }
+    const float gmax = cam.ray_distances[2];
+    StepResult g = kMiss;
+    if (ray_begin(s, cam, go, gd, 0.0f, gmax, 2u, true)) {
+        do {
+            g = ray_advance(s, w, cam, h);
+        } while (g == kContinue);
+    }
+    if (g != kHit) hit_init_miss(h, go, gd, gmax);
+    if (P.gi_hits) store_hit(&P.gi_hits[k], h, g == kHit);
+    // warp-aggregated count of GI rays
+    const uint32_t m = __activemask();
+    if (((threadIdx.x + threadIdx.y * blockDim.x) & 31u) == (uint32_t)(__ffs(m) - 1)) atomicAdd(&P.scratch->gi_rays, (unsigned long long)__popc(m));
+}
+
+enum : uint32_t { kIdle = 0u, kPrimary = 1u, kGi = 2u };
+
+__global__ void __launch_bounds__(256) frame_persistent_kernel(const FrameParams P,
+                                                               const __grid_constant__ arc_camera_uniforms cam) {
+    const World& w = P.world;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    const f3 eye{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]};
+    const bool underwater = (cam.point_light_count[1] & 0xFFFFu) != 0u;
+    const float gmax = cam.ray_distances[2];
+    RayState s;
+    HitInfo h;
+    uint32_t phase = kIdle;
+    uint32_t px = 0, py = 0;
+    bool exhausted = false;
+    unsigned long long gi_count = 0;
+
+    for (;;) {
+        // Refill idle lanes from the queue (one atomic per warp).
+        const uint32_t idle = __ballot_sync(0xFFFFFFFFu, phase == kIdle);
+        if (!exhausted && (__popc(idle) >= (int)P.refill_threshold || idle == 0xFFFFFFFFu)) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(&P.scratch->queue_head, (uint32_t)__popc(idle));
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base + (uint32_t)__popc(idle) >= P.queue_len) exhausted = true;
+            if (phase == kIdle) {
+                const uint32_t q = base + __popc(idle & lt_mask);
+                if (q < P.queue_len) {
+                    pixel_of(P, q, &px, &py);
+                    if (px < P.width && py < P.height) {
+                        const f3 dir = camera_dir(cam, px, py, P.width, P.height);
+                        if (ray_begin(s, cam, eye, dir, 0.0f, 250.0f, 0u, underwater)) {
+                            phase = kPrimary;
+                        } else {
+                            hit_init_miss(h, eye, dir, 250.0f);
+                            uint32_t dw, nw;
+                            primary_store(P, cam, px, py, dir, false, h, &dw, &nw);
+                            if (P.do_gi && P.gi_hits) store_no_ray(&P.gi_hits[(size_t)py * P.width + px]);
+                        }
+                    }
+                }
+            }
+        }
+        if (__ballot_sync(0xFFFFFFFFu, phase != kIdle) == 0u) {
+            if (exhausted) break;
+            continue;
+        }
+        if (phase == kIdle) continue;
+        const StepResult r = ray_advance(s, w, cam, h);
+        if (r == kContinue) continue;
+        if (phase == kPrimary) {
+            const f3 dir = s.dir;
+            if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
+            uint32_t dw, nw;
+            primary_store(P, cam, px, py, dir, r == kHit, h, &dw, &nw);
+            phase = kIdle;
+            if (P.do_gi) {
+                f3 go, gd;
+                if (gi_setup(w, cam, px, py, P.width, P.height, dw, nw, &go, &gd)) {
+                    ++gi_count;
+                    if (ray_begin(s, cam, go, gd, 0.0f, gmax, 2u, true)) {
+                        phase = kGi;
+                    } else {
+                        hit_init_miss(h, go, gd, gmax);
+                        if (P.gi_hits) store_hit(&P.gi_hits[(size_t)py * P.width + px], h, false);
+                    }
+                } else if (P.gi_hits) {
+                    store_no_ray(&P.gi_hits[(size_t)py * P.width + px]);
+                }
+            }
+        } else {
+            if (r != kHit) hit_init_miss(h, mul3s(s.vo, ARC_VOXEL_SIZE), s.dir, gmax);
+            if (P.gi_hits) store_hit(&P.gi_hits[(size_t)py * P.width + px], h, r == kHit);
+            phase = kIdle;
+        }
+    }
+    // warp-reduce the GI ray count
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) gi_count += __shfl_down_sync(0xFFFFFFFFu, gi_count, o);
+    if (lane == 0 && gi_count) atomicAdd(&P.scratch->gi_rays, gi_count);
+}
+
+__global__ void secondary_kernel(const FrameParams P, const __grid_constant__ arc_camera_uniforms cam) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.width || y >= P.height) return;
+    const size_t k = (size_t)y * P.width + x;
+    const uint32_t dw = P.gbuf_depth_mat[2 * k], nw = P.gbuf_norm_motion[2 * k];
+    f3 go, gd;
+    if (!gi_setup(P.world, cam, x, y, P.width, P.height, dw, nw, &go, &gd)) {
+        store_no_ray(&P.gi_hits[k]);
+        return;
+    }
+    const float gmax = cam.ray_distances[2];
+    RayState s;
+    HitInfo h;
+    StepResult g = kMiss;
+    if (ray_begin(s, cam, go, gd, 0.0f, gmax, 2u, true)) {
+        do {
+            g = ray_advance(s, P.world, cam, h);
+        } while (g == kContinue);
+    }
+    if (g != kHit) hit_init_miss(h, go, gd, gmax);
+    store_hit(&P.gi_hits[k], h, g == kHit);
+}
+
+__global__ void rays_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, const arc_ray* __restrict__ rays,
+                            uint32_t n, float max_dist_m, uint32_t lod_bias, uint32_t ignore_water,
+                            arc_hit_record* __restrict__ hits) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* rp = reinterpret_cast<const float*>(&rays[i]);
+    const f3 o{rp[0], rp[1], rp[2]}, d{rp[3], rp[4], rp[5]};
+    RayState s;
+    HitInfo h;
+    StepResult r = kMiss;
+    if (ray_begin(s, cam, o, d, 0.0f, max_dist_m, lod_bias, ignore_water != 0u)) {
+        do {
+            r = ray_advance(s, w, cam, h);
+        } while (r == kContinue);
+    }
+    if (r != kHit) hit_init_miss(h, o, d, max_dist_m);
+    store_hit(&hits[i], h, r == kHit);
+}
+
+__global__ void shadow_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, const arc_ray* __restrict__ rays,
+                              uint32_t n, float max_dist_m, float* __restrict__ vis) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* rp = reinterpret_cast<const float*>(&rays[i]);
+    vis[i] = shadow_vis(w, cam, f3{rp[0], rp[1], rp[2]}, f3{rp[3], rp[4], rp[5]}, max_dist_m);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Host launchers (called by the C ABI on the context's stream)
+// ------------------------------------------------------------------------------------------------
+
+cudaError_t launch_frame(const FrameParams& P, const arc_camera_uniforms& cam, const arc_launch_config& cfg,
+                         int n_sm, cudaStream_t st) {
+    if (cfg.variant == 0u) {
+        const uint32_t bw = 8u, bh = cfg.block_threads / 8u;
+        dim3 block(bw, bh);
+        dim3 grid((P.width + bw - 1u) / bw, (P.height + bh - 1u) / bh);
+        frame_plain_kernel<<<grid, block, 0, st>>>(P, cam);
+        return cudaGetLastError();
+    }
+    int per_sm = (int)cfg.blocks_per_sm;
+    if (per_sm <= 0) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, frame_persistent_kernel, (int)cfg.block_threads, 0);
+        if (e != cudaSuccess) return e;
+        if (per_sm <= 0) per_sm = 1;
+    }
+    frame_persistent_kernel<<<n_sm * per_sm, cfg.block_threads, 0, st>>>(P, cam);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_secondary(const FrameParams& P, const arc_camera_uniforms& cam, cudaStream_t st) {
+    dim3 block(8, 8);
+    dim3 grid((P.width + 7u) / 8u, (P.height + 7u) / 8u);
+    secondary_kernel<<<grid, block, 0, st>>>(P, cam);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rays(const World& w, const arc_camera_uniforms& cam, const arc_ray* rays, uint32_t n, float max_dist_m,
+                        uint32_t lod_bias, int ignore_water, arc_hit_record* hits, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    rays_kernel<<<(n + 127u) / 128u, 128, 0, st>>>(w, cam, rays, n, max_dist_m, lod_bias, ignore_water ? 1u : 0u, hits);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shadow(const World& w, const arc_camera_uniforms& cam, const arc_ray* rays, uint32_t n, float max_dist_m,
+                          float* vis, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    shadow_kernel<<<(n + 127u) / 128u, 128, 0, st>>>(w, cam, rays, n, max_dist_m, vis);
+    return cudaGetLastError();
+}
+
+}  // namespace arc

@@ -1,0 +1,392 @@
+// arc_sharc.cu — SHARC voxel-surfel radiance cache on the GPU.
+//
+//   sharc_update_kernel   sharc_update.wgsl main (shaders/sharc_update.wgsl:148-191): one thread per
+//                         screen tile traces x0 -> x1 (GI bounce), a sun shadow ray and one more
+//                         bounce at x1, then deposits L_o(x1) with a CAS slot claim and fixed-point adds.
+//   sharc_resolve_kernel  sharc_resolve.wgsl main (shaders/sharc_resolve.wgsl:13-70): EMA fold, aging,
+//                         eviction, accumulator clear; one thread per slot.
+//   sharc_query_kernel    query_sharc (shaders/common/sharc_query.wgsl:125-146) on a batch.
+// Compiled with the canonical arithmetic flags (arc_math.cuh).
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+
+#include "arc_ctx.h"
+
+namespace arc {
+
+struct SharcBuffers {
+    uint32_t* keys;
+    uint32_t* accum;
+    uint4* resolved;
+};
+
+// sharc_make_key (shaders/common/sharc.wgsl:69-93).
+__device__ __forceinline__ void sharc_key(f3 pos, f3 n, f3 cam, float jx, float jy, uint32_t* bucket, uint32_t* key) {
+    const float d = length3(sub3(pos, cam));
+    const int fl = floor_log2(fmaxf(d, 4.0f) * 0.25f);
+    const uint32_t lod = fl < 0 ? 0u : (fl > 3 ? 3u : (uint32_t)fl);
+    const float s = 0.25f * (float)(1u << lod);
+    f3 a = sub3(pos, mul3s(n, 0.02f));
+    if (jx != 0.0f || jy != 0.0f) {
+        f3 t, b;
+        make_basis(n, &t, &b);
+        const float k = 0.42f * s;
+        a.x += (t.x * jx + b.x * jy) * k;
+        a.y += (t.y * jx + b.y * jy) * k;
+        a.z += (t.z * jx + b.z * jy) * k;
+    }
+    const uint32_t cx = (uint32_t)((int)floorf(__fdiv_rn(a.x, s)) + 16384);
+    const uint32_t cy = (uint32_t)((int)floorf(__fdiv_rn(a.y, s)) + 16384);
+    const uint32_t cz = (uint32_t)((int)floorf(__fdiv_rn(a.z, s)) + 16384);
+    const uint32_t nid = face_id(n);
+    const uint32_t bk = pcg_hash((cx * 73856093u) ^ (cy * 19349663u) ^ (cz * 83492791u) ^ (nid * 2654435761u) ^ (lod * 38069u)) &
+                        (ARC_SHARC_BUCKETS - 1u);
+    *bucket = bk;
+    *key = pcg_hash(bk ^ (cx * 1013904223u) ^ (cy * 1664525u) ^ (cz * 2891336453u) ^ (nid << 20) ^ (lod << 24)) |
+           ARC_SHARC_KEY_VALID_BIT;
+}
+
+__device__ __forceinline__ f3 slot_radiance(uint4 s) {
+    return f3{f16_value(s.y & 0xFFFFu), f16_value(s.y >> 16), f16_value(s.z & 0xFFFFu)};
+}
+
+// sharc_lookup / query_sharc (shaders/common/sharc_query.wgsl:125-146); w = 1 on hit.
+__device__ __forceinline__ float4 sharc_lookup(const uint4* res, uint32_t bucket, uint32_t key) {
+    const uint32_t base = bucket * ARC_SHARC_WAYS;
+#pragma unroll
+    for (uint32_t i = 0; i < ARC_SHARC_WAYS; ++i) {
+        const uint4 s = res[base + i];
+        if (s.x == key) {
+            const f3 r = slot_radiance(s);
+            return make_float4(r.x, r.y, r.z, 1.0f);
+        }
+    }
+    return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+__device__ __forceinline__ float4 sharc_query(const uint4* res, f3 pos, f3 n, f3 cam, float jx, float jy) {
+    uint32_t b, k;
+    if (jx != 0.0f || jy != 0.0f) {
+        sharc_key(pos, n, cam, jx, jy, &b, &k);
+        const float4 r = sharc_lookup(res, b, k);
+        if (r.w > 0.5f) return r;
+    }
+    sharc_key(pos, n, cam, 0.0f, 0.0f, &b, &k);
+    return sharc_lookup(res, b, k);
+}
+
+// sharc_claim_slot + sharc_deposit (shaders/sharc_update.wgsl:108-144). atomicCAS is strong, so the
+// WGSL retry after a spurious weak-CAS failure is not needed.
+__device__ __forceinline__ void sharc_deposit(const SharcBuffers& S, uint32_t bucket, uint32_t key, f3 rad) {
+    const uint32_t base = bucket * ARC_SHARC_WAYS;
+    uint32_t slot = ARC_SHARC_NO_SLOT;
+    for (uint32_t i = 0; i < ARC_SHARC_WAYS && slot == ARC_SHARC_NO_SLOT; ++i)
+        if (reinterpret_cast<volatile uint32_t*>(S.keys)[base + i] == key) slot = base + i;
+    for (uint32_t i = 0; i < ARC_SHARC_WAYS && slot == ARC_SHARC_NO_SLOT; ++i) {
+        const uint32_t old = atomicCAS(&S.keys[base + i], 0u, key);
+        if (old == 0u || old == key) slot = base + i;
+    }
+    if (slot == ARC_SHARC_NO_SLOT) return;
+    const uint32_t a = slot * 4u;
+    atomicAdd(&S.accum[a], f2u(clampf(rad.x, 0.0f, ARC_SHARC_MAX_RADIANCE) * ARC_SHARC_FIXED_SCALE));
+    atomicAdd(&S.accum[a + 1u], f2u(clampf(rad.y, 0.0f, ARC_SHARC_MAX_RADIANCE) * ARC_SHARC_FIXED_SCALE));
+    atomicAdd(&S.accum[a + 2u], f2u(clampf(rad.z, 0.0f, ARC_SHARC_MAX_RADIANCE) * ARC_SHARC_FIXED_SCALE));
+    atomicAdd(&S.accum[a + 3u], 1u);
+}
+
+// eval_sky_radiance (shaders/common/types.wgsl:500-523).
+__device__ __forceinline__ f3 sky_radiance(f3 dir, f3 sun) {
+    const float day_t = clampf(__fdiv_rn(sun.y + 0.05f, 0.30f), 0.0f, 1.0f);
+    const float tw_t = clampf(1.0f - __fdiv_rn(fabsf(sun.y - 0.02f), 0.22f), 0.0f, 1.0f);
+    const float horizon = powi(1.0f - clampf(dir.y, 0.0f, 1.0f), 3u);
+    const f3 sz{mixf(0.0015f, 0.08f, day_t), mixf(0.0025f, 0.22f, day_t), mixf(0.0055f, 0.55f, day_t)};
+    f3 sh{mixf(0.0035f, 0.38f, day_t), mixf(0.0065f, 0.50f, day_t), mixf(0.0120f, 0.68f, day_t)};
+    const float tw = tw_t * 0.75f;
+    sh = f3{mixf(sh.x, 0.65f, tw), mixf(sh.y, 0.25f, tw), mixf(sh.z, 0.10f, tw)};
+    f3 sky{mixf(sz.x, sh.x, horizon), mixf(sz.y, sh.y, horizon), mixf(sz.z, sh.z, horizon)};
+    if (sun.y > -0.12f) {
+        const float p = powi(fmaxf(dot3(dir, sun), 0.0f), 14u);
+        const float m = fmaxf(day_t, tw_t);
+        sky.x += ((0.85f * p) * 0.35f) * m;
+        sky.y += ((0.52f * p) * 0.35f) * m;
+        sky.z += ((0.24f * p) * 0.35f) * m;
+    }
+    return sky;
+}
+
+struct Surface {
+    bool hit;
+    float t_m;
+    f3 pos, normal, albedo, emission;
+};
+
+// sharc_trace_surface (shaders/sharc_update.wgsl:32-64) without rigid bodies.
+__device__ __forceinline__ Surface trace_surface(const World& w, const arc_camera_uniforms& cam, f3 o, f3 d, float max_dist) {
+    Surface out;
+    out.hit = false;
+    RayState s;
+    HitInfo h;
+    StepResult r = kMiss;
+    if (ray_begin(s, cam, o, d, 0.0f, max_dist, 2u, true)) {
+        do {
+            r = ray_advance(s, w, cam, h);
+        } while (r == kContinue);
+    }
+    if (r != kHit) return out;
+    const float4 alb = __ldg(&w.palette[2u * h.mat]);
+    const float4 em = __ldg(&w.palette[2u * h.mat + 1u]);
+    const float lr = __fdiv_rn((float)(h.lod_payload & 0xFFu), 255.0f);
+    const float lg = __fdiv_rn((float)((h.lod_payload >> 8) & 0xFFu), 255.0f);
+    const float lb = __fdiv_rn((float)((h.lod_payload >> 16) & 0xFFu), 255.0f);
+    out.hit = true;
+    out.t_m = h.t_voxels * ARC_VOXEL_SIZE;
+    out.pos = h.hit_pos_m;
+    out.normal = h.normal;
+    out.albedo = f3{mixf(alb.x, lr, 0.55f), mixf(alb.y, lg, 0.55f), mixf(alb.z, lb, 0.55f)};
+    out.emission = f3{em.x, em.y, em.z};
+    return out;
+}
+
+__global__ void sharc_update_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, const SharcBuffers S,
+                                    const uint32_t* __restrict__ gdm, const uint32_t* __restrict__ gnm, uint32_t W,
+                                    uint32_t H) {
+    const uint32_t tile = (cam.quality_flags[3] & 0xFFu) <= 12u ? 16u : 8u;
+    const uint32_t tiles_x = (W + tile - 1u) / tile, tiles_y = (H + tile - 1u) / tile;
+    const uint32_t gx = blockIdx.x * blockDim.x + threadIdx.x, gy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (gx >= tiles_x || gy >= tiles_y) return;
+    const uint32_t frame = __float_as_uint(cam.cam_up_frame[3]);
+    const uint32_t hsh = pcg_hash(gx * 1973u + gy * 9277u + frame * 26699u + 0x51ED270Bu);
+    const uint32_t px = umin(gx * tile + (hsh & (tile - 1u)), W - 1u);
+    const uint32_t py = umin(gy * tile + ((hsh >> 8) & (tile - 1u)), H - 1u);
+    const size_t p = (size_t)py * W + px;
+    const float depth = __uint_as_float(gdm[2 * p]);
+    if (depth >= 1e4f) return;
+    const f3 eye{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]};
+    const f3 x0 = add3(eye, mul3s(camera_dir(cam, px, py, W, H), depth));
+    float ox, oy;
+    unpack2x16snorm(gnm[2 * p], &ox, &oy);
+    const f3 n0 = oct_decode(ox, oy);
+    const f3 sun{cam.sun_dir_intensity[0], cam.sun_dir_intensity[1], cam.sun_dir_intensity[2]};
+    const float sun_power = cam.sun_dir_intensity[3];
+    const float bounce_max = fminf(cam.ray_distances[2], tile == 16u ? 10.0f : 16.0f);
+    float a0, a1, b0, b1;
+    gradient_noise((float)px, (float)py, frame, &a0, &a1);
+    gradient_noise((float)px + 37.0f, (float)py + 91.0f, frame + 4099u, &b0, &b1);
+    f3 t, b;
+    make_basis(n0, &t, &b);
+    const f3 d0 = cosine_sample(a0, a1, n0, t, b);
+    const Surface s1 = trace_surface(w, cam, add3(x0, mul3s(n0, 0.10f)), d0, bounce_max);
+    if (!s1.hit) return;
+    // sharc_shade_surface (shaders/sharc_update.wgsl:68-105)
+    const f3 n = s1.normal;
+    f3 direct{0.0f, 0.0f, 0.0f};
+    const float ndl = fmaxf(dot3(n, sun), 0.0f);
+    if (ndl > 0.001f && sun_power > 0.01f) {
+        const float vis = shadow_vis(w, cam, add3(s1.pos, mul3s(n, 0.10f)), sun, 32.0f);
+        direct = f3{(((1.0f * sun_power) * ndl) * vis) * 0.55f, (((0.90f * sun_power) * ndl) * vis) * 0.55f,
+                    (((0.75f * sun_power) * ndl) * vis) * 0.55f};
+    }
+    make_basis(n, &t, &b);
+    const f3 bd = cosine_sample(b0, b1, n, t, b);
+    const f3 bo = add3(s1.pos, mul3s(n, 0.10f));
+    const Surface s2 = trace_surface(w, cam, bo, bd, bounce_max);
+    f3 g{0.0f, 0.0f, 0.0f};
+    if (s2.hit) {
+        const float att = __fdiv_rn(1.0f, (1.0f + s2.t_m * 0.06f) + (s2.t_m * s2.t_m) * 0.025f);
+        const float ndl_em = fmaxf(dot3(n, bd), 0.25f);
+        g.x += ((s2.emission.x * 1.15f) * att) * ndl_em;
+        g.y += ((s2.emission.y * 1.15f) * att) * ndl_em;
+        g.z += ((s2.emission.z * 1.15f) * att) * ndl_em;
+        const float4 q = sharc_query(S.resolved, s2.pos, s2.normal, eye, 0.0f, 0.0f);
+        g.x += q.x;
+        g.y += q.y;
+        g.z += q.z;
+    } else {
+        const float end_y = bo.y + bd.y * bounce_max;
+        if (bd.y > 0.15f && end_y >= 32.0f) {
+            const float esc = clampf(__fdiv_rn(bd.y - 0.15f, 0.35f), 0.0f, 1.0f);
+            const f3 sky = sky_radiance(bd, sun);
+            g.x += (sky.x * 0.45f) * esc;
+            g.y += (sky.y * 0.45f) * esc;
+            g.z += (sky.z * 0.45f) * esc;
+        }
+    }
+    const f3 rad{s1.albedo.x * (direct.x + g.x), s1.albedo.y * (direct.y + g.y), s1.albedo.z * (direct.z + g.z)};
+    uint32_t bk, key;
+    sharc_key(s1.pos, s1.normal, eye, 0.0f, 0.0f, &bk, &key);
+    sharc_deposit(S, bk, key, rad);
+}
+
+__global__ void sharc_resolve_kernel(SharcBuffers S) {
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= ARC_SHARC_SLOTS) return;
+    const uint32_t key = S.keys[slot];
+    if (key == 0u) {
+        S.resolved[slot] = make_uint4(0u, 0u, 0u, 0u);
+        return;
+    }
+    const uint32_t a = slot * 4u;
+    const uint32_t count = S.accum[a + 3u];
+    const uint4 prev = S.resolved[slot];
+    const bool prev_valid = prev.x == key;
+    f3 rad{0.0f, 0.0f, 0.0f};
+    uint32_t hist = 0u, stale = 0u;
+    if (prev_valid) {
+        rad = slot_radiance(prev);
+        hist = (prev.z >> 16) & 0xFFu;
+        stale = (prev.z >> 24) & 0xFFu;
+    }
+    if (count > 0u) {
+        const float inv = __fdiv_rn(1.0f, (float)count * ARC_SHARC_FIXED_SCALE);
+        const f3 smp{(float)S.accum[a] * inv, (float)S.accum[a + 1u] * inv, (float)S.accum[a + 2u] * inv};
+        hist = umin(hist + 1u, 255u);
+        const float alpha = __fdiv_rn(1.0f, fminf((float)hist, ARC_SHARC_HISTORY_CAP));
+        rad = f3{mixf(rad.x, smp.x, alpha), mixf(rad.y, smp.y, alpha), mixf(rad.z, smp.z, alpha)};
+        stale = 0u;
+        reinterpret_cast<uint4*>(S.accum)[slot] = make_uint4(0u, 0u, 0u, 0u);
+    } else {
+        stale += 1u;
+        if (!prev_valid || stale > ARC_SHARC_STALE_EVICT_AGE) {
+            S.keys[slot] = 0u;
+            S.resolved[slot] = make_uint4(0u, 0u, 0u, 0u);
+            return;
+        }
+    }
+    const float cr = clampf(rad.x, 0.0f, ARC_SHARC_MAX_RADIANCE), cg = clampf(rad.y, 0.0f, ARC_SHARC_MAX_RADIANCE),
+                cb = clampf(rad.z, 0.0f, ARC_SHARC_MAX_RADIANCE);
+    S.resolved[slot] = make_uint4(key, pack2x16float(cr, cg), f16_bits(cb) | ((hist & 0xFFu) << 16) | ((stale & 0xFFu) << 24), 0u);
+}
+
+__global__ void sharc_query_kernel(const uint4* __restrict__ res, const float* __restrict__ pos, const float* __restrict__ nrm,
+                                   const float* __restrict__ jit, uint32_t n, f3 cam, float4* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const f3 p{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]}, q{nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]};
+    const float jx = jit ? jit[2 * i] : 0.0f, jy = jit ? jit[2 * i + 1] : 0.0f;
+    out[i] = sharc_query(res, p, q, cam, jx, jy);
+}
+
+__global__ void sharc_deposit_kernel(SharcBuffers S, f3 pos, f3 n, f3 cam, f3 rad, uint32_t count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    uint32_t b, k;
+    sharc_key(pos, n, cam, 0.0f, 0.0f, &b, &k);
+    sharc_deposit(S, b, k, rad);
+}
+
+}  // namespace arc
+
+namespace {
+
+int sharc_err(arc_ctx* c, int code, const std::string& m) {
+    c->err = m;
+    return code;
+}
+
+int ensure_sharc(arc_ctx* c) {
+    if (c->d_sharc_keys) return ARC_OK;
+    cudaError_t e;
+    if ((e = cudaMalloc((void**)&c->d_sharc_keys, ARC_SHARC_SLOTS * 4u)) != cudaSuccess ||
+        (e = cudaMalloc((void**)&c->d_sharc_accum, ARC_SHARC_SLOTS * 16u)) != cudaSuccess ||
+        (e = cudaMalloc((void**)&c->d_sharc_resolved, ARC_SHARC_SLOTS * 16u)) != cudaSuccess)
+        return sharc_err(c, ARC_E_CUDA, std::string("SHARC allocation: ") + cudaGetErrorString(e));
+    cudaMemsetAsync(c->d_sharc_keys, 0, ARC_SHARC_SLOTS * 4u, c->stream);
+    cudaMemsetAsync(c->d_sharc_accum, 0, ARC_SHARC_SLOTS * 16u, c->stream);
+    cudaMemsetAsync(c->d_sharc_resolved, 0, ARC_SHARC_SLOTS * 16u, c->stream);
+    return ARC_OK;
+}
+
+arc::SharcBuffers bufs(arc_ctx* c) {
+    return arc::SharcBuffers{c->d_sharc_keys, c->d_sharc_accum, reinterpret_cast<uint4*>(c->d_sharc_resolved)};
+}
+
+int launch_check(arc_ctx* c, const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return sharc_err(c, ARC_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return ARC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int arc_sharc_reset(arc_ctx* c) {
+    if (!c) return ARC_E_INVALID_ARG;
+    int rc = ensure_sharc(c);
+    if (rc) return rc;
+    cudaMemsetAsync(c->d_sharc_keys, 0, ARC_SHARC_SLOTS * 4u, c->stream);
+    cudaMemsetAsync(c->d_sharc_accum, 0, ARC_SHARC_SLOTS * 16u, c->stream);
+    cudaMemsetAsync(c->d_sharc_resolved, 0, ARC_SHARC_SLOTS * 16u, c->stream);
+    return launch_check(c, "arc_sharc_reset");
+}
+
+int arc_sharc_update_dev(arc_ctx* c, uint32_t width, uint32_t height, const uint32_t* gdm, const uint32_t* gnm) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if (!gdm || !gnm || width == 0 || height == 0) return sharc_err(c, ARC_E_INVALID_ARG, "bad G-buffer");
+    if ((c->cam.world_grid_dims[3] & 0xFFFFu) != width || (c->cam.world_grid_dims[3] >> 16) != height)
+        return sharc_err(c, ARC_E_INVALID_ARG, "frame size differs from camera world_grid_dims.w");
+    if ((rc = ensure_sharc(c))) return rc;
+    const uint32_t tile = (c->cam.quality_flags[3] & 0xFFu) <= 12u ? 16u : 8u;
+    const uint32_t tx = (width + tile - 1u) / tile, ty = (height + tile - 1u) / tile;
+    dim3 block(8, 8), grid((tx + 7u) / 8u, (ty + 7u) / 8u);
+    arc::sharc_update_kernel<<<grid, block, 0, c->stream>>>(c->world(), c->cam, bufs(c), gdm, gnm, width, height);
+    return launch_check(c, "sharc_update_kernel");
+}
+
+int arc_sharc_resolve(arc_ctx* c) {
+    if (!c) return ARC_E_INVALID_ARG;
+    int rc = ensure_sharc(c);
+    if (rc) return rc;
+    arc::sharc_resolve_kernel<<<ARC_SHARC_SLOTS / 256u, 256, 0, c->stream>>>(bufs(c));
+    return launch_check(c, "sharc_resolve_kernel");
+}
+
+int arc_sharc_query_dev(arc_ctx* c, const float* pos, const float* normal, const float* jitter, uint32_t n, float* out) {
+    if (!c) return ARC_E_INVALID_ARG;
+    if (!c->have_cam) return sharc_err(c, ARC_E_NO_CAMERA, "no camera set");
+    if (n && (!pos || !normal || !out)) return sharc_err(c, ARC_E_INVALID_ARG, "null buffer");
+    int rc = ensure_sharc(c);
+    if (rc || n == 0) return rc;
+    const arc::f3 cam{c->cam.cam_pos_time[0], c->cam.cam_pos_time[1], c->cam.cam_pos_time[2]};
+    arc::sharc_query_kernel<<<(n + 127u) / 128u, 128, 0, c->stream>>>(reinterpret_cast<const uint4*>(c->d_sharc_resolved), pos,
+                                                                      normal, jitter, n, cam, reinterpret_cast<float4*>(out));
+    return launch_check(c, "sharc_query_kernel");
+}
+
+int arc_sharc_deposit_dev(arc_ctx* c, const float pos[3], const float normal[3], const float cam_pos[3], const float rad[3],
+                          uint32_t n_threads) {
+    if (!c || !pos || !normal || !cam_pos || !rad) return ARC_E_INVALID_ARG;
+    int rc = ensure_sharc(c);
+    if (rc || n_threads == 0) return rc;
+    arc::sharc_deposit_kernel<<<(n_threads + 63u) / 64u, 64, 0, c->stream>>>(
+        bufs(c), arc::f3{pos[0], pos[1], pos[2]}, arc::f3{normal[0], normal[1], normal[2]},
+        arc::f3{cam_pos[0], cam_pos[1], cam_pos[2]}, arc::f3{rad[0], rad[1], rad[2]}, n_threads);
+    return launch_check(c, "sharc_deposit_kernel");
+}
+
+int arc_sharc_download(arc_ctx* c, uint32_t* keys, uint32_t* accum, arc_sharc_slot* resolved) {
+    if (!c) return ARC_E_INVALID_ARG;
+    int rc = ensure_sharc(c);
+    if (rc) return rc;
+    if (keys) cudaMemcpyAsync(keys, c->d_sharc_keys, ARC_SHARC_SLOTS * 4u, cudaMemcpyDeviceToHost, c->stream);
+    if (accum) cudaMemcpyAsync(accum, c->d_sharc_accum, ARC_SHARC_SLOTS * 16u, cudaMemcpyDeviceToHost, c->stream);
+    if (resolved) cudaMemcpyAsync(resolved, c->d_sharc_resolved, ARC_SHARC_SLOTS * 16u, cudaMemcpyDeviceToHost, c->stream);
+    if ((rc = launch_check(c, "arc_sharc_download"))) return rc;
+    return arc_ctx_finish(c);
+}
+
+int arc_sharc_upload(arc_ctx* c, const uint32_t* keys, const uint32_t* accum, const arc_sharc_slot* resolved) {
+    if (!c) return ARC_E_INVALID_ARG;
+    int rc = ensure_sharc(c);
+    if (rc) return rc;
+    if (keys) cudaMemcpyAsync(c->d_sharc_keys, keys, ARC_SHARC_SLOTS * 4u, cudaMemcpyHostToDevice, c->stream);
+    if (accum) cudaMemcpyAsync(c->d_sharc_accum, accum, ARC_SHARC_SLOTS * 16u, cudaMemcpyHostToDevice, c->stream);
+    if (resolved) cudaMemcpyAsync(c->d_sharc_resolved, resolved, ARC_SHARC_SLOTS * 16u, cudaMemcpyHostToDevice, c->stream);
+    if ((rc = launch_check(c, "arc_sharc_upload"))) return rc;
+    return arc_ctx_finish(c);
+}
+
+}  // extern "C"

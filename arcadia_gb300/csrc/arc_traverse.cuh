@@ -1,0 +1,472 @@
+// arc_traverse.cuh — the hierarchical 64-tree DDA as a resumable per-lane state machine.
+//
+// trace_world_64tree_from (shaders/common/traversal64.wgsl:226-556) is split into ray_begin
+// (lines 234-300: setup, world clip, step budget) and ray_advance (one iteration of the outer loop
+// at 302-553: chunk MTF cache, empty-chunk skip, ray-cone LOD, ancestor restart, descent by
+// popcount, leaf/LOD hit). A kernel calls ray_advance until it stops returning kContinue, so a
+// persistent warp can swap a finished lane for a new ray between iterations without changing any
+// DDA decision.
+//
+// Node fetches are single 16-byte read-only loads (ld.global.nc.v4) of the AoS Node64 pool; brick
+// reads fetch the one 32-bit word that holds the voxel. Every pool index is range-checked; an
+// out-of-range index records a bit in the context's status word and reads as empty space, so a
+// corrupt pool cannot fault the device.
+//
+// One deliberate deviation from the WGSL, shared with the CPU oracle: the hit distance is
+// (enter_coord - origin) / dir on the entry axis, not enter_coord * inv_dir + (-origin * inv_dir)
+// (traversal64.wgsl:468-472), whose cancellation breaks 1e-5 relative depth far from the origin.
+// The DDA decisions and the face choice keep the WGSL form.
+#pragma once
+
+#include "arc_math.cuh"
+#include "../../include/arc/layout.h"
+
+namespace arc {
+
+constexpr uint32_t kStatusNodeRange = 1u;
+constexpr uint32_t kStatusBrickRange = 2u;
+constexpr uint32_t kStatusRootRange = 4u;
+
+struct World {
+    const uint32_t* __restrict__ roots;
+    const uint4* __restrict__ nodes;
+    const uint32_t* __restrict__ bricks;  // 16 words per brick
+    const float4* __restrict__ palette;   // 2 float4 per material
+    uint32_t n_nodes;
+    uint32_t n_bricks;
+    uint32_t n_roots;
+    uint32_t* status;
+};
+
+__device__ __forceinline__ uint4 load_node(const World& w, uint32_t idx) {
+    if (idx >= w.n_nodes) {
+        atomicOr(w.status, kStatusNodeRange);
+        return make_uint4(0u, 0u, 0u, 0u);
+    }
+    return __ldg(&w.nodes[idx]);
+}
+
+__device__ __forceinline__ uint32_t load_brick_mat(const World& w, uint32_t brick, uint32_t bit) {
+    if (brick >= w.n_bricks) {
+        atomicOr(w.status, kStatusBrickRange);
+        return 0u;
+    }
+    uint32_t word = __ldg(&w.bricks[brick * 16u + (bit >> 2)]);
+    return (word >> ((bit & 3u) * 8u)) & 0xFFu;
+}
+
+__device__ __forceinline__ uint32_t load_root(const World& w, uint32_t c_idx) {
+    if (c_idx >= w.n_roots) {
+        atomicOr(w.status, kStatusRootRange);
+        return ARC_EMPTY_CHUNK;
+    }
+    return __ldg(&w.roots[c_idx]);
+}
+
+__device__ __forceinline__ bool has_child(uint32_t lo, uint32_t hi, uint32_t b) {
+    return (((b < 32u ? lo : hi) >> (b & 31u)) & 1u) != 0u;
+}
+
+// base + popcount of the occupied children below bit b (traversal64.wgsl:32-40).
+__device__ __forceinline__ uint32_t child_index(const uint4& n, uint32_t b) {
+    uint32_t prefix = (1u << (b & 31u)) - 1u;
+    uint32_t rank = b < 32u ? __popc(n.x & prefix) : __popc(n.x) + __popc(n.y & prefix);
+    return (n.z & ARC_PTR_INDEX_MASK) + rank;
+}
+
+enum StepResult : uint32_t { kContinue = 0u, kHit = 1u, kMiss = 2u };
+
+struct RayState {
+    f3 vo;    // origin, voxel units
+    f3 dir;   // unit direction as given
+    f3 inv;   // 1 / safe_dir
+    f3 noi;   // -vo * inv
+    float t, t_limit;
+    uint32_t vx, vy, vz;
+    uint32_t px, py, pz;      // previous vi
+    uint32_t mtf_c0, mtf_c1;  // packed chunk coords (x | y << 10 | z << 20), 0xFFFFFFFF = none
+    uint32_t mtf_root0, mtf_root1;
+    uint4 l1, l2, l3;         // ancestor restart cache (levels shift 4, 2, 0)
+    uint32_t cached_shift;
+    uint32_t step, max_steps;
+    uint32_t mode;            // lod_bias | ignore_water << 2
+};
+
+struct HitInfo {
+    float t_voxels;   // accurate plane-entry distance (voxels)
+    f3 hit_pos_m;
+    f3 normal;
+    uint32_t mat;
+    uint32_t lod_payload;
+    uint32_t vx, vy, vz;
+    uint32_t shift;
+    uint32_t voxel_hash;
+    float contact_ao;
+};
+
+// Default (miss) outcome of trace_world_64tree_from (traversal64.wgsl:234-242).
+__device__ __forceinline__ void hit_init_miss(HitInfo& h, f3 origin_m, f3 dir, float max_dist_m) {
+    h.t_voxels = max_dist_m * ARC_VOXELS_PER_METER;
+    h.hit_pos_m = add3(origin_m, mul3s(dir, max_dist_m));
+    h.normal = f3{0.0f, 1.0f, 0.0f};
+    h.mat = ARC_MAT_AIR;
+    h.lod_payload = 0u;
+    h.vx = h.vy = h.vz = 0xFFFFFFFFu;
+    h.shift = 0u;
+    h.voxel_hash = 0u;
+    h.contact_ao = 1.0f;
+}
+
+__device__ __forceinline__ float safe_component(float d) { return fabsf(d) < 1e-7f ? 1e-7f : d; }
+
+// Setup of trace_world_64tree_from; returns false when the ray misses the world outright.
+__device__ __forceinline__ bool ray_begin(RayState& s, const arc_camera_uniforms& cam, f3 origin_m, f3 dir,
+                                          float start_t_m, float max_dist_m, uint32_t lod_bias, bool ignore_water) {
+    s.vo = mul3s(origin_m, ARC_VOXELS_PER_METER);
+    s.dir = dir;
+    float max_t_v = max_dist_m * ARC_VOXELS_PER_METER;
+    float start_t_v = fmaxf(start_t_m * ARC_VOXELS_PER_METER, 0.0f);
+    s.inv = f3{__fdiv_rn(1.0f, safe_component(dir.x)), __fdiv_rn(1.0f, safe_component(dir.y)),
+               __fdiv_rn(1.0f, safe_component(dir.z))};
+    const float wx = (float)cam.world_grid_dims[0] * ARC_CHUNK_DIM_F;
+    const float wy = (float)cam.world_grid_dims[1] * ARC_CHUNK_DIM_F;
+    const float wz = (float)cam.world_grid_dims[2] * ARC_CHUNK_DIM_F;
+    // intersect_aabb(vo, inv, 0, world_max) (traversal64.wgsl:134-142)
+    float ax0 = ((s.inv.x > 0.0f ? 0.0f : wx) - s.vo.x) * s.inv.x;
+    float ay0 = ((s.inv.y > 0.0f ? 0.0f : wy) - s.vo.y) * s.inv.y;
+    float az0 = ((s.inv.z > 0.0f ? 0.0f : wz) - s.vo.z) * s.inv.z;
+    float ax1 = ((s.inv.x > 0.0f ? wx : 0.0f) - s.vo.x) * s.inv.x;
+    float ay1 = ((s.inv.y > 0.0f ? wy : 0.0f) - s.vo.y) * s.inv.y;
+    float az1 = ((s.inv.z > 0.0f ? wz : 0.0f) - s.vo.z) * s.inv.z;
+    float w_enter = fmaxf(fmaxf(ax0, ay0), az0);
+    float w_exit = fminf(fminf(ax1, ay1), az1);
+    float t_enter = fmaxf(w_enter, start_t_v);
+    if (w_exit < t_enter || t_enter >= max_t_v) return false;
+    s.t = t_enter;
+    s.t_limit = fminf(w_exit, max_t_v);
+    s.max_steps = lod_bias == 0u ? cam.ray_steps[0] : (lod_bias == 1u ? cam.ray_steps[1] : cam.ray_steps[2]);
+    s.noi = f3{-s.vo.x * s.inv.x, -s.vo.y * s.inv.y, -s.vo.z * s.inv.z};
+    float st = s.t + 1e-4f;
+    s.vx = f2u(clampf(s.vo.x + dir.x * st, 0.0f, wx - 1e-3f));
+    s.vy = f2u(clampf(s.vo.y + dir.y * st, 0.0f, wy - 1e-3f));
+    s.vz = f2u(clampf(s.vo.z + dir.z * st, 0.0f, wz - 1e-3f));
+    s.px = s.py = s.pz = 0xFFFFFFFFu;
+    s.mtf_c0 = s.mtf_c1 = 0xFFFFFFFFu;
+    s.mtf_root0 = s.mtf_root1 = ARC_EMPTY_CHUNK;
+    s.l1 = s.l2 = s.l3 = make_uint4(0u, 0u, 0u, 0u);
+    s.cached_shift = 6u;
+    s.step = 0u;
+    s.mode = lod_bias | (ignore_water ? 4u : 0u);
+    return true;
+}
+
+// step_dda_box (traversal64.wgsl:152-179) over the box [bmin, bmin + span)^3.
+__device__ __forceinline__ void step_box(RayState& s, uint32_t bx, uint32_t by, uint32_t bz, uint32_t span) {
+    const bool pxd = s.inv.x >= 0.0f, pyd = s.inv.y >= 0.0f, pzd = s.inv.z >= 0.0f;
+    uint32_t ex = pxd ? bx + span : bx, ey = pyd ? by + span : by, ez = pzd ? bz + span : bz;
+    float tx = (float)ex * s.inv.x + s.noi.x;
+    float ty = (float)ey * s.inv.y + s.noi.y;
+    float tz = (float)ez * s.inv.z + s.noi.z;
+    float t_exit = fminf(fminf(tx, ty), tz);
+    float next_t = fmaxf(s.t, t_exit);
+    bool is_x = tx <= ty && tx <= tz;
+    bool is_y = !is_x && (ty <= tz);
+    bool is_z = !is_x && !is_y;
+    uint32_t ox = ex - (pxd ? 0u : 1u), oy = ey - (pyd ? 0u : 1u), oz = ez - (pzd ? 0u : 1u);
+    uint32_t ix = uclamp(f2u(fmaxf(s.vo.x + s.dir.x * next_t, 0.0f)), bx, bx + span - 1u);
+    uint32_t iy = uclamp(f2u(fmaxf(s.vo.y + s.dir.y * next_t, 0.0f)), by, by + span - 1u);
+    uint32_t iz = uclamp(f2u(fmaxf(s.vo.z + s.dir.z * next_t, 0.0f)), bz, bz + span - 1u);
+    s.t = next_t;
+    s.vx = is_x ? ox : ix;
+    s.vy = is_y ? oy : iy;
+    s.vz = is_z ? oz : iz;
+}
+
+// eval_leaf_bitwise_ao (traversal64.wgsl:60-131).
+__device__ __forceinline__ float leaf_ao(uint32_t lo, uint32_t hi, uint32_t cx, uint32_t cy, uint32_t cz, f3 n, f3 hp) {
+    float fx = clampf(fractf(hp.x), 0.0f, 1.0f);
+    float fy = clampf(fractf(hp.y), 0.0f, 1.0f);
+    float fz = clampf(fractf(hp.z), 0.0f, 1.0f);
+    int nx = (int)cx + (int)n.x, ny = (int)cy + (int)n.y, nz = (int)cz + (int)n.z;
+    if (nx < 0 || nx > 3 || ny < 0 || ny > 3 || nz < 0 || nz > 3) return 1.0f;
+    uint32_t bb = ((uint32_t)nz << 4) | ((uint32_t)ny << 2) | (uint32_t)nx;
+    float occ = 0.0f;
+    if (fabsf(n.y) > 0.5f) {
+        if (nx > 0 && has_child(lo, hi, bb - 1u)) occ += (1.0f - fx) * 0.42f;
+        if (nx < 3 && has_child(lo, hi, bb + 1u)) occ += fx * 0.42f;
+        if (nz > 0 && has_child(lo, hi, bb - 16u)) occ += (1.0f - fz) * 0.42f;
+        if (nz < 3 && has_child(lo, hi, bb + 16u)) occ += fz * 0.42f;
+    } else if (fabsf(n.x) > 0.5f) {
+        if (ny > 0 && has_child(lo, hi, bb - 4u)) occ += (1.0f - fy) * 0.42f;
+        if (ny < 3 && has_child(lo, hi, bb + 4u)) occ += fy * 0.42f;
+        if (nz > 0 && has_child(lo, hi, bb - 16u)) occ += (1.0f - fz) * 0.42f;
+        if (nz < 3 && has_child(lo, hi, bb + 16u)) occ += fz * 0.42f;
+    } else {
+        if (nx > 0 && has_child(lo, hi, bb - 1u)) occ += (1.0f - fx) * 0.42f;
+        if (nx < 3 && has_child(lo, hi, bb + 1u)) occ += fx * 0.42f;
+        if (ny > 0 && has_child(lo, hi, bb - 4u)) occ += (1.0f - fy) * 0.42f;
+        if (ny < 3 && has_child(lo, hi, bb + 4u)) occ += fy * 0.42f;
+    }
+    return clampf(1.0f - occ, 0.35f, 1.0f);
+}
+
+// One outer-loop iteration of trace_world_64tree_from (traversal64.wgsl:302-553).
+__device__ __forceinline__ StepResult ray_advance(RayState& s, const World& w, const arc_camera_uniforms& cam,
+                                                  HitInfo& h) {
+    if (s.step >= s.max_steps) return kMiss;
+    if (s.t >= s.t_limit) return kMiss;
+    const uint32_t gx = cam.world_grid_dims[0], gy = cam.world_grid_dims[1], gz = cam.world_grid_dims[2];
+    if (s.vx >= (gx << 8) || s.vy >= (gy << 8) || s.vz >= (gz << 8)) return kMiss;
+
+    const uint32_t diff = (s.px ^ s.vx) | (s.py ^ s.vy) | (s.pz ^ s.vz);
+    s.px = s.vx;
+    s.py = s.vy;
+    s.pz = s.vz;
+    uint32_t root_idx = s.mtf_root0;
+    if (diff >= 256u) {
+        const uint32_t cxk = s.vx >> 8, cyk = s.vy >> 8, czk = s.vz >> 8;
+        const uint32_t c = cxk | (cyk << 10) | (czk << 20);
+        s.cached_shift = 6u;
+        if (c == s.mtf_c1) {
+            root_idx = s.mtf_root1;
+        } else {
+            root_idx = load_root(w, cxk + cyk * gx + czk * gx * gy);
+        }
+        s.mtf_c1 = s.mtf_c0;
+        s.mtf_root1 = s.mtf_root0;
+        s.mtf_c0 = c;
+        s.mtf_root0 = root_idx;
+    }
+    if (root_idx == ARC_EMPTY_CHUNK) {
+        step_box(s, s.vx & ~255u, s.vy & ~255u, s.vz & ~255u, 256u);
+        s.step++;
+        return kContinue;
+    }
+
+    const uint32_t lod_bias = s.mode & 3u;
+    const bool ignore_water = (s.mode & 4u) != 0u;
+    uint32_t min_shift = 0u;
+    if (lod_bias == 0u) {
+        if (s.t > cam.lod_settings[0] * ARC_VOXELS_PER_METER || s.step > cam.quality_flags[0]) min_shift = 2u;
+    } else if (lod_bias == 1u) {
+        const float sec_t = cam.lod_settings[1] * ARC_VOXELS_PER_METER;
+        if (s.t > sec_t * 2.2857f || s.step > cam.quality_flags[1]) min_shift = 4u;
+        else if (s.t > sec_t) min_shift = 2u;
+    } else {
+        if (s.t > cam.lod_settings[2] * ARC_VOXELS_PER_METER || s.step > ((cam.quality_flags[3] >> 16) & 0xFFu)) min_shift = 2u;
+    }
+
+    uint4 node;
+    uint32_t shift;
+    if (diff < 4u && min_shift == 0u && s.cached_shift == 0u) {
+        node = s.l3;
+        shift = 0u;
+    } else if (diff < 16u && min_shift <= 2u && s.cached_shift <= 2u) {
+        node = s.l2;
+        shift = 2u;
+    } else if (diff < 64u && min_shift <= 4u && s.cached_shift <= 4u) {
+        node = s.l1;
+        shift = 4u;
+    } else {
+        node = load_node(w, root_idx);
+        shift = 6u;
+    }
+    s.cached_shift = shift;
+
+    const uint32_t lx = s.vx & 255u, ly = s.vy & 255u, lz = s.vz & 255u;
+    for (;;) {
+        const uint32_t cx = (lx >> shift) & 3u, cy = (ly >> shift) & 3u, cz = (lz >> shift) & 3u;
+        const uint32_t b = (cz << 4) | (cy << 2) | cx;
+        if (ignore_water && (node.z & ARC_IS_UNIFORM_FLAG) != 0u && ((node.w >> 24) & 0xFFu) == ARC_MAT_WATER_CRYSTAL) {
+            const uint32_t span = 4u << shift;
+            step_box(s, s.vx & ~(span - 1u), s.vy & ~(span - 1u), s.vz & ~(span - 1u), span);
+            break;
+        }
+        const uint32_t span = 1u << shift;
+        const uint32_t bx = s.vx & ~(span - 1u), by = s.vy & ~(span - 1u), bz = s.vz & ~(span - 1u);
+        if (!has_child(node.x, node.y, b)) {
+            step_box(s, bx, by, bz, span);
+            break;
+        }
+        const bool is_leaf = (node.z & ARC_IS_LEAF_FLAG) != 0u;
+        if (is_leaf || shift <= min_shift) {
+            uint32_t mat = (node.w >> 24) & 0xFFu;
+            if (is_leaf && (node.z & ARC_IS_UNIFORM_FLAG) == 0u) mat = load_brick_mat(w, node.z & ARC_PTR_INDEX_MASK, b);
+            if (ignore_water && mat == ARC_MAT_WATER_CRYSTAL) {
+                step_box(s, bx, by, bz, span);
+                break;
+            }
+            if (mat != ARC_MAT_AIR) {
+                const bool pxd = s.inv.x >= 0.0f, pyd = s.inv.y >= 0.0f, pzd = s.inv.z >= 0.0f;
+                const uint32_t ex = pxd ? bx : bx + span, ey = pyd ? by : by + span, ez = pzd ? bz : bz + span;
+                const float tx = (float)ex * s.inv.x + s.noi.x;
+                const float ty = (float)ey * s.inv.y + s.noi.y;
+                const float tz = (float)ez * s.inv.z + s.noi.z;
+                const float max_t = fmaxf(fmaxf(tx, ty), tz);
+                // accurate entry distance on the entry axis (ties: x, then y)
+                float t_acc;
+                if (tx >= ty && tx >= tz) t_acc = __fdiv_rn((float)ex - s.vo.x, safe_component(s.dir.x));
+                else if (ty >= tz) t_acc = __fdiv_rn((float)ey - s.vo.y, safe_component(s.dir.y));
+                else t_acc = __fdiv_rn((float)ez - s.vo.z, safe_component(s.dir.z));
+                const float exact_t = fmaxf(t_acc, 0.0f);
+                const f3 hp = add3(s.vo, mul3s(s.dir, exact_t));
+                h.t_voxels = exact_t;
+                h.hit_pos_m = mul3s(hp, ARC_VOXEL_SIZE);
+                const float eps = 1e-4f * fmaxf(max_t * 0.01f, 1.0f);
+                const float cand_x = fabsf(tx - max_t) <= eps ? fabsf(s.dir.x) : 0.0f;
+                const float cand_y = fabsf(ty - max_t) <= eps ? fabsf(s.dir.y) : 0.0f;
+                const float cand_z = fabsf(tz - max_t) <= eps ? fabsf(s.dir.z) : 0.0f;
+                f3 n{0.0f, 0.0f, 0.0f};
+                if (cand_x >= cand_y && cand_x >= cand_z && cand_x > 0.0f) n.x = -signf(s.dir.x);
+                else if (cand_y >= cand_z && cand_y > 0.0f) n.y = -signf(s.dir.y);
+                else if (cand_z > 0.0f) n.z = -signf(s.dir.z);
+                else if (tx >= ty && tx >= tz) n.x = -signf(s.dir.x);
+                else if (ty >= tz) n.y = -signf(s.dir.y);
+                else n.z = -signf(s.dir.z);
+                h.normal = n;
+                h.mat = mat;
+                h.lod_payload = node.w;
+                h.vx = s.vx;
+                h.vy = s.vy;
+                h.vz = s.vz;
+                h.shift = shift;
+                h.voxel_hash = pcg_hash((s.vx * 73856093u) ^ (s.vy * 19349663u) ^ (s.vz * 83492791u));
+                h.contact_ao = 1.0f;
+                if (shift == 0u && lod_bias == 0u) {
+                    const float hit_dist_m = s.t * ARC_VOXEL_SIZE;
+                    const float raw = __uint_as_float(cam.point_light_count[3]);
+                    const float ao_max = raw < 1.0f ? 24.0f : raw;
+                    if (hit_dist_m < ao_max) {
+                        const float raw_ao = leaf_ao(node.x, node.y, cx, cy, cz, n, hp);
+                        const float wgt = 1.0f - smoothstepf(ao_max * 0.5f, ao_max, hit_dist_m);
+                        h.contact_ao = mixf(1.0f, raw_ao, wgt);
+                    }
+                }
+                return kHit;
+            }
+            step_box(s, bx, by, bz, span);
+            break;
+        }
+        node = load_node(w, child_index(node, b));
+        shift -= 2u;
+        s.cached_shift = shift;
+        if (shift == 4u) s.l1 = node;
+        else if (shift == 2u) s.l2 = node;
+        else if (shift == 0u) s.l3 = node;
+    }
+    s.step++;
+    return kContinue;
+}
+
+// trace_shadow_vis (traversal64.wgsl:571-773): 1.0 unoccluded, 0.0 occluded.
+__device__ __forceinline__ float shadow_vis(const World& w, const arc_camera_uniforms& cam, f3 origin_m, f3 dir,
+                                            float max_dist_m) {
+    const f3 vo = mul3s(origin_m, ARC_VOXELS_PER_METER);
+    const float max_t_v = max_dist_m * ARC_VOXELS_PER_METER;
+    RayState s;
+    s.vo = vo;
+    s.dir = dir;
+    s.inv = f3{__fdiv_rn(1.0f, safe_component(dir.x)), __fdiv_rn(1.0f, safe_component(dir.y)),
+               __fdiv_rn(1.0f, safe_component(dir.z))};
+    const uint32_t gx = cam.world_grid_dims[0], gy = cam.world_grid_dims[1], gz = cam.world_grid_dims[2];
+    const float wx = (float)gx * ARC_CHUNK_DIM_F, wy = (float)gy * ARC_CHUNK_DIM_F, wz = (float)gz * ARC_CHUNK_DIM_F;
+    float ax0 = ((s.inv.x > 0.0f ? 0.0f : wx) - vo.x) * s.inv.x;
+    float ay0 = ((s.inv.y > 0.0f ? 0.0f : wy) - vo.y) * s.inv.y;
+    float az0 = ((s.inv.z > 0.0f ? 0.0f : wz) - vo.z) * s.inv.z;
+    float ax1 = ((s.inv.x > 0.0f ? wx : 0.0f) - vo.x) * s.inv.x;
+    float ay1 = ((s.inv.y > 0.0f ? wy : 0.0f) - vo.y) * s.inv.y;
+    float az1 = ((s.inv.z > 0.0f ? wz : 0.0f) - vo.z) * s.inv.z;
+    float w_enter = fmaxf(fmaxf(ax0, ay0), az0);
+    float w_exit = fminf(fminf(ax1, ay1), az1);
+    if (w_exit < fmaxf(w_enter, 0.0f) || w_enter >= max_t_v) return 1.0f;
+    s.t = fmaxf(w_enter, 0.0f);
+    s.t_limit = fminf(w_exit, max_t_v);
+    const uint32_t max_steps = cam.ray_steps[3];
+    s.noi = f3{-vo.x * s.inv.x, -vo.y * s.inv.y, -vo.z * s.inv.z};
+    float st = s.t + 1e-4f;
+    s.vx = f2u(clampf(vo.x + dir.x * st, 0.0f, wx - 1e-3f));
+    s.vy = f2u(clampf(vo.y + dir.y * st, 0.0f, wy - 1e-3f));
+    s.vz = f2u(clampf(vo.z + dir.z * st, 0.0f, wz - 1e-3f));
+    uint32_t px = 0xFFFFFFFFu, py = 0xFFFFFFFFu, pz = 0xFFFFFFFFu;
+    uint32_t cached_shift = 6u;
+    uint4 l1 = make_uint4(0, 0, 0, 0), l2 = l1, l3 = l1;
+    uint32_t cached_root = ARC_EMPTY_CHUNK;
+    for (uint32_t step = 0; step < max_steps; ++step) {
+        if (s.t >= s.t_limit) break;
+        if (s.vx >= (gx << 8) || s.vy >= (gy << 8) || s.vz >= (gz << 8)) {
+            s.t = s.t_limit;
+            break;
+        }
+        const uint32_t diff = (px ^ s.vx) | (py ^ s.vy) | (pz ^ s.vz);
+        px = s.vx;
+        py = s.vy;
+        pz = s.vz;
+        uint32_t root_idx = cached_root;
+        if (diff >= 256u) {
+            cached_shift = 6u;
+            root_idx = load_root(w, (s.vx >> 8) + (s.vy >> 8) * gx + (s.vz >> 8) * gx * gy);
+            cached_root = root_idx;
+        }
+        if (root_idx == ARC_EMPTY_CHUNK) {
+            step_box(s, s.vx & ~255u, s.vy & ~255u, s.vz & ~255u, 256u);
+            continue;
+        }
+        uint32_t min_shift = 0u;
+        if (s.t > 48.0f || step > 6u) min_shift = 2u;
+        if (s.t > 192.0f || step > 16u) min_shift = 4u;
+        uint4 node;
+        uint32_t shift;
+        if (diff < 4u && min_shift == 0u && cached_shift == 0u) { node = l3; shift = 0u; }
+        else if (diff < 16u && min_shift <= 2u && cached_shift <= 2u) { node = l2; shift = 2u; }
+        else if (diff < 64u && min_shift <= 4u && cached_shift <= 4u) { node = l1; shift = 4u; }
+        else { node = load_node(w, root_idx); shift = 6u; }
+        cached_shift = shift;
+        const uint32_t lx = s.vx & 255u, ly = s.vy & 255u, lz = s.vz & 255u;
+        for (;;) {
+            const uint32_t b = (((lz >> shift) & 3u) << 4) | (((ly >> shift) & 3u) << 2) | ((lx >> shift) & 3u);
+            if ((node.z & ARC_IS_UNIFORM_FLAG) != 0u && ((node.w >> 24) & 0xFFu) == ARC_MAT_WATER_CRYSTAL) {
+                const uint32_t span = 4u << shift;
+                step_box(s, s.vx & ~(span - 1u), s.vy & ~(span - 1u), s.vz & ~(span - 1u), span);
+                break;
+            }
+            const uint32_t span = 1u << shift;
+            const uint32_t bx = s.vx & ~(span - 1u), by = s.vy & ~(span - 1u), bz = s.vz & ~(span - 1u);
+            if (!has_child(node.x, node.y, b)) {
+                step_box(s, bx, by, bz, span);
+                break;
+            }
+            if ((node.z & ARC_IS_LEAF_FLAG) != 0u || shift <= min_shift) {
+                if (((node.w >> 24) & 0xFFu) == ARC_MAT_WATER_CRYSTAL) {
+                    step_box(s, bx, by, bz, span);
+                    break;
+                }
+                return 0.0f;
+            }
+            node = load_node(w, child_index(node, b));
+            shift -= 2u;
+            cached_shift = shift;
+            if (shift == 4u) l1 = node;
+            else if (shift == 2u) l2 = node;
+            else if (shift == 0u) l3 = node;
+        }
+    }
+    if (s.t < s.t_limit) {
+        if ((vo.y + dir.y * s.t) * ARC_VOXEL_SIZE < 32.0f) return 0.0f;
+    }
+    return 1.0f;
+}
+
+// Pinhole camera ray (primary_gbuffer.wgsl:103-115, reconstruct_ray_dir types.wgsl:334-345).
+__device__ __forceinline__ f3 camera_dir(const arc_camera_uniforms& cam, uint32_t x, uint32_t y, uint32_t W, uint32_t H) {
+    const float u = __fdiv_rn(((float)x + 0.5f) + cam.jitter_brush_dt[0], (float)W);
+    const float v = __fdiv_rn(((float)y + 0.5f) + cam.jitter_brush_dt[1], (float)H);
+    const float nx = u * 2.0f - 1.0f, ny = 1.0f - v * 2.0f;
+    const float th = cam.cam_forward_fov[3];
+    const float sx = (nx * cam.cam_right_aspect[3]) * th, sy = ny * th;
+    f3 r{(cam.cam_forward_fov[0] + cam.cam_right_aspect[0] * sx) + cam.cam_up_frame[0] * sy,
+         (cam.cam_forward_fov[1] + cam.cam_right_aspect[1] * sx) + cam.cam_up_frame[1] * sy,
+         (cam.cam_forward_fov[2] + cam.cam_right_aspect[2] * sx) + cam.cam_up_frame[2] * sy};
+    return normalize3(r);
+}
+
+}  // namespace arc

@@ -1,0 +1,353 @@
+#!/usr/bin/env python
+"""Throughput of the 64-tree DDA traversal (primary G-buffer + 1 GI ray per hit pixel) on GB300.
+
+Workload (the 1024^3 config): seeded heightfield + 3D value-noise caves, 4x4x4 chunks of 256^3 (a
+5-level 64-tree world), 1920x1080 pinhole primary rays (FOV 70, 30 degrees down) plus one cosine-
+weighted GI ray per hit pixel (Pass-2A sampling), up to 512 DDA steps per ray, LOD pushed out of
+reach. A step is one frame. Prints one JSON line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value     Mrays/s with pools and outputs resident in HBM, frame kernel timed with CUDA events on the
+          library's stream, L2 flushed (256 MiB write) before every timed frame.
+e2e       the same metric through the C ABI with host buffers (arc_trace_frame: launch + D2H of the
+          G-buffer and both hit arrays every frame), wall-clock.
+reference the reference's CPU ray query (WorldMap::raycast_meters -> raycast_chunk_tree, restated in
+          C in oracle/) on all host cores, full frames.
+Multi-GPU: replicas only (each rank traces its own frame); value = all ranks' rays / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mrays/s on 1 GB300 (primary+GI)"
+UNIT = "Mrays/s"
+SCENE = "c2_1024_caves"
+WIDTH, HEIGHT = 1920, 1080
+WORKLOAD = ("1024^3 caves world (4^3 chunks, 5-level 64-tree), 1920x1080 primary + 1 cosine GI ray per hit "
+            "pixel, <=512 DDA steps per ray")
+
+
+def _args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=100)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--variant", type=int, default=1, help="0 plain kernel, 1 persistent kernel")
+    return p.parse_args()
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _camera(scene, frame):
+    from arcadia_gb300 import layout as L
+
+    return L.default_camera_for(scene, WIDTH, HEIGHT, quality=L.quality_parity(512), frame_index=frame)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while the GPU works."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(device)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.strip() == "Active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)["hbm_gbs"], "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def _profile_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from a committed ncu summary (profiles/*.txt), if any."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for fn in sorted(os.listdir(d)):
+        if not fn.endswith(".txt"):
+            continue
+        txt = open(os.path.join(d, fn)).read()
+        if f"kernel={kernel}" in txt and f"workload={SCENE}" in txt:
+            for line in txt.splitlines():
+                if line.startswith("dram_bytes_per_launch="):
+                    return float(line.split("=", 1)[1])
+    return None
+
+
+def cpu_leg(scene_name, seconds, threads, reference_query=True, frame=0):
+    """Times the CPU restatement on whole frames (pixel stride 1) until `seconds` of work are done."""
+    from arcadia_gb300 import layout as L
+    from oracle import pyorc
+
+    scene = L.SCENES[scene_name]
+    world = pyorc.build_world(scene)
+    cam = _camera(scene, frame)
+    pyorc.frame_sample(world, cam, 64, threads, cpu_query=reference_query)  # warm-up
+    rays = frames = 0
+    t0 = time.perf_counter()
+    while True:
+        r = pyorc.frame_sample(world, cam, 1, threads, cpu_query=reference_query)
+        rays += r[0]
+        frames += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return rays / dt / 1e6, frames, dt, world, cam
+
+
+def bytes_per_pixel(world, cam, threads):
+    """Algorithmic bytes per pixel path (primary + GI) from the instrumented oracle (every 16th pixel)."""
+    from oracle import pyorc
+
+    r = pyorc.frame_sample(world, cam, 16, threads, cpu_query=False)
+    return r[4] / r[1]
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    from arcadia_gb300 import layout as L
+    from oracle import pyorc
+
+    scene = L.SCENES[SCENE]
+    world = pyorc.build_world(scene)
+    for i in range(args.warmup):
+        pyorc.frame_sample(world, _camera(scene, i), 1, threads, cpu_query=True)
+    rays = 0
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        rays += pyorc.frame_sample(world, _camera(scene, args.warmup + i), 1, threads, cpu_query=True)[0]
+    dt = time.perf_counter() - t0
+    v = rays / dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "scene": SCENE, "width": WIDTH, "height": HEIGHT, "parallelism": "host cores"},
+        "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full frames ({WIDTH}x{HEIGHT} primary + GI) through the C restatement "
+                                   "of WorldMap::raycast_meters -> raycast_chunk_tree"},
+        "e2e": {"value": round(v, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    from arcadia_gb300 import build as nbuild
+    from arcadia_gb300 import layout as L
+    from arcadia_gb300 import native
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    nbuild.build()
+    scene = L.SCENES[SCENE]
+    roots, nodes, bricks, _ = native.build_world(scene)
+    pal = native.default_palette()
+    t = native.Tracer(local)
+    t.upload_world(scene.grid, roots, nodes, bricks, pal)
+    t.set_launch_config(variant=args.variant)
+    stream = torch.cuda.ExternalStream(t.stream(), device=torch.device("cuda", local))
+    npx = WIDTH * HEIGHT
+    dev = torch.device("cuda", local)
+    gdm = torch.empty(npx * 2, dtype=torch.int32, device=dev)
+    gnm = torch.empty(npx * 2, dtype=torch.int32, device=dev)
+    gaa = torch.empty(npx, dtype=torch.int32, device=dev)
+    hits = torch.empty(npx * 5, dtype=torch.int32, device=dev)
+    gi = torch.empty(npx * 5, dtype=torch.int32, device=dev)
+    n_gi = torch.zeros(max(args.steps, 1), dtype=torch.int64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def frame(i, slot):
+        t.set_camera(_camera(scene, i))
+        t.trace_frame_dev(WIDTH, HEIGHT, gdm.data_ptr(), gnm.data_ptr(), gaa.data_ptr(), hits.data_ptr(), gi.data_ptr(),
+                          n_gi.data_ptr() + 8 * slot)
+
+    clocks = ClockSampler(local)
+    for i in range(args.warmup):
+        frame(i, 0)
+    t.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            starts[i].record(stream)
+            frame(args.warmup + i, i)
+            ends[i].record(stream)
+    t.synchronize()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(ms)
+    rays = args.steps * npx + int(n_gi.sum().item())
+    if ws > 1:
+        tt = torch.tensor([total_ms, float(rays)], dtype=torch.float64, device=dev)
+        mx = tt.clone()
+        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.SUM)
+        total_ms, rays = float(mx[0]), float(tt[1])
+    value = rays / (total_ms * 1e-3) / 1e6
+
+    # plain one-thread-per-pixel kernel, same frames (the "vs plain kernel" comparison)
+    t.set_launch_config(variant=0)
+    plain_ms = []
+    np_frames = min(args.steps, 20)
+    with torch.cuda.stream(stream):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(np_frames)]
+        for i in range(np_frames):
+            flush.fill_(i & 0xFF)
+            ev[i][0].record(stream)
+            frame(args.warmup + i, i)
+            ev[i][1].record(stream)
+    t.synchronize()
+    plain_ms = [a.elapsed_time(b) for a, b in ev]
+    plain_rays = np_frames * npx + int(n_gi[:np_frames].sum().item())
+    plain_value = plain_rays / (sum(plain_ms) * 1e-3) / 1e6
+    t.set_launch_config(variant=args.variant)
+
+    # end to end through the C ABI with host (pinned) buffers
+    pin = {k: torch.empty(n, dtype=torch.int32).pin_memory().numpy() for k, n in
+           (("gdm", npx * 2), ("gnm", npx * 2), ("gaa", npx), ("hits", npx * 5), ("gi", npx * 5))}
+    from arcadia_gb300.native import _p, lib
+    import ctypes
+
+    e2e_frames = min(args.steps, 20)
+    cnt = ctypes.c_uint64()
+    e2e_rays = 0
+    for i in range(2):
+        t.set_camera(_camera(scene, i))
+        lib().arc_trace_frame(t.ctx, WIDTH, HEIGHT, _p(pin["gdm"]), _p(pin["gnm"]), _p(pin["gaa"]), _p(pin["hits"]),
+                              _p(pin["gi"]), ctypes.byref(cnt))
+    t0 = time.perf_counter()
+    for i in range(e2e_frames):
+        t.set_camera(_camera(scene, args.warmup + i))
+        rc = lib().arc_trace_frame(t.ctx, WIDTH, HEIGHT, _p(pin["gdm"]), _p(pin["gnm"]), _p(pin["gaa"]), _p(pin["hits"]),
+                                   _p(pin["gi"]), ctypes.byref(cnt))
+        if rc:
+            raise native.ArcError(rc, t.last_error())
+        e2e_rays += npx + cnt.value
+    e2e_dt = time.perf_counter() - t0
+    clk = clocks.stop()
+    e2e_value = e2e_rays / e2e_dt / 1e6
+    cfg = t.launch_config()
+    t.close()
+
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    cpu = None
+    bpp = None
+    if not args.no_cpu_baseline:
+        v, frames, dt, world, cam = cpu_leg(SCENE, args.cpu_seconds, threads, reference_query=True, frame=args.warmup)
+        cpu = {"value": round(v, 3), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{frames} full frame(s) ({WIDTH}x{HEIGHT} primary + GI) in {dt:.1f} s through the C "
+                         "restatement of WorldMap::raycast_meters -> raycast_chunk_tree"}
+        bpp = bytes_per_pixel(world, cam, threads)
+    peak, peak_kind = _peaks()
+    avg_ms = total_ms / args.steps if ws == 1 else statistics.mean(ms)
+    roofline = None
+    if bpp is not None:
+        achieved = bpp * npx / (statistics.mean(ms) * 1e-3) / 1e9
+        traffic = _profile_traffic("frame_persistent_kernel" if args.variant == 1 else "frame_plain_kernel")
+        roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                    "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
+                    "algorithmic_bytes_per_pixel": round(bpp, 2)}
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(avg_ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic (seeded heightfield + caves)",
+        "config": {"workload": WORKLOAD, "scene": SCENE, "width": WIDTH, "height": HEIGHT,
+                   "parallelism": f"replicas x{ws}", "l2": "flushed before every timed frame (256 MiB write)",
+                   "kernel": "persistent" if cfg.variant == 1 else "plain",
+                   "launch": {"block_threads": cfg.block_threads, "blocks_per_sm": cfg.blocks_per_sm,
+                              "tile": [cfg.tile_w, cfg.tile_h], "refill_threshold": cfg.refill_threshold}},
+        "plain_kernel": {"value": round(plain_value, 3), "unit": UNIT, "ms_per_step": round(statistics.mean(plain_ms), 4)},
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": 480,
+                "d2h_bytes_per_step": npx * 60 + 8 + 16},
+        "gpu_launches": args.steps,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = _args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,136 @@
+/*
+ * arc/arc_trace.h — C ABI of the GB300 64-tree traversal library (libarc_trace.so).
+ *
+ * The library stands in for three WGSL compute passes of Arcadia's renderer and the pool uploads
+ * that feed them. Each entry point names the reference interface it replaces:
+ *
+ *   arc_upload_world     Group0 pool upload: create_group0_resources
+ *                        (crates/arcadia-render/src/gpu_pools.rs:124-261) of the WorldMap pools
+ *                        (crates/arcadia-world/src/world_map.rs:37-42, 158-205)
+ *   arc_apply_patch      Renderer::apply_world_patches (crates/arcadia-render/src/renderer.rs:147-315)
+ *                        of one GpuPatch (crates/arcadia-world/src/world_map.rs:20-27)
+ *   arc_set_camera       queue.write_buffer of CameraUniforms (renderer.rs:362-366)
+ *   arc_trace_primary    record_primary_raymarch_pass (crates/arcadia-render/src/pipeline.rs:150-166)
+ *                        -> primary_raymarch (shaders/primary_gbuffer.wgsl:93-312)
+ *   arc_trace_secondary  the Pass-2A GI secondary ray (shaders/lighting_restir_gi.wgsl:195-209)
+ *   arc_trace_frame      primary + GI secondary in one persistent launch (no reference counterpart:
+ *                        the fusion of the two passes above)
+ *   arc_trace_rays       trace_world_64tree (shaders/common/traversal64.wgsl:559-567) on a ray batch
+ *   arc_sharc_update     record_sharc_update_pass (crates/arcadia-render/src/sharc.rs:225-241)
+ *                        -> sharc_update.wgsl main (shaders/sharc_update.wgsl:148-191)
+ *   arc_sharc_resolve    record_sharc_resolve_pass (sharc.rs:244-256) -> sharc_resolve.wgsl:13-70
+ *   arc_sharc_query      query_sharc (shaders/common/sharc_query.wgsl:138-146) on a batch
+ *
+ * Conventions: library-owned device memory lives behind an opaque arc_ctx; caller-owned host
+ * memory is copied in and out inside the call (the *_dev variants take device pointers and
+ * copy nothing). Every function returns an int status, 0 = ARC_OK, negative = ARC_E_*; no C++
+ * exception crosses the ABI. One CUDA stream per context. A context is thread-compatible, not
+ * thread-safe: calls on one context must not overlap.
+ */
+#ifndef ARC_TRACE_H
+#define ARC_TRACE_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include "layout.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ARC_OK 0
+#define ARC_E_INVALID_ARG -1
+#define ARC_E_CUDA -2
+#define ARC_E_NO_WORLD -3
+#define ARC_E_INVALID_POOL -4
+#define ARC_E_OUT_OF_MEMORY -5
+#define ARC_E_DEVICE_CHECK -6 /* a device-side range check found an index outside the pools */
+#define ARC_E_NO_CAMERA -7
+#define ARC_E_CAPACITY -8
+
+typedef struct arc_ctx arc_ctx;
+
+/* Scheduling of the traversal kernels. variant 0 = one thread per pixel/ray on a 2D grid;
+ * variant 1 = persistent warps that refill idle lanes from a global ray queue. */
+typedef struct arc_launch_config {
+    uint32_t variant;
+    uint32_t block_threads;    /* threads per CTA (multiple of 32) */
+    uint32_t blocks_per_sm;    /* persistent variant: resident CTAs per SM (0 = occupancy maximum) */
+    uint32_t tile_w, tile_h;   /* pixel tile a warp's 32 consecutive queue entries cover (tile_w*tile_h = 32) */
+    uint32_t refill_threshold; /* persistent variant: refill when at least this many lanes are idle */
+} arc_launch_config;
+
+typedef struct arc_stats {
+    float last_kernel_ms;      /* device time of the last traversal launch (CUDA events) */
+    uint64_t rays_traced;      /* primary + secondary rays of the last launch */
+    uint32_t device_status;    /* bit mask of device-side range check failures */
+    uint32_t n_sm;
+} arc_stats;
+
+int arc_create(int device, arc_ctx** out);
+int arc_destroy(arc_ctx* ctx);
+int arc_last_error(const arc_ctx* ctx, char* buf, size_t n);
+int arc_synchronize(arc_ctx* ctx);
+/* cudaStream_t of the context, for callers that order their own work after it */
+int arc_get_stream(arc_ctx* ctx, void** stream);
+int arc_set_launch_config(arc_ctx* ctx, const arc_launch_config* cfg);
+int arc_get_launch_config(const arc_ctx* ctx, arc_launch_config* cfg);
+int arc_get_stats(const arc_ctx* ctx, arc_stats* out);
+
+/* Pools as WorldMap packs them. The pools are validated (every child pointer, brick index and root
+ * in range) before upload; node/brick capacity reserves headroom for patches. */
+int arc_upload_world(arc_ctx* ctx, const uint32_t grid[3], const uint32_t* roots, uint32_t n_roots,
+                     const arc_node64* nodes, uint32_t n_nodes, const arc_brick64* bricks, uint32_t n_bricks,
+                     const arc_material* palette, uint32_t node_headroom, uint32_t brick_headroom);
+int arc_apply_patch(arc_ctx* ctx, uint32_t chunk_flat_idx, uint32_t new_root_node_idx, uint32_t node_offset,
+                    const arc_node64* nodes, uint32_t n_nodes, uint32_t brick_offset, const arc_brick64* bricks,
+                    uint32_t n_bricks);
+int arc_set_camera(arc_ctx* ctx, const arc_camera_uniforms* cam);
+
+/* Primary pass: G-buffer (gbuf_depth_mat and gbuf_norm_motion: 2 u32 per pixel, gbuf_albedo_ao:
+ * 1 u32 per pixel, row-major width x height) and optional per-pixel hit records. Width and height
+ * must match the camera's world_grid_dims.w. */
+int arc_trace_primary(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbuf_depth_mat,
+                      uint32_t* gbuf_norm_motion, uint32_t* gbuf_albedo_ao, arc_hit_record* hits);
+int arc_trace_primary_dev(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbuf_depth_mat,
+                          uint32_t* gbuf_norm_motion, uint32_t* gbuf_albedo_ao, arc_hit_record* hits);
+/* GI secondary ray per hit pixel from a G-buffer; gi_hits per pixel (face ARC_FACE_NONE and flags 0
+ * for pixels without a primary hit). */
+int arc_trace_secondary(arc_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* gbuf_depth_mat,
+                        const uint32_t* gbuf_norm_motion, arc_hit_record* gi_hits);
+int arc_trace_secondary_dev(arc_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* gbuf_depth_mat,
+                            const uint32_t* gbuf_norm_motion, arc_hit_record* gi_hits);
+/* Both passes in one launch: writes the G-buffer, primary hits and GI hits (any output may be NULL
+ * except the G-buffer). n_gi_out (optional) receives the number of GI rays traced. */
+int arc_trace_frame(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbuf_depth_mat, uint32_t* gbuf_norm_motion,
+                    uint32_t* gbuf_albedo_ao, arc_hit_record* hits, arc_hit_record* gi_hits, uint64_t* n_gi_out);
+int arc_trace_frame_dev(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbuf_depth_mat,
+                        uint32_t* gbuf_norm_motion, uint32_t* gbuf_albedo_ao, arc_hit_record* hits,
+                        arc_hit_record* gi_hits, uint64_t* n_gi_dev);
+/* trace_world_64tree on a batch of rays (origin m, unit dir). */
+int arc_trace_rays(arc_ctx* ctx, const arc_ray* rays, uint32_t n, float max_dist_m, uint32_t lod_bias,
+                   int ignore_water, arc_hit_record* hits);
+int arc_trace_rays_dev(arc_ctx* ctx, const arc_ray* rays, uint32_t n, float max_dist_m, uint32_t lod_bias,
+                       int ignore_water, arc_hit_record* hits);
+/* trace_shadow_vis on a batch (1.0 visible / 0.0 occluded per ray). */
+int arc_shadow_rays_dev(arc_ctx* ctx, const arc_ray* rays, uint32_t n, float max_dist_m, float* vis);
+
+/* SHARC radiance cache, library-owned (keys 512 KB, accumulators 2 MB, resolved slots 2 MB). */
+int arc_sharc_reset(arc_ctx* ctx);
+int arc_sharc_update_dev(arc_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* gbuf_depth_mat,
+                         const uint32_t* gbuf_norm_motion);
+int arc_sharc_resolve(arc_ctx* ctx);
+int arc_sharc_query_dev(arc_ctx* ctx, const float* pos, const float* normal, const float* jitter, uint32_t n,
+                        float* out_rgbw);
+int arc_sharc_download(arc_ctx* ctx, uint32_t* keys, uint32_t* accum, arc_sharc_slot* resolved);
+int arc_sharc_upload(arc_ctx* ctx, const uint32_t* keys, const uint32_t* accum, const arc_sharc_slot* resolved);
+/* Test hook mirroring the reference's SHARC GPU harness (crates/arcadia-render/tests/sharc_gpu.rs:18-29):
+ * n_threads device threads each deposit rad at (pos, normal) as seen from cam_pos. */
+int arc_sharc_deposit_dev(arc_ctx* ctx, const float pos[3], const float normal[3], const float cam_pos[3],
+                          const float rad[3], uint32_t n_threads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ARC_TRACE_H */

@@ -1,0 +1,343 @@
+"""ctypes front end of the CPU oracle (``oracle/_build/liborc.so``).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg
+of ``bench.py``. The product (``arcadia_gb300``) never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from arcadia_gb300.layout import (
+    BRICK_DTYPE,
+    CAMERA_DTYPE,
+    HIT_DTYPE,
+    MATERIAL_DTYPE,
+    NODE_DTYPE,
+    RAY_DTYPE,
+    SHARC_SLOT_DTYPE,
+    IS_LEAF_FLAG,
+    IS_UNIFORM_FLAG,
+    PTR_INDEX_MASK,
+    SceneParams,
+)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liborc.so")
+_lib = None
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+class _Scene(C.Structure):
+    _fields_ = [
+        ("grid", C.c_uint32 * 3),
+        ("seed", C.c_uint32),
+        ("caves", C.c_uint32),
+        ("cave_threshold", C.c_float),
+        ("height_lo", C.c_float),
+        ("height_hi", C.c_float),
+    ]
+
+
+class _Pools(C.Structure):
+    _fields_ = [
+        ("grid", C.c_uint32 * 3),
+        ("n_chunks", C.c_uint32),
+        ("roots", C.POINTER(C.c_uint32)),
+        ("nodes", C.c_void_p),
+        ("n_nodes", C.c_uint32),
+        ("bricks", C.c_void_p),
+        ("n_bricks", C.c_uint32),
+        ("solid_voxels", C.c_uint64),
+    ]
+
+
+class _World(C.Structure):
+    _fields_ = [
+        ("roots", C.c_void_p),
+        ("nodes", C.c_void_p),
+        ("n_nodes", C.c_uint32),
+        ("bricks", C.c_void_p),
+        ("n_bricks", C.c_uint32),
+        ("palette", C.c_void_p),
+    ]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        _lib = C.CDLL(_LIB_PATH)
+        vp, u32, f32, i32 = C.c_void_p, C.c_uint32, C.c_float, C.c_int
+        _lib.orc_build_world.argtypes = [C.POINTER(_Scene), C.POINTER(_Pools)]
+        _lib.orc_free_pools.argtypes = [C.POINTER(_Pools)]
+        _lib.orc_default_palette.argtypes = [vp]
+        _lib.orc_build_chunk_dense.argtypes = [vp, vp, vp, C.POINTER(u32), vp, C.POINTER(u32)]
+        _lib.orc_trace_rays.argtypes = [C.POINTER(_World), vp, vp, u32, f32, u32, i32, vp, vp, i32]
+        _lib.orc_primary.argtypes = [C.POINTER(_World), vp, u32, u32, u32, u32, vp, vp, vp, vp, vp, i32]
+        _lib.orc_gi_rays.argtypes = [C.POINTER(_World), vp, u32, u32, u32, u32, vp, vp, vp, vp, vp, i32]
+        _lib.orc_frame_sample.argtypes = [C.POINTER(_World), vp, u32, i32, vp, vp, vp]
+        _lib.orc_frame_sample.restype = C.c_uint64
+        _lib.orc_cpu_frame_sample.argtypes = [C.POINTER(_World), vp, u32, i32, vp, vp, vp]
+        _lib.orc_cpu_frame_sample.restype = C.c_uint64
+        _lib.orc_cpu_raycast.argtypes = [C.POINTER(_World), vp, vp, u32, f32, vp, i32]
+        _lib.orc_raycast_chunk_local.argtypes = [C.POINTER(_World), u32, vp, vp, f32, vp, vp, vp]
+        _lib.orc_raycast_chunk_local.restype = C.c_int
+        _lib.orc_depth_fp64.argtypes = [vp, vp, vp, u32]
+        _lib.orc_depth_fp64.restype = C.c_double
+        _lib.orc_sharc_make_key.argtypes = [vp, vp, vp, vp, vp, vp]
+        _lib.orc_sharc_deposit.argtypes = [vp, vp, u32, u32, vp]
+        _lib.orc_sharc_deposit.restype = u32
+        _lib.orc_sharc_resolve.argtypes = [vp, vp, vp]
+        _lib.orc_sharc_query.argtypes = [vp, vp, vp, vp, vp, vp]
+        _lib.orc_sharc_update.argtypes = [C.POINTER(_World), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+        _lib.orc_shadow_vis.argtypes = [C.POINTER(_World), vp, vp, vp, f32, vp]
+        _lib.orc_shadow_vis.restype = f32
+        _lib.orc_test_sincos.argtypes = [vp, u32, vp, vp]
+        _lib.orc_test_f16.argtypes = [vp, u32, vp]
+        _lib.orc_test_powi.argtypes = [vp, u32, u32, vp]
+        _lib.orc_scene_heightmap.argtypes = [C.POINTER(_Scene), vp]
+        _lib.orc_scene_voxel.argtypes = [C.POINTER(_Scene), vp, u32, u32, u32]
+        _lib.orc_scene_voxel.restype = u32
+        _lib.orc_test_scene_volume.argtypes = [C.POINTER(_Scene), u32, u32, u32, vp]
+    return _lib
+
+
+def _p(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data
+
+
+def default_palette() -> np.ndarray:
+    pal = np.zeros(256, MATERIAL_DTYPE)
+    lib().orc_default_palette(_p(pal))
+    return pal
+
+
+class World:
+    """Flat GPU-ready pools (chunk roots, Node64 pool, LeafBrick64 pool, palette)."""
+
+    def __init__(self, grid, roots, nodes, bricks, palette=None):
+        self.grid = tuple(int(g) for g in grid)
+        self.roots = np.ascontiguousarray(roots, np.uint32)
+        self.nodes = np.ascontiguousarray(nodes).view(NODE_DTYPE)
+        self.bricks = np.ascontiguousarray(bricks).view(BRICK_DTYPE)
+        self.palette = default_palette() if palette is None else np.ascontiguousarray(palette).view(MATERIAL_DTYPE)
+        self._w = _World(
+            _p(self.roots), _p(self.nodes), len(self.nodes), _p(self.bricks), len(self.bricks), _p(self.palette)
+        )
+
+    @property
+    def cw(self):
+        return C.byref(self._w)
+
+
+def build_world(scene: SceneParams) -> World:
+    s = _Scene((C.c_uint32 * 3)(*scene.grid), scene.seed, int(scene.caves), scene.cave_threshold, scene.height_lo,
+               scene.height_hi)
+    p = _Pools()
+    lib().orc_build_world(C.byref(s), C.byref(p))
+    n_ch = p.n_chunks
+    roots = np.ctypeslib.as_array(p.roots, shape=(n_ch,)).copy()
+    nodes = np.frombuffer((C.c_char * (16 * p.n_nodes)).from_address(p.nodes), dtype=NODE_DTYPE).copy()
+    bricks = np.frombuffer((C.c_char * (64 * p.n_bricks)).from_address(p.bricks), dtype=BRICK_DTYPE).copy()
+    solid = p.solid_voxels
+    lib().orc_free_pools(C.byref(p))
+    w = World(scene.grid, roots, nodes, bricks)
+    w.solid_voxels = solid
+    return w
+
+
+def build_chunk_dense(vol: np.ndarray, palette: np.ndarray | None = None):
+    """ChunkTree64::from_generator over a dense (z, y, x) u8 volume with no region hint."""
+    vol = np.ascontiguousarray(vol, np.uint8)
+    assert vol.shape == (256, 256, 256)
+    pal = default_palette() if palette is None else palette
+    nn, nb = C.c_uint32(0), C.c_uint32(0)
+    lib().orc_build_chunk_dense(_p(vol), _p(pal), None, C.byref(nn), None, C.byref(nb))
+    nodes = np.zeros(nn.value, NODE_DTYPE)
+    bricks = np.zeros(max(nb.value, 1), BRICK_DTYPE)
+    lib().orc_build_chunk_dense(_p(vol), _p(pal), _p(nodes), C.byref(nn), _p(bricks), C.byref(nb))
+    return nodes, bricks[: nb.value]
+
+
+def world_from_chunk(nodes: np.ndarray, bricks: np.ndarray, palette=None) -> World:
+    """One-chunk world: relocate a chunk's local tree behind the reserved empty node/brick 0
+    (world_map.rs:167-203)."""
+    out = np.zeros(len(nodes) + 1, NODE_DTYPE)
+    rel = nodes.copy()
+    ptr = rel["child_ptr"].astype(np.uint64)
+    flags = ptr & (IS_LEAF_FLAG | IS_UNIFORM_FLAG)
+    local = ptr & PTR_INDEX_MASK
+    is_leaf = (ptr & IS_LEAF_FLAG) != 0
+    is_uni = (ptr & IS_UNIFORM_FLAG) != 0
+    new = np.where(is_leaf, np.where(is_uni, flags, flags | (local + 1)), flags | (local + 1))
+    empty = (rel["mask_low"] == 0) & (rel["mask_high"] == 0)
+    new = np.where(empty, 0, new)
+    rel["child_ptr"] = new.astype(np.uint32)
+    rel["lod_payload"] = np.where(empty, 0, rel["lod_payload"])
+    out[1:] = rel
+    b = np.zeros(len(bricks) + 1, BRICK_DTYPE)
+    b[1:] = bricks
+    roots = np.array([1 if not empty[0] else 0xFFFFFFFF], np.uint32)
+    return World((1, 1, 1), roots, out, b, palette)
+
+
+def trace_rays(world: World, cam: np.ndarray, rays: np.ndarray, max_dist_m: float, lod_bias: int, ignore_water: bool,
+               threads: int = 8, want_bytes: bool = False):
+    n = len(rays)
+    hits = np.zeros(n, HIT_DTYPE)
+    by = np.zeros(n, np.uint32) if want_bytes else None
+    lib().orc_trace_rays(world.cw, _p(cam), _p(np.ascontiguousarray(rays, RAY_DTYPE)), n, max_dist_m, lod_bias,
+                         int(ignore_water), _p(hits), _p(by), threads)
+    return (hits, by) if want_bytes else hits
+
+
+def primary(world: World, cam: np.ndarray, rect=None, threads: int = 8):
+    w = int(cam["world_grid_dims"][0][3] & 0xFFFF)
+    h = int(cam["world_grid_dims"][0][3] >> 16)
+    x0, y0, x1, y1 = rect or (0, 0, w, h)
+    gdm = np.zeros((h * w, 2), np.uint32)
+    gnm = np.zeros((h * w, 2), np.uint32)
+    gaa = np.zeros(h * w, np.uint32)
+    hits = np.zeros(h * w, HIT_DTYPE)
+    by = np.zeros(h * w, np.uint32)
+    lib().orc_primary(world.cw, _p(cam), x0, y0, x1, y1, _p(gdm), _p(gnm), _p(gaa), _p(hits), _p(by), threads)
+    return gdm, gnm, gaa, hits, by
+
+
+def gi_rays(world: World, cam: np.ndarray, gdm, gnm, rect=None, threads: int = 8):
+    w = int(cam["world_grid_dims"][0][3] & 0xFFFF)
+    h = int(cam["world_grid_dims"][0][3] >> 16)
+    x0, y0, x1, y1 = rect or (0, 0, w, h)
+    rays = np.zeros(h * w, RAY_DTYPE)
+    hits = np.zeros(h * w, HIT_DTYPE)
+    by = np.zeros(h * w, np.uint32)
+    lib().orc_gi_rays(world.cw, _p(cam), x0, y0, x1, y1, _p(gdm), _p(gnm), _p(rays), _p(hits), _p(by), threads)
+    return rays, hits, by
+
+
+def frame_sample(world: World, cam: np.ndarray, stride: int, threads: int, cpu_query: bool = False):
+    """Primary + GI rays of every ``stride``-th pixel; returns (rays, primary, gi, checksum, bytes).
+
+    ``cpu_query`` selects the reference CPU ray query (raycast_meters) instead of the WGSL
+    transcription; bytes (the instrumented algorithmic byte count) are only counted for the latter."""
+    npri, ngi, cs = np.zeros(1, np.uint64), np.zeros(1, np.uint64), np.zeros(1, np.uint64)
+    fn = lib().orc_cpu_frame_sample if cpu_query else lib().orc_frame_sample
+    total = fn(world.cw, _p(cam), stride, threads, _p(npri), _p(ngi), _p(cs))
+    by = 0 if cpu_query else int(C.c_uint64.in_dll(lib(), "orc_last_sample_bytes").value)
+    return int(total), int(npri[0]), int(ngi[0]), int(cs[0]), by
+
+
+def cpu_raycast(world: World, rays: np.ndarray, max_dist_m: float, threads: int = 8):
+    hits = np.zeros(len(rays), HIT_DTYPE)
+    grid = np.array(world.grid, np.uint32)
+    lib().orc_cpu_raycast(world.cw, _p(grid), _p(np.ascontiguousarray(rays, RAY_DTYPE)), len(rays), max_dist_m,
+                          _p(hits), threads)
+    return hits
+
+
+def raycast_chunk_local(world: World, origin_v, dir_, max_dist_v):
+    o = np.asarray(origin_v, np.float32)
+    d = np.asarray(dir_, np.float32)
+    out = np.zeros(4, np.float32)
+    vox = np.zeros(3, np.int32)
+    mat = np.zeros(1, np.uint32)
+    ok = lib().orc_raycast_chunk_local(world.cw, int(world.roots[0]), _p(o), _p(d), max_dist_v, _p(out), _p(vox),
+                                       _p(mat))
+    if not ok:
+        return None
+    return {"distance": float(out[0]), "normal": tuple(float(v) for v in out[1:]), "voxel": tuple(int(v) for v in vox),
+            "mat": int(mat[0])}
+
+
+def depth_fp64(origin_m, dir_, cell_min, span: int) -> float:
+    o = np.asarray(origin_m, np.float32)
+    d = np.asarray(dir_, np.float32)
+    c = np.asarray(cell_min, np.int32)
+    return lib().orc_depth_fp64(_p(o), _p(d), _p(c), span)
+
+
+def shadow_vis(world: World, cam, origin_m, dir_, max_dist_m) -> float:
+    o = np.asarray(origin_m, np.float32)
+    d = np.asarray(dir_, np.float32)
+    return lib().orc_shadow_vis(world.cw, _p(cam), _p(o), _p(d), max_dist_m, None)
+
+
+class Sharc:
+    """Host-side SHARC state (keys, fixed-point accumulators, resolved slots)."""
+
+    def __init__(self):
+        self.keys = np.zeros(131072, np.uint32)
+        self.accum = np.zeros(131072 * 4, np.uint32)
+        self.resolved = np.zeros(131072, SHARC_SLOT_DTYPE)
+
+    def make_key(self, pos, normal, cam_pos, jitter=(0.0, 0.0)):
+        b, k = np.zeros(1, np.uint32), np.zeros(1, np.uint32)
+        args = [np.asarray(v, np.float32) for v in (pos, normal, cam_pos, jitter)]
+        lib().orc_sharc_make_key(*[_p(a) for a in args], _p(b), _p(k))
+        return int(b[0]), int(k[0])
+
+    def deposit(self, pos, normal, cam_pos, rad):
+        b, k = self.make_key(pos, normal, cam_pos)
+        r = np.asarray(rad, np.float32)
+        return lib().orc_sharc_deposit(_p(self.keys), _p(self.accum), b, k, _p(r))
+
+    def resolve(self, passes: int = 1):
+        for _ in range(passes):
+            lib().orc_sharc_resolve(_p(self.keys), _p(self.accum), _p(self.resolved))
+
+    def query(self, pos, normal, cam_pos, jitter=(0.0, 0.0)):
+        out = np.zeros(4, np.float32)
+        args = [np.asarray(v, np.float32) for v in (pos, normal, cam_pos, jitter)]
+        lib().orc_sharc_query(_p(self.resolved), *[_p(a) for a in args], _p(out))
+        return out
+
+    def update(self, world: World, cam, gdm, gnm, resolved_prev=None):
+        w = int(cam["world_grid_dims"][0][3] & 0xFFFF)
+        h = int(cam["world_grid_dims"][0][3] >> 16)
+        tile = 16 if (int(cam["quality_flags"][0][3]) & 0xFF) <= 12 else 8
+        nt = ((w + tile - 1) // tile) * ((h + tile - 1) // tile)
+        tk, tb, tv = np.zeros(nt, np.uint32), np.zeros(nt, np.uint32), np.zeros(nt, np.uint32)
+        tr = np.zeros((nt, 3), np.float32)
+        prev = self.resolved if resolved_prev is None else resolved_prev
+        lib().orc_sharc_update(world.cw, _p(cam), _p(gdm), _p(gnm), _p(prev), _p(self.keys), _p(self.accum), _p(tk),
+                               _p(tb), _p(tr), _p(tv))
+        return tk, tb, tr, tv
+
+
+def sincos(x: np.ndarray):
+    x = np.ascontiguousarray(x, np.float32)
+    s, c = np.zeros_like(x), np.zeros_like(x)
+    lib().orc_test_sincos(_p(x), len(x), _p(s), _p(c))
+    return s, c
+
+
+def f16_bits(x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros(len(x), np.uint16)
+    lib().orc_test_f16(_p(x), len(x), _p(out))
+    return out
+
+
+def powi(x: np.ndarray, e: int) -> np.ndarray:
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros_like(x)
+    lib().orc_test_powi(_p(x), len(x), e, _p(out))
+    return out
+
+
+def scene_volume(scene: SceneParams, chunk=(0, 0, 0)) -> np.ndarray:
+    """Dense (z, y, x) u8 materials of one chunk of a synthetic scene (per-voxel evaluation)."""
+    s = _Scene((C.c_uint32 * 3)(*scene.grid), scene.seed, int(scene.caves), scene.cave_threshold, scene.height_lo,
+               scene.height_hi)
+    vol = np.zeros((256, 256, 256), np.uint8)
+    lib().orc_test_scene_volume(C.byref(s), chunk[0], chunk[1], chunk[2], _p(vol))
+    return vol
