@@ -146,6 +146,7 @@ int arc_create(int device, arc_ctx** out) {
     c->cfg.tile_w = 8;
     c->cfg.tile_h = 4;
     c->cfg.refill_threshold = 8;
+    c->cfg.reg_blocks = 1;
     *out = c;
     return ARC_OK;
 }
@@ -192,12 +193,13 @@ int arc_get_stream(arc_ctx* c, void** stream) {
 int arc_set_launch_config(arc_ctx* c, const arc_launch_config* cfg) {
     if (!c || !cfg) return ARC_E_INVALID_ARG;
     if (cfg->variant > 1u) return set_err(c, ARC_E_INVALID_ARG, "variant must be 0 or 1");
-    if (cfg->block_threads == 0 || cfg->block_threads % 32u || cfg->block_threads > 1024u)
-        return set_err(c, ARC_E_INVALID_ARG, "block_threads must be a multiple of 32 in [32, 1024]");
+    if (cfg->block_threads == 0 || cfg->block_threads % 32u)
+        return set_err(c, ARC_E_INVALID_ARG, "block_threads must be a multiple of 32");
     if (cfg->variant == 0u && cfg->block_threads % 8u) return set_err(c, ARC_E_INVALID_ARG, "plain variant needs block_threads % 8 == 0");
     if (cfg->tile_w * cfg->tile_h != 32u) return set_err(c, ARC_E_INVALID_ARG, "tile_w * tile_h must be 32");
     if (cfg->refill_threshold < 1u || cfg->refill_threshold > 32u) return set_err(c, ARC_E_INVALID_ARG, "refill_threshold in [1, 32]");
-    if (cfg->variant == 1u && cfg->block_threads > 256u) return set_err(c, ARC_E_INVALID_ARG, "persistent variant: block_threads <= 256");
+    if (cfg->block_threads > 256u) return set_err(c, ARC_E_INVALID_ARG, "block_threads <= 256");
+    if (cfg->reg_blocks < 1u || cfg->reg_blocks > 4u) return set_err(c, ARC_E_INVALID_ARG, "reg_blocks in [1, 4]");
     c->cfg = *cfg;
     return ARC_OK;
 }

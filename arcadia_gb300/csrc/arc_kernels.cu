@@ -161,7 +161,9 @@ __device__ __forceinline__ void pixel_of(const FrameParams& P, uint32_t q, uint3
 // Frame kernels
 // ------------------------------------------------------------------------------------------------
 
-__global__ void frame_plain_kernel(const FrameParams P, const __grid_constant__ arc_camera_uniforms cam) {
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) frame_plain_kernel(const FrameParams P,
+                                                                   const __grid_constant__ arc_camera_uniforms cam) {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= P.width || y >= P.height) return;
@@ -203,8 +205,9 @@ __global__ void frame_plain_kernel(const FrameParams P, const __grid_constant__ 
 
 enum : uint32_t { kIdle = 0u, kPrimary = 1u, kGi = 2u };
 
-__global__ void __launch_bounds__(256) frame_persistent_kernel(const FrameParams P,
-                                                               const __grid_constant__ arc_camera_uniforms cam) {
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) frame_persistent_kernel(const FrameParams P,
+                                                                     const __grid_constant__ arc_camera_uniforms cam) {
     const World& w = P.world;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt_mask = (1u << lane) - 1u;
@@ -338,23 +341,35 @@ __global__ void shadow_kernel(const World w, const __grid_constant__ arc_camera_
 // Host launchers (called by the C ABI on the context's stream)
 // ------------------------------------------------------------------------------------------------
 
-cudaError_t launch_frame(const FrameParams& P, const arc_camera_uniforms& cam, const arc_launch_config& cfg,
-                         int n_sm, cudaStream_t st) {
+template <int MINB>
+cudaError_t launch_frame_t(const FrameParams& P, const arc_camera_uniforms& cam, const arc_launch_config& cfg, int n_sm,
+                           cudaStream_t st) {
     if (cfg.variant == 0u) {
         const uint32_t bw = 8u, bh = cfg.block_threads / 8u;
         dim3 block(bw, bh);
         dim3 grid((P.width + bw - 1u) / bw, (P.height + bh - 1u) / bh);
-        frame_plain_kernel<<<grid, block, 0, st>>>(P, cam);
+        frame_plain_kernel<MINB><<<grid, block, 0, st>>>(P, cam);
         return cudaGetLastError();
     }
     int per_sm = (int)cfg.blocks_per_sm;
     if (per_sm <= 0) {
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, frame_persistent_kernel, (int)cfg.block_threads, 0);
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, frame_persistent_kernel<MINB>,
+                                                                      (int)cfg.block_threads, 0);
         if (e != cudaSuccess) return e;
         if (per_sm <= 0) per_sm = 1;
     }
-    frame_persistent_kernel<<<n_sm * per_sm, cfg.block_threads, 0, st>>>(P, cam);
+    frame_persistent_kernel<MINB><<<n_sm * per_sm, cfg.block_threads, 0, st>>>(P, cam);
     return cudaGetLastError();
+}
+
+cudaError_t launch_frame(const FrameParams& P, const arc_camera_uniforms& cam, const arc_launch_config& cfg, int n_sm,
+                         cudaStream_t st) {
+    switch (cfg.reg_blocks) {
+        case 2: return launch_frame_t<2>(P, cam, cfg, n_sm, st);
+        case 3: return launch_frame_t<3>(P, cam, cfg, n_sm, st);
+        case 4: return launch_frame_t<4>(P, cam, cfg, n_sm, st);
+        default: return launch_frame_t<1>(P, cam, cfg, n_sm, st);
+    }
 }
 
 cudaError_t launch_secondary(const FrameParams& P, const arc_camera_uniforms& cam, cudaStream_t st) {

@@ -91,6 +91,7 @@ class LaunchConfig(C.Structure):
         ("tile_w", C.c_uint32),
         ("tile_h", C.c_uint32),
         ("refill_threshold", C.c_uint32),
+        ("reg_blocks", C.c_uint32),
     ]
 
 

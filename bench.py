@@ -48,7 +48,12 @@ def _args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--variant", type=int, default=1, help="0 plain kernel, 1 persistent kernel")
+    p.add_argument("--variant", type=int, default=None, help="0 plain kernel, 1 persistent kernel (default: tuned)")
+    p.add_argument("--reg-blocks", type=int, default=None, help="register budget (CTAs/SM the kernel is built for)")
+    p.add_argument("--block-threads", type=int, default=None)
+    p.add_argument("--width", type=int, default=WIDTH)
+    p.add_argument("--height", type=int, default=HEIGHT)
+    p.add_argument("--frame-only", action="store_true", help="time only the frame kernel (profiling runs)")
     return p.parse_args()
 
 
@@ -59,10 +64,11 @@ def _dist():
     return ws, rank, local
 
 
-def _camera(scene, frame):
+def _camera(scene, frame, width=None, height=None):
     from arcadia_gb300 import layout as L
 
-    return L.default_camera_for(scene, WIDTH, HEIGHT, quality=L.quality_parity(512), frame_index=frame)
+    return L.default_camera_for(scene, width or WIDTH, height or HEIGHT, quality=L.quality_parity(512),
+                                frame_index=frame)
 
 
 class ClockSampler:
@@ -210,9 +216,13 @@ def run_ours(args):
     pal = native.default_palette()
     t = native.Tracer(local)
     t.upload_world(scene.grid, roots, nodes, bricks, pal)
-    t.set_launch_config(variant=args.variant)
+    knobs = {k: v for k, v in (("variant", args.variant), ("reg_blocks", args.reg_blocks),
+                               ("block_threads", args.block_threads)) if v is not None}
+    if knobs:
+        t.set_launch_config(**knobs)
+    W_, H_ = args.width, args.height
     stream = torch.cuda.ExternalStream(t.stream(), device=torch.device("cuda", local))
-    npx = WIDTH * HEIGHT
+    npx = W_ * H_
     dev = torch.device("cuda", local)
     gdm = torch.empty(npx * 2, dtype=torch.int32, device=dev)
     gnm = torch.empty(npx * 2, dtype=torch.int32, device=dev)
@@ -223,8 +233,8 @@ def run_ours(args):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
     def frame(i, slot):
-        t.set_camera(_camera(scene, i))
-        t.trace_frame_dev(WIDTH, HEIGHT, gdm.data_ptr(), gnm.data_ptr(), gaa.data_ptr(), hits.data_ptr(), gi.data_ptr(),
+        t.set_camera(_camera(scene, i, W_, H_))
+        t.trace_frame_dev(W_, H_, gdm.data_ptr(), gnm.data_ptr(), gaa.data_ptr(), hits.data_ptr(), gi.data_ptr(),
                           n_gi.data_ptr() + 8 * slot)
 
     clocks = ClockSampler(local)
@@ -256,10 +266,17 @@ def run_ours(args):
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.SUM)
         total_ms, rays = float(mx[0]), float(tt[1])
     value = rays / (total_ms * 1e-3) / 1e6
+    cfg = t.launch_config()
+    if args.frame_only:
+        t.close()
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": round(value, 3), "unit": UNIT, "frame_only": True,
+                              "width": W_, "height": H_, "ms_per_step": round(statistics.mean(ms), 4),
+                              "variant": cfg.variant, "reg_blocks": cfg.reg_blocks}), flush=True)
+        return
 
     # plain one-thread-per-pixel kernel, same frames (the "vs plain kernel" comparison)
     t.set_launch_config(variant=0)
-    plain_ms = []
     np_frames = min(args.steps, 20)
     with torch.cuda.stream(stream):
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(np_frames)]
@@ -272,7 +289,7 @@ def run_ours(args):
     plain_ms = [a.elapsed_time(b) for a, b in ev]
     plain_rays = np_frames * npx + int(n_gi[:np_frames].sum().item())
     plain_value = plain_rays / (sum(plain_ms) * 1e-3) / 1e6
-    t.set_launch_config(variant=args.variant)
+    t.set_launch_config(variant=cfg.variant)
 
     # end to end through the C ABI with host (pinned) buffers
     pin = {k: torch.empty(n, dtype=torch.int32).pin_memory().numpy() for k, n in
@@ -298,7 +315,6 @@ def run_ours(args):
     e2e_dt = time.perf_counter() - t0
     clk = clocks.stop()
     e2e_value = e2e_rays / e2e_dt / 1e6
-    cfg = t.launch_config()
     t.close()
 
     if rank != 0:
@@ -317,7 +333,7 @@ def run_ours(args):
     roofline = None
     if bpp is not None:
         achieved = bpp * npx / (statistics.mean(ms) * 1e-3) / 1e9
-        traffic = _profile_traffic("frame_persistent_kernel" if args.variant == 1 else "frame_plain_kernel")
+        traffic = _profile_traffic("frame_persistent_kernel" if cfg.variant == 1 else "frame_plain_kernel")
         roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
                     "algorithmic_bytes_per_pixel": round(bpp, 2)}
@@ -329,7 +345,8 @@ def run_ours(args):
                    "parallelism": f"replicas x{ws}", "l2": "flushed before every timed frame (256 MiB write)",
                    "kernel": "persistent" if cfg.variant == 1 else "plain",
                    "launch": {"block_threads": cfg.block_threads, "blocks_per_sm": cfg.blocks_per_sm,
-                              "tile": [cfg.tile_w, cfg.tile_h], "refill_threshold": cfg.refill_threshold}},
+                              "tile": [cfg.tile_w, cfg.tile_h], "refill_threshold": cfg.refill_threshold,
+                              "reg_blocks": cfg.reg_blocks}},
         "plain_kernel": {"value": round(plain_value, 3), "unit": UNIT, "ms_per_step": round(statistics.mean(plain_ms), 4)},
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": 480,
                 "d2h_bytes_per_step": npx * 60 + 8 + 16},

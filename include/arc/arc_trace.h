@@ -58,6 +58,7 @@ typedef struct arc_launch_config {
     uint32_t blocks_per_sm;    /* persistent variant: resident CTAs per SM (0 = occupancy maximum) */
     uint32_t tile_w, tile_h;   /* pixel tile a warp's 32 consecutive queue entries cover (tile_w*tile_h = 32) */
     uint32_t refill_threshold; /* persistent variant: refill when at least this many lanes are idle */
+    uint32_t reg_blocks;       /* register budget: kernel built for at least this many 256-thread CTAs per SM (1-4) */
 } arc_launch_config;
 
 typedef struct arc_stats {
