@@ -145,8 +145,8 @@ int arc_create(int device, arc_ctx** out) {
     c->cfg.blocks_per_sm = 0;
     c->cfg.tile_w = 8;
     c->cfg.tile_h = 4;
-    c->cfg.refill_threshold = 8;
-    c->cfg.reg_blocks = 1;
+    c->cfg.refill_threshold = 24;
+    c->cfg.reg_blocks = 4;
     *out = c;
     return ARC_OK;
 }
@@ -166,6 +166,9 @@ int arc_destroy(arc_ctx* c) {
     cudaFree(c->d_sharc_accum);
     cudaFree(c->d_sharc_resolved);
     cudaFree(c->d_sharc_stage);
+    cudaFree(c->d_nrc_w32);
+    cudaFree(c->d_nrc_w16);
+    cudaFree(c->d_nrc_loss);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -495,6 +498,53 @@ int arc_trace_rays(arc_ctx* c, const arc_ray* rays, uint32_t n, float max_dist_m
     ARC_CK(c, cudaMemcpyAsync(d_rays, rays, (size_t)n * 24, cudaMemcpyHostToDevice, c->stream));
     if ((rc = arc_trace_rays_dev(c, d_rays, n, max_dist_m, lod_bias, ignore_water, d_hits))) return rc;
     ARC_CK(c, cudaMemcpyAsync(hits, d_hits, (size_t)n * 20, cudaMemcpyDeviceToHost, c->stream));
+    return arc_ctx_finish(c);
+}
+
+// Autotuner: times each candidate launch configuration on the caller's frame (median of `frames`
+// launches after one warm-up, CUDA events on the context stream) and installs the fastest.
+int arc_autotune_frame_dev(arc_ctx* c, uint32_t width, uint32_t height, uint32_t* gdm, uint32_t* gnm, uint32_t* gaa,
+                           arc_hit_record* hits, arc_hit_record* gi_hits, uint32_t frames, arc_launch_config* best_out,
+                           float* best_ms) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if ((rc = check_dims(c, width, height))) return rc;
+    if (!gdm || !gnm || !gaa) return set_err(c, ARC_E_INVALID_ARG, "null G-buffer");
+    if (frames == 0) frames = 3;
+    std::vector<arc_launch_config> cands;
+    const uint32_t tiles[3][2] = {{8, 4}, {4, 8}, {16, 2}};
+    for (uint32_t rb : {2u, 3u, 4u})
+        for (uint32_t thr : {8u, 16u, 24u, 28u})
+            for (uint32_t bt : {128u, 256u}) cands.push_back(arc_launch_config{1u, bt, 0u, 8u, 4u, thr, rb});
+    for (const auto& t : tiles) cands.push_back(arc_launch_config{1u, 256u, 0u, t[0], t[1], 24u, 4u});
+    for (uint32_t rb : {3u, 4u})
+        for (uint32_t bt : {64u, 128u, 256u}) cands.push_back(arc_launch_config{0u, bt, 0u, 8u, 4u, 8u, rb});
+    const arc_launch_config saved = c->cfg;
+    float best = 1e30f;
+    arc_launch_config best_cfg = saved;
+    std::vector<float> ms(frames);
+    for (const arc_launch_config& cfg : cands) {
+        c->cfg = cfg;
+        for (uint32_t f = 0; f <= frames; ++f) {
+            if ((rc = arc_trace_frame_dev(c, width, height, gdm, gnm, gaa, hits, gi_hits, nullptr))) {
+                c->cfg = saved;
+                return rc;
+            }
+            ARC_CK(c, cudaEventSynchronize(c->ev1));
+            float t = 0.0f;
+            ARC_CK(c, cudaEventElapsedTime(&t, c->ev0, c->ev1));
+            if (f) ms[f - 1] = t;
+        }
+        std::sort(ms.begin(), ms.end());
+        const float med = ms[frames / 2];
+        if (med < best) {
+            best = med;
+            best_cfg = cfg;
+        }
+    }
+    c->cfg = best_cfg;
+    if (best_out) *best_out = best_cfg;
+    if (best_ms) *best_ms = best;
     return arc_ctx_finish(c);
 }
 

@@ -40,6 +40,16 @@ struct arc_ctx {
     arc_sharc_slot* d_sharc_resolved = nullptr;
     void* d_sharc_stage = nullptr;
     size_t sharc_stage_bytes = 0;
+    uint32_t sharc_mode = 0;  // 0 reference shading, 1 one-bounce estimator of the cache comparison
+
+    // neural radiance cache: FP32 masters, Adam moments, gradient (contiguous), FP16 layouts, loss
+    float* d_nrc_w32 = nullptr;
+    float* d_nrc_m = nullptr;
+    float* d_nrc_v = nullptr;
+    float* d_nrc_grad = nullptr;
+    void* d_nrc_w16 = nullptr;
+    float* d_nrc_loss = nullptr;
+    uint32_t nrc_step = 0;
 
     arc_launch_config cfg{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;

@@ -96,60 +96,6 @@ __device__ __forceinline__ void primary_store(const FrameParams& P, const arc_ca
     *normal_word = n0;
 }
 
-// probe_emissive_macro_candidate (lighting_restir_gi.wgsl:20-54).
-__device__ __forceinline__ float probe_emissive(const World& w, const arc_camera_uniforms& cam, f3 pos, f3 d, float dist) {
-    const f3 vp = mul3s(add3(pos, mul3s(d, dist)), ARC_VOXELS_PER_METER);
-    const uint32_t gx = cam.world_grid_dims[0], gy = cam.world_grid_dims[1], gz = cam.world_grid_dims[2];
-    if (vp.x < 0.0f || vp.y < 0.0f || vp.z < 0.0f) return 0.0f;
-    if (vp.x >= (float)gx * ARC_CHUNK_DIM_F || vp.y >= (float)gy * ARC_CHUNK_DIM_F || vp.z >= (float)gz * ARC_CHUNK_DIM_F)
-        return 0.0f;
-    const uint32_t vx = f2u(vp.x), vy = f2u(vp.y), vz = f2u(vp.z);
-    const uint32_t root_idx = load_root(w, (vx >> 8) + (vy >> 8) * gx + (vz >> 8) * gx * gy);
-    if (root_idx == ARC_EMPTY_CHUNK) return 0.0f;
-    const uint32_t lx = vx & 255u, ly = vy & 255u, lz = vz & 255u;
-    const uint4 root = load_node(w, root_idx);
-    const uint32_t b0 = (((lz >> 6) & 3u) << 4) | (((ly >> 6) & 3u) << 2) | ((lx >> 6) & 3u);
-    if (!has_child(root.x, root.y, b0)) return 0.0f;
-    uint32_t m_id;
-    if (root.z & ARC_IS_LEAF_FLAG) {
-        m_id = (root.w >> 24) & 0xFFu;
-    } else {
-        const uint4 l1 = load_node(w, child_index(root, b0));
-        const uint32_t b1 = (((lz >> 4) & 3u) << 4) | (((ly >> 4) & 3u) << 2) | ((lx >> 4) & 3u);
-        if (!has_child(l1.x, l1.y, b1)) return 0.0f;
-        m_id = (l1.w >> 24) & 0xFFu;
-    }
-    const float4 em = __ldg(&w.palette[2u * m_id + 1u]);
-    return (em.x * 0.333f + em.y * 0.333f) + em.z * 0.333f;
-}
-
-// GI secondary ray of a hit pixel from its G-buffer words (lighting_restir_gi.wgsl:69-87, 195-209).
-__device__ __forceinline__ bool gi_setup(const World& w, const arc_camera_uniforms& cam, uint32_t x, uint32_t y,
-                                         uint32_t W, uint32_t H, uint32_t depth_word, uint32_t normal_word, f3* origin,
-                                         f3* dir) {
-    const float hit_dist = __uint_as_float(depth_word);
-    if (hit_dist >= 1e4f) return false;
-    const f3 rd = camera_dir(cam, x, y, W, H);
-    const f3 eye{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]};
-    const f3 hp = add3(eye, mul3s(rd, hit_dist));
-    float ox, oy;
-    unpack2x16snorm(normal_word, &ox, &oy);
-    const f3 n = oct_decode(ox, oy);
-    float u1, u2;
-    gradient_noise((float)x, (float)y, __float_as_uint(cam.cam_up_frame[3]), &u1, &u2);
-    const f3 sn = normalize3(f3{n.x + 0.0f, n.y + 0.22f, n.z + 0.0f});
-    f3 bt, bb;
-    make_basis(sn, &bt, &bb);
-    f3 bd = cosine_sample(u1, u2, sn, bt, bb);
-    const f3 cd = cosine_sample(fractf(u1 + 0.5f), fractf(u2 + 0.381966f), sn, bt, bb);
-    const float em_near = probe_emissive(w, cam, hp, cd, 1.25f);
-    const float em_mid = probe_emissive(w, cam, hp, cd, 3.0f);
-    if (fmaxf(em_near, em_mid) > 0.25f) bd = cd;
-    *origin = add3(hp, mul3s(n, 0.10f));
-    *dir = bd;
-    return true;
-}
-
 __device__ __forceinline__ void pixel_of(const FrameParams& P, uint32_t q, uint32_t* x, uint32_t* y) {
     const uint32_t tile = q >> 5, within = q & 31u;
     const uint32_t tx = tile % P.tiles_x, ty = tile / P.tiles_x;
@@ -217,9 +163,9 @@ __global__ void __launch_bounds__(256, MINB) frame_persistent_kernel(const Frame
     RayState s;
     HitInfo h;
     uint32_t phase = kIdle;
-    uint32_t px = 0, py = 0;
+    uint32_t pxy = 0;  // pixel x | y << 16
     bool exhausted = false;
-    unsigned long long gi_count = 0;
+    uint32_t gi_count = 0;
 
     for (;;) {
         // Refill idle lanes from the queue (one atomic per warp).
@@ -232,7 +178,9 @@ __global__ void __launch_bounds__(256, MINB) frame_persistent_kernel(const Frame
             if (phase == kIdle) {
                 const uint32_t q = base + __popc(idle & lt_mask);
                 if (q < P.queue_len) {
+                    uint32_t px, py;
                     pixel_of(P, q, &px, &py);
+                    pxy = px | (py << 16);
                     if (px < P.width && py < P.height) {
                         const f3 dir = camera_dir(cam, px, py, P.width, P.height);
                         if (ray_begin(s, cam, eye, dir, 0.0f, 250.0f, 0u, underwater)) {
@@ -254,6 +202,7 @@ __global__ void __launch_bounds__(256, MINB) frame_persistent_kernel(const Frame
         if (phase == kIdle) continue;
         const StepResult r = ray_advance(s, w, cam, h);
         if (r == kContinue) continue;
+        const uint32_t px = pxy & 0xFFFFu, py = pxy >> 16;
         if (phase == kPrimary) {
             const f3 dir = s.dir;
             if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
@@ -283,7 +232,7 @@ __global__ void __launch_bounds__(256, MINB) frame_persistent_kernel(const Frame
     // warp-reduce the GI ray count
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) gi_count += __shfl_down_sync(0xFFFFFFFFu, gi_count, o);
-    if (lane == 0 && gi_count) atomicAdd(&P.scratch->gi_rays, gi_count);
+    if (lane == 0 && gi_count) atomicAdd(&P.scratch->gi_rays, (unsigned long long)gi_count);
 }
 
 __global__ void secondary_kernel(const FrameParams P, const __grid_constant__ arc_camera_uniforms cam) {

@@ -1,0 +1,528 @@
+// arc_nrc.cu — neural radiance cache: fused tensor-core inference and training (sm_103a).
+//
+// No reference counterpart: the NRC stands in for SHARC's hashed lookup (query_sharc,
+// shaders/common/sharc_query.wgsl:138-146) at secondary hits.
+//
+// Network: 9 inputs (position in [0,1]^3, normal, view direction) -> sin/cos(2^k pi v), k = 0..11
+// (216 features, index = input*24 + 2k + {0 sin, 1 cos}) -> 5 x 64 ReLU -> 3 linear outputs, no
+// biases. FP32 master weights (compact, W[out][in] per layer) with FP16 copies in two padded
+// layouts: forward W[out][in_pad] and transposed WT[in][out_pad] for the backward pass. Activations
+// move between layers in registers: the m16n8k16 accumulator fragment of two adjacent 8-column tiles
+// is exactly the A fragment of the next layer's 16-wide k step, so ReLU + FP16 packing is all the
+// conversion a layer needs. Products run on mma.sync.m16n8k16.f32.f16.f16.f32 (FP32 accumulation).
+//
+// Training (one fused kernel per batch): a CTA of 4 warps takes 64 samples at a time; each warp runs
+// the forward pass for 16 samples and stores the transposed activations in shared memory; the backward
+// pass runs layer by layer (dZ in registers, dZ^T in a double-buffered shared tile), and after each
+// layer all warps compute that layer's weight-gradient tiles dW = dZ^T A over the 64 samples on the
+// tensor cores and add them to the FP32 gradient with red.global.add.v2.f32. A loss scale of 128 keeps
+// the FP16 gradients in range; Adam divides it out.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "arc_ctx.h"
+
+namespace nrc {
+
+constexpr int kIn = 9, kEnc = 216, kEncPad = 224, kW = 64, kOut = 3;
+constexpr int kParams = kEnc * kW + 4 * kW * kW + kOut * kW;  // 30400
+// compact FP32 master offsets per layer
+__host__ __device__ constexpr int off(int l) { return l == 0 ? 0 : (l == 6 ? kParams : kEnc * kW + (l - 1) * kW * kW); }
+// FP16 forward layout W[out][in_pad]
+constexpr int kS1 = 232, kS = 72;
+constexpr int kF1 = 0, kF2 = 64 * kS1;  // layer 2..5 at kF2 + (l-2)*64*kS
+constexpr int kF6 = kF2 + 4 * 64 * kS;
+constexpr int kFwdHalves = kF6 + 8 * kS;  // 33856
+// FP16 transposed layout WT[in][out_pad] (layers 2..6)
+constexpr int kST6 = 24;
+constexpr int kT2 = kFwdHalves;
+constexpr int kT6 = kT2 + 4 * 64 * kS;
+constexpr int kAllHalves = kT6 + 64 * kST6;  // 53824
+constexpr float kLossScale = 128.0f;
+// training activations (per CTA of 64 samples; sample stride kSS)
+constexpr int kSS = 72;
+constexpr int kXT = 0;                       // [224][kSS]
+constexpr int kHT = kXT + kEncPad * kSS;     // 5 x [64][kSS]
+constexpr int kDZ = kHT + 5 * 64 * kSS;      // 2 x [64][kSS]
+constexpr int kActHalves = kDZ + 2 * 64 * kSS;
+
+__host__ __device__ constexpr int fwd_off(int l) { return l == 1 ? kF1 : (l <= 5 ? kF2 + (l - 2) * 64 * kS : kF6); }
+__host__ __device__ constexpr int fwd_stride(int l) { return l == 1 ? kS1 : kS; }
+
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack_h2(float lo, float hi) {
+    __half2 h = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+__device__ __forceinline__ uint32_t lds32(const __half* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+__device__ __forceinline__ void red_add2(float* p, float a, float b) {
+    asm volatile("red.global.add.v2.f32 [%0], {%1, %2};\n" ::"l"(p), "f"(a), "f"(b) : "memory");
+}
+
+// Encoded features (f, f+1) = (sin, cos)(2^k pi v) of the even feature index f.
+__device__ __forceinline__ uint32_t enc_pair(const float (&v)[kIn], int f) {
+    if (f >= kEnc) return 0u;
+    const int i = f / 24, k = (f % 24) >> 1;
+    float x = v[0];
+#pragma unroll
+    for (int q = 1; q < kIn; ++q) x = (i == q) ? v[q] : x;  // register select, no local-memory indexing
+    float s, c;
+    sincospif(ldexpf(x, k), &s, &c);
+    return pack_h2(s, c);
+}
+
+// Layer with K = 64 from A fragments held in registers: acc[nt] += A * W_l^T (8 output tiles).
+__device__ __forceinline__ void layer64(const __half* sw, int l, const uint32_t (&a)[4][4], float (&acc)[8][4], int gid,
+                                        int tig) {
+    const __half* W = sw + fwd_off(l);
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+        const __half* row = W + (nt * 8 + gid) * kS + 2 * tig;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) mma16816(acc[nt], a[j], lds32(row + 16 * j), lds32(row + 16 * j + 8));
+    }
+}
+
+__device__ __forceinline__ void relu_to_a(const float (&acc)[8][4], uint32_t (&a)[4][4]) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        a[j][0] = pack_h2(fmaxf(acc[2 * j][0], 0.0f), fmaxf(acc[2 * j][1], 0.0f));
+        a[j][1] = pack_h2(fmaxf(acc[2 * j][2], 0.0f), fmaxf(acc[2 * j][3], 0.0f));
+        a[j][2] = pack_h2(fmaxf(acc[2 * j + 1][0], 0.0f), fmaxf(acc[2 * j + 1][1], 0.0f));
+        a[j][3] = pack_h2(fmaxf(acc[2 * j + 1][2], 0.0f), fmaxf(acc[2 * j + 1][3], 0.0f));
+    }
+}
+
+__device__ __forceinline__ void load_inputs(const float* __restrict__ in, uint32_t n, uint32_t row, float (&v)[kIn]) {
+#pragma unroll
+    for (int i = 0; i < kIn; ++i) v[i] = row < n ? __ldg(&in[(size_t)row * kIn + i]) : 0.0f;
+}
+
+// Forward of one warp's 16 rows up to the output tile (acc6), optionally storing transposed activations.
+template <bool kStore>
+__device__ __forceinline__ void forward16(const __half* sw, __half* act, const float (&v0)[kIn], const float (&v1)[kIn],
+                                          int gid, int tig, int s0, float (&acc6)[4]) {
+    float acc[8][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+    for (int j = 0; j < kEncPad / 16; ++j) {
+        uint32_t a[4];
+        const int f = 16 * j + 2 * tig;
+        a[0] = enc_pair(v0, f);
+        a[1] = enc_pair(v1, f);
+        a[2] = enc_pair(v0, f + 8);
+        a[3] = enc_pair(v1, f + 8);
+        if (kStore) {
+            __half* x = act + kXT;
+            const __half2 p0 = *reinterpret_cast<__half2*>(&a[0]), p1 = *reinterpret_cast<__half2*>(&a[1]);
+            const __half2 p2 = *reinterpret_cast<__half2*>(&a[2]), p3 = *reinterpret_cast<__half2*>(&a[3]);
+            x[f * kSS + s0 + gid] = p0.x;
+            x[(f + 1) * kSS + s0 + gid] = p0.y;
+            x[f * kSS + s0 + gid + 8] = p1.x;
+            x[(f + 1) * kSS + s0 + gid + 8] = p1.y;
+            x[(f + 8) * kSS + s0 + gid] = p2.x;
+            x[(f + 9) * kSS + s0 + gid] = p2.y;
+            x[(f + 8) * kSS + s0 + gid + 8] = p3.x;
+            x[(f + 9) * kSS + s0 + gid + 8] = p3.y;
+        }
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const __half* row = sw + kF1 + (nt * 8 + gid) * kS1 + 16 * j + 2 * tig;
+            mma16816(acc[nt], a, lds32(row), lds32(row + 8));
+        }
+    }
+    uint32_t a[4][4];
+    for (int l = 2; l <= 6; ++l) {
+        relu_to_a(acc, a);
+        if (kStore) {  // A_{l-1}^T
+            __half* h = act + kHT + (l - 2) * 64 * kSS;
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                const int c = nt * 8 + 2 * tig;
+                const uint32_t lo = a[nt >> 1][(nt & 1) * 2], hi = a[nt >> 1][(nt & 1) * 2 + 1];
+                const __half2 p = *reinterpret_cast<const __half2*>(&lo), q = *reinterpret_cast<const __half2*>(&hi);
+                h[c * kSS + s0 + gid] = p.x;
+                h[(c + 1) * kSS + s0 + gid] = p.y;
+                h[c * kSS + s0 + gid + 8] = q.x;
+                h[(c + 1) * kSS + s0 + gid + 8] = q.y;
+            }
+        }
+        if (l < 6) {
+            layer64(sw, l, a, acc, gid, tig);
+        } else {
+            acc6[0] = acc6[1] = acc6[2] = acc6[3] = 0.0f;
+            const __half* row = sw + kF6 + gid * kS + 2 * tig;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) mma16816(acc6, a[j], lds32(row + 16 * j), lds32(row + 16 * j + 8));
+        }
+    }
+}
+
+__device__ __forceinline__ void load_weights_smem(__half* sw, const __half* __restrict__ w16, int halves) {
+    const uint4* src = reinterpret_cast<const uint4*>(w16);
+    uint4* dst = reinterpret_cast<uint4*>(sw);
+    for (int i = threadIdx.x; i < halves / 8; i += blockDim.x) dst[i] = src[i];
+}
+
+__global__ void __launch_bounds__(128) infer_kernel(const __half* __restrict__ w16, const float* __restrict__ in,
+                                                    uint32_t n, float* __restrict__ out) {
+    extern __shared__ __align__(16) __half smem[];
+    load_weights_smem(smem, w16, kFwdHalves);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
+    const uint32_t warps = blockDim.x >> 5, tiles = (n + 15u) / 16u;
+    for (uint32_t t = blockIdx.x * warps + (threadIdx.x >> 5); t < tiles; t += gridDim.x * warps) {
+        const uint32_t r0 = t * 16u + gid, r1 = r0 + 8u;
+        float v0[kIn], v1[kIn], y[4];
+        load_inputs(in, n, r0, v0);
+        load_inputs(in, n, r1, v1);
+        forward16<false>(smem, nullptr, v0, v1, gid, tig, 0, y);
+        // output tile columns 2*tig, 2*tig+1 (valid: 0..2)
+        if (tig == 0) {
+            if (r0 < n) { out[r0 * 3] = y[0]; out[r0 * 3 + 1] = y[1]; }
+            if (r1 < n) { out[r1 * 3] = y[2]; out[r1 * 3 + 1] = y[3]; }
+        } else if (tig == 1) {
+            if (r0 < n) out[r0 * 3 + 2] = y[0];
+            if (r1 < n) out[r1 * 3 + 2] = y[2];
+        }
+    }
+}
+
+// dW_l tiles over the CTA's 64 samples: D[m][n] = sum_s dZT[m][s] * AT[n][s]; m < mrows, n < ncols.
+__device__ __forceinline__ void weight_grad(const __half* dzt, const __half* at, int mtiles, int ntiles, int mrows,
+                                            int ncols, float* __restrict__ g, int warp, int gid, int tig) {
+    const int tiles = mtiles * ntiles;
+    for (int tt = warp; tt < tiles; tt += 4) {
+        const int mt = tt / ntiles, nt = tt % ntiles;
+        float d[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {
+            uint32_t a[4];
+            const __half* ar = dzt + (mt * 16 + gid) * kSS + ks * 16 + 2 * tig;
+            a[0] = lds32(ar);
+            a[1] = lds32(ar + 8 * kSS);
+            a[2] = lds32(ar + 8);
+            a[3] = lds32(ar + 8 * kSS + 8);
+            const __half* br = at + (nt * 8 + gid) * kSS + ks * 16 + 2 * tig;
+            mma16816(d, a, lds32(br), lds32(br + 8));
+        }
+        const int m0 = mt * 16 + gid, n0 = nt * 8 + 2 * tig;
+        if (n0 < ncols) {
+            if (m0 < mrows) red_add2(&g[m0 * ncols + n0], d[0], d[1]);
+            if (m0 + 8 < mrows) red_add2(&g[(m0 + 8) * ncols + n0], d[2], d[3]);
+        }
+    }
+}
+
+// Stores a 16x64 tile of dZ (C fragments) transposed into dzt and returns its A fragments.
+__device__ __forceinline__ void store_dz(const float (&dz)[8][4], __half* dzt, int s0, int gid, int tig, uint32_t (&a)[4][4]) {
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        const int c = nt * 8 + 2 * tig;
+        dzt[c * kSS + s0 + gid] = __float2half_rn(dz[nt][0]);
+        dzt[(c + 1) * kSS + s0 + gid] = __float2half_rn(dz[nt][1]);
+        dzt[c * kSS + s0 + gid + 8] = __float2half_rn(dz[nt][2]);
+        dzt[(c + 1) * kSS + s0 + gid + 8] = __float2half_rn(dz[nt][3]);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        a[j][0] = pack_h2(dz[2 * j][0], dz[2 * j][1]);
+        a[j][1] = pack_h2(dz[2 * j][2], dz[2 * j][3]);
+        a[j][2] = pack_h2(dz[2 * j + 1][0], dz[2 * j + 1][1]);
+        a[j][3] = pack_h2(dz[2 * j + 1][2], dz[2 * j + 1][3]);
+    }
+}
+
+// dA_{l-1} = dZ_l W_l (B from WT_l), masked by A_{l-1} > 0 read from its transposed tile.
+__device__ __forceinline__ void backward64(const __half* sw, int l, const uint32_t (&a)[4][4], const __half* at_prev,
+                                           int s0, int gid, int tig, float (&dz)[8][4]) {
+    const __half* WT = sw + kT2 + (l - 2) * 64 * kS;
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        dz[nt][0] = dz[nt][1] = dz[nt][2] = dz[nt][3] = 0.0f;
+        const __half* row = WT + (nt * 8 + gid) * kS + 2 * tig;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) mma16816(dz[nt], a[j], lds32(row + 16 * j), lds32(row + 16 * j + 8));
+        const int c = nt * 8 + 2 * tig;
+        if (!(__half2float(at_prev[c * kSS + s0 + gid]) > 0.0f)) dz[nt][0] = 0.0f;
+        if (!(__half2float(at_prev[(c + 1) * kSS + s0 + gid]) > 0.0f)) dz[nt][1] = 0.0f;
+        if (!(__half2float(at_prev[c * kSS + s0 + gid + 8]) > 0.0f)) dz[nt][2] = 0.0f;
+        if (!(__half2float(at_prev[(c + 1) * kSS + s0 + gid + 8]) > 0.0f)) dz[nt][3] = 0.0f;
+    }
+}
+
+__global__ void __launch_bounds__(128) train_kernel(const __half* __restrict__ w16, const float* __restrict__ in,
+                                                    const float* __restrict__ target, uint32_t n, float inv_norm,
+                                                    float* __restrict__ grad, float* __restrict__ loss_sum) {
+    extern __shared__ __align__(16) __half smem[];
+    __half* sw = smem;                      // forward + transposed weights
+    __half* act = smem + kAllHalves;        // XT, HT1..5, dZT x2
+    load_weights_smem(sw, w16, kAllHalves);
+    const int lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3, warp = threadIdx.x >> 5;
+    const int s0 = warp * 16;
+    const uint32_t tiles = (n + 63u) / 64u;
+    float my_loss = 0.0f;
+    __syncthreads();
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const uint32_t r0 = tile * 64u + s0 + gid, r1 = r0 + 8u;
+        float v0[kIn], v1[kIn], y[4];
+        load_inputs(in, n, r0, v0);
+        load_inputs(in, n, r1, v1);
+        forward16<true>(sw, act, v0, v1, gid, tig, s0, y);
+        // relative L2: dL/dy = 2 (y - t) / (y^2 + 0.01) / N, scaled; cols 2*tig, 2*tig+1 of rows r0, r1
+        float dy[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int col = 2 * tig + (e & 1);
+            const uint32_t r = e < 2 ? r0 : r1;
+            if (col < kOut && r < n) {
+                const float t = __ldg(&target[(size_t)r * 3 + col]);
+                const float den = y[e] * y[e] + 0.01f;
+                my_loss += (y[e] - t) * (y[e] - t) / den;
+                dy[e] = 2.0f * (y[e] - t) / den * inv_norm * kLossScale;
+            }
+        }
+        // layer 6: dZ6 = dY (16 x 3, K padded to 16) -> dZT6 in buffer 0 (rows 0..15)
+        __half* dzt0 = act + kDZ;
+        __half* dzt1 = act + kDZ + 64 * kSS;
+        {
+            const int c = 2 * tig;
+            // rows 0..7 of dZT6 hold outputs 0..7 (only 0..2 non-zero); write all 8 so padding is zero
+            dzt0[c * kSS + s0 + gid] = __float2half_rn(dy[0]);
+            dzt0[(c + 1) * kSS + s0 + gid] = __float2half_rn(dy[1]);
+            dzt0[c * kSS + s0 + gid + 8] = __float2half_rn(dy[2]);
+            dzt0[(c + 1) * kSS + s0 + gid + 8] = __float2half_rn(dy[3]);
+            dzt0[(c + 8) * kSS + s0 + gid] = __float2half_rn(0.0f);
+            dzt0[(c + 9) * kSS + s0 + gid] = __float2half_rn(0.0f);
+            dzt0[(c + 8) * kSS + s0 + gid + 8] = __float2half_rn(0.0f);
+            dzt0[(c + 9) * kSS + s0 + gid + 8] = __float2half_rn(0.0f);
+        }
+        uint32_t a6[4] = {pack_h2(dy[0], dy[1]), pack_h2(dy[2], dy[3]), 0u, 0u};
+        float dz[8][4];
+        {
+            // dA5 = dZ6 W6 (B = WT6[in][out_pad 16]), masked by A5 > 0
+            const __half* at5 = act + kHT + 4 * 64 * kSS;
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                dz[nt][0] = dz[nt][1] = dz[nt][2] = dz[nt][3] = 0.0f;
+                const __half* row = sw + kT6 + (nt * 8 + gid) * kST6 + 2 * tig;
+                mma16816(dz[nt], a6, lds32(row), lds32(row + 8));
+                const int c = nt * 8 + 2 * tig;
+                if (!(__half2float(at5[c * kSS + s0 + gid]) > 0.0f)) dz[nt][0] = 0.0f;
+                if (!(__half2float(at5[(c + 1) * kSS + s0 + gid]) > 0.0f)) dz[nt][1] = 0.0f;
+                if (!(__half2float(at5[c * kSS + s0 + gid + 8]) > 0.0f)) dz[nt][2] = 0.0f;
+                if (!(__half2float(at5[(c + 1) * kSS + s0 + gid + 8]) > 0.0f)) dz[nt][3] = 0.0f;
+            }
+        }
+        __syncthreads();
+        weight_grad(dzt0, act + kHT + 4 * 64 * kSS, 1, 8, kOut, kW, grad + off(5), warp, gid, tig);
+        // layers 5..1
+        for (int l = 5; l >= 1; --l) {
+            __half* dzt = (l & 1) ? dzt1 : dzt0;
+            uint32_t a[4][4];
+            store_dz(dz, dzt, s0, gid, tig, a);
+            if (l > 1) backward64(sw, l, a, act + kHT + (l - 2) * 64 * kSS, s0, gid, tig, dz);
+            __syncthreads();
+            if (l > 1) weight_grad(dzt, act + kHT + (l - 2) * 64 * kSS, 4, 8, kW, kW, grad + off(l - 1), warp, gid, tig);
+            else weight_grad(dzt, act + kXT, 4, 28, kW, kEnc, grad + off(0), warp, gid, tig);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) my_loss += __shfl_down_sync(0xFFFFFFFFu, my_loss, o);
+    if (lane == 0) atomicAdd(loss_sum, my_loss);
+}
+
+// Adam on the FP32 masters, then refresh both FP16 layouts.
+__global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
+                            const float* __restrict__ g, __half* __restrict__ w16, float lr, float c1, float c2,
+                            float inv_scale) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kParams) return;
+    const float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
+    const float gi = g[i] * inv_scale;
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] = wi;
+    int l = 0;
+    while (i >= off(l + 1)) ++l;
+    const int din = l == 0 ? kEnc : kW, local = i - off(l), o = local / din, k = local % din;
+    const __half h = __float2half_rn(wi);
+    w16[fwd_off(l + 1) + o * fwd_stride(l + 1) + k] = h;
+    if (l >= 1 && l <= 4) w16[kT2 + (l - 1) * 64 * kS + k * kS + o] = h;
+    if (l == 5) w16[kT6 + k * kST6 + o] = h;
+}
+
+// FP16 layouts from the masters (used after init / set_weights; padding stays zero).
+__global__ void pack_kernel(const float* __restrict__ w, __half* __restrict__ w16) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kParams) return;
+    int l = 0;
+    while (i >= off(l + 1)) ++l;
+    const int din = l == 0 ? kEnc : kW, local = i - off(l), o = local / din, k = local % din;
+    const __half h = __float2half_rn(w[i]);
+    w16[fwd_off(l + 1) + o * fwd_stride(l + 1) + k] = h;
+    if (l >= 1 && l <= 4) w16[kT2 + (l - 1) * 64 * kS + k * kS + o] = h;
+    if (l == 5) w16[kT6 + k * kST6 + o] = h;
+}
+
+}  // namespace nrc
+
+// ------------------------------------------------------------------------------------------------
+// C ABI
+// ------------------------------------------------------------------------------------------------
+
+namespace {
+
+int nrc_err(arc_ctx* c, int code, const std::string& m) {
+    c->err = m;
+    return code;
+}
+
+int nrc_cuda(arc_ctx* c, cudaError_t e, const char* what) {
+    return nrc_err(c, ARC_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define NRC_CK(expr)                                        \
+    do {                                                    \
+        cudaError_t e__ = (expr);                           \
+        if (e__ != cudaSuccess) return nrc_cuda(c, e__, #expr); \
+    } while (0)
+
+int ensure_nrc(arc_ctx* c) {
+    if (c->d_nrc_w32) return ARC_OK;
+    NRC_CK(cudaMalloc((void**)&c->d_nrc_w32, sizeof(float) * nrc::kParams * 4));
+    c->d_nrc_m = c->d_nrc_w32 + nrc::kParams;
+    c->d_nrc_v = c->d_nrc_m + nrc::kParams;
+    c->d_nrc_grad = c->d_nrc_v + nrc::kParams;
+    NRC_CK(cudaMalloc(&c->d_nrc_w16, sizeof(__half) * nrc::kAllHalves));
+    NRC_CK(cudaMalloc((void**)&c->d_nrc_loss, sizeof(float)));
+    NRC_CK(cudaMemsetAsync(c->d_nrc_w32, 0, sizeof(float) * nrc::kParams * 4, c->stream));
+    NRC_CK(cudaMemsetAsync(c->d_nrc_w16, 0, sizeof(__half) * nrc::kAllHalves, c->stream));
+    NRC_CK(cudaFuncSetAttribute(nrc::infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                nrc::kFwdHalves * (int)sizeof(__half)));
+    NRC_CK(cudaFuncSetAttribute(nrc::train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (nrc::kAllHalves + nrc::kActHalves) * (int)sizeof(__half)));
+    c->nrc_step = 0;
+    return ARC_OK;
+}
+
+// Uniform(-sqrt(6/fan_in), sqrt(6/fan_in)) from a splitmix64 stream (He-uniform for the ReLU layers).
+void init_weights(std::vector<float>& w, uint32_t seed) {
+    uint64_t s = 0x9E3779B97F4A7C15ull ^ seed;
+    auto next = [&]() {
+        uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    for (int l = 0; l < 6; ++l) {
+        const int din = l == 0 ? nrc::kEnc : nrc::kW;
+        const float bound = std::sqrt(6.0f / (float)din);
+        for (int i = nrc::off(l); i < nrc::off(l + 1); ++i) {
+            const float u = (float)((next() >> 40) * (1.0 / 16777216.0));
+            w[i] = (2.0f * u - 1.0f) * bound;
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int arc_nrc_init(arc_ctx* c, uint32_t seed) {
+    if (!c) return ARC_E_INVALID_ARG;
+    int rc = ensure_nrc(c);
+    if (rc) return rc;
+    std::vector<float> w(nrc::kParams);
+    init_weights(w, seed);
+    return arc_nrc_set_weights(c, w.data());
+}
+
+int arc_nrc_set_weights(arc_ctx* c, const float* w) {
+    if (!c || !w) return ARC_E_INVALID_ARG;
+    int rc = ensure_nrc(c);
+    if (rc) return rc;
+    NRC_CK(cudaMemcpyAsync(c->d_nrc_w32, w, sizeof(float) * nrc::kParams, cudaMemcpyHostToDevice, c->stream));
+    NRC_CK(cudaMemsetAsync(c->d_nrc_m, 0, sizeof(float) * nrc::kParams * 2, c->stream));
+    nrc::pack_kernel<<<(nrc::kParams + 255) / 256, 256, 0, c->stream>>>(c->d_nrc_w32, static_cast<__half*>(c->d_nrc_w16));
+    NRC_CK(cudaGetLastError());
+    c->nrc_step = 0;
+    return arc_ctx_finish(c);
+}
+
+int arc_nrc_get_weights(arc_ctx* c, float* w) {
+    if (!c || !w) return ARC_E_INVALID_ARG;
+    int rc = ensure_nrc(c);
+    if (rc) return rc;
+    NRC_CK(cudaMemcpyAsync(w, c->d_nrc_w32, sizeof(float) * nrc::kParams, cudaMemcpyDeviceToHost, c->stream));
+    return arc_ctx_finish(c);
+}
+
+int arc_nrc_query_dev(arc_ctx* c, const float* inputs, uint32_t n, float* out) {
+    if (!c) return ARC_E_INVALID_ARG;
+    if (n && (!inputs || !out)) return nrc_err(c, ARC_E_INVALID_ARG, "null buffer");
+    int rc = ensure_nrc(c);
+    if (rc || n == 0) return rc;
+    const uint32_t tiles = (n + 15u) / 16u;
+    const uint32_t blocks = std::min<uint32_t>((tiles + 3u) / 4u, (uint32_t)c->n_sm * 3u);
+    nrc::infer_kernel<<<blocks, 128, nrc::kFwdHalves * sizeof(__half), c->stream>>>(static_cast<const __half*>(c->d_nrc_w16), inputs, n, out);
+    NRC_CK(cudaGetLastError());
+    return ARC_OK;
+}
+
+// Loss-scaled gradient of one batch into d_nrc_grad (zeroed first); exposed for the gradient check.
+int arc_nrc_grad_dev(arc_ctx* c, const float* inputs, const float* targets, uint32_t n, float* grad_out) {
+    if (!c || !inputs || !targets || n == 0) return ARC_E_INVALID_ARG;
+    int rc = ensure_nrc(c);
+    if (rc) return rc;
+    NRC_CK(cudaMemsetAsync(c->d_nrc_grad, 0, sizeof(float) * nrc::kParams, c->stream));
+    NRC_CK(cudaMemsetAsync(c->d_nrc_loss, 0, sizeof(float), c->stream));
+    const uint32_t tiles = (n + 63u) / 64u;
+    const uint32_t blocks = std::min<uint32_t>(tiles, (uint32_t)c->n_sm);
+    nrc::train_kernel<<<blocks, 128, (nrc::kAllHalves + nrc::kActHalves) * sizeof(__half), c->stream>>>(
+        static_cast<const __half*>(c->d_nrc_w16), inputs, targets, n, 1.0f / (float)n, c->d_nrc_grad, c->d_nrc_loss);
+    NRC_CK(cudaGetLastError());
+    if (grad_out)
+        NRC_CK(cudaMemcpyAsync(grad_out, c->d_nrc_grad, sizeof(float) * nrc::kParams, cudaMemcpyDeviceToDevice, c->stream));
+    return ARC_OK;
+}
+
+int arc_nrc_train_step_dev(arc_ctx* c, const float* inputs, const float* targets, uint32_t n, float lr, float* loss_host) {
+    int rc = arc_nrc_grad_dev(c, inputs, targets, n, nullptr);
+    if (rc) return rc;
+    c->nrc_step += 1;
+    const float c1 = 1.0f - std::pow(0.9f, (float)c->nrc_step), c2 = 1.0f - std::pow(0.99f, (float)c->nrc_step);
+    nrc::adam_kernel<<<(nrc::kParams + 255) / 256, 256, 0, c->stream>>>(c->d_nrc_w32, c->d_nrc_m, c->d_nrc_v,
+                                                                       c->d_nrc_grad, static_cast<__half*>(c->d_nrc_w16), lr, c1, c2,
+                                                                       1.0f / nrc::kLossScale);
+    NRC_CK(cudaGetLastError());
+    if (loss_host) {
+        float l = 0.0f;
+        NRC_CK(cudaMemcpyAsync(&l, c->d_nrc_loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+        if ((rc = arc_ctx_finish(c))) return rc;
+        *loss_host = l / (float)n;
+    }
+    return ARC_OK;
+}
+
+}  // extern "C"

@@ -149,9 +149,44 @@ __device__ __forceinline__ Surface trace_surface(const World& w, const arc_camer
     return out;
 }
 
+// One-bounce radiance estimator of the cache comparison (sun directional light + constant sky, Lambertian):
+// L = albedo * (c_sun max(n.l, 0) V(x, l) + L_sky [cosine-sampled ray from x escapes within 64 m]),
+// c_sun = sun_power * (1, 0.9, 0.75) * 0.55 as in sharc_shade_surface. One sample per call.
+__device__ __forceinline__ f3 onebounce(const World& w, const arc_camera_uniforms& cam, f3 pos, f3 n, f3 albedo,
+                                        uint32_t seed) {
+    const f3 sun{cam.sun_dir_intensity[0], cam.sun_dir_intensity[1], cam.sun_dir_intensity[2]};
+    const float sun_power = cam.sun_dir_intensity[3];
+    const f3 o = add3(pos, mul3s(n, 0.10f));
+    f3 l{0.0f, 0.0f, 0.0f};
+    const float ndl = fmaxf(dot3(n, sun), 0.0f);
+    if (ndl > 0.001f && sun_power > 0.01f) {
+        const float k = ((sun_power * ndl) * shadow_vis(w, cam, o, sun, 32.0f)) * 0.55f;
+        l = f3{1.0f * k, 0.90f * k, 0.75f * k};
+    }
+    const uint32_t h1 = pcg_hash(seed), h2 = pcg_hash(h1 ^ 0x68E31DA4u);
+    const float u1 = (float)(h1 >> 8) * (1.0f / 16777216.0f), u2 = (float)(h2 >> 8) * (1.0f / 16777216.0f);
+    f3 t, b;
+    make_basis(n, &t, &b);
+    const f3 d = cosine_sample(u1, u2, n, t, b);
+    RayState s;
+    HitInfo hh;
+    StepResult r = kMiss;
+    if (ray_begin(s, cam, o, d, 0.0f, 64.0f, 2u, true)) {
+        do {
+            r = ray_advance(s, w, cam, hh);
+        } while (r == kContinue);
+    }
+    if (r != kHit) {
+        l.x += 0.30f;
+        l.y += 0.42f;
+        l.z += 0.60f;
+    }
+    return f3{albedo.x * l.x, albedo.y * l.y, albedo.z * l.z};
+}
+
 __global__ void sharc_update_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, const SharcBuffers S,
                                     const uint32_t* __restrict__ gdm, const uint32_t* __restrict__ gnm, uint32_t W,
-                                    uint32_t H) {
+                                    uint32_t H, uint32_t mode) {
     const uint32_t tile = (cam.quality_flags[3] & 0xFFu) <= 12u ? 16u : 8u;
     const uint32_t tiles_x = (W + tile - 1u) / tile, tiles_y = (H + tile - 1u) / tile;
     const uint32_t gx = blockIdx.x * blockDim.x + threadIdx.x, gy = blockIdx.y * blockDim.y + threadIdx.y;
@@ -179,6 +214,13 @@ __global__ void sharc_update_kernel(const World w, const __grid_constant__ arc_c
     const f3 d0 = cosine_sample(a0, a1, n0, t, b);
     const Surface s1 = trace_surface(w, cam, add3(x0, mul3s(n0, 0.10f)), d0, bounce_max);
     if (!s1.hit) return;
+    if (mode == 1u) {  // cache-comparison estimator instead of sharc_shade_surface
+        const f3 rad = onebounce(w, cam, s1.pos, s1.normal, s1.albedo, hsh ^ (frame * 0x9E3779B9u));
+        uint32_t bk, key;
+        sharc_key(s1.pos, s1.normal, eye, 0.0f, 0.0f, &bk, &key);
+        sharc_deposit(S, bk, key, rad);
+        return;
+    }
     // sharc_shade_surface (shaders/sharc_update.wgsl:68-105)
     const f3 n = s1.normal;
     f3 direct{0.0f, 0.0f, 0.0f};
@@ -276,6 +318,111 @@ __global__ void sharc_deposit_kernel(SharcBuffers S, f3 pos, f3 n, f3 cam, f3 ra
     sharc_deposit(S, b, k, rad);
 }
 
+// GI hit points of a frame: per pixel with a primary hit, the Pass-2A GI ray is traced again from the
+// G-buffer and its hit recorded as position, normal, SHARC surface albedo and the 9 NRC inputs
+// (position / world extent, normal, view direction = -ray direction).
+__global__ void gi_points_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, const uint32_t* __restrict__ gdm,
+                                 const uint32_t* __restrict__ gnm, uint32_t W, uint32_t H, float* __restrict__ pos,
+                                 float* __restrict__ nrm, float* __restrict__ alb, float* __restrict__ nrc_in,
+                                 uint32_t* __restrict__ valid, unsigned long long* __restrict__ n_valid) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const size_t k = (size_t)y * W + x;
+    f3 o, d;
+    uint32_t ok = 0u;
+    if (gi_setup(w, cam, x, y, W, H, gdm[2 * k], gnm[2 * k], &o, &d)) {
+        RayState s;
+        HitInfo h;
+        StepResult r = kMiss;
+        if (ray_begin(s, cam, o, d, 0.0f, cam.ray_distances[2], 2u, true)) {
+            do {
+                r = ray_advance(s, w, cam, h);
+            } while (r == kContinue);
+        }
+        if (r == kHit) {
+            ok = 1u;
+            const float4 a = __ldg(&w.palette[2u * h.mat]);
+            const float lr = __fdiv_rn((float)(h.lod_payload & 0xFFu), 255.0f);
+            const float lg = __fdiv_rn((float)((h.lod_payload >> 8) & 0xFFu), 255.0f);
+            const float lb = __fdiv_rn((float)((h.lod_payload >> 16) & 0xFFu), 255.0f);
+            pos[3 * k] = h.hit_pos_m.x;
+            pos[3 * k + 1] = h.hit_pos_m.y;
+            pos[3 * k + 2] = h.hit_pos_m.z;
+            nrm[3 * k] = h.normal.x;
+            nrm[3 * k + 1] = h.normal.y;
+            nrm[3 * k + 2] = h.normal.z;
+            alb[3 * k] = mixf(a.x, lr, 0.55f);
+            alb[3 * k + 1] = mixf(a.y, lg, 0.55f);
+            alb[3 * k + 2] = mixf(a.z, lb, 0.55f);
+            const float ex = (float)cam.world_grid_dims[0] * 16.0f, ey = (float)cam.world_grid_dims[1] * 16.0f,
+                        ez = (float)cam.world_grid_dims[2] * 16.0f;
+            float* q = nrc_in + 9 * k;
+            q[0] = __fdiv_rn(h.hit_pos_m.x, ex);
+            q[1] = __fdiv_rn(h.hit_pos_m.y, ey);
+            q[2] = __fdiv_rn(h.hit_pos_m.z, ez);
+            q[3] = h.normal.x;
+            q[4] = h.normal.y;
+            q[5] = h.normal.z;
+            q[6] = -d.x;
+            q[7] = -d.y;
+            q[8] = -d.z;
+        }
+    }
+    valid[k] = ok;
+    const uint32_t m = __ballot_sync(__activemask(), ok != 0u);
+    if (ok && (threadIdx.x + threadIdx.y * blockDim.x) % 32u == (uint32_t)(__ffs(m) - 1)) atomicAdd(n_valid, (unsigned long long)__popc(m));
+}
+
+__global__ void onebounce_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, const uint32_t* __restrict__ idx,
+                                 uint32_t n, const float* __restrict__ pos, const float* __restrict__ nrm,
+                                 const float* __restrict__ alb, uint32_t spp, uint32_t seed, uint32_t accumulate,
+                                 float* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t p = idx ? idx[i] : i;
+    const f3 x{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]}, nn{nrm[3 * p], nrm[3 * p + 1], nrm[3 * p + 2]};
+    const f3 a{alb[3 * p], alb[3 * p + 1], alb[3 * p + 2]};
+    f3 sum{0.0f, 0.0f, 0.0f};
+    for (uint32_t k = 0; k < spp; ++k) {
+        const f3 l = onebounce(w, cam, x, nn, a, pcg_hash(p * 0x9E3779B9u ^ pcg_hash(seed + k * 0x632BE5ABu)));
+        sum.x += l.x;
+        sum.y += l.y;
+        sum.z += l.z;
+    }
+    const float inv = __fdiv_rn(1.0f, (float)spp);
+    if (accumulate) {
+        out[3 * i] += sum.x * inv;
+        out[3 * i + 1] += sum.y * inv;
+        out[3 * i + 2] += sum.z * inv;
+    } else {
+        out[3 * i] = sum.x * inv;
+        out[3 * i + 1] = sum.y * inv;
+        out[3 * i + 2] = sum.z * inv;
+    }
+}
+
+// NRC training samples: every valid GI point is taken with probability accept (PCG per pixel and frame);
+// a taken point gets a slot from the counter (up to max_n) and a 1-spp one-bounce target.
+__global__ void train_samples_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, uint32_t n_px,
+                                     const uint32_t* __restrict__ valid, const float* __restrict__ pos,
+                                     const float* __restrict__ nrm, const float* __restrict__ alb,
+                                     const float* __restrict__ nrc_in, float accept, uint32_t seed, uint32_t max_n,
+                                     float* __restrict__ train_in, float* __restrict__ train_t, uint32_t* __restrict__ count) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_px || !valid[p]) return;
+    const uint32_t h = pcg_hash(p ^ pcg_hash(seed));
+    if ((float)(h >> 8) * (1.0f / 16777216.0f) >= accept) return;
+    const uint32_t slot = atomicAdd(count, 1u);
+    if (slot >= max_n) return;
+    const f3 l = onebounce(w, cam, f3{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]}, f3{nrm[3 * p], nrm[3 * p + 1], nrm[3 * p + 2]},
+                           f3{alb[3 * p], alb[3 * p + 1], alb[3 * p + 2]}, pcg_hash(h ^ 0xB5297A4Du));
+#pragma unroll
+    for (int k = 0; k < 9; ++k) train_in[(size_t)slot * 9 + k] = nrc_in[(size_t)p * 9 + k];
+    train_t[3 * slot] = l.x;
+    train_t[3 * slot + 1] = l.y;
+    train_t[3 * slot + 2] = l.z;
+}
+
 }  // namespace arc
 
 namespace {
@@ -332,8 +479,54 @@ int arc_sharc_update_dev(arc_ctx* c, uint32_t width, uint32_t height, const uint
     const uint32_t tile = (c->cam.quality_flags[3] & 0xFFu) <= 12u ? 16u : 8u;
     const uint32_t tx = (width + tile - 1u) / tile, ty = (height + tile - 1u) / tile;
     dim3 block(8, 8), grid((tx + 7u) / 8u, (ty + 7u) / 8u);
-    arc::sharc_update_kernel<<<grid, block, 0, c->stream>>>(c->world(), c->cam, bufs(c), gdm, gnm, width, height);
+    arc::sharc_update_kernel<<<grid, block, 0, c->stream>>>(c->world(), c->cam, bufs(c), gdm, gnm, width, height,
+                                                            c->sharc_mode);
     return launch_check(c, "sharc_update_kernel");
+}
+
+int arc_sharc_set_mode(arc_ctx* c, uint32_t mode) {
+    if (!c || mode > 1u) return ARC_E_INVALID_ARG;
+    c->sharc_mode = mode;
+    return ARC_OK;
+}
+
+int arc_gi_points_dev(arc_ctx* c, uint32_t width, uint32_t height, const uint32_t* gdm, const uint32_t* gnm, float* pos,
+                      float* nrm, float* albedo, float* nrc_in, uint32_t* valid, uint64_t* n_valid) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if (!gdm || !gnm || !pos || !nrm || !albedo || !nrc_in || !valid || !n_valid) return sharc_err(c, ARC_E_INVALID_ARG, "null buffer");
+    if ((c->cam.world_grid_dims[3] & 0xFFFFu) != width || (c->cam.world_grid_dims[3] >> 16) != height)
+        return sharc_err(c, ARC_E_INVALID_ARG, "frame size differs from camera world_grid_dims.w");
+    cudaMemsetAsync(n_valid, 0, sizeof(uint64_t), c->stream);
+    dim3 block(8, 8), grid((width + 7u) / 8u, (height + 7u) / 8u);
+    arc::gi_points_kernel<<<grid, block, 0, c->stream>>>(c->world(), c->cam, gdm, gnm, width, height, pos, nrm, albedo,
+                                                         nrc_in, valid, reinterpret_cast<unsigned long long*>(n_valid));
+    return launch_check(c, "gi_points_kernel");
+}
+
+int arc_onebounce_dev(arc_ctx* c, const uint32_t* idx, uint32_t n, const float* pos, const float* nrm, const float* albedo,
+                      uint32_t spp, uint32_t seed, int accumulate, float* out) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if (n == 0) return ARC_OK;
+    if (!pos || !nrm || !albedo || !out || spp == 0) return sharc_err(c, ARC_E_INVALID_ARG, "null buffer or spp 0");
+    arc::onebounce_kernel<<<(n + 127u) / 128u, 128, 0, c->stream>>>(c->world(), c->cam, idx, n, pos, nrm, albedo, spp, seed,
+                                                                     accumulate ? 1u : 0u, out);
+    return launch_check(c, "onebounce_kernel");
+}
+
+int arc_nrc_train_samples_dev(arc_ctx* c, uint32_t n_px, const uint32_t* valid, const float* pos, const float* nrm,
+                              const float* albedo, const float* nrc_in, float accept, uint32_t seed, uint32_t max_n,
+                              float* train_in, float* train_t, uint32_t* count) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if (!valid || !pos || !nrm || !albedo || !nrc_in || !train_in || !train_t || !count) return sharc_err(c, ARC_E_INVALID_ARG, "null buffer");
+    cudaMemsetAsync(count, 0, sizeof(uint32_t), c->stream);
+    if (n_px == 0) return ARC_OK;
+    arc::train_samples_kernel<<<(n_px + 127u) / 128u, 128, 0, c->stream>>>(c->world(), c->cam, n_px, valid, pos, nrm, albedo,
+                                                                            nrc_in, accept, seed, max_n, train_in, train_t,
+                                                                            count);
+    return launch_check(c, "train_samples_kernel");
 }
 
 int arc_sharc_resolve(arc_ctx* c) {

@@ -79,8 +79,7 @@ enum StepResult : uint32_t { kContinue = 0u, kHit = 1u, kMiss = 2u };
 struct RayState {
     f3 vo;    // origin, voxel units
     f3 dir;   // unit direction as given
-    f3 inv;   // 1 / safe_dir
-    f3 noi;   // -vo * inv
+    f3 inv;   // 1 / safe_dir (-vo * inv, the reference's neg_orig_inv, is recomputed where used: same bits)
     float t, t_limit;
     uint32_t vx, vy, vz;
     uint32_t px, py, pz;      // previous vi
@@ -88,9 +87,19 @@ struct RayState {
     uint32_t mtf_root0, mtf_root1;
     uint4 l1, l2, l3;         // ancestor restart cache (levels shift 4, 2, 0)
     uint32_t cached_shift;
-    uint32_t step, max_steps;
+    uint32_t step;
     uint32_t mode;            // lod_bias | ignore_water << 2
 };
+
+__device__ __forceinline__ float noi_x(const RayState& s) { return -s.vo.x * s.inv.x; }
+__device__ __forceinline__ float noi_y(const RayState& s) { return -s.vo.y * s.inv.y; }
+__device__ __forceinline__ float noi_z(const RayState& s) { return -s.vo.z * s.inv.z; }
+
+// Step budget of the ray class (traversal64.wgsl:262-267).
+__device__ __forceinline__ uint32_t max_steps_of(const arc_camera_uniforms& cam, uint32_t mode) {
+    const uint32_t lod_bias = mode & 3u;
+    return lod_bias == 0u ? cam.ray_steps[0] : (lod_bias == 1u ? cam.ray_steps[1] : cam.ray_steps[2]);
+}
 
 struct HitInfo {
     float t_voxels;   // accurate plane-entry distance (voxels)
@@ -144,8 +153,6 @@ __device__ __forceinline__ bool ray_begin(RayState& s, const arc_camera_uniforms
     if (w_exit < t_enter || t_enter >= max_t_v) return false;
     s.t = t_enter;
     s.t_limit = fminf(w_exit, max_t_v);
-    s.max_steps = lod_bias == 0u ? cam.ray_steps[0] : (lod_bias == 1u ? cam.ray_steps[1] : cam.ray_steps[2]);
-    s.noi = f3{-s.vo.x * s.inv.x, -s.vo.y * s.inv.y, -s.vo.z * s.inv.z};
     float st = s.t + 1e-4f;
     s.vx = f2u(clampf(s.vo.x + dir.x * st, 0.0f, wx - 1e-3f));
     s.vy = f2u(clampf(s.vo.y + dir.y * st, 0.0f, wy - 1e-3f));
@@ -164,9 +171,9 @@ __device__ __forceinline__ bool ray_begin(RayState& s, const arc_camera_uniforms
 __device__ __forceinline__ void step_box(RayState& s, uint32_t bx, uint32_t by, uint32_t bz, uint32_t span) {
     const bool pxd = s.inv.x >= 0.0f, pyd = s.inv.y >= 0.0f, pzd = s.inv.z >= 0.0f;
     uint32_t ex = pxd ? bx + span : bx, ey = pyd ? by + span : by, ez = pzd ? bz + span : bz;
-    float tx = (float)ex * s.inv.x + s.noi.x;
-    float ty = (float)ey * s.inv.y + s.noi.y;
-    float tz = (float)ez * s.inv.z + s.noi.z;
+    float tx = (float)ex * s.inv.x + noi_x(s);
+    float ty = (float)ey * s.inv.y + noi_y(s);
+    float tz = (float)ez * s.inv.z + noi_z(s);
     float t_exit = fminf(fminf(tx, ty), tz);
     float next_t = fmaxf(s.t, t_exit);
     bool is_x = tx <= ty && tx <= tz;
@@ -210,10 +217,68 @@ __device__ __forceinline__ float leaf_ao(uint32_t lo, uint32_t hi, uint32_t cx, 
     return clampf(1.0f - occ, 0.35f, 1.0f);
 }
 
+// Hit resolution of a solid cell (traversal64.wgsl:467-521): accurate entry distance, tie-broken
+// face normal, voxel hash and contact AO. It has a single call site in ray_advance.
+__device__ __forceinline__ void resolve_hit(const RayState& s, const arc_camera_uniforms& cam, uint4 node, uint32_t mat,
+                                         uint32_t bx, uint32_t by, uint32_t bz, uint32_t span, uint32_t shift, uint32_t b,
+                                         HitInfo& h) {
+    const bool pxd = s.inv.x >= 0.0f, pyd = s.inv.y >= 0.0f, pzd = s.inv.z >= 0.0f;
+    const uint32_t ex = pxd ? bx : bx + span, ey = pyd ? by : by + span, ez = pzd ? bz : bz + span;
+    const float tx = (float)ex * s.inv.x + noi_x(s);
+    const float ty = (float)ey * s.inv.y + noi_y(s);
+    const float tz = (float)ez * s.inv.z + noi_z(s);
+    const float max_t = fmaxf(fmaxf(tx, ty), tz);
+    // accurate entry distance on the entry axis (ties: x, then y)
+    float t_acc;
+    if (tx >= ty && tx >= tz) t_acc = __fdiv_rn((float)ex - s.vo.x, safe_component(s.dir.x));
+    else if (ty >= tz) t_acc = __fdiv_rn((float)ey - s.vo.y, safe_component(s.dir.y));
+    else t_acc = __fdiv_rn((float)ez - s.vo.z, safe_component(s.dir.z));
+    const float exact_t = fmaxf(t_acc, 0.0f);
+    const f3 hp = add3(s.vo, mul3s(s.dir, exact_t));
+    h.t_voxels = exact_t;
+    h.hit_pos_m = mul3s(hp, ARC_VOXEL_SIZE);
+    const float eps = 1e-4f * fmaxf(max_t * 0.01f, 1.0f);
+    const float cand_x = fabsf(tx - max_t) <= eps ? fabsf(s.dir.x) : 0.0f;
+    const float cand_y = fabsf(ty - max_t) <= eps ? fabsf(s.dir.y) : 0.0f;
+    const float cand_z = fabsf(tz - max_t) <= eps ? fabsf(s.dir.z) : 0.0f;
+    f3 n{0.0f, 0.0f, 0.0f};
+    if (cand_x >= cand_y && cand_x >= cand_z && cand_x > 0.0f) n.x = -signf(s.dir.x);
+    else if (cand_y >= cand_z && cand_y > 0.0f) n.y = -signf(s.dir.y);
+    else if (cand_z > 0.0f) n.z = -signf(s.dir.z);
+    else if (tx >= ty && tx >= tz) n.x = -signf(s.dir.x);
+    else if (ty >= tz) n.y = -signf(s.dir.y);
+    else n.z = -signf(s.dir.z);
+    h.normal = n;
+    h.mat = mat;
+    h.lod_payload = node.w;
+    h.vx = s.vx;
+    h.vy = s.vy;
+    h.vz = s.vz;
+    h.shift = shift;
+    h.voxel_hash = pcg_hash((s.vx * 73856093u) ^ (s.vy * 19349663u) ^ (s.vz * 83492791u));
+    h.contact_ao = 1.0f;
+    if (shift == 0u && (s.mode & 3u) == 0u) {
+        const float hit_dist_m = s.t * ARC_VOXEL_SIZE;
+        const float raw = __uint_as_float(cam.point_light_count[3]);
+        const float ao_max = raw < 1.0f ? 24.0f : raw;
+        if (hit_dist_m < ao_max) {
+            const float raw_ao = leaf_ao(node.x, node.y, b & 3u, (b >> 2) & 3u, b >> 4, n, hp);
+            const float wgt = 1.0f - smoothstepf(ao_max * 0.5f, ao_max, hit_dist_m);
+            h.contact_ao = mixf(1.0f, raw_ao, wgt);
+        }
+    }
+}
+
 // One outer-loop iteration of trace_world_64tree_from (traversal64.wgsl:302-553).
+//
+// Every branch of the reference loop ends in step_dda_box over some box: the whole chunk (empty
+// chunk, 337-352), the uniform water node (398-417), the empty child cell (419-436), the water leaf
+// cell (451-465) or the air leaf cell (525-537). Here the branches only choose the box's span and one
+// convergent step_box runs after them, so lanes that took different branches step together instead
+// of executing five inlined copies one after another. Decisions and their order are unchanged.
 __device__ __forceinline__ StepResult ray_advance(RayState& s, const World& w, const arc_camera_uniforms& cam,
                                                   HitInfo& h) {
-    if (s.step >= s.max_steps) return kMiss;
+    if (s.step >= max_steps_of(cam, s.mode)) return kMiss;
     if (s.t >= s.t_limit) return kMiss;
     const uint32_t gx = cam.world_grid_dims[0], gy = cam.world_grid_dims[1], gz = cam.world_grid_dims[2];
     if (s.vx >= (gx << 8) || s.vy >= (gy << 8) || s.vz >= (gz << 8)) return kMiss;
@@ -237,123 +302,70 @@ __device__ __forceinline__ StepResult ray_advance(RayState& s, const World& w, c
         s.mtf_c0 = c;
         s.mtf_root0 = root_idx;
     }
-    if (root_idx == ARC_EMPTY_CHUNK) {
-        step_box(s, s.vx & ~255u, s.vy & ~255u, s.vz & ~255u, 256u);
-        s.step++;
-        return kContinue;
-    }
 
-    const uint32_t lod_bias = s.mode & 3u;
-    const bool ignore_water = (s.mode & 4u) != 0u;
-    uint32_t min_shift = 0u;
-    if (lod_bias == 0u) {
-        if (s.t > cam.lod_settings[0] * ARC_VOXELS_PER_METER || s.step > cam.quality_flags[0]) min_shift = 2u;
-    } else if (lod_bias == 1u) {
-        const float sec_t = cam.lod_settings[1] * ARC_VOXELS_PER_METER;
-        if (s.t > sec_t * 2.2857f || s.step > cam.quality_flags[1]) min_shift = 4u;
-        else if (s.t > sec_t) min_shift = 2u;
-    } else {
-        if (s.t > cam.lod_settings[2] * ARC_VOXELS_PER_METER || s.step > ((cam.quality_flags[3] >> 16) & 0xFFu)) min_shift = 2u;
-    }
-
-    uint4 node;
-    uint32_t shift;
-    if (diff < 4u && min_shift == 0u && s.cached_shift == 0u) {
-        node = s.l3;
-        shift = 0u;
-    } else if (diff < 16u && min_shift <= 2u && s.cached_shift <= 2u) {
-        node = s.l2;
-        shift = 2u;
-    } else if (diff < 64u && min_shift <= 4u && s.cached_shift <= 4u) {
-        node = s.l1;
-        shift = 4u;
-    } else {
-        node = load_node(w, root_idx);
-        shift = 6u;
-    }
-    s.cached_shift = shift;
-
-    const uint32_t lx = s.vx & 255u, ly = s.vy & 255u, lz = s.vz & 255u;
-    for (;;) {
-        const uint32_t cx = (lx >> shift) & 3u, cy = (ly >> shift) & 3u, cz = (lz >> shift) & 3u;
-        const uint32_t b = (cz << 4) | (cy << 2) | cx;
-        if (ignore_water && (node.z & ARC_IS_UNIFORM_FLAG) != 0u && ((node.w >> 24) & 0xFFu) == ARC_MAT_WATER_CRYSTAL) {
-            const uint32_t span = 4u << shift;
-            step_box(s, s.vx & ~(span - 1u), s.vy & ~(span - 1u), s.vz & ~(span - 1u), span);
-            break;
+    uint32_t span = 256u;  // empty chunk: leave the whole chunk
+    if (root_idx != ARC_EMPTY_CHUNK) {
+        const uint32_t lod_bias = s.mode & 3u;
+        const bool ignore_water = (s.mode & 4u) != 0u;
+        uint32_t min_shift = 0u;
+        if (lod_bias == 0u) {
+            if (s.t > cam.lod_settings[0] * ARC_VOXELS_PER_METER || s.step > cam.quality_flags[0]) min_shift = 2u;
+        } else if (lod_bias == 1u) {
+            const float sec_t = cam.lod_settings[1] * ARC_VOXELS_PER_METER;
+            if (s.t > sec_t * 2.2857f || s.step > cam.quality_flags[1]) min_shift = 4u;
+            else if (s.t > sec_t) min_shift = 2u;
+        } else {
+            if (s.t > cam.lod_settings[2] * ARC_VOXELS_PER_METER || s.step > ((cam.quality_flags[3] >> 16) & 0xFFu))
+                min_shift = 2u;
         }
-        const uint32_t span = 1u << shift;
-        const uint32_t bx = s.vx & ~(span - 1u), by = s.vy & ~(span - 1u), bz = s.vz & ~(span - 1u);
-        if (!has_child(node.x, node.y, b)) {
-            step_box(s, bx, by, bz, span);
-            break;
+
+        uint4 node;
+        uint32_t shift;
+        if (diff < 4u && min_shift == 0u && s.cached_shift == 0u) {
+            node = s.l3;
+            shift = 0u;
+        } else if (diff < 16u && min_shift <= 2u && s.cached_shift <= 2u) {
+            node = s.l2;
+            shift = 2u;
+        } else if (diff < 64u && min_shift <= 4u && s.cached_shift <= 4u) {
+            node = s.l1;
+            shift = 4u;
+        } else {
+            node = load_node(w, root_idx);
+            shift = 6u;
         }
-        const bool is_leaf = (node.z & ARC_IS_LEAF_FLAG) != 0u;
-        if (is_leaf || shift <= min_shift) {
-            uint32_t mat = (node.w >> 24) & 0xFFu;
-            if (is_leaf && (node.z & ARC_IS_UNIFORM_FLAG) == 0u) mat = load_brick_mat(w, node.z & ARC_PTR_INDEX_MASK, b);
-            if (ignore_water && mat == ARC_MAT_WATER_CRYSTAL) {
-                step_box(s, bx, by, bz, span);
+        s.cached_shift = shift;
+
+        const uint32_t lx = s.vx & 255u, ly = s.vy & 255u, lz = s.vz & 255u;
+        for (;;) {
+            const uint32_t b = (((lz >> shift) & 3u) << 4) | (((ly >> shift) & 3u) << 2) | ((lx >> shift) & 3u);
+            if (ignore_water && (node.z & ARC_IS_UNIFORM_FLAG) != 0u && ((node.w >> 24) & 0xFFu) == ARC_MAT_WATER_CRYSTAL) {
+                span = 4u << shift;  // uniform water node
                 break;
             }
-            if (mat != ARC_MAT_AIR) {
-                const bool pxd = s.inv.x >= 0.0f, pyd = s.inv.y >= 0.0f, pzd = s.inv.z >= 0.0f;
-                const uint32_t ex = pxd ? bx : bx + span, ey = pyd ? by : by + span, ez = pzd ? bz : bz + span;
-                const float tx = (float)ex * s.inv.x + s.noi.x;
-                const float ty = (float)ey * s.inv.y + s.noi.y;
-                const float tz = (float)ez * s.inv.z + s.noi.z;
-                const float max_t = fmaxf(fmaxf(tx, ty), tz);
-                // accurate entry distance on the entry axis (ties: x, then y)
-                float t_acc;
-                if (tx >= ty && tx >= tz) t_acc = __fdiv_rn((float)ex - s.vo.x, safe_component(s.dir.x));
-                else if (ty >= tz) t_acc = __fdiv_rn((float)ey - s.vo.y, safe_component(s.dir.y));
-                else t_acc = __fdiv_rn((float)ez - s.vo.z, safe_component(s.dir.z));
-                const float exact_t = fmaxf(t_acc, 0.0f);
-                const f3 hp = add3(s.vo, mul3s(s.dir, exact_t));
-                h.t_voxels = exact_t;
-                h.hit_pos_m = mul3s(hp, ARC_VOXEL_SIZE);
-                const float eps = 1e-4f * fmaxf(max_t * 0.01f, 1.0f);
-                const float cand_x = fabsf(tx - max_t) <= eps ? fabsf(s.dir.x) : 0.0f;
-                const float cand_y = fabsf(ty - max_t) <= eps ? fabsf(s.dir.y) : 0.0f;
-                const float cand_z = fabsf(tz - max_t) <= eps ? fabsf(s.dir.z) : 0.0f;
-                f3 n{0.0f, 0.0f, 0.0f};
-                if (cand_x >= cand_y && cand_x >= cand_z && cand_x > 0.0f) n.x = -signf(s.dir.x);
-                else if (cand_y >= cand_z && cand_y > 0.0f) n.y = -signf(s.dir.y);
-                else if (cand_z > 0.0f) n.z = -signf(s.dir.z);
-                else if (tx >= ty && tx >= tz) n.x = -signf(s.dir.x);
-                else if (ty >= tz) n.y = -signf(s.dir.y);
-                else n.z = -signf(s.dir.z);
-                h.normal = n;
-                h.mat = mat;
-                h.lod_payload = node.w;
-                h.vx = s.vx;
-                h.vy = s.vy;
-                h.vz = s.vz;
-                h.shift = shift;
-                h.voxel_hash = pcg_hash((s.vx * 73856093u) ^ (s.vy * 19349663u) ^ (s.vz * 83492791u));
-                h.contact_ao = 1.0f;
-                if (shift == 0u && lod_bias == 0u) {
-                    const float hit_dist_m = s.t * ARC_VOXEL_SIZE;
-                    const float raw = __uint_as_float(cam.point_light_count[3]);
-                    const float ao_max = raw < 1.0f ? 24.0f : raw;
-                    if (hit_dist_m < ao_max) {
-                        const float raw_ao = leaf_ao(node.x, node.y, cx, cy, cz, n, hp);
-                        const float wgt = 1.0f - smoothstepf(ao_max * 0.5f, ao_max, hit_dist_m);
-                        h.contact_ao = mixf(1.0f, raw_ao, wgt);
-                    }
+            span = 1u << shift;
+            if (!has_child(node.x, node.y, b)) break;  // empty child cell
+            const bool is_leaf = (node.z & ARC_IS_LEAF_FLAG) != 0u;
+            if (is_leaf || shift <= min_shift) {
+                uint32_t mat = (node.w >> 24) & 0xFFu;
+                if (is_leaf && (node.z & ARC_IS_UNIFORM_FLAG) == 0u) mat = load_brick_mat(w, node.z & ARC_PTR_INDEX_MASK, b);
+                if (ignore_water && mat == ARC_MAT_WATER_CRYSTAL) break;  // water cell
+                if (mat != ARC_MAT_AIR) {
+                    resolve_hit(s, cam, node, mat, s.vx & ~(span - 1u), s.vy & ~(span - 1u), s.vz & ~(span - 1u), span,
+                                shift, b, h);
+                    return kHit;
                 }
-                return kHit;
+                break;  // air leaf cell
             }
-            step_box(s, bx, by, bz, span);
-            break;
+            node = load_node(w, child_index(node, b));
+            shift -= 2u;
+            s.cached_shift = shift;
+            if (shift == 4u) s.l1 = node;
+            else if (shift == 2u) s.l2 = node;
+            else if (shift == 0u) s.l3 = node;
         }
-        node = load_node(w, child_index(node, b));
-        shift -= 2u;
-        s.cached_shift = shift;
-        if (shift == 4u) s.l1 = node;
-        else if (shift == 2u) s.l2 = node;
-        else if (shift == 0u) s.l3 = node;
     }
+    step_box(s, s.vx & ~(span - 1u), s.vy & ~(span - 1u), s.vz & ~(span - 1u), span);
     s.step++;
     return kContinue;
 }
@@ -382,7 +394,6 @@ __device__ __forceinline__ float shadow_vis(const World& w, const arc_camera_uni
     s.t = fmaxf(w_enter, 0.0f);
     s.t_limit = fminf(w_exit, max_t_v);
     const uint32_t max_steps = cam.ray_steps[3];
-    s.noi = f3{-vo.x * s.inv.x, -vo.y * s.inv.y, -vo.z * s.inv.z};
     float st = s.t + 1e-4f;
     s.vx = f2u(clampf(vo.x + dir.x * st, 0.0f, wx - 1e-3f));
     s.vy = f2u(clampf(vo.y + dir.y * st, 0.0f, wy - 1e-3f));
@@ -467,6 +478,60 @@ __device__ __forceinline__ f3 camera_dir(const arc_camera_uniforms& cam, uint32_
          (cam.cam_forward_fov[1] + cam.cam_right_aspect[1] * sx) + cam.cam_up_frame[1] * sy,
          (cam.cam_forward_fov[2] + cam.cam_right_aspect[2] * sx) + cam.cam_up_frame[2] * sy};
     return normalize3(r);
+}
+
+// probe_emissive_macro_candidate (lighting_restir_gi.wgsl:20-54).
+__device__ __forceinline__ float probe_emissive(const World& w, const arc_camera_uniforms& cam, f3 pos, f3 d, float dist) {
+    const f3 vp = mul3s(add3(pos, mul3s(d, dist)), ARC_VOXELS_PER_METER);
+    const uint32_t gx = cam.world_grid_dims[0], gy = cam.world_grid_dims[1], gz = cam.world_grid_dims[2];
+    if (vp.x < 0.0f || vp.y < 0.0f || vp.z < 0.0f) return 0.0f;
+    if (vp.x >= (float)gx * ARC_CHUNK_DIM_F || vp.y >= (float)gy * ARC_CHUNK_DIM_F || vp.z >= (float)gz * ARC_CHUNK_DIM_F)
+        return 0.0f;
+    const uint32_t vx = f2u(vp.x), vy = f2u(vp.y), vz = f2u(vp.z);
+    const uint32_t root_idx = load_root(w, (vx >> 8) + (vy >> 8) * gx + (vz >> 8) * gx * gy);
+    if (root_idx == ARC_EMPTY_CHUNK) return 0.0f;
+    const uint32_t lx = vx & 255u, ly = vy & 255u, lz = vz & 255u;
+    const uint4 root = load_node(w, root_idx);
+    const uint32_t b0 = (((lz >> 6) & 3u) << 4) | (((ly >> 6) & 3u) << 2) | ((lx >> 6) & 3u);
+    if (!has_child(root.x, root.y, b0)) return 0.0f;
+    uint32_t m_id;
+    if (root.z & ARC_IS_LEAF_FLAG) {
+        m_id = (root.w >> 24) & 0xFFu;
+    } else {
+        const uint4 l1 = load_node(w, child_index(root, b0));
+        const uint32_t b1 = (((lz >> 4) & 3u) << 4) | (((ly >> 4) & 3u) << 2) | ((lx >> 4) & 3u);
+        if (!has_child(l1.x, l1.y, b1)) return 0.0f;
+        m_id = (l1.w >> 24) & 0xFFu;
+    }
+    const float4 em = __ldg(&w.palette[2u * m_id + 1u]);
+    return (em.x * 0.333f + em.y * 0.333f) + em.z * 0.333f;
+}
+
+// GI secondary ray of a hit pixel from its G-buffer words (lighting_restir_gi.wgsl:69-87, 195-209).
+__device__ __forceinline__ bool gi_setup(const World& w, const arc_camera_uniforms& cam, uint32_t x, uint32_t y,
+                                         uint32_t W, uint32_t H, uint32_t depth_word, uint32_t normal_word, f3* origin,
+                                         f3* dir) {
+    const float hit_dist = __uint_as_float(depth_word);
+    if (hit_dist >= 1e4f) return false;
+    const f3 rd = camera_dir(cam, x, y, W, H);
+    const f3 eye{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]};
+    const f3 hp = add3(eye, mul3s(rd, hit_dist));
+    float ox, oy;
+    unpack2x16snorm(normal_word, &ox, &oy);
+    const f3 n = oct_decode(ox, oy);
+    float u1, u2;
+    gradient_noise((float)x, (float)y, __float_as_uint(cam.cam_up_frame[3]), &u1, &u2);
+    const f3 sn = normalize3(f3{n.x + 0.0f, n.y + 0.22f, n.z + 0.0f});
+    f3 bt, bb;
+    make_basis(sn, &bt, &bb);
+    f3 bd = cosine_sample(u1, u2, sn, bt, bb);
+    const f3 cd = cosine_sample(fractf(u1 + 0.5f), fractf(u2 + 0.381966f), sn, bt, bb);
+    const float em_near = probe_emissive(w, cam, hp, cd, 1.25f);
+    const float em_mid = probe_emissive(w, cam, hp, cd, 3.0f);
+    if (fmaxf(em_near, em_mid) > 0.25f) bd = cd;
+    *origin = add3(hp, mul3s(n, 0.10f));
+    *dir = bd;
+    return true;
 }
 
 }  // namespace arc

@@ -46,6 +46,7 @@ SIGNATURES = {
     "arc_synchronize": [_vp],
     "arc_get_stream": [_vp, C.POINTER(_vp)],
     "arc_set_launch_config": [_vp, _vp],
+    "arc_autotune_frame_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _u32, _vp, _vp],
     "arc_get_launch_config": [_vp, _vp],
     "arc_get_stats": [_vp, _vp],
     "arc_upload_world": [_vp, _vp, _vp, _u32, _vp, _u32, _vp, _u32, _vp, _u32, _u32],
@@ -67,6 +68,16 @@ SIGNATURES = {
     "arc_sharc_download": [_vp, _vp, _vp, _vp],
     "arc_sharc_upload": [_vp, _vp, _vp, _vp],
     "arc_sharc_deposit_dev": [_vp, _vp, _vp, _vp, _vp, _u32],
+    "arc_sharc_set_mode": [_vp, _u32],
+    "arc_gi_points_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "arc_onebounce_dev": [_vp, _vp, _u32, _vp, _vp, _vp, _u32, _u32, _i32, _vp],
+    "arc_nrc_train_samples_dev": [_vp, _u32, _vp, _vp, _vp, _vp, _vp, _f32, _u32, _u32, _vp, _vp, _vp],
+    "arc_nrc_init": [_vp, _u32],
+    "arc_nrc_set_weights": [_vp, _vp],
+    "arc_nrc_get_weights": [_vp, _vp],
+    "arc_nrc_query_dev": [_vp, _vp, _u32, _vp],
+    "arc_nrc_grad_dev": [_vp, _vp, _vp, _u32, _vp],
+    "arc_nrc_train_step_dev": [_vp, _vp, _vp, _u32, _f32, _vp],
     "arc_default_palette": [_vp],
     "arc_world_build": [_vp, _vp, _i32, C.POINTER(_vp)],
     "arc_world_info": [_vp, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u64)],
@@ -219,6 +230,13 @@ class Tracer:
         for k, v in kw.items():
             setattr(cfg, k, v)
         self._check(lib().arc_set_launch_config(self._ctx, C.byref(cfg)), "arc_set_launch_config")
+
+    def autotune_frame_dev(self, w, h, gdm, gnm, gaa, hits=0, gi=0, frames=3):
+        best = LaunchConfig()
+        ms = C.c_float()
+        self._check(lib().arc_autotune_frame_dev(self._ctx, w, h, gdm, gnm, gaa, hits or None, gi or None, frames,
+                                                 C.byref(best), C.byref(ms)), "arc_autotune_frame_dev")
+        return best, ms.value
 
     def launch_config(self) -> LaunchConfig:
         cfg = LaunchConfig()

@@ -75,6 +75,12 @@ int arc_synchronize(arc_ctx* ctx);
 /* cudaStream_t of the context, for callers that order their own work after it */
 int arc_get_stream(arc_ctx* ctx, void** stream);
 int arc_set_launch_config(arc_ctx* ctx, const arc_launch_config* cfg);
+/* Times candidate launch configurations (variant x block size x register budget x refill threshold x
+ * tile shape) on the caller's frame, installs the fastest and returns it with its median frame time.
+ * No counterpart in the reference (its dispatch shape is fixed at 8x8). */
+int arc_autotune_frame_dev(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbuf_depth_mat,
+                           uint32_t* gbuf_norm_motion, uint32_t* gbuf_albedo_ao, arc_hit_record* hits,
+                           arc_hit_record* gi_hits, uint32_t frames, arc_launch_config* best, float* best_ms);
 int arc_get_launch_config(const arc_ctx* ctx, arc_launch_config* cfg);
 int arc_get_stats(const arc_ctx* ctx, arc_stats* out);
 
@@ -129,6 +135,36 @@ int arc_sharc_upload(arc_ctx* ctx, const uint32_t* keys, const uint32_t* accum, 
  * n_threads device threads each deposit rad at (pos, normal) as seen from cam_pos. */
 int arc_sharc_deposit_dev(arc_ctx* ctx, const float pos[3], const float normal[3], const float cam_pos[3],
                           const float rad[3], uint32_t n_threads);
+
+/* Cache comparison (NRC vs SHARC) on identical light transport. Both caches then learn the one-bounce
+ * estimator L = albedo * (c_sun max(n.l,0) V(x) + L_sky [cosine ray from x escapes]), c_sun = sun_power *
+ * (1, 0.9, 0.75) * 0.55, L_sky = (0.30, 0.42, 0.60). mode 0 = reference sharc_shade_surface (default),
+ * mode 1 = that estimator in arc_sharc_update_dev. No counterpart in the reference. */
+int arc_sharc_set_mode(arc_ctx* ctx, uint32_t mode);
+/* GI hit points of a frame (per pixel: position, normal, albedo, 9 NRC inputs, valid flag). */
+int arc_gi_points_dev(arc_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* gbuf_depth_mat,
+                      const uint32_t* gbuf_norm_motion, float* pos, float* normal, float* albedo, float* nrc_in,
+                      uint32_t* valid, uint64_t* n_valid);
+/* Mean of spp one-bounce samples at points idx[i] (idx may be NULL = identity); accumulate adds. */
+int arc_onebounce_dev(arc_ctx* ctx, const uint32_t* idx, uint32_t n, const float* pos, const float* normal,
+                      const float* albedo, uint32_t spp, uint32_t seed, int accumulate, float* out);
+/* NRC training samples: each valid point taken with probability accept, up to max_n, 1-spp targets. */
+int arc_nrc_train_samples_dev(arc_ctx* ctx, uint32_t n_px, const uint32_t* valid, const float* pos,
+                              const float* normal, const float* albedo, const float* nrc_in, float accept,
+                              uint32_t seed, uint32_t max_n, float* train_in, float* train_t, uint32_t* count);
+
+/* Neural radiance cache (no reference counterpart: it stands in for query_sharc at secondary hits).
+ * 9 inputs per query: position normalised to [0,1]^3, normal, view direction; 3 outputs (RGB).
+ * 30,400 FP32 master weights: W1[64][216], W2..W5[64][64], W6[3][64], row-major, no biases. */
+int arc_nrc_init(arc_ctx* ctx, uint32_t seed);
+int arc_nrc_set_weights(arc_ctx* ctx, const float* weights);
+int arc_nrc_get_weights(arc_ctx* ctx, float* weights);
+int arc_nrc_query_dev(arc_ctx* ctx, const float* inputs, uint32_t n, float* out_rgb);
+/* Loss-scaled (x128) weight gradient of the mean relative-L2 loss of one batch (device output). */
+int arc_nrc_grad_dev(arc_ctx* ctx, const float* inputs, const float* targets, uint32_t n, float* grad_out);
+/* One Adam step (lr; beta 0.9/0.99) on a batch; loss_host (optional) receives the batch loss. */
+int arc_nrc_train_step_dev(arc_ctx* ctx, const float* inputs, const float* targets, uint32_t n, float lr,
+                           float* loss_host);
 
 #ifdef __cplusplus
 }

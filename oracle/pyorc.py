@@ -108,6 +108,11 @@ def lib():
         _lib.orc_scene_voxel.argtypes = [C.POINTER(_Scene), vp, u32, u32, u32]
         _lib.orc_scene_voxel.restype = u32
         _lib.orc_test_scene_volume.argtypes = [C.POINTER(_Scene), u32, u32, u32, vp]
+        _lib.orc_nrc_param_count.restype = u32
+        _lib.orc_nrc_forward.argtypes = [vp, vp, u32, vp, vp]
+        _lib.orc_nrc_grad.argtypes = [vp, vp, vp, u32, vp]
+        _lib.orc_nrc_grad.restype = C.c_double
+        _lib.orc_nrc_adam.argtypes = [vp, vp, vp, vp, u32, u32, f32]
     return _lib
 
 
@@ -341,3 +346,32 @@ def scene_volume(scene: SceneParams, chunk=(0, 0, 0)) -> np.ndarray:
     vol = np.zeros((256, 256, 256), np.uint8)
     lib().orc_test_scene_volume(C.byref(s), chunk[0], chunk[1], chunk[2], _p(vol))
     return vol
+
+
+NRC_PARAMS = 30400
+
+
+def nrc_forward(weights: np.ndarray, inputs: np.ndarray) -> np.ndarray:
+    """FP64 reference of the NRC forward pass (FP16-quantised weights and activations)."""
+    w = np.ascontiguousarray(weights, np.float32)
+    x = np.ascontiguousarray(inputs, np.float32)
+    out = np.zeros((len(x), 3), np.float64)
+    lib().orc_nrc_forward(_p(w), _p(x), len(x), _p(out), None)
+    return out
+
+
+def nrc_grad(weights: np.ndarray, inputs: np.ndarray, targets: np.ndarray):
+    """(loss, gradient) of the mean relative-L2 loss in FP64."""
+    w = np.ascontiguousarray(weights, np.float32)
+    x = np.ascontiguousarray(inputs, np.float32)
+    t = np.ascontiguousarray(targets, np.float32)
+    g = np.zeros(NRC_PARAMS, np.float64)
+    loss = lib().orc_nrc_grad(_p(w), _p(x), _p(t), len(x), _p(g))
+    return loss, g
+
+
+def nrc_adam(weights, m, v, grad, step: int, lr: float):
+    for a in (weights, m, v):
+        assert a.dtype == np.float32 and a.flags.c_contiguous
+    g = np.ascontiguousarray(grad, np.float32)
+    lib().orc_nrc_adam(_p(weights), _p(m), _p(v), _p(g), NRC_PARAMS, step, lr)
