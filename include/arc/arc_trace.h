@@ -114,6 +114,15 @@ int arc_trace_frame(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbu
 int arc_trace_frame_dev(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbuf_depth_mat,
                         uint32_t* gbuf_norm_motion, uint32_t* gbuf_albedo_ao, arc_hit_record* hits,
                         arc_hit_record* gi_hits, uint64_t* n_gi_dev);
+/* arc_trace_frame_dev without any device allocation, for callers that cannot call cudaMalloc while
+ * they trace (a renderer whose frame loop runs under a no-allocation rule or its own memory budget).
+ * No counterpart in the reference. The kernels' scratch (queue head, GI-ray counter) lives in a
+ * 256-byte static device array instead of context memory; frames above 2^26 pixels are rejected with
+ * ARC_E_CAPACITY. All calls share that array, so calls overlapping on one device race; the first call
+ * on a device looks up the array's address and should come before any stream capture. */
+int arc_trace_frame_noalloc(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbuf_depth_mat,
+                            uint32_t* gbuf_norm_motion, uint32_t* gbuf_albedo_ao, arc_hit_record* hits,
+                            arc_hit_record* gi_hits, uint64_t* n_gi_dev);
 /* trace_world_64tree on a batch of rays (origin m, unit dir). */
 int arc_trace_rays(arc_ctx* ctx, const arc_ray* rays, uint32_t n, float max_dist_m, uint32_t lod_bias,
                    int ignore_water, arc_hit_record* hits);
