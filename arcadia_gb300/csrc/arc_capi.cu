@@ -98,6 +98,11 @@ int arc_ctx_check_ready(arc_ctx* c, bool need_cam) {
 int arc_ctx_finish(arc_ctx* c) {
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamSynchronize");
+    if (c->timing_pending) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) c->last_ms = ms;
+        c->timing_pending = false;
+    }
     uint32_t st = 0;
     e = cudaMemcpy(&st, c->d_status, sizeof st, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(c, e, "status readback");
@@ -109,6 +114,34 @@ int arc_ctx_finish(arc_ctx* c) {
         cudaStreamSynchronize(c->stream);
         return set_err(c, ARC_E_DEVICE_CHECK, b);
     }
+    return ARC_OK;
+}
+
+// Device table of World records: slot 0 = the context's main world, slots 1.. = arc_upload_world_slot.
+int arc_ctx_sync_world_table(arc_ctx* c) {
+    if (!c->d_worlds) {
+        cudaError_t e = cudaMalloc((void**)&c->d_worlds, sizeof(arc::World) * arc_ctx::kSlots);
+        if (e != cudaSuccess) return cuda_fail(c, e, "world table");
+    }
+    arc::World tab[arc_ctx::kSlots];
+    memset(tab, 0, sizeof tab);
+    tab[0] = c->world();
+    for (int i = 1; i < arc_ctx::kSlots; ++i) {
+        const arc_ctx::Slot& sl = c->slots[i];
+        if (!sl.valid) continue;
+        tab[i].roots = sl.d_roots;
+        tab[i].nodes = reinterpret_cast<const uint4*>(sl.d_nodes);
+        tab[i].bricks = reinterpret_cast<const uint32_t*>(sl.d_bricks);
+        tab[i].palette = reinterpret_cast<const float4*>(sl.d_palette);
+        tab[i].n_nodes = sl.n_nodes;
+        tab[i].n_bricks = sl.n_bricks;
+        tab[i].n_roots = sl.n_roots;
+        tab[i].status = c->d_status;
+    }
+    cudaError_t e = cudaMemcpyAsync(c->d_worlds, tab, sizeof tab, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "world table upload");
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "world table upload");
     return ARC_OK;
 }
 
@@ -166,6 +199,17 @@ int arc_destroy(arc_ctx* c) {
     cudaFree(c->d_sharc_accum);
     cudaFree(c->d_sharc_resolved);
     cudaFree(c->d_sharc_stage);
+    for (int i = 1; i < arc_ctx::kSlots; ++i) {
+        cudaFree(c->slots[i].d_roots);
+        cudaFree(c->slots[i].d_nodes);
+        cudaFree(c->slots[i].d_bricks);
+        cudaFree(c->slots[i].d_palette);
+    }
+    cudaFree(c->d_worlds);
+    cudaFree(c->d_views);
+    if (c->h_views) cudaFreeHost(c->h_views);
+    if (c->views_exec) cudaGraphExecDestroy(c->views_exec);
+    if (c->views_graph) cudaGraphDestroy(c->views_graph);
     cudaFree(c->d_nrc_w32);
     cudaFree(c->d_nrc_w16);
     cudaFree(c->d_nrc_loss);
@@ -269,7 +313,48 @@ int arc_upload_world(arc_ctx* c, const uint32_t grid[3], const uint32_t* roots, 
     c->n_bricks = std::max<uint32_t>(n_bricks, 1u);
     c->cap_bricks = (uint32_t)cap_bricks;
     c->have_world = true;
-    return ARC_OK;
+    return arc_ctx_sync_world_table(c);
+}
+
+int arc_upload_world_slot(arc_ctx* c, uint32_t slot, const uint32_t grid[3], const uint32_t* roots, uint32_t n_roots,
+                          const arc_node64* nodes, uint32_t n_nodes, const arc_brick64* bricks, uint32_t n_bricks,
+                          const arc_material* palette) {
+    if (!c) return ARC_E_INVALID_ARG;
+    if (slot == 0) return arc_upload_world(c, grid, roots, n_roots, nodes, n_nodes, bricks, n_bricks, palette, 0, 0);
+    if (slot >= (uint32_t)arc_ctx::kSlots) return set_err(c, ARC_E_INVALID_ARG, "world slot out of range");
+    if (!grid || !roots || !nodes || !palette || n_nodes == 0) return set_err(c, ARC_E_INVALID_ARG, "null pool");
+    if (n_bricks && !bricks) return set_err(c, ARC_E_INVALID_ARG, "null brick pool");
+    for (int i = 0; i < 3; ++i)
+        if (grid[i] == 0 || grid[i] > 1024u) return set_err(c, ARC_E_INVALID_ARG, "grid dims must be in [1, 1024]");
+    if ((uint64_t)grid[0] * grid[1] * grid[2] != n_roots) return set_err(c, ARC_E_INVALID_ARG, "n_roots != grid volume");
+    for (uint32_t i = 0; i < n_roots; ++i)
+        if (roots[i] != ARC_EMPTY_CHUNK && roots[i] >= n_nodes) return set_err(c, ARC_E_INVALID_POOL, "root out of range");
+    int rc = validate_nodes(c, nodes, n_nodes, n_nodes, n_bricks, 0);
+    if (rc) return rc;
+    ARC_CK(c, cudaStreamSynchronize(c->stream));
+    arc_ctx::Slot& sl = c->slots[slot];
+    cudaFree(sl.d_roots);
+    cudaFree(sl.d_nodes);
+    cudaFree(sl.d_bricks);
+    sl = arc_ctx::Slot();
+    const uint32_t nb = std::max<uint32_t>(n_bricks, 1u);
+    ARC_CK(c, cudaMalloc((void**)&sl.d_roots, sizeof(uint32_t) * n_roots));
+    ARC_CK(c, cudaMalloc((void**)&sl.d_nodes, sizeof(arc_node64) * n_nodes));
+    ARC_CK(c, cudaMalloc((void**)&sl.d_bricks, sizeof(arc_brick64) * nb));
+    ARC_CK(c, cudaMalloc((void**)&sl.d_palette, sizeof(arc_material) * 256));
+    ARC_CK(c, cudaMemcpyAsync(sl.d_roots, roots, sizeof(uint32_t) * n_roots, cudaMemcpyHostToDevice, c->stream));
+    ARC_CK(c, cudaMemcpyAsync(sl.d_nodes, nodes, sizeof(arc_node64) * n_nodes, cudaMemcpyHostToDevice, c->stream));
+    if (n_bricks) ARC_CK(c, cudaMemcpyAsync(sl.d_bricks, bricks, sizeof(arc_brick64) * n_bricks, cudaMemcpyHostToDevice, c->stream));
+    else ARC_CK(c, cudaMemsetAsync(sl.d_bricks, 0, sizeof(arc_brick64), c->stream));
+    ARC_CK(c, cudaMemcpyAsync(sl.d_palette, palette, sizeof(arc_material) * 256, cudaMemcpyHostToDevice, c->stream));
+    sl.grid[0] = grid[0];
+    sl.grid[1] = grid[1];
+    sl.grid[2] = grid[2];
+    sl.n_roots = n_roots;
+    sl.n_nodes = n_nodes;
+    sl.n_bricks = nb;
+    sl.valid = true;
+    return arc_ctx_sync_world_table(c);
 }
 
 int arc_apply_patch(arc_ctx* c, uint32_t chunk, uint32_t new_root, uint32_t node_offset, const arc_node64* nodes,
@@ -498,6 +583,159 @@ int arc_trace_rays(arc_ctx* c, const arc_ray* rays, uint32_t n, float max_dist_m
     ARC_CK(c, cudaMemcpyAsync(d_rays, rays, (size_t)n * 24, cudaMemcpyHostToDevice, c->stream));
     if ((rc = arc_trace_rays_dev(c, d_rays, n, max_dist_m, lod_bias, ignore_water, d_hits))) return rc;
     ARC_CK(c, cudaMemcpyAsync(hits, d_hits, (size_t)n * 20, cudaMemcpyDeviceToHost, c->stream));
+    return arc_ctx_finish(c);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Batched views: many cameras over several worlds in one persistent launch, optionally replayed
+// from a captured CUDA graph (memset of the scratch, upload of the view table from a pinned mirror,
+// the kernel, and the GI-count copy). A new graph is captured when the view count, the GI-count
+// destination or the launch configuration changes; otherwise the frame only rewrites the mirror.
+// ------------------------------------------------------------------------------------------------
+
+static int views_prepare(arc_ctx* c, const arc_view_desc* views, uint32_t n, uint32_t* queue_len) {
+    if (!c || !views || n == 0) return set_err(c, ARC_E_INVALID_ARG, "no views");
+    if (!c->have_world) return set_err(c, ARC_E_NO_WORLD, "no world uploaded");
+    if (n > c->views_cap) {
+        cudaFree(c->d_views);
+        if (c->h_views) cudaFreeHost(c->h_views);
+        c->d_views = nullptr;
+        c->h_views = nullptr;
+        c->views_cap = 0;
+        ARC_CK(c, cudaMalloc((void**)&c->d_views, sizeof(arc::ViewDev) * n));
+        ARC_CK(c, cudaMallocHost((void**)&c->h_views, sizeof(arc::ViewDev) * n));
+        c->views_cap = n;
+        if (c->views_exec) cudaGraphExecDestroy(c->views_exec);
+        if (c->views_graph) cudaGraphDestroy(c->views_graph);
+        c->views_exec = nullptr;
+        c->views_graph = nullptr;
+    }
+    ARC_CK(c, cudaStreamSynchronize(c->stream));  // the previous launch has read the mirror
+    uint64_t q = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const arc_view_desc& d = views[i];
+        const uint32_t slot = d.world_slot;
+        if (slot >= (uint32_t)arc_ctx::kSlots) return set_err(c, ARC_E_INVALID_ARG, "view world slot out of range");
+        const uint32_t* g = slot == 0 ? c->grid : c->slots[slot].grid;
+        if (slot != 0 && !c->slots[slot].valid) return set_err(c, ARC_E_NO_WORLD, "view names an empty world slot");
+        if (d.cam.world_grid_dims[0] != g[0] || d.cam.world_grid_dims[1] != g[1] || d.cam.world_grid_dims[2] != g[2])
+            return set_err(c, ARC_E_INVALID_ARG, "view camera grid differs from its world");
+        if (d.width == 0 || d.height == 0 || (d.cam.world_grid_dims[3] & 0xFFFFu) != d.width ||
+            (d.cam.world_grid_dims[3] >> 16) != d.height)
+            return set_err(c, ARC_E_INVALID_ARG, "view size differs from its camera world_grid_dims.w");
+        if (!d.gbuf_depth_mat || !d.gbuf_norm_motion || !d.gbuf_albedo_ao) return set_err(c, ARC_E_INVALID_ARG, "null G-buffer");
+        arc::ViewDev& v = c->h_views[i];
+        memset(&v, 0, sizeof v);
+        v.cam = d.cam;
+        v.slot = slot;
+        v.width = d.width;
+        v.height = d.height;
+        v.tiles_x = (d.width + c->cfg.tile_w - 1u) / c->cfg.tile_w;
+        v.queue_begin = (uint32_t)q;
+        v.gbuf_depth_mat = d.gbuf_depth_mat;
+        v.gbuf_norm_motion = d.gbuf_norm_motion;
+        v.gbuf_albedo_ao = d.gbuf_albedo_ao;
+        v.hits = d.hits;
+        v.gi_hits = d.gi_hits;
+        q += (uint64_t)v.tiles_x * ((d.height + c->cfg.tile_h - 1u) / c->cfg.tile_h) * 32u;
+        if (q > (1ull << 31)) return set_err(c, ARC_E_CAPACITY, "batch exceeds 2^31 queue entries");
+    }
+    *queue_len = (uint32_t)q;
+    return ARC_OK;
+}
+
+static int views_enqueue(arc_ctx* c, uint32_t n, uint32_t queue_len, uint64_t* n_gi_dev) {
+    arc::ViewsParams V;
+    V.views = c->d_views;
+    V.n_views = n;
+    V.worlds = c->d_worlds;
+    V.scratch = c->d_scratch;
+    V.queue_len = queue_len;
+    V.tile_w = c->cfg.tile_w;
+    V.tile_h = c->cfg.tile_h;
+    V.refill_threshold = c->cfg.refill_threshold;
+    ARC_CK(c, cudaMemsetAsync(c->d_scratch, 0, sizeof(arc::Scratch), c->stream));
+    ARC_CK(c, cudaMemcpyAsync(c->d_views, c->h_views, sizeof(arc::ViewDev) * n, cudaMemcpyHostToDevice, c->stream));
+    ARC_CK(c, arc::launch_views(V, c->cfg, c->n_sm, c->stream));
+    if (n_gi_dev)
+        ARC_CK(c, cudaMemcpyAsync(n_gi_dev, &c->d_scratch->gi_rays, sizeof(uint64_t), cudaMemcpyDeviceToDevice, c->stream));
+    return ARC_OK;
+}
+
+int arc_trace_views_dev(arc_ctx* c, const arc_view_desc* views, uint32_t n_views, uint64_t* n_gi_dev, int use_graph) {
+    uint32_t queue_len = 0;
+    int rc = views_prepare(c, views, n_views, &queue_len);
+    if (rc) return rc;
+    ARC_CK(c, cudaEventRecord(c->ev0, c->stream));
+    if (!use_graph) {
+        if ((rc = views_enqueue(c, n_views, queue_len, n_gi_dev))) return rc;
+    } else {
+        const bool same = c->views_exec && c->graph_n_views == n_views && c->graph_n_gi == n_gi_dev &&
+                          c->graph_queue_len == queue_len && memcmp(&c->graph_cfg, &c->cfg, sizeof c->cfg) == 0;
+        if (!same) {
+            if (c->views_exec) cudaGraphExecDestroy(c->views_exec);
+            if (c->views_graph) cudaGraphDestroy(c->views_graph);
+            c->views_exec = nullptr;
+            c->views_graph = nullptr;
+            ARC_CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            rc = views_enqueue(c, n_views, queue_len, n_gi_dev);
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+            if (rc) {
+                if (g) cudaGraphDestroy(g);
+                return rc;
+            }
+            if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+            c->views_graph = g;
+            ARC_CK(c, cudaGraphInstantiate(&c->views_exec, g, 0));
+            c->graph_n_views = n_views;
+            c->graph_n_gi = n_gi_dev;
+            c->graph_queue_len = queue_len;
+            c->graph_cfg = c->cfg;
+        }
+        ARC_CK(c, cudaGraphLaunch(c->views_exec, c->stream));
+    }
+    ARC_CK(c, cudaEventRecord(c->ev1, c->stream));
+    c->timing_pending = true;
+    return ARC_OK;
+}
+
+int arc_autotune_views_dev(arc_ctx* c, const arc_view_desc* views, uint32_t n_views, uint32_t frames,
+                           arc_launch_config* best_out, float* best_ms) {
+    if (!c) return ARC_E_INVALID_ARG;
+    if (frames == 0) frames = 3;
+    std::vector<arc_launch_config> cands;
+    for (uint32_t rb : {2u, 3u, 4u})
+        for (uint32_t thr : {8u, 16u, 24u, 28u})
+            for (uint32_t bt : {128u, 256u}) cands.push_back(arc_launch_config{1u, bt, 0u, 8u, 4u, thr, rb});
+    cands.push_back(arc_launch_config{1u, 256u, 0u, 4u, 8u, 24u, 4u});
+    cands.push_back(arc_launch_config{1u, 256u, 0u, 16u, 2u, 24u, 4u});
+    const arc_launch_config saved = c->cfg;
+    float best = 1e30f;
+    arc_launch_config best_cfg = saved;
+    std::vector<float> ms(frames);
+    int rc = ARC_OK;
+    for (const arc_launch_config& cfg : cands) {
+        c->cfg = cfg;
+        for (uint32_t f = 0; f <= frames && !rc; ++f) {
+            rc = arc_trace_views_dev(c, views, n_views, nullptr, 0);
+            if (rc) break;
+            cudaEventSynchronize(c->ev1);
+            float t = 0.0f;
+            cudaEventElapsedTime(&t, c->ev0, c->ev1);
+            if (f) ms[f - 1] = t;
+        }
+        if (rc) break;
+        std::sort(ms.begin(), ms.end());
+        if (ms[frames / 2] < best) {
+            best = ms[frames / 2];
+            best_cfg = cfg;
+        }
+    }
+    c->cfg = rc ? saved : best_cfg;
+    if (rc) return rc;
+    if (best_out) *best_out = best_cfg;
+    if (best_ms) *best_ms = best;
     return arc_ctx_finish(c);
 }
 

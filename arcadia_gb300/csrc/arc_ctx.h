@@ -26,6 +26,29 @@ struct arc_ctx {
     arc_camera_uniforms cam{};
     bool have_cam = false;
 
+    // extra worlds for batched multi-view launches (slot 0 is the world above)
+    static constexpr int kSlots = 8;
+    struct Slot {
+        uint32_t grid[3] = {0, 0, 0};
+        uint32_t n_roots = 0, n_nodes = 0, n_bricks = 0;
+        uint32_t* d_roots = nullptr;
+        arc_node64* d_nodes = nullptr;
+        arc_brick64* d_bricks = nullptr;
+        arc_material* d_palette = nullptr;
+        bool valid = false;
+    } slots[kSlots];
+    arc::World* d_worlds = nullptr;  // device table of kSlots World records
+
+    // batched views: device table, pinned host mirror, captured graph
+    arc::ViewDev* d_views = nullptr;
+    arc::ViewDev* h_views = nullptr;
+    uint32_t views_cap = 0;
+    cudaGraph_t views_graph = nullptr;
+    cudaGraphExec_t views_exec = nullptr;
+    uint32_t graph_n_views = 0, graph_queue_len = 0;
+    uint64_t* graph_n_gi = nullptr;
+    arc_launch_config graph_cfg{};
+
     arc::Scratch* d_scratch = nullptr;
     uint32_t* d_status = nullptr;
     uint32_t last_status = 0;
@@ -64,3 +87,4 @@ struct arc_ctx {
 int arc_ctx_check_ready(arc_ctx* c, bool need_cam);
 int arc_ctx_finish(arc_ctx* c);
 int arc_ctx_stage(arc_ctx* c, size_t bytes, void** out);
+int arc_ctx_sync_world_table(arc_ctx* c);

@@ -47,9 +47,10 @@ __device__ __forceinline__ void store_no_ray(arc_hit_record* p) {
 // G-buffer words of one pixel (primary_gbuffer.wgsl:138-143 miss, 145-311 hit; no rigid bodies and
 // no water / mirror / underwater shading branches). Returns the packed depth and normal words the
 // GI ray is generated from.
-__device__ __forceinline__ void primary_store(const FrameParams& P, const arc_camera_uniforms& cam, uint32_t x,
-                                              uint32_t y, f3 dir, bool hit, const HitInfo& h, uint32_t* depth_word,
-                                              uint32_t* normal_word) {
+template <class Out>
+__device__ __forceinline__ void primary_store(const Out& P, const float4* __restrict__ palette,
+                                              const arc_camera_uniforms& cam, uint32_t x, uint32_t y, f3 dir, bool hit,
+                                              const HitInfo& h, uint32_t* depth_word, uint32_t* normal_word) {
     const size_t k = (size_t)y * P.width + x;
     if (P.hits) store_hit(&P.hits[k], h, hit);
     if (!hit) {
@@ -64,8 +65,8 @@ __device__ __forceinline__ void primary_store(const FrameParams& P, const arc_ca
         return;
     }
     const float hit_dist = h.t_voxels * ARC_VOXEL_SIZE;
-    const float4 alb_r = __ldg(&P.world.palette[2u * h.mat]);
-    const float4 em_m = __ldg(&P.world.palette[2u * h.mat + 1u]);
+    const float4 alb_r = __ldg(&palette[2u * h.mat]);
+    const float4 em_m = __ldg(&palette[2u * h.mat + 1u]);
     const float vrw = 1.0f - smoothstepf(18.0f, 48.0f, hit_dist);
     const float vr = (__fdiv_rn((float)(h.voxel_hash & 0xFFu), 255.0f) * 2.0f - 1.0f) * vrw;
     const float k_var = 1.0f + vr * em_m.w;
@@ -127,7 +128,7 @@ __global__ void __launch_bounds__(256, MINB) frame_plain_kernel(const FrameParam
     }
     if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
     uint32_t dw, nw;
-    primary_store(P, cam, x, y, dir, r == kHit, h, &dw, &nw);
+    primary_store(P, w.palette, cam, x, y, dir, r == kHit, h, &dw, &nw);
     if (!P.do_gi) return;
     const size_t k = (size_t)y * P.width + x;
     f3 go, gd;
@@ -188,7 +189,7 @@ __global__ void __launch_bounds__(256, MINB) frame_persistent_kernel(const Frame
                         } else {
                             hit_init_miss(h, eye, dir, 250.0f);
                             uint32_t dw, nw;
-                            primary_store(P, cam, px, py, dir, false, h, &dw, &nw);
+                            primary_store(P, w.palette, cam, px, py, dir, false, h, &dw, &nw);
                             if (P.do_gi && P.gi_hits) store_no_ray(&P.gi_hits[(size_t)py * P.width + px]);
                         }
                     }
@@ -207,7 +208,7 @@ __global__ void __launch_bounds__(256, MINB) frame_persistent_kernel(const Frame
             const f3 dir = s.dir;
             if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
             uint32_t dw, nw;
-            primary_store(P, cam, px, py, dir, r == kHit, h, &dw, &nw);
+            primary_store(P, w.palette, cam, px, py, dir, r == kHit, h, &dw, &nw);
             phase = kIdle;
             if (P.do_gi) {
                 f3 go, gd;
@@ -286,6 +287,101 @@ __global__ void shadow_kernel(const World w, const __grid_constant__ arc_camera_
     vis[i] = shadow_vis(w, cam, f3{rp[0], rp[1], rp[2]}, f3{rp[3], rp[4], rp[5]}, max_dist_m);
 }
 
+// Persistent kernel over many views (several worlds, mixed resolutions) in one launch. The queue is
+// the concatenation of every view's 32-pixel tiles; a lane finds its view by binary search over the
+// views' queue offsets and reads that view's camera block and world from global memory (L1-cached),
+// so the per-ray work is exactly the single-view kernel's.
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) views_persistent_kernel(const ViewsParams V) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    RayState s;
+    HitInfo h;
+    uint32_t phase = kIdle;
+    uint32_t pxy = 0, v = 0;
+    bool exhausted = false;
+    uint32_t gi_count = 0;
+    for (;;) {
+        const uint32_t idle = __ballot_sync(0xFFFFFFFFu, phase == kIdle);
+        if (!exhausted && (__popc(idle) >= (int)V.refill_threshold || idle == 0xFFFFFFFFu)) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(&V.scratch->queue_head, (uint32_t)__popc(idle));
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base + (uint32_t)__popc(idle) >= V.queue_len) exhausted = true;
+            if (phase == kIdle) {
+                const uint32_t q = base + __popc(idle & lt_mask);
+                if (q < V.queue_len) {
+                    uint32_t lo = 0, hi = V.n_views;  // last view with queue_begin <= q
+                    while (hi - lo > 1u) {
+                        const uint32_t mid = (lo + hi) >> 1;
+                        if (V.views[mid].queue_begin <= q) lo = mid; else hi = mid;
+                    }
+                    v = lo;
+                    const ViewDev& vd = V.views[v];
+                    const uint32_t local = q - vd.queue_begin, tile = local >> 5, within = local & 31u;
+                    const uint32_t px = (tile % vd.tiles_x) * V.tile_w + within % V.tile_w;
+                    const uint32_t py = (tile / vd.tiles_x) * V.tile_h + within / V.tile_w;
+                    pxy = px | (py << 16);
+                    if (px < vd.width && py < vd.height) {
+                        const arc_camera_uniforms& cam = vd.cam;
+                        const f3 eye{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]};
+                        const f3 dir = camera_dir(cam, px, py, vd.width, vd.height);
+                        const bool underwater = (cam.point_light_count[1] & 0xFFFFu) != 0u;
+                        if (ray_begin(s, cam, eye, dir, 0.0f, 250.0f, 0u, underwater)) {
+                            phase = kPrimary;
+                        } else {
+                            hit_init_miss(h, eye, dir, 250.0f);
+                            uint32_t dw, nw;
+                            primary_store(vd, V.worlds[vd.slot].palette, cam, px, py, dir, false, h, &dw, &nw);
+                            if (vd.gi_hits) store_no_ray(&vd.gi_hits[(size_t)py * vd.width + px]);
+                        }
+                    }
+                }
+            }
+        }
+        if (__ballot_sync(0xFFFFFFFFu, phase != kIdle) == 0u) {
+            if (exhausted) break;
+            continue;
+        }
+        if (phase == kIdle) continue;
+        const ViewDev& vd = V.views[v];
+        const arc_camera_uniforms& cam = vd.cam;
+        const World& w = V.worlds[vd.slot];
+        const StepResult r = ray_advance(s, w, cam, h);
+        if (r == kContinue) continue;
+        const uint32_t px = pxy & 0xFFFFu, py = pxy >> 16;
+        const size_t k = (size_t)py * vd.width + px;
+        if (phase == kPrimary) {
+            const f3 eye{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]};
+            const f3 dir = s.dir;
+            if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
+            uint32_t dw, nw;
+            primary_store(vd, w.palette, cam, px, py, dir, r == kHit, h, &dw, &nw);
+            phase = kIdle;
+            f3 go, gd;
+            if (gi_setup(w, cam, px, py, vd.width, vd.height, dw, nw, &go, &gd)) {
+                ++gi_count;
+                const float gmax = cam.ray_distances[2];
+                if (ray_begin(s, cam, go, gd, 0.0f, gmax, 2u, true)) {
+                    phase = kGi;
+                } else {
+                    hit_init_miss(h, go, gd, gmax);
+                    if (vd.gi_hits) store_hit(&vd.gi_hits[k], h, false);
+                }
+            } else if (vd.gi_hits) {
+                store_no_ray(&vd.gi_hits[k]);
+            }
+        } else {
+            if (r != kHit) hit_init_miss(h, mul3s(s.vo, ARC_VOXEL_SIZE), s.dir, cam.ray_distances[2]);
+            if (vd.gi_hits) store_hit(&vd.gi_hits[k], h, r == kHit);
+            phase = kIdle;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) gi_count += __shfl_down_sync(0xFFFFFFFFu, gi_count, o);
+    if (lane == 0 && gi_count) atomicAdd(&V.scratch->gi_rays, (unsigned long long)gi_count);
+}
+
 // ------------------------------------------------------------------------------------------------
 // Host launchers (called by the C ABI on the context's stream)
 // ------------------------------------------------------------------------------------------------
@@ -318,6 +414,28 @@ cudaError_t launch_frame(const FrameParams& P, const arc_camera_uniforms& cam, c
         case 3: return launch_frame_t<3>(P, cam, cfg, n_sm, st);
         case 4: return launch_frame_t<4>(P, cam, cfg, n_sm, st);
         default: return launch_frame_t<1>(P, cam, cfg, n_sm, st);
+    }
+}
+
+template <int MINB>
+cudaError_t launch_views_t(const ViewsParams& V, const arc_launch_config& cfg, int n_sm, cudaStream_t st) {
+    int per_sm = (int)cfg.blocks_per_sm;
+    if (per_sm <= 0) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, views_persistent_kernel<MINB>,
+                                                                      (int)cfg.block_threads, 0);
+        if (e != cudaSuccess) return e;
+        if (per_sm <= 0) per_sm = 1;
+    }
+    views_persistent_kernel<MINB><<<n_sm * per_sm, cfg.block_threads, 0, st>>>(V);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_views(const ViewsParams& V, const arc_launch_config& cfg, int n_sm, cudaStream_t st) {
+    switch (cfg.reg_blocks) {
+        case 2: return launch_views_t<2>(V, cfg, n_sm, st);
+        case 3: return launch_views_t<3>(V, cfg, n_sm, st);
+        case 4: return launch_views_t<4>(V, cfg, n_sm, st);
+        default: return launch_views_t<1>(V, cfg, n_sm, st);
     }
 }
 

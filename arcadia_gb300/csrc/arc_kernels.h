@@ -38,6 +38,28 @@ struct FrameParams {
     uint32_t tile_w, tile_h, tiles_x, queue_len, refill_threshold;
 };
 
+// One view of a batched launch: camera block, world slot, resolution, queue offset, outputs.
+struct ViewDev {
+    arc_camera_uniforms cam;
+    uint32_t slot, width, height, tiles_x;
+    uint32_t queue_begin, pad0, pad1, pad2;
+    uint32_t* gbuf_depth_mat;
+    uint32_t* gbuf_norm_motion;
+    uint32_t* gbuf_albedo_ao;
+    arc_hit_record* hits;
+    arc_hit_record* gi_hits;
+    void* pad3;
+};
+
+struct ViewsParams {
+    const ViewDev* views;
+    uint32_t n_views;
+    const World* worlds;
+    Scratch* scratch;
+    uint32_t queue_len, tile_w, tile_h, refill_threshold;
+};
+
+cudaError_t launch_views(const ViewsParams& V, const arc_launch_config& cfg, int n_sm, cudaStream_t st);
 cudaError_t launch_frame(const FrameParams& P, const arc_camera_uniforms& cam, const arc_launch_config& cfg, int n_sm,
                          cudaStream_t st);
 cudaError_t launch_secondary(const FrameParams& P, const arc_camera_uniforms& cam, cudaStream_t st);

@@ -1,0 +1,198 @@
+"""Radiance-cache comparison at secondary hits: neural radiance cache vs SHARC (the 1024^3 caves config).
+
+Both caches learn the same quantity, the one-bounce radiance L(x) at the hit of each pixel's GI ray
+(sun directional light with a shadow ray + constant sky through one cosine-sampled ray; see
+``arc_onebounce_dev``), so the comparison is about the caching method alone:
+
+  shared per frame  primary G-buffer (arc_trace_primary_dev) + GI hit points (arc_gi_points_dev)
+  SHARC pipeline    arc_sharc_update_dev (tile-seeded paths, estimator deposits, mode 1) +
+                    arc_sharc_resolve + arc_sharc_query_dev at every GI hit
+  NRC pipeline      arc_nrc_train_samples_dev (65,536 one-bounce samples) + arc_nrc_train_step_dev
+                    (fused forward/backward/Adam) + arc_nrc_query_dev at every GI hit
+
+Quality is the relative MSE, mean((pred - ref)^2 / (ref^2 + 0.01)), against a 4096-spp reference of
+the estimator at a fixed set of GI hit points. The reference is traced in FP32 on the GPU (64
+launches of 64 spp) and accumulated in FP64 on the host.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import statistics
+import time
+
+import numpy as np
+
+from . import layout as L
+from . import native
+
+TRAIN_SAMPLES = 65536
+REF_SPP_PER_LAUNCH = 64
+REF_LAUNCHES = 64
+
+
+def rel_mse(pred: np.ndarray, ref: np.ndarray) -> float:
+    pred = pred.astype(np.float64)
+    return float(np.mean((pred - ref) ** 2 / (ref ** 2 + 0.01)))
+
+
+class CacheComparison:
+    def __init__(self, tracer: native.Tracer, scene: L.SceneParams, width: int, height: int, quality=None):
+        import torch
+
+        self.torch = torch
+        self.t = tracer
+        self.scene = scene
+        self.w, self.h = width, height
+        self.q = quality or L.quality_high()
+        n = width * height
+        dev = torch.device("cuda")
+        i32 = torch.int32
+        self.gdm = torch.empty(n * 2, dtype=i32, device=dev)
+        self.gnm = torch.empty(n * 2, dtype=i32, device=dev)
+        self.gaa = torch.empty(n, dtype=i32, device=dev)
+        self.pos = torch.zeros((n, 3), dtype=torch.float32, device=dev)
+        self.nrm = torch.zeros((n, 3), dtype=torch.float32, device=dev)
+        self.alb = torch.zeros((n, 3), dtype=torch.float32, device=dev)
+        self.nin = torch.zeros((n, 9), dtype=torch.float32, device=dev)
+        self.valid = torch.zeros(n, dtype=i32, device=dev)
+        self.n_valid = torch.zeros(1, dtype=torch.int64, device=dev)
+        self.sharc_out = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+        self.nrc_out = torch.zeros((n, 3), dtype=torch.float32, device=dev)
+        self.train_in = torch.zeros((TRAIN_SAMPLES, 9), dtype=torch.float32, device=dev)
+        self.train_t = torch.zeros((TRAIN_SAMPLES, 3), dtype=torch.float32, device=dev)
+        self.count = torch.zeros(1, dtype=i32, device=dev)
+        self.stream = torch.cuda.ExternalStream(tracer.stream())
+        self.lib = native.lib()
+        self.frame = 0
+        self.last_valid = n
+
+    def camera(self, frame):
+        return L.default_camera_for(self.scene, self.w, self.h, quality=self.q, frame_index=frame)
+
+    def _ck(self, rc, what):
+        if rc:
+            raise native.ArcError(rc, f"{what}: {self.t.last_error()}")
+
+    def _event(self):
+        e = self.torch.cuda.Event(enable_timing=True)
+        e.record(self.stream)
+        return e
+
+    def shared(self, frame):
+        """Primary pass + GI hit points of `frame`; returns its device time in ms."""
+        self.t.set_camera(self.camera(frame))
+        a = self._event()
+        self.t.trace_primary_dev(self.w, self.h, self.gdm.data_ptr(), self.gnm.data_ptr(), self.gaa.data_ptr())
+        self._ck(self.lib.arc_gi_points_dev(self.t.ctx, self.w, self.h, self.gdm.data_ptr(), self.gnm.data_ptr(),
+                                            self.pos.data_ptr(), self.nrm.data_ptr(), self.alb.data_ptr(),
+                                            self.nin.data_ptr(), self.valid.data_ptr(), self.n_valid.data_ptr()),
+                 "arc_gi_points_dev")
+        b = self._event()
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    def sharc_frame(self):
+        a = self._event()
+        self._ck(self.lib.arc_sharc_update_dev(self.t.ctx, self.w, self.h, self.gdm.data_ptr(), self.gnm.data_ptr()),
+                 "arc_sharc_update_dev")
+        self._ck(self.lib.arc_sharc_resolve(self.t.ctx), "arc_sharc_resolve")
+        self._ck(self.lib.arc_sharc_query_dev(self.t.ctx, self.pos.data_ptr(), self.nrm.data_ptr(), None,
+                                              self.w * self.h, self.sharc_out.data_ptr()), "arc_sharc_query_dev")
+        b = self._event()
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    def nrc_frame(self, seed, lr=1e-3):
+        n_px = self.w * self.h
+        accept = min(1.0, 1.25 * TRAIN_SAMPLES / max(self.last_valid, 1))
+        a = self._event()
+        self._ck(self.lib.arc_nrc_train_samples_dev(self.t.ctx, n_px, self.valid.data_ptr(), self.pos.data_ptr(),
+                                                    self.nrm.data_ptr(), self.alb.data_ptr(), self.nin.data_ptr(),
+                                                    C.c_float(accept), seed, TRAIN_SAMPLES, self.train_in.data_ptr(),
+                                                    self.train_t.data_ptr(), self.count.data_ptr()),
+                 "arc_nrc_train_samples_dev")
+        n_train = min(int(self.count.item()), TRAIN_SAMPLES)  # one small read per frame
+        if n_train:
+            self._ck(self.lib.arc_nrc_train_step_dev(self.t.ctx, self.train_in.data_ptr(), self.train_t.data_ptr(),
+                                                     n_train, C.c_float(lr), None), "arc_nrc_train_step_dev")
+        self._ck(self.lib.arc_nrc_query_dev(self.t.ctx, self.nin.data_ptr(), n_px, self.nrc_out.data_ptr()),
+                 "arc_nrc_query_dev")
+        b = self._event()
+        b.synchronize()
+        self.last_valid = int(self.n_valid.item())
+        return a.elapsed_time(b), n_train
+
+    def reference(self, idx: np.ndarray, seed=12345):
+        """4096-spp one-bounce reference at pixels idx (FP32 launches, FP64 host accumulation)."""
+        torch = self.torch
+        d_idx = torch.from_numpy(idx.astype(np.int32)).cuda()
+        out = torch.zeros((len(idx), 3), dtype=torch.float32, device="cuda")
+        acc = np.zeros((len(idx), 3), np.float64)
+        for k in range(REF_LAUNCHES):
+            self._ck(self.lib.arc_onebounce_dev(self.t.ctx, d_idx.data_ptr(), len(idx), self.pos.data_ptr(),
+                                                self.nrm.data_ptr(), self.alb.data_ptr(), REF_SPP_PER_LAUNCH,
+                                                seed + 7919 * k, 0, out.data_ptr()), "arc_onebounce_dev")
+            torch.cuda.synchronize()
+            acc += out.cpu().numpy().astype(np.float64)
+        return acc / REF_LAUNCHES
+
+    def one_sample(self, idx: np.ndarray, seed=999):
+        """1-spp estimate at pixels idx: the method without any cache."""
+        torch = self.torch
+        d_idx = torch.from_numpy(idx.astype(np.int32)).cuda()
+        out = torch.zeros((len(idx), 3), dtype=torch.float32, device="cuda")
+        self._ck(self.lib.arc_onebounce_dev(self.t.ctx, d_idx.data_ptr(), len(idx), self.pos.data_ptr(),
+                                            self.nrm.data_ptr(), self.alb.data_ptr(), 1, seed, 0, out.data_ptr()),
+                 "arc_onebounce_dev")
+        torch.cuda.synchronize()
+        return out.cpu().numpy()
+
+
+def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920, height=1080, frames=60,
+                   eval_points=16384, seed=7):
+    """Runs both pipelines for `frames` frames on a static camera and scores them on the last frame."""
+    scene = L.SCENES[scene_name]
+    cc = CacheComparison(tracer, scene, width, height)
+    lib = cc.lib
+    cc._ck(lib.arc_sharc_set_mode(tracer.ctx, 1), "arc_sharc_set_mode")
+    tracer.sharc_reset()
+    cc._ck(lib.arc_nrc_init(tracer.ctx, seed), "arc_nrc_init")
+    shared_ms, sharc_ms, nrc_ms = [], [], []
+    for f in range(frames):
+        shared_ms.append(cc.shared(f))
+        sharc_ms.append(cc.sharc_frame())
+        nrc_ms.append(cc.nrc_frame(seed * 1000003 + f)[0])
+    valid = cc.valid.cpu().numpy().astype(bool)
+    cand = np.nonzero(valid)[0]
+    idx = cand[np.linspace(0, len(cand) - 1, min(eval_points, len(cand))).astype(np.int64)]
+    ref = cc.reference(idx)
+    sharc = cc.sharc_out.cpu().numpy()[idx]
+    nrc = cc.nrc_out.cpu().numpy()[idx]
+    raw = cc.one_sample(idx)
+    sharc_hit = sharc[:, 3] > 0.5
+    # untrained network, same points (the method without the learned part)
+    cc._ck(lib.arc_nrc_init(tracer.ctx, seed), "arc_nrc_init")
+    cc._ck(lib.arc_nrc_query_dev(tracer.ctx, cc.nin.data_ptr(), width * height, cc.nrc_out.data_ptr()), "query")
+    tracer.synchronize()
+    untrained = cc.nrc_out.cpu().numpy()[idx]
+    cc._ck(lib.arc_sharc_set_mode(tracer.ctx, 0), "arc_sharc_set_mode")
+    steady = slice(frames // 2, None)
+    return {
+        "frames": frames,
+        "width": width,
+        "height": height,
+        "eval_points": int(len(idx)),
+        "reference_spp": REF_SPP_PER_LAUNCH * REF_LAUNCHES,
+        "shared_ms_per_frame": round(statistics.mean(shared_ms[steady]), 4),
+        "nrc_cache_ms_per_frame": round(statistics.mean(nrc_ms[steady]), 4),
+        "sharc_cache_ms_per_frame": round(statistics.mean(sharc_ms[steady]), 4),
+        "nrc_ms_per_frame": round(statistics.mean(shared_ms[steady]) + statistics.mean(nrc_ms[steady]), 4),
+        "sharc_ms_per_frame": round(statistics.mean(shared_ms[steady]) + statistics.mean(sharc_ms[steady]), 4),
+        "rel_mse_nrc": rel_mse(nrc, ref),
+        "rel_mse_sharc": rel_mse(sharc[:, :3], ref),
+        "sharc_hit_fraction": float(sharc_hit.mean()),
+        "rel_mse_sharc_on_hits": rel_mse(sharc[sharc_hit, :3], ref[sharc_hit]) if sharc_hit.any() else None,
+        "rel_mse_nrc_on_sharc_hits": rel_mse(nrc[sharc_hit], ref[sharc_hit]) if sharc_hit.any() else None,
+        "rel_mse_1spp": rel_mse(raw, ref),
+        "rel_mse_untrained_nrc": rel_mse(untrained, ref),
+    }

@@ -53,6 +53,14 @@ CAMERA_DTYPE = np.dtype(
         ("prev_cam_pos", "<f4", (4,)),
     ]
 )
+VIEW_DTYPE = np.dtype(
+    [
+        ("world_slot", "<u4"), ("width", "<u4"), ("height", "<u4"), ("pad", "<u4"), ("cam", CAMERA_DTYPE),
+        ("gbuf_depth_mat", "<u8"), ("gbuf_norm_motion", "<u8"), ("gbuf_albedo_ao", "<u8"), ("hits", "<u8"),
+        ("gi_hits", "<u8"),
+    ]
+)
+assert VIEW_DTYPE.itemsize == 536
 assert NODE_DTYPE.itemsize == 16 and BRICK_DTYPE.itemsize == 64 and MATERIAL_DTYPE.itemsize == 32
 assert CAMERA_DTYPE.itemsize == 480 and SHARC_SLOT_DTYPE.itemsize == 16
 assert RAY_DTYPE.itemsize == 24 and HIT_DTYPE.itemsize == 20

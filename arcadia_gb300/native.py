@@ -52,6 +52,9 @@ SIGNATURES = {
     "arc_upload_world": [_vp, _vp, _vp, _u32, _vp, _u32, _vp, _u32, _vp, _u32, _u32],
     "arc_apply_patch": [_vp, _u32, _u32, _u32, _vp, _u32, _u32, _vp, _u32],
     "arc_set_camera": [_vp, _vp],
+    "arc_upload_world_slot": [_vp, _u32, _vp, _vp, _u32, _vp, _u32, _vp, _u32, _vp],
+    "arc_trace_views_dev": [_vp, _vp, _u32, _vp, _i32],
+    "arc_autotune_views_dev": [_vp, _vp, _u32, _u32, _vp, _vp],
     "arc_trace_primary": [_vp, _u32, _u32, _vp, _vp, _vp, _vp],
     "arc_trace_primary_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp],
     "arc_trace_secondary": [_vp, _u32, _u32, _vp, _vp, _vp],
@@ -296,6 +299,29 @@ class Tracer:
         self._check(lib().arc_trace_rays(self._ctx, _p(rays), len(rays), max_dist_m, lod_bias, int(ignore_water), _p(hits)),
                     "arc_trace_rays")
         return hits
+
+    def upload_world_slot(self, slot, grid, roots, nodes, bricks, palette):
+        g = np.asarray(grid, np.uint32)
+        roots = np.ascontiguousarray(roots, np.uint32)
+        nodes = np.ascontiguousarray(nodes).view(NODE_DTYPE)
+        bricks = np.ascontiguousarray(bricks).view(BRICK_DTYPE)
+        pal = np.ascontiguousarray(palette).view(MATERIAL_DTYPE)
+        self._check(lib().arc_upload_world_slot(self._ctx, slot, _p(g), _p(roots), len(roots), _p(nodes), len(nodes),
+                                                _p(bricks), len(bricks), _p(pal)), "arc_upload_world_slot")
+
+    def trace_views_dev(self, views: np.ndarray, n_gi=0, use_graph=True):
+        """views: numpy array of layout.VIEW_DTYPE (device output pointers filled in)."""
+        self._views = np.ascontiguousarray(views)
+        self._check(lib().arc_trace_views_dev(self._ctx, _p(self._views), len(self._views), n_gi or None,
+                                              int(use_graph)), "arc_trace_views_dev")
+
+    def autotune_views_dev(self, views: np.ndarray, frames=3):
+        best = LaunchConfig()
+        ms = C.c_float()
+        self._views = np.ascontiguousarray(views)
+        self._check(lib().arc_autotune_views_dev(self._ctx, _p(self._views), len(self._views), frames, C.byref(best),
+                                                 C.byref(ms)), "arc_autotune_views_dev")
+        return best, ms.value
 
     # passes (device pointers) -------------------------------------------------------------------
     def trace_frame_dev(self, w, h, gdm, gnm, gaa, hits=0, gi=0, n_gi=0):

@@ -55,6 +55,9 @@ def _args():
     p.add_argument("--height", type=int, default=HEIGHT)
     p.add_argument("--frame-only", action="store_true", help="time only the frame kernel (profiling runs)")
     p.add_argument("--no-autotune", action="store_true", help="keep the library's default launch configuration")
+    p.add_argument("--no-batched", action="store_true", help="skip the multi-view batch section")
+    p.add_argument("--no-nrc", action="store_true", help="skip the radiance-cache comparison section")
+    p.add_argument("--nrc-frames", type=int, default=60)
     return p.parse_args()
 
 
@@ -152,6 +155,11 @@ def _profile_traffic(kernel: str):
                 if line.startswith("dram_bytes_per_launch="):
                     return float(line.split("=", 1)[1])
     return None
+
+
+def _graph_ms(tracer):
+    """Device time between the context's start/end events around the last launch."""
+    return float(tracer.stats().last_kernel_ms)
 
 
 def cpu_leg(scene_name, seconds, threads, reference_query=True, frame=0):
@@ -337,6 +345,40 @@ def run_ours(args):
         e2e_rays += npx + cnt.value
     e2e_dt = time.perf_counter() - t0
     e2e_value = e2e_rays / e2e_dt / 1e6
+
+    # radiance caches at secondary hits on this world (NRC vs SHARC, same light transport)
+    nrc = None
+    if not args.no_nrc:
+        from arcadia_gb300 import gi_cache
+
+        t.set_launch_config(variant=cfg.variant)
+        nrc = gi_cache.run_comparison(t, SCENE, W_, H_, frames=args.nrc_frames)
+        nrc["unit"] = "ms/frame"
+        nrc["network"] = "216-64x5-3 FP16 weights, FP32 accumulation, mma.sync m16n8k16"
+
+    # many views over several worlds in one persistent launch replayed from a CUDA graph
+    batched = None
+    if not args.no_batched:
+        from arcadia_gb300.batch import BENCH_SCENES, Batch
+
+        b = Batch(t, BENCH_SCENES, 16)
+        best, _ = t.autotune_views_dev(b.table, frames=2)
+        n_gi_b = torch.zeros(1, dtype=torch.int64, device=dev)
+        b.trace(n_gi_b.data_ptr(), use_graph=True)  # capture + first replay
+        t.synchronize()
+        b_ms = []
+        for i in range(5):
+            b.set_frame(1 + i)
+            b.trace(n_gi_b.data_ptr(), use_graph=True)
+            t.synchronize()
+            b_ms.append(_graph_ms(t))
+        n_gi_last = int(n_gi_b.item())
+        batched = {"value": round((b.pixels + n_gi_last) / (statistics.mean(b_ms) * 1e-3) / 1e6, 3), "unit": UNIT,
+                   "views": len(b.views), "scenes": BENCH_SCENES, "pixels_per_frame": b.pixels,
+                   "gi_rays_last_frame": n_gi_last, "ms_per_frame": round(statistics.mean(b_ms), 3),
+                   "cuda_graph": True, "launches_per_frame": 1,
+                   "launch": {"block_threads": best.block_threads, "reg_blocks": best.reg_blocks,
+                              "refill_threshold": best.refill_threshold, "tile": [best.tile_w, best.tile_h]}}
     t.close()
     clk = clocks.stop() if clocks else None
 
@@ -377,6 +419,8 @@ def run_ours(args):
         "gpu_launches": args.steps,
         "roofline": roofline,
         "cpu_baseline": cpu,
+        "nrc": nrc,
+        "batched": batched,
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)

@@ -93,6 +93,24 @@ int arc_apply_patch(arc_ctx* ctx, uint32_t chunk_flat_idx, uint32_t new_root_nod
                     const arc_node64* nodes, uint32_t n_nodes, uint32_t brick_offset, const arc_brick64* bricks,
                     uint32_t n_bricks);
 int arc_set_camera(arc_ctx* ctx, const arc_camera_uniforms* cam);
+/* Extra worlds for batched launches (slots 1..7; slot 0 is the arc_upload_world world). No counterpart
+ * in the reference, which renders one WorldMap. */
+int arc_upload_world_slot(arc_ctx* ctx, uint32_t slot, const uint32_t grid[3], const uint32_t* roots, uint32_t n_roots,
+                          const arc_node64* nodes, uint32_t n_nodes, const arc_brick64* bricks, uint32_t n_bricks,
+                          const arc_material* palette);
+
+/* One view of a batched launch: world slot, resolution, camera block, device outputs. */
+typedef struct arc_view_desc {
+    uint32_t world_slot;
+    uint32_t width, height;
+    uint32_t pad;
+    arc_camera_uniforms cam;
+    uint32_t* gbuf_depth_mat;
+    uint32_t* gbuf_norm_motion;
+    uint32_t* gbuf_albedo_ao;
+    arc_hit_record* hits;    /* may be NULL */
+    arc_hit_record* gi_hits; /* may be NULL */
+} arc_view_desc;
 
 /* Primary pass: G-buffer (gbuf_depth_mat and gbuf_norm_motion: 2 u32 per pixel, gbuf_albedo_ao:
  * 1 u32 per pixel, row-major width x height) and optional per-pixel hit records. Width and height
@@ -123,6 +141,14 @@ int arc_trace_frame_dev(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t*
 int arc_trace_frame_noalloc(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbuf_depth_mat,
                             uint32_t* gbuf_norm_motion, uint32_t* gbuf_albedo_ao, arc_hit_record* hits,
                             arc_hit_record* gi_hits, uint64_t* n_gi_dev);
+/* Primary + GI rays of many views (several worlds, mixed resolutions) in one persistent launch; with
+ * use_graph the launch is captured once into a CUDA graph and replayed (re-captured when the view
+ * count, n_gi_dev or the launch configuration changes). Outputs per view as arc_trace_frame_dev.
+ * No counterpart in the reference (one view per frame there). */
+int arc_trace_views_dev(arc_ctx* ctx, const arc_view_desc* views, uint32_t n_views, uint64_t* n_gi_dev, int use_graph);
+/* Autotuner of the batched launch (block size x register budget x refill threshold x tile shape). */
+int arc_autotune_views_dev(arc_ctx* ctx, const arc_view_desc* views, uint32_t n_views, uint32_t frames,
+                           arc_launch_config* best, float* best_ms);
 /* trace_world_64tree on a batch of rays (origin m, unit dir). */
 int arc_trace_rays(arc_ctx* ctx, const arc_ray* rays, uint32_t n, float max_dist_m, uint32_t lod_bias,
                    int ignore_water, arc_hit_record* hits);
