@@ -71,6 +71,9 @@ struct arc_ctx {
     float* d_nrc_v = nullptr;
     float* d_nrc_grad = nullptr;
     void* d_nrc_w16 = nullptr;
+    float* d_nrc_ema = nullptr;       // exponential moving average of the weights (inference)
+    void* d_nrc_w16_ema = nullptr;    // its FP16 forward layout
+    float nrc_ema_decay = 0.99f;
     float* d_nrc_loss = nullptr;
     uint32_t nrc_step = 0;
 

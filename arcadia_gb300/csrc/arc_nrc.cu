@@ -181,7 +181,7 @@ __device__ __forceinline__ void load_weights_smem(__half* sw, const __half* __re
 }
 
 __global__ void __launch_bounds__(128) infer_kernel(const __half* __restrict__ w16, const float* __restrict__ in,
-                                                    uint32_t n, float* __restrict__ out) {
+                                                    const float* __restrict__ albedo, uint32_t n, float* __restrict__ out) {
     extern __shared__ __align__(16) __half smem[];
     load_weights_smem(smem, w16, kFwdHalves);
     __syncthreads();
@@ -193,7 +193,12 @@ __global__ void __launch_bounds__(128) infer_kernel(const __half* __restrict__ w
         load_inputs(in, n, r0, v0);
         load_inputs(in, n, r1, v1);
         forward16<false>(smem, nullptr, v0, v1, gid, tig, 0, y);
-        // output tile columns 2*tig, 2*tig+1 (valid: 0..2)
+        // output tile columns 2*tig, 2*tig+1 (valid: 0..2), times the albedo when one is given
+        if (albedo && tig < 2) {
+            const uint32_t c = 2u * tig;  // tig 1 holds column 2 only (y[1], y[3] are padding)
+            if (r0 < n) { y[0] *= __ldg(&albedo[r0 * 3 + c]); y[1] *= tig == 0 ? __ldg(&albedo[r0 * 3 + 1]) : 1.0f; }
+            if (r1 < n) { y[2] *= __ldg(&albedo[r1 * 3 + c]); y[3] *= tig == 0 ? __ldg(&albedo[r1 * 3 + 1]) : 1.0f; }
+        }
         if (tig == 0) {
             if (r0 < n) { out[r0 * 3] = y[0]; out[r0 * 3 + 1] = y[1]; }
             if (r1 < n) { out[r1 * 3] = y[2]; out[r1 * 3 + 1] = y[3]; }
@@ -349,10 +354,11 @@ __global__ void __launch_bounds__(128) train_kernel(const __half* __restrict__ w
     if (lane == 0) atomicAdd(loss_sum, my_loss);
 }
 
-// Adam on the FP32 masters, then refresh both FP16 layouts.
+// Adam on the FP32 masters, then refresh both FP16 layouts; the weight EMA (and its FP16 forward
+// layout, which inference reads) follows: ema = decay * ema + (1 - decay) * w.
 __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
-                            const float* __restrict__ g, __half* __restrict__ w16, float lr, float c1, float c2,
-                            float inv_scale) {
+                            const float* __restrict__ g, __half* __restrict__ w16, float* __restrict__ ema,
+                            __half* __restrict__ w16_ema, float decay, float lr, float c1, float c2, float inv_scale) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams) return;
     const float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
@@ -370,10 +376,15 @@ __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float*
     w16[fwd_off(l + 1) + o * fwd_stride(l + 1) + k] = h;
     if (l >= 1 && l <= 4) w16[kT2 + (l - 1) * 64 * kS + k * kS + o] = h;
     if (l == 5) w16[kT6 + k * kST6 + o] = h;
+    const float e = decay * ema[i] + (1.0f - decay) * wi;
+    ema[i] = e;
+    w16_ema[fwd_off(l + 1) + o * fwd_stride(l + 1) + k] = __float2half_rn(e);
 }
 
-// FP16 layouts from the masters (used after init / set_weights; padding stays zero).
-__global__ void pack_kernel(const float* __restrict__ w, __half* __restrict__ w16) {
+// FP16 layouts from the masters (used after init / set_weights; padding stays zero); the EMA restarts
+// from the same weights.
+__global__ void pack_kernel(const float* __restrict__ w, __half* __restrict__ w16, float* __restrict__ ema,
+                            __half* __restrict__ w16_ema) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams) return;
     int l = 0;
@@ -383,6 +394,8 @@ __global__ void pack_kernel(const float* __restrict__ w, __half* __restrict__ w1
     w16[fwd_off(l + 1) + o * fwd_stride(l + 1) + k] = h;
     if (l >= 1 && l <= 4) w16[kT2 + (l - 1) * 64 * kS + k * kS + o] = h;
     if (l == 5) w16[kT6 + k * kST6 + o] = h;
+    ema[i] = w[i];
+    w16_ema[fwd_off(l + 1) + o * fwd_stride(l + 1) + k] = h;
 }
 
 }  // namespace nrc
@@ -410,14 +423,17 @@ int nrc_cuda(arc_ctx* c, cudaError_t e, const char* what) {
 
 int ensure_nrc(arc_ctx* c) {
     if (c->d_nrc_w32) return ARC_OK;
-    NRC_CK(cudaMalloc((void**)&c->d_nrc_w32, sizeof(float) * nrc::kParams * 4));
+    NRC_CK(cudaMalloc((void**)&c->d_nrc_w32, sizeof(float) * nrc::kParams * 5));
     c->d_nrc_m = c->d_nrc_w32 + nrc::kParams;
     c->d_nrc_v = c->d_nrc_m + nrc::kParams;
     c->d_nrc_grad = c->d_nrc_v + nrc::kParams;
+    c->d_nrc_ema = c->d_nrc_grad + nrc::kParams;
     NRC_CK(cudaMalloc(&c->d_nrc_w16, sizeof(__half) * nrc::kAllHalves));
+    NRC_CK(cudaMalloc(&c->d_nrc_w16_ema, sizeof(__half) * nrc::kFwdHalves));
     NRC_CK(cudaMalloc((void**)&c->d_nrc_loss, sizeof(float)));
-    NRC_CK(cudaMemsetAsync(c->d_nrc_w32, 0, sizeof(float) * nrc::kParams * 4, c->stream));
+    NRC_CK(cudaMemsetAsync(c->d_nrc_w32, 0, sizeof(float) * nrc::kParams * 5, c->stream));
     NRC_CK(cudaMemsetAsync(c->d_nrc_w16, 0, sizeof(__half) * nrc::kAllHalves, c->stream));
+    NRC_CK(cudaMemsetAsync(c->d_nrc_w16_ema, 0, sizeof(__half) * nrc::kFwdHalves, c->stream));
     NRC_CK(cudaFuncSetAttribute(nrc::infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 nrc::kFwdHalves * (int)sizeof(__half)));
     NRC_CK(cudaFuncSetAttribute(nrc::train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -426,7 +442,7 @@ int ensure_nrc(arc_ctx* c) {
     return ARC_OK;
 }
 
-// Uniform(-sqrt(6/fan_in), sqrt(6/fan_in)) from a splitmix64 stream (He-uniform for the ReLU layers).
+// Uniform(-b, b) weights from a splitmix64 stream.
 void init_weights(std::vector<float>& w, uint32_t seed) {
     uint64_t s = 0x9E3779B97F4A7C15ull ^ seed;
     auto next = [&]() {
@@ -437,7 +453,9 @@ void init_weights(std::vector<float>& w, uint32_t seed) {
     };
     for (int l = 0; l < 6; ++l) {
         const int din = l == 0 ? nrc::kEnc : nrc::kW;
-        const float bound = std::sqrt(6.0f / (float)din);
+        // He-uniform for the ReLU layers; the linear output layer starts 10x smaller so the first
+        // predictions sit near zero instead of far above the radiance scale
+        const float bound = std::sqrt(6.0f / (float)din) * (l == 5 ? 0.1f : 1.0f);
         for (int i = nrc::off(l); i < nrc::off(l + 1); ++i) {
             const float u = (float)((next() >> 40) * (1.0 / 16777216.0));
             w[i] = (2.0f * u - 1.0f) * bound;
@@ -464,7 +482,8 @@ int arc_nrc_set_weights(arc_ctx* c, const float* w) {
     if (rc) return rc;
     NRC_CK(cudaMemcpyAsync(c->d_nrc_w32, w, sizeof(float) * nrc::kParams, cudaMemcpyHostToDevice, c->stream));
     NRC_CK(cudaMemsetAsync(c->d_nrc_m, 0, sizeof(float) * nrc::kParams * 2, c->stream));
-    nrc::pack_kernel<<<(nrc::kParams + 255) / 256, 256, 0, c->stream>>>(c->d_nrc_w32, static_cast<__half*>(c->d_nrc_w16));
+    nrc::pack_kernel<<<(nrc::kParams + 255) / 256, 256, 0, c->stream>>>(c->d_nrc_w32, static_cast<__half*>(c->d_nrc_w16),
+                                                                       c->d_nrc_ema, static_cast<__half*>(c->d_nrc_w16_ema));
     NRC_CK(cudaGetLastError());
     c->nrc_step = 0;
     return arc_ctx_finish(c);
@@ -478,14 +497,32 @@ int arc_nrc_get_weights(arc_ctx* c, float* w) {
     return arc_ctx_finish(c);
 }
 
-int arc_nrc_query_dev(arc_ctx* c, const float* inputs, uint32_t n, float* out) {
+int arc_nrc_get_ema_weights(arc_ctx* c, float* w) {
+    if (!c || !w) return ARC_E_INVALID_ARG;
+    int rc = ensure_nrc(c);
+    if (rc) return rc;
+    NRC_CK(cudaMemcpyAsync(w, c->d_nrc_ema, sizeof(float) * nrc::kParams, cudaMemcpyDeviceToHost, c->stream));
+    return arc_ctx_finish(c);
+}
+
+int arc_nrc_set_ema_decay(arc_ctx* c, float decay) {
+    if (!c) return ARC_E_INVALID_ARG;
+    if (!(decay >= 0.0f && decay < 1.0f)) {
+        c->err = "EMA decay must lie in [0, 1)";
+        return ARC_E_INVALID_ARG;
+    }
+    c->nrc_ema_decay = decay;
+    return ARC_OK;
+}
+
+int arc_nrc_query_dev(arc_ctx* c, const float* inputs, const float* albedo, uint32_t n, float* out) {
     if (!c) return ARC_E_INVALID_ARG;
     if (n && (!inputs || !out)) return nrc_err(c, ARC_E_INVALID_ARG, "null buffer");
     int rc = ensure_nrc(c);
     if (rc || n == 0) return rc;
     const uint32_t tiles = (n + 15u) / 16u;
     const uint32_t blocks = std::min<uint32_t>((tiles + 3u) / 4u, (uint32_t)c->n_sm * 3u);
-    nrc::infer_kernel<<<blocks, 128, nrc::kFwdHalves * sizeof(__half), c->stream>>>(static_cast<const __half*>(c->d_nrc_w16), inputs, n, out);
+    nrc::infer_kernel<<<blocks, 128, nrc::kFwdHalves * sizeof(__half), c->stream>>>(static_cast<const __half*>(c->d_nrc_w16_ema), inputs, albedo, n, out);
     NRC_CK(cudaGetLastError());
     return ARC_OK;
 }
@@ -512,9 +549,9 @@ int arc_nrc_train_step_dev(arc_ctx* c, const float* inputs, const float* targets
     if (rc) return rc;
     c->nrc_step += 1;
     const float c1 = 1.0f - std::pow(0.9f, (float)c->nrc_step), c2 = 1.0f - std::pow(0.99f, (float)c->nrc_step);
-    nrc::adam_kernel<<<(nrc::kParams + 255) / 256, 256, 0, c->stream>>>(c->d_nrc_w32, c->d_nrc_m, c->d_nrc_v,
-                                                                       c->d_nrc_grad, static_cast<__half*>(c->d_nrc_w16), lr, c1, c2,
-                                                                       1.0f / nrc::kLossScale);
+    nrc::adam_kernel<<<(nrc::kParams + 255) / 256, 256, 0, c->stream>>>(
+        c->d_nrc_w32, c->d_nrc_m, c->d_nrc_v, c->d_nrc_grad, static_cast<__half*>(c->d_nrc_w16), c->d_nrc_ema,
+        static_cast<__half*>(c->d_nrc_w16_ema), c->nrc_ema_decay, lr, c1, c2, 1.0f / nrc::kLossScale);
     NRC_CK(cudaGetLastError());
     if (loss_host) {
         float l = 0.0f;

@@ -118,9 +118,18 @@ __device__ __forceinline__ f3 sky_radiance(f3 dir, f3 sun) {
 
 struct Surface {
     bool hit;
+    uint32_t mat;
     float t_m;
     f3 pos, normal, albedo, emission;
 };
+
+// Lambertian albedo of the cache comparison: per material id, each channel drawn from U[0.1, 0.9]
+// by a PCG stream (the same value wherever the material appears).
+__device__ __forceinline__ f3 cmp_albedo(uint32_t mat) {
+    const uint32_t h0 = pcg_hash(mat * 3u + 0x2545F491u), h1 = pcg_hash(h0 ^ 0x9E3779B9u), h2 = pcg_hash(h1 ^ 0x85EBCA6Bu);
+    const float s = 0.8f / 16777216.0f;
+    return f3{0.1f + (float)(h0 >> 8) * s, 0.1f + (float)(h1 >> 8) * s, 0.1f + (float)(h2 >> 8) * s};
+}
 
 // sharc_trace_surface (shaders/sharc_update.wgsl:32-64) without rigid bodies.
 __device__ __forceinline__ Surface trace_surface(const World& w, const arc_camera_uniforms& cam, f3 o, f3 d, float max_dist) {
@@ -141,6 +150,7 @@ __device__ __forceinline__ Surface trace_surface(const World& w, const arc_camer
     const float lg = __fdiv_rn((float)((h.lod_payload >> 8) & 0xFFu), 255.0f);
     const float lb = __fdiv_rn((float)((h.lod_payload >> 16) & 0xFFu), 255.0f);
     out.hit = true;
+    out.mat = h.mat;
     out.t_m = h.t_voxels * ARC_VOXEL_SIZE;
     out.pos = h.hit_pos_m;
     out.normal = h.normal;
@@ -215,7 +225,7 @@ __global__ void sharc_update_kernel(const World w, const __grid_constant__ arc_c
     const Surface s1 = trace_surface(w, cam, add3(x0, mul3s(n0, 0.10f)), d0, bounce_max);
     if (!s1.hit) return;
     if (mode == 1u) {  // cache-comparison estimator instead of sharc_shade_surface
-        const f3 rad = onebounce(w, cam, s1.pos, s1.normal, s1.albedo, hsh ^ (frame * 0x9E3779B9u));
+        const f3 rad = onebounce(w, cam, s1.pos, s1.normal, cmp_albedo(s1.mat), hsh ^ (frame * 0x9E3779B9u));
         uint32_t bk, key;
         sharc_key(s1.pos, s1.normal, eye, 0.0f, 0.0f, &bk, &key);
         sharc_deposit(S, bk, key, rad);
@@ -319,7 +329,7 @@ __global__ void sharc_deposit_kernel(SharcBuffers S, f3 pos, f3 n, f3 cam, f3 ra
 }
 
 // GI hit points of a frame: per pixel with a primary hit, the Pass-2A GI ray is traced again from the
-// G-buffer and its hit recorded as position, normal, SHARC surface albedo and the 9 NRC inputs
+// G-buffer and its hit recorded as position, normal, material albedo (cmp_albedo) and the 9 NRC inputs
 // (position / world extent, normal, view direction = -ray direction).
 __global__ void gi_points_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, const uint32_t* __restrict__ gdm,
                                  const uint32_t* __restrict__ gnm, uint32_t W, uint32_t H, float* __restrict__ pos,
@@ -341,19 +351,16 @@ __global__ void gi_points_kernel(const World w, const __grid_constant__ arc_came
         }
         if (r == kHit) {
             ok = 1u;
-            const float4 a = __ldg(&w.palette[2u * h.mat]);
-            const float lr = __fdiv_rn((float)(h.lod_payload & 0xFFu), 255.0f);
-            const float lg = __fdiv_rn((float)((h.lod_payload >> 8) & 0xFFu), 255.0f);
-            const float lb = __fdiv_rn((float)((h.lod_payload >> 16) & 0xFFu), 255.0f);
+            const f3 a = cmp_albedo(h.mat);
             pos[3 * k] = h.hit_pos_m.x;
             pos[3 * k + 1] = h.hit_pos_m.y;
             pos[3 * k + 2] = h.hit_pos_m.z;
             nrm[3 * k] = h.normal.x;
             nrm[3 * k + 1] = h.normal.y;
             nrm[3 * k + 2] = h.normal.z;
-            alb[3 * k] = mixf(a.x, lr, 0.55f);
-            alb[3 * k + 1] = mixf(a.y, lg, 0.55f);
-            alb[3 * k + 2] = mixf(a.z, lb, 0.55f);
+            alb[3 * k] = a.x;
+            alb[3 * k + 1] = a.y;
+            alb[3 * k + 2] = a.z;
             const float ex = (float)cam.world_grid_dims[0] * 16.0f, ey = (float)cam.world_grid_dims[1] * 16.0f,
                         ez = (float)cam.world_grid_dims[2] * 16.0f;
             float* q = nrc_in + 9 * k;
@@ -402,10 +409,12 @@ __global__ void onebounce_kernel(const World w, const __grid_constant__ arc_came
 }
 
 // NRC training samples: every valid GI point is taken with probability accept (PCG per pixel and frame);
-// a taken point gets a slot from the counter (up to max_n) and a 1-spp one-bounce target.
+// a taken point gets a slot from the counter (up to max_n) and a 1-spp one-bounce target demodulated by
+// the albedo (the estimator with albedo 1: the network learns the light arriving at the surface, and
+// the query multiplies the albedo back in).
 __global__ void train_samples_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, uint32_t n_px,
                                      const uint32_t* __restrict__ valid, const float* __restrict__ pos,
-                                     const float* __restrict__ nrm, const float* __restrict__ alb,
+                                     const float* __restrict__ nrm,
                                      const float* __restrict__ nrc_in, float accept, uint32_t seed, uint32_t max_n,
                                      float* __restrict__ train_in, float* __restrict__ train_t, uint32_t* __restrict__ count) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -415,7 +424,7 @@ __global__ void train_samples_kernel(const World w, const __grid_constant__ arc_
     const uint32_t slot = atomicAdd(count, 1u);
     if (slot >= max_n) return;
     const f3 l = onebounce(w, cam, f3{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]}, f3{nrm[3 * p], nrm[3 * p + 1], nrm[3 * p + 2]},
-                           f3{alb[3 * p], alb[3 * p + 1], alb[3 * p + 2]}, pcg_hash(h ^ 0xB5297A4Du));
+                           f3{1.0f, 1.0f, 1.0f}, pcg_hash(h ^ 0xB5297A4Du));
 #pragma unroll
     for (int k = 0; k < 9; ++k) train_in[(size_t)slot * 9 + k] = nrc_in[(size_t)p * 9 + k];
     train_t[3 * slot] = l.x;
@@ -516,15 +525,14 @@ int arc_onebounce_dev(arc_ctx* c, const uint32_t* idx, uint32_t n, const float* 
 }
 
 int arc_nrc_train_samples_dev(arc_ctx* c, uint32_t n_px, const uint32_t* valid, const float* pos, const float* nrm,
-                              const float* albedo, const float* nrc_in, float accept, uint32_t seed, uint32_t max_n,
-                              float* train_in, float* train_t, uint32_t* count) {
+                              const float* nrc_in, float accept, uint32_t seed, uint32_t max_n, float* train_in,
+                              float* train_t, uint32_t* count) {
     int rc = arc_ctx_check_ready(c, true);
     if (rc) return rc;
-    if (!valid || !pos || !nrm || !albedo || !nrc_in || !train_in || !train_t || !count) return sharc_err(c, ARC_E_INVALID_ARG, "null buffer");
+    if (!valid || !pos || !nrm || !nrc_in || !train_in || !train_t || !count) return sharc_err(c, ARC_E_INVALID_ARG, "null buffer");
     cudaMemsetAsync(count, 0, sizeof(uint32_t), c->stream);
     if (n_px == 0) return ARC_OK;
-    arc::train_samples_kernel<<<(n_px + 127u) / 128u, 128, 0, c->stream>>>(c->world(), c->cam, n_px, valid, pos, nrm, albedo,
-                                                                            nrc_in, accept, seed, max_n, train_in, train_t,
+    arc::train_samples_kernel<<<(n_px + 127u) / 128u, 128, 0, c->stream>>>(c->world(), c->cam, n_px, valid, pos, nrm, nrc_in, accept, seed, max_n, train_in, train_t,
                                                                             count);
     return launch_check(c, "train_samples_kernel");
 }

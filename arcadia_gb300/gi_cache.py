@@ -10,6 +10,11 @@ Both caches learn the same quantity, the one-bounce radiance L(x) at the hit of 
   NRC pipeline      arc_nrc_train_samples_dev (65,536 one-bounce samples) + arc_nrc_train_step_dev
                     (fused forward/backward/Adam) + arc_nrc_query_dev at every GI hit
 
+The surfaces are Lambertian with one albedo per material (U[0.1, 0.9] per channel). SHARC caches the
+reflected radiance as the reference does. The network learns the demodulated quantity L / albedo,
+which depends only on position and normal (the inputs it is given), and the query multiplies the
+albedo back in.
+
 Quality is the relative MSE, mean((pred - ref)^2 / (ref^2 + 0.01)), against a 4096-spp reference of
 the estimator at a fixed set of GI hit points. The reference is traced in FP32 on the GPU (64
 launches of 64 spp) and accumulated in FP64 on the host.
@@ -102,21 +107,25 @@ class CacheComparison:
         b.synchronize()
         return a.elapsed_time(b)
 
-    def nrc_frame(self, seed, lr=1e-3):
+    def nrc_frame(self, seed, lr=1e-3, steps=8):
+        """Training samples, `steps` Adam steps on equal slices of them, then inference at every pixel."""
         n_px = self.w * self.h
         accept = min(1.0, 1.25 * TRAIN_SAMPLES / max(self.last_valid, 1))
         a = self._event()
         self._ck(self.lib.arc_nrc_train_samples_dev(self.t.ctx, n_px, self.valid.data_ptr(), self.pos.data_ptr(),
-                                                    self.nrm.data_ptr(), self.alb.data_ptr(), self.nin.data_ptr(),
-                                                    C.c_float(accept), seed, TRAIN_SAMPLES, self.train_in.data_ptr(),
-                                                    self.train_t.data_ptr(), self.count.data_ptr()),
+                                                    self.nrm.data_ptr(), self.nin.data_ptr(), C.c_float(accept), seed,
+                                                    TRAIN_SAMPLES, self.train_in.data_ptr(), self.train_t.data_ptr(),
+                                                    self.count.data_ptr()),
                  "arc_nrc_train_samples_dev")
+        self._event().synchronize()  # the counter is written on the tracer's stream
         n_train = min(int(self.count.item()), TRAIN_SAMPLES)  # one small read per frame
-        if n_train:
-            self._ck(self.lib.arc_nrc_train_step_dev(self.t.ctx, self.train_in.data_ptr(), self.train_t.data_ptr(),
-                                                     n_train, C.c_float(lr), None), "arc_nrc_train_step_dev")
-        self._ck(self.lib.arc_nrc_query_dev(self.t.ctx, self.nin.data_ptr(), n_px, self.nrc_out.data_ptr()),
-                 "arc_nrc_query_dev")
+        per = n_train // steps
+        for k in range(steps if per else 0):
+            self._ck(self.lib.arc_nrc_train_step_dev(self.t.ctx, self.train_in[k * per:].data_ptr(),
+                                                     self.train_t[k * per:].data_ptr(), per, C.c_float(lr), None),
+                     "arc_nrc_train_step_dev")
+        self._ck(self.lib.arc_nrc_query_dev(self.t.ctx, self.nin.data_ptr(), self.alb.data_ptr(), n_px,
+                                            self.nrc_out.data_ptr()), "arc_nrc_query_dev")
         b = self._event()
         b.synchronize()
         self.last_valid = int(self.n_valid.item())
@@ -148,9 +157,10 @@ class CacheComparison:
         return out.cpu().numpy()
 
 
-def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920, height=1080, frames=60,
-                   eval_points=16384, seed=7):
-    """Runs both pipelines for `frames` frames on a static camera and scores them on the last frame."""
+def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920, height=1080, frames=300,
+                   eval_points=16384, seed=7, steps_per_frame=8, lr=1e-3, curve=(30, 60, 120)):
+    """Runs both pipelines for `frames` frames on a static camera and scores them on the last frame;
+    `curve` lists earlier frames at which both are scored as well (8192 points each)."""
     scene = L.SCENES[scene_name]
     cc = CacheComparison(tracer, scene, width, height)
     lib = cc.lib
@@ -158,10 +168,17 @@ def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920
     tracer.sharc_reset()
     cc._ck(lib.arc_nrc_init(tracer.ctx, seed), "arc_nrc_init")
     shared_ms, sharc_ms, nrc_ms = [], [], []
+    conv = []
     for f in range(frames):
         shared_ms.append(cc.shared(f))
         sharc_ms.append(cc.sharc_frame())
-        nrc_ms.append(cc.nrc_frame(seed * 1000003 + f)[0])
+        nrc_ms.append(cc.nrc_frame(seed * 1000003 + f, lr=lr, steps=steps_per_frame)[0])
+        if f + 1 in curve and f + 1 < frames:
+            cand = np.nonzero(cc.valid.cpu().numpy().astype(bool))[0]
+            ci = cand[np.linspace(0, len(cand) - 1, min(8192, len(cand))).astype(np.int64)]
+            cref = cc.reference(ci)
+            conv.append({"frame": f + 1, "rel_mse_nrc": rel_mse(cc.nrc_out.cpu().numpy()[ci], cref),
+                         "rel_mse_sharc": rel_mse(cc.sharc_out.cpu().numpy()[ci][:, :3], cref)})
     valid = cc.valid.cpu().numpy().astype(bool)
     cand = np.nonzero(valid)[0]
     idx = cand[np.linspace(0, len(cand) - 1, min(eval_points, len(cand))).astype(np.int64)]
@@ -172,13 +189,16 @@ def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920
     sharc_hit = sharc[:, 3] > 0.5
     # untrained network, same points (the method without the learned part)
     cc._ck(lib.arc_nrc_init(tracer.ctx, seed), "arc_nrc_init")
-    cc._ck(lib.arc_nrc_query_dev(tracer.ctx, cc.nin.data_ptr(), width * height, cc.nrc_out.data_ptr()), "query")
+    cc._ck(lib.arc_nrc_query_dev(tracer.ctx, cc.nin.data_ptr(), cc.alb.data_ptr(), width * height, cc.nrc_out.data_ptr()),
+           "query")
     tracer.synchronize()
     untrained = cc.nrc_out.cpu().numpy()[idx]
     cc._ck(lib.arc_sharc_set_mode(tracer.ctx, 0), "arc_sharc_set_mode")
     steady = slice(frames // 2, None)
     return {
         "frames": frames,
+        "train_steps_per_frame": steps_per_frame,
+        "lr": lr,
         "width": width,
         "height": height,
         "eval_points": int(len(idx)),
@@ -195,4 +215,5 @@ def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920
         "rel_mse_nrc_on_sharc_hits": rel_mse(nrc[sharc_hit], ref[sharc_hit]) if sharc_hit.any() else None,
         "rel_mse_1spp": rel_mse(raw, ref),
         "rel_mse_untrained_nrc": rel_mse(untrained, ref),
+        "convergence": conv,
     }

@@ -57,7 +57,7 @@ def _args():
     p.add_argument("--no-autotune", action="store_true", help="keep the library's default launch configuration")
     p.add_argument("--no-batched", action="store_true", help="skip the multi-view batch section")
     p.add_argument("--no-nrc", action="store_true", help="skip the radiance-cache comparison section")
-    p.add_argument("--nrc-frames", type=int, default=60)
+    p.add_argument("--nrc-frames", type=int, default=300)
     return p.parse_args()
 
 

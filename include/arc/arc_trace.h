@@ -176,17 +176,19 @@ int arc_sharc_deposit_dev(arc_ctx* ctx, const float pos[3], const float normal[3
  * (1, 0.9, 0.75) * 0.55, L_sky = (0.30, 0.42, 0.60). mode 0 = reference sharc_shade_surface (default),
  * mode 1 = that estimator in arc_sharc_update_dev. No counterpart in the reference. */
 int arc_sharc_set_mode(arc_ctx* ctx, uint32_t mode);
-/* GI hit points of a frame (per pixel: position, normal, albedo, 9 NRC inputs, valid flag). */
+/* GI hit points of a frame (per pixel: position, normal, albedo, 9 NRC inputs, valid flag). The albedo
+ * is the comparison's Lambertian albedo per material id, each channel from U[0.1, 0.9]. */
 int arc_gi_points_dev(arc_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* gbuf_depth_mat,
                       const uint32_t* gbuf_norm_motion, float* pos, float* normal, float* albedo, float* nrc_in,
                       uint32_t* valid, uint64_t* n_valid);
 /* Mean of spp one-bounce samples at points idx[i] (idx may be NULL = identity); accumulate adds. */
 int arc_onebounce_dev(arc_ctx* ctx, const uint32_t* idx, uint32_t n, const float* pos, const float* normal,
                       const float* albedo, uint32_t spp, uint32_t seed, int accumulate, float* out);
-/* NRC training samples: each valid point taken with probability accept, up to max_n, 1-spp targets. */
+/* NRC training samples: each valid point taken with probability accept, up to max_n, 1-spp targets
+ * demodulated by the albedo (the estimator with albedo 1). */
 int arc_nrc_train_samples_dev(arc_ctx* ctx, uint32_t n_px, const uint32_t* valid, const float* pos,
-                              const float* normal, const float* albedo, const float* nrc_in, float accept,
-                              uint32_t seed, uint32_t max_n, float* train_in, float* train_t, uint32_t* count);
+                              const float* normal, const float* nrc_in, float accept, uint32_t seed,
+                              uint32_t max_n, float* train_in, float* train_t, uint32_t* count);
 
 /* Neural radiance cache (no reference counterpart: it stands in for query_sharc at secondary hits).
  * 9 inputs per query: position normalised to [0,1]^3, normal, view direction; 3 outputs (RGB).
@@ -194,7 +196,13 @@ int arc_nrc_train_samples_dev(arc_ctx* ctx, uint32_t n_px, const uint32_t* valid
 int arc_nrc_init(arc_ctx* ctx, uint32_t seed);
 int arc_nrc_set_weights(arc_ctx* ctx, const float* weights);
 int arc_nrc_get_weights(arc_ctx* ctx, float* weights);
-int arc_nrc_query_dev(arc_ctx* ctx, const float* inputs, uint32_t n, float* out_rgb);
+/* Inference reads an exponential moving average of the weights, ema = decay * ema + (1 - decay) * w
+ * after every Adam step (decay 0.99 by default; 0 = the latest weights). set_weights / init restart
+ * it from the given weights. */
+int arc_nrc_set_ema_decay(arc_ctx* ctx, float decay);
+int arc_nrc_get_ema_weights(arc_ctx* ctx, float* weights);
+/* out_rgb[i] = albedo[i] * network(inputs[i]) per channel; albedo may be NULL (network output only). */
+int arc_nrc_query_dev(arc_ctx* ctx, const float* inputs, const float* albedo, uint32_t n, float* out_rgb);
 /* Loss-scaled (x128) weight gradient of the mean relative-L2 loss of one batch (device output). */
 int arc_nrc_grad_dev(arc_ctx* ctx, const float* inputs, const float* targets, uint32_t n, float* grad_out);
 /* One Adam step (lr; beta 0.9/0.99) on a batch; loss_host (optional) receives the batch loss. */

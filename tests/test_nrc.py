@@ -127,11 +127,18 @@ def test_gpu_inference_matches_oracle(orc, tracer):
     _set(tracer, w)
     dx = torch.from_numpy(x).cuda()
     dy = torch.zeros((len(x), 3), dtype=torch.float32, device="cuda")
-    assert lib().arc_nrc_query_dev(tracer.ctx, dx.data_ptr(), len(x), dy.data_ptr()) == 0
+    assert lib().arc_nrc_query_dev(tracer.ctx, dx.data_ptr(), None, len(x), dy.data_ptr()) == 0
     tracer.synchronize()
     y = dy.cpu().numpy()
     ref = orc.nrc_forward(w, x)
     assert np.all(np.abs(y - ref) <= 2e-2 * np.abs(ref) + 2e-3), np.max(np.abs(y - ref))
+    # albedo epilogue: one FP32 multiply per channel of the same network output
+    alb = np.random.default_rng(3).uniform(0.1, 0.9, (len(x), 3)).astype(np.float32)
+    dm = torch.zeros_like(dy)
+    assert lib().arc_nrc_query_dev(tracer.ctx, dx.data_ptr(), torch.from_numpy(alb).cuda().data_ptr(), len(x),
+                                   dm.data_ptr()) == 0
+    tracer.synchronize()
+    np.testing.assert_array_equal(dm.cpu().numpy(), y * alb)
 
 
 @pytest.mark.gpu
@@ -202,3 +209,36 @@ def test_gpu_training_reduces_loss(tracer):
         losses.append(loss.value)
     assert np.isfinite(losses).all()
     assert np.mean(losses[-10:]) < 0.1 * np.mean(losses[:3]), (losses[:3], losses[-3:])
+
+
+@pytest.mark.gpu
+def test_gpu_weight_ema_feeds_inference(orc, tracer):
+    """After each Adam step ema = d * ema + (1 - d) * w (FP32), and the query evaluates the EMA weights."""
+    import torch
+    from arcadia_gb300.native import lib
+
+    x, t = _data(2048, 15)
+    w = _weights(16)
+    _set(tracer, w)
+    d = np.float32(0.9)
+    assert lib().arc_nrc_set_ema_decay(tracer.ctx, float(d)) == 0
+    try:
+        dx, dt = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
+        ema = w.copy()
+        for _ in range(3):
+            assert lib().arc_nrc_train_step_dev(tracer.ctx, dx.data_ptr(), dt.data_ptr(), len(x), 1e-3, None) == 0
+            wk = np.zeros(30400, np.float32)
+            assert lib().arc_nrc_get_weights(tracer.ctx, wk.ctypes.data) == 0
+            ema = d * ema + (np.float32(1) - d) * wk
+        eg = np.zeros(30400, np.float32)
+        assert lib().arc_nrc_get_ema_weights(tracer.ctx, eg.ctypes.data) == 0
+        np.testing.assert_allclose(eg, ema, atol=1e-6)
+        assert np.abs(eg - wk).max() > 1e-4  # the EMA lags the latest weights
+        dy = torch.zeros((len(x), 3), dtype=torch.float32, device="cuda")
+        assert lib().arc_nrc_query_dev(tracer.ctx, dx.data_ptr(), None, len(x), dy.data_ptr()) == 0
+        tracer.synchronize()
+        y, ref = dy.cpu().numpy(), orc.nrc_forward(eg, x)
+        assert np.all(np.abs(y - ref) <= 2e-2 * np.abs(ref) + 2e-3), np.max(np.abs(y - ref))
+        assert lib().arc_nrc_set_ema_decay(tracer.ctx, 1.0) != 0  # outside [0, 1)
+    finally:
+        assert lib().arc_nrc_set_ema_decay(tracer.ctx, 0.99) == 0
