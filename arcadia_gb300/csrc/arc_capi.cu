@@ -213,6 +213,8 @@ int arc_destroy(arc_ctx* c) {
     cudaFree(c->d_nrc_w32);
     cudaFree(c->d_nrc_w16);
     cudaFree(c->d_nrc_w16_ema);
+    cudaFree(c->d_nrc_batch);
+    cudaFree(c->d_nrc_gate);
     cudaFree(c->d_nrc_loss);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);

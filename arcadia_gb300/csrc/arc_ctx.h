@@ -76,6 +76,11 @@ struct arc_ctx {
     float nrc_ema_decay = 0.99f;
     float* d_nrc_loss = nullptr;
     uint32_t nrc_step = 0;
+    // per-frame training batch of arc_nrc_train_frame_dev: inputs (9 floats) + targets (3), and the
+    // gate word (the batch size, 0 when the frame has no GI hit) that the training kernels read
+    float* d_nrc_batch = nullptr;
+    uint32_t nrc_batch_cap = 0;
+    uint32_t* d_nrc_gate = nullptr;
 
     arc_launch_config cfg{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -89,5 +94,11 @@ struct arc_ctx {
 
 int arc_ctx_check_ready(arc_ctx* c, bool need_cam);
 int arc_ctx_finish(arc_ctx* c);
+// NRC training samples drawn from a compacted list of GI hit points (defined with the estimator in
+// arc_sharc.cu): sample i takes list[hash(i, seed) mod *n_valid] and its demodulated 1-spp target;
+// gate receives n_samples, or 0 when *n_valid is 0.
+extern "C" int arc_launch_train_samples_list(arc_ctx* c, const uint32_t* list, const unsigned long long* n_valid,
+                                             const float* pos, const float* nrm, const float* nrc_in, uint32_t seed,
+                                             uint32_t n_samples, float* train_in, float* train_t, uint32_t* gate);
 int arc_ctx_stage(arc_ctx* c, size_t bytes, void** out);
 int arc_ctx_sync_world_table(arc_ctx* c);

@@ -110,6 +110,7 @@ __device__ __forceinline__ void relu_to_a(const float (&acc)[8][4], uint32_t (&a
 }
 
 __device__ __forceinline__ void load_inputs(const float* __restrict__ in, uint32_t n, uint32_t row, float (&v)[kIn]) {
+    // training batch rows (row < n)
 #pragma unroll
     for (int i = 0; i < kIn; ++i) v[i] = row < n ? __ldg(&in[(size_t)row * kIn + i]) : 0.0f;
 }
@@ -180,31 +181,46 @@ __device__ __forceinline__ void load_weights_smem(__half* sw, const __half* __re
     for (int i = threadIdx.x; i < halves / 8; i += blockDim.x) dst[i] = src[i];
 }
 
+// Query rows j < n (n = min(n, *n_dev) when n_dev is given); row j reads and writes point list[j] when a
+// list is given, else point j.
 __global__ void __launch_bounds__(128) infer_kernel(const __half* __restrict__ w16, const float* __restrict__ in,
-                                                    const float* __restrict__ albedo, uint32_t n, float* __restrict__ out) {
+                                                    const float* __restrict__ albedo, uint32_t n, float* __restrict__ out,
+                                                    const uint32_t* __restrict__ list,
+                                                    const unsigned long long* __restrict__ n_dev) {
     extern __shared__ __align__(16) __half smem[];
+    if (n_dev) {
+        const unsigned long long nd = *n_dev;
+        n = nd < n ? (uint32_t)nd : n;
+    }
     load_weights_smem(smem, w16, kFwdHalves);
     __syncthreads();
     const int lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
     const uint32_t warps = blockDim.x >> 5, tiles = (n + 15u) / 16u;
     for (uint32_t t = blockIdx.x * warps + (threadIdx.x >> 5); t < tiles; t += gridDim.x * warps) {
-        const uint32_t r0 = t * 16u + gid, r1 = r0 + 8u;
+        const uint32_t j0 = t * 16u + gid, j1 = j0 + 8u;
+        const bool ok0 = j0 < n, ok1 = j1 < n;
+        const uint32_t p0 = list ? (ok0 ? __ldg(&list[j0]) : 0u) : j0;
+        const uint32_t p1 = list ? (ok1 ? __ldg(&list[j1]) : 0u) : j1;
         float v0[kIn], v1[kIn], y[4];
-        load_inputs(in, n, r0, v0);
-        load_inputs(in, n, r1, v1);
-        forward16<false>(smem, nullptr, v0, v1, gid, tig, 0, y);
-        // output tile columns 2*tig, 2*tig+1 (valid: 0..2), times the albedo when one is given
-        if (albedo && tig < 2) {
-            const uint32_t c = 2u * tig;  // tig 1 holds column 2 only (y[1], y[3] are padding)
-            if (r0 < n) { y[0] *= __ldg(&albedo[r0 * 3 + c]); y[1] *= tig == 0 ? __ldg(&albedo[r0 * 3 + 1]) : 1.0f; }
-            if (r1 < n) { y[2] *= __ldg(&albedo[r1 * 3 + c]); y[3] *= tig == 0 ? __ldg(&albedo[r1 * 3 + 1]) : 1.0f; }
+#pragma unroll
+        for (int i = 0; i < kIn; ++i) {
+            v0[i] = ok0 ? __ldg(&in[(size_t)p0 * kIn + i]) : 0.0f;
+            v1[i] = ok1 ? __ldg(&in[(size_t)p1 * kIn + i]) : 0.0f;
         }
-        if (tig == 0) {
-            if (r0 < n) { out[r0 * 3] = y[0]; out[r0 * 3 + 1] = y[1]; }
-            if (r1 < n) { out[r1 * 3] = y[2]; out[r1 * 3 + 1] = y[3]; }
-        } else if (tig == 1) {
-            if (r0 < n) out[r0 * 3 + 2] = y[0];
-            if (r1 < n) out[r1 * 3 + 2] = y[2];
+        forward16<false>(smem, nullptr, v0, v1, gid, tig, 0, y);
+        // output tile columns 2*tig, 2*tig+1 (valid: 0..2; tig 1 holds column 2 only), times the albedo
+        if (tig < 2) {
+            const size_t c = 2u * tig;
+            if (ok0) {
+                const size_t o = (size_t)p0 * 3 + c;
+                out[o] = albedo ? y[0] * __ldg(&albedo[o]) : y[0];
+                if (tig == 0) out[o + 1] = albedo ? y[1] * __ldg(&albedo[o + 1]) : y[1];
+            }
+            if (ok1) {
+                const size_t o = (size_t)p1 * 3 + c;
+                out[o] = albedo ? y[2] * __ldg(&albedo[o]) : y[2];
+                if (tig == 0) out[o + 1] = albedo ? y[3] * __ldg(&albedo[o + 1]) : y[3];
+            }
         }
     }
 }
@@ -274,8 +290,10 @@ __device__ __forceinline__ void backward64(const __half* sw, int l, const uint32
 
 __global__ void __launch_bounds__(128) train_kernel(const __half* __restrict__ w16, const float* __restrict__ in,
                                                     const float* __restrict__ target, uint32_t n, float inv_norm,
-                                                    float* __restrict__ grad, float* __restrict__ loss_sum) {
+                                                    float* __restrict__ grad, float* __restrict__ loss_sum,
+                                                    const uint32_t* __restrict__ gate) {
     extern __shared__ __align__(16) __half smem[];
+    if (gate && *gate == 0u) return;  // empty frame batch: no gradient (uniform over the grid)
     __half* sw = smem;                      // forward + transposed weights
     __half* act = smem + kAllHalves;        // XT, HT1..5, dZT x2
     load_weights_smem(sw, w16, kAllHalves);
@@ -358,9 +376,10 @@ __global__ void __launch_bounds__(128) train_kernel(const __half* __restrict__ w
 // layout, which inference reads) follows: ema = decay * ema + (1 - decay) * w.
 __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
                             const float* __restrict__ g, __half* __restrict__ w16, float* __restrict__ ema,
-                            __half* __restrict__ w16_ema, float decay, float lr, float c1, float c2, float inv_scale) {
+                            __half* __restrict__ w16_ema, float decay, float lr, float c1, float c2, float inv_scale,
+                            const uint32_t* __restrict__ gate) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= kParams) return;
+    if (i >= kParams || (gate && *gate == 0u)) return;
     const float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
     const float gi = g[i] * inv_scale;
     const float mi = b1 * m[i] + (1.0f - b1) * gi;
@@ -463,6 +482,39 @@ void init_weights(std::vector<float>& w, uint32_t seed) {
     }
 }
 
+int launch_infer(arc_ctx* c, const float* inputs, const float* albedo, uint32_t n, float* out, const uint32_t* list,
+                 const unsigned long long* n_dev) {
+    const uint32_t tiles = (n + 15u) / 16u;
+    const uint32_t blocks = std::min<uint32_t>((tiles + 3u) / 4u, (uint32_t)c->n_sm * 3u);
+    nrc::infer_kernel<<<blocks, 128, nrc::kFwdHalves * sizeof(__half), c->stream>>>(
+        static_cast<const __half*>(c->d_nrc_w16_ema), inputs, albedo, n, out, list, n_dev);
+    NRC_CK(cudaGetLastError());
+    return ARC_OK;
+}
+
+// Loss-scaled gradient of one batch into d_nrc_grad (zeroed first) and its loss sum into d_nrc_loss.
+int launch_grad(arc_ctx* c, const float* inputs, const float* targets, uint32_t n, const uint32_t* gate) {
+    NRC_CK(cudaMemsetAsync(c->d_nrc_grad, 0, sizeof(float) * nrc::kParams, c->stream));
+    NRC_CK(cudaMemsetAsync(c->d_nrc_loss, 0, sizeof(float), c->stream));
+    const uint32_t tiles = (n + 63u) / 64u;
+    const uint32_t blocks = std::min<uint32_t>(tiles, (uint32_t)c->n_sm);
+    nrc::train_kernel<<<blocks, 128, (nrc::kAllHalves + nrc::kActHalves) * sizeof(__half), c->stream>>>(
+        static_cast<const __half*>(c->d_nrc_w16), inputs, targets, n, 1.0f / (float)n, c->d_nrc_grad, c->d_nrc_loss, gate);
+    NRC_CK(cudaGetLastError());
+    return ARC_OK;
+}
+
+// One Adam step from d_nrc_grad; the host step counter sets the bias correction.
+int launch_adam(arc_ctx* c, float lr, const uint32_t* gate) {
+    c->nrc_step += 1;
+    const float c1 = 1.0f - std::pow(0.9f, (float)c->nrc_step), c2 = 1.0f - std::pow(0.99f, (float)c->nrc_step);
+    nrc::adam_kernel<<<(nrc::kParams + 255) / 256, 256, 0, c->stream>>>(
+        c->d_nrc_w32, c->d_nrc_m, c->d_nrc_v, c->d_nrc_grad, static_cast<__half*>(c->d_nrc_w16), c->d_nrc_ema,
+        static_cast<__half*>(c->d_nrc_w16_ema), c->nrc_ema_decay, lr, c1, c2, 1.0f / nrc::kLossScale, gate);
+    NRC_CK(cudaGetLastError());
+    return ARC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -520,44 +572,68 @@ int arc_nrc_query_dev(arc_ctx* c, const float* inputs, const float* albedo, uint
     if (n && (!inputs || !out)) return nrc_err(c, ARC_E_INVALID_ARG, "null buffer");
     int rc = ensure_nrc(c);
     if (rc || n == 0) return rc;
-    const uint32_t tiles = (n + 15u) / 16u;
-    const uint32_t blocks = std::min<uint32_t>((tiles + 3u) / 4u, (uint32_t)c->n_sm * 3u);
-    nrc::infer_kernel<<<blocks, 128, nrc::kFwdHalves * sizeof(__half), c->stream>>>(static_cast<const __half*>(c->d_nrc_w16_ema), inputs, albedo, n, out);
-    NRC_CK(cudaGetLastError());
-    return ARC_OK;
+    return launch_infer(c, inputs, albedo, n, out, nullptr, nullptr);
 }
 
-// Loss-scaled gradient of one batch into d_nrc_grad (zeroed first); exposed for the gradient check.
+int arc_nrc_query_list_dev(arc_ctx* c, const uint32_t* list, const uint64_t* n_dev, uint32_t max_n, const float* inputs,
+                           const float* albedo, float* out) {
+    if (!c) return ARC_E_INVALID_ARG;
+    if (max_n && (!list || !n_dev || !inputs || !out)) return nrc_err(c, ARC_E_INVALID_ARG, "null buffer");
+    int rc = ensure_nrc(c);
+    if (rc || max_n == 0) return rc;
+    return launch_infer(c, inputs, albedo, max_n, out, list, reinterpret_cast<const unsigned long long*>(n_dev));
+}
+
 int arc_nrc_grad_dev(arc_ctx* c, const float* inputs, const float* targets, uint32_t n, float* grad_out) {
     if (!c || !inputs || !targets || n == 0) return ARC_E_INVALID_ARG;
     int rc = ensure_nrc(c);
     if (rc) return rc;
-    NRC_CK(cudaMemsetAsync(c->d_nrc_grad, 0, sizeof(float) * nrc::kParams, c->stream));
-    NRC_CK(cudaMemsetAsync(c->d_nrc_loss, 0, sizeof(float), c->stream));
-    const uint32_t tiles = (n + 63u) / 64u;
-    const uint32_t blocks = std::min<uint32_t>(tiles, (uint32_t)c->n_sm);
-    nrc::train_kernel<<<blocks, 128, (nrc::kAllHalves + nrc::kActHalves) * sizeof(__half), c->stream>>>(
-        static_cast<const __half*>(c->d_nrc_w16), inputs, targets, n, 1.0f / (float)n, c->d_nrc_grad, c->d_nrc_loss);
-    NRC_CK(cudaGetLastError());
+    if ((rc = launch_grad(c, inputs, targets, n, nullptr))) return rc;
     if (grad_out)
         NRC_CK(cudaMemcpyAsync(grad_out, c->d_nrc_grad, sizeof(float) * nrc::kParams, cudaMemcpyDeviceToDevice, c->stream));
     return ARC_OK;
 }
 
 int arc_nrc_train_step_dev(arc_ctx* c, const float* inputs, const float* targets, uint32_t n, float lr, float* loss_host) {
-    int rc = arc_nrc_grad_dev(c, inputs, targets, n, nullptr);
+    if (!c || !inputs || !targets || n == 0) return ARC_E_INVALID_ARG;
+    int rc = ensure_nrc(c);
     if (rc) return rc;
-    c->nrc_step += 1;
-    const float c1 = 1.0f - std::pow(0.9f, (float)c->nrc_step), c2 = 1.0f - std::pow(0.99f, (float)c->nrc_step);
-    nrc::adam_kernel<<<(nrc::kParams + 255) / 256, 256, 0, c->stream>>>(
-        c->d_nrc_w32, c->d_nrc_m, c->d_nrc_v, c->d_nrc_grad, static_cast<__half*>(c->d_nrc_w16), c->d_nrc_ema,
-        static_cast<__half*>(c->d_nrc_w16_ema), c->nrc_ema_decay, lr, c1, c2, 1.0f / nrc::kLossScale);
-    NRC_CK(cudaGetLastError());
+    if ((rc = launch_grad(c, inputs, targets, n, nullptr)) || (rc = launch_adam(c, lr, nullptr))) return rc;
     if (loss_host) {
         float l = 0.0f;
         NRC_CK(cudaMemcpyAsync(&l, c->d_nrc_loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
         if ((rc = arc_ctx_finish(c))) return rc;
         *loss_host = l / (float)n;
+    }
+    return ARC_OK;
+}
+
+int arc_nrc_train_frame_dev(arc_ctx* c, const uint32_t* list, const uint64_t* n_valid, const float* pos,
+                            const float* normal, const float* nrc_in, uint32_t seed, uint32_t n_samples,
+                            uint32_t steps, float lr) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if (!list || !n_valid || !pos || !normal || !nrc_in) return nrc_err(c, ARC_E_INVALID_ARG, "null buffer");
+    if (steps == 0 || n_samples < steps) return nrc_err(c, ARC_E_INVALID_ARG, "need 1 <= steps <= n_samples");
+    if ((rc = ensure_nrc(c))) return rc;
+    if (c->nrc_batch_cap < n_samples) {
+        cudaFree(c->d_nrc_batch);
+        c->d_nrc_batch = nullptr;
+        c->nrc_batch_cap = 0;
+        NRC_CK(cudaMalloc((void**)&c->d_nrc_batch, sizeof(float) * 12u * (size_t)n_samples));
+        c->nrc_batch_cap = n_samples;
+    }
+    if (!c->d_nrc_gate) NRC_CK(cudaMalloc((void**)&c->d_nrc_gate, sizeof(uint32_t)));
+    float* train_in = c->d_nrc_batch;
+    float* train_t = c->d_nrc_batch + 9u * (size_t)n_samples;
+    if ((rc = arc_launch_train_samples_list(c, list, reinterpret_cast<const unsigned long long*>(n_valid), pos, normal,
+                                            nrc_in, seed, n_samples, train_in, train_t, c->d_nrc_gate)))
+        return rc;
+    const uint32_t per = n_samples / steps;
+    for (uint32_t k = 0; k < steps; ++k) {
+        if ((rc = launch_grad(c, train_in + 9u * (size_t)k * per, train_t + 3u * (size_t)k * per, per, c->d_nrc_gate)) ||
+            (rc = launch_adam(c, lr, c->d_nrc_gate)))
+            return rc;
     }
     return ARC_OK;
 }

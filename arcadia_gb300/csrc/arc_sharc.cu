@@ -9,6 +9,7 @@
 // Compiled with the canonical arithmetic flags (arc_math.cuh).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <string>
 
@@ -334,7 +335,8 @@ __global__ void sharc_deposit_kernel(SharcBuffers S, f3 pos, f3 n, f3 cam, f3 ra
 __global__ void gi_points_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, const uint32_t* __restrict__ gdm,
                                  const uint32_t* __restrict__ gnm, uint32_t W, uint32_t H, float* __restrict__ pos,
                                  float* __restrict__ nrm, float* __restrict__ alb, float* __restrict__ nrc_in,
-                                 uint32_t* __restrict__ valid, unsigned long long* __restrict__ n_valid) {
+                                 uint32_t* __restrict__ valid, unsigned long long* __restrict__ n_valid,
+                                 uint32_t* __restrict__ list) {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= W || y >= H) return;
     const size_t k = (size_t)y * W + x;
@@ -376,8 +378,14 @@ __global__ void gi_points_kernel(const World w, const __grid_constant__ arc_came
         }
     }
     valid[k] = ok;
-    const uint32_t m = __ballot_sync(__activemask(), ok != 0u);
-    if (ok && (threadIdx.x + threadIdx.y * blockDim.x) % 32u == (uint32_t)(__ffs(m) - 1)) atomicAdd(n_valid, (unsigned long long)__popc(m));
+    // warp-aggregated slot in the compacted list (order across warps is arbitrary)
+    const uint32_t act = __activemask();
+    const uint32_t m = __ballot_sync(act, ok != 0u);
+    const uint32_t lane = (threadIdx.x + threadIdx.y * blockDim.x) & 31u;
+    unsigned long long base = 0ull;
+    if (m && lane == (uint32_t)(__ffs(m) - 1)) base = atomicAdd(n_valid, (unsigned long long)__popc(m));
+    if (m) base = __shfl_sync(act, base, __ffs(m) - 1);
+    if (ok && list) list[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)k;
 }
 
 __global__ void onebounce_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, const uint32_t* __restrict__ idx,
@@ -408,28 +416,41 @@ __global__ void onebounce_kernel(const World w, const __grid_constant__ arc_came
     }
 }
 
-// NRC training samples: every valid GI point is taken with probability accept (PCG per pixel and frame);
-// a taken point gets a slot from the counter (up to max_n) and a 1-spp one-bounce target demodulated by
-// the albedo (the estimator with albedo 1: the network learns the light arriving at the surface, and
-// the query multiplies the albedo back in).
-__global__ void train_samples_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, uint32_t n_px,
-                                     const uint32_t* __restrict__ valid, const float* __restrict__ pos,
-                                     const float* __restrict__ nrm,
-                                     const float* __restrict__ nrc_in, float accept, uint32_t seed, uint32_t max_n,
-                                     float* __restrict__ train_in, float* __restrict__ train_t, uint32_t* __restrict__ count) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n_px || !valid[p]) return;
-    const uint32_t h = pcg_hash(p ^ pcg_hash(seed));
-    if ((float)(h >> 8) * (1.0f / 16777216.0f) >= accept) return;
-    const uint32_t slot = atomicAdd(count, 1u);
-    if (slot >= max_n) return;
+// NRC training samples from the compacted GI hit list: sample i takes list[j], j = hash(i, seed) scaled
+// to [0, n_valid) (with replacement), and the 1-spp estimator with albedo 1 at that point.
+__global__ void train_samples_list_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam,
+                                          const uint32_t* __restrict__ list, const unsigned long long* __restrict__ n_valid,
+                                          const float* __restrict__ pos, const float* __restrict__ nrm,
+                                          const float* __restrict__ nrc_in, uint32_t seed, uint32_t n_samples,
+                                          float* __restrict__ train_in, float* __restrict__ train_t, uint32_t* __restrict__ gate) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_samples) return;
+    const unsigned long long nv = *n_valid;
+    if (i == 0) *gate = nv ? n_samples : 0u;
+    if (!nv) return;
+    const uint32_t h = pcg_hash(i ^ pcg_hash(seed));
+    const uint32_t j = (uint32_t)(((unsigned long long)h * nv) >> 32);
+    const uint32_t p = __ldg(&list[j]);
     const f3 l = onebounce(w, cam, f3{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]}, f3{nrm[3 * p], nrm[3 * p + 1], nrm[3 * p + 2]},
                            f3{1.0f, 1.0f, 1.0f}, pcg_hash(h ^ 0xB5297A4Du));
 #pragma unroll
-    for (int k = 0; k < 9; ++k) train_in[(size_t)slot * 9 + k] = nrc_in[(size_t)p * 9 + k];
-    train_t[3 * slot] = l.x;
-    train_t[3 * slot + 1] = l.y;
-    train_t[3 * slot + 2] = l.z;
+    for (int k = 0; k < 9; ++k) train_in[(size_t)i * 9 + k] = nrc_in[(size_t)p * 9 + k];
+    train_t[3 * (size_t)i] = l.x;
+    train_t[3 * (size_t)i + 1] = l.y;
+    train_t[3 * (size_t)i + 2] = l.z;
+}
+
+__global__ void sharc_query_list_kernel(const uint4* __restrict__ res, const uint32_t* __restrict__ list,
+                                        const unsigned long long* __restrict__ n_dev, uint32_t max_n,
+                                        const float* __restrict__ pos, const float* __restrict__ nrm, f3 cam,
+                                        float4* __restrict__ out) {
+    const unsigned long long nd = *n_dev;
+    const uint32_t n = nd < max_n ? (uint32_t)nd : max_n;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t i = __ldg(&list[j]);
+        const f3 p{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]}, q{nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]};
+        out[i] = sharc_query(res, p, q, cam, 0.0f, 0.0f);
+    }
 }
 
 }  // namespace arc
@@ -500,7 +521,7 @@ int arc_sharc_set_mode(arc_ctx* c, uint32_t mode) {
 }
 
 int arc_gi_points_dev(arc_ctx* c, uint32_t width, uint32_t height, const uint32_t* gdm, const uint32_t* gnm, float* pos,
-                      float* nrm, float* albedo, float* nrc_in, uint32_t* valid, uint64_t* n_valid) {
+                      float* nrm, float* albedo, float* nrc_in, uint32_t* valid, uint64_t* n_valid, uint32_t* list) {
     int rc = arc_ctx_check_ready(c, true);
     if (rc) return rc;
     if (!gdm || !gnm || !pos || !nrm || !albedo || !nrc_in || !valid || !n_valid) return sharc_err(c, ARC_E_INVALID_ARG, "null buffer");
@@ -509,8 +530,31 @@ int arc_gi_points_dev(arc_ctx* c, uint32_t width, uint32_t height, const uint32_
     cudaMemsetAsync(n_valid, 0, sizeof(uint64_t), c->stream);
     dim3 block(8, 8), grid((width + 7u) / 8u, (height + 7u) / 8u);
     arc::gi_points_kernel<<<grid, block, 0, c->stream>>>(c->world(), c->cam, gdm, gnm, width, height, pos, nrm, albedo,
-                                                         nrc_in, valid, reinterpret_cast<unsigned long long*>(n_valid));
+                                                         nrc_in, valid, reinterpret_cast<unsigned long long*>(n_valid), list);
     return launch_check(c, "gi_points_kernel");
+}
+
+int arc_launch_train_samples_list(arc_ctx* c, const uint32_t* list, const unsigned long long* n_valid, const float* pos,
+                                  const float* nrm, const float* nrc_in, uint32_t seed, uint32_t n_samples,
+                                  float* train_in, float* train_t, uint32_t* gate) {
+    arc::train_samples_list_kernel<<<(n_samples + 127u) / 128u, 128, 0, c->stream>>>(
+        c->world(), c->cam, list, n_valid, pos, nrm, nrc_in, seed, n_samples, train_in, train_t, gate);
+    return launch_check(c, "train_samples_list_kernel");
+}
+
+int arc_sharc_query_list_dev(arc_ctx* c, const uint32_t* list, const uint64_t* n_dev, uint32_t max_n, const float* pos,
+                             const float* normal, float* out) {
+    if (!c) return ARC_E_INVALID_ARG;
+    if (!c->have_cam) return sharc_err(c, ARC_E_NO_CAMERA, "no camera set");
+    if (max_n && (!list || !n_dev || !pos || !normal || !out)) return sharc_err(c, ARC_E_INVALID_ARG, "null buffer");
+    int rc = ensure_sharc(c);
+    if (rc || max_n == 0) return rc;
+    const arc::f3 cam{c->cam.cam_pos_time[0], c->cam.cam_pos_time[1], c->cam.cam_pos_time[2]};
+    const uint32_t blocks = std::min<uint32_t>((max_n + 255u) / 256u, (uint32_t)c->n_sm * 8u);
+    arc::sharc_query_list_kernel<<<blocks, 256, 0, c->stream>>>(reinterpret_cast<const uint4*>(c->d_sharc_resolved), list,
+                                                                reinterpret_cast<const unsigned long long*>(n_dev), max_n,
+                                                                pos, normal, cam, reinterpret_cast<float4*>(out));
+    return launch_check(c, "sharc_query_list_kernel");
 }
 
 int arc_onebounce_dev(arc_ctx* c, const uint32_t* idx, uint32_t n, const float* pos, const float* nrm, const float* albedo,
@@ -522,19 +566,6 @@ int arc_onebounce_dev(arc_ctx* c, const uint32_t* idx, uint32_t n, const float* 
     arc::onebounce_kernel<<<(n + 127u) / 128u, 128, 0, c->stream>>>(c->world(), c->cam, idx, n, pos, nrm, albedo, spp, seed,
                                                                      accumulate ? 1u : 0u, out);
     return launch_check(c, "onebounce_kernel");
-}
-
-int arc_nrc_train_samples_dev(arc_ctx* c, uint32_t n_px, const uint32_t* valid, const float* pos, const float* nrm,
-                              const float* nrc_in, float accept, uint32_t seed, uint32_t max_n, float* train_in,
-                              float* train_t, uint32_t* count) {
-    int rc = arc_ctx_check_ready(c, true);
-    if (rc) return rc;
-    if (!valid || !pos || !nrm || !nrc_in || !train_in || !train_t || !count) return sharc_err(c, ARC_E_INVALID_ARG, "null buffer");
-    cudaMemsetAsync(count, 0, sizeof(uint32_t), c->stream);
-    if (n_px == 0) return ARC_OK;
-    arc::train_samples_kernel<<<(n_px + 127u) / 128u, 128, 0, c->stream>>>(c->world(), c->cam, n_px, valid, pos, nrm, nrc_in, accept, seed, max_n, train_in, train_t,
-                                                                            count);
-    return launch_check(c, "train_samples_kernel");
 }
 
 int arc_sharc_resolve(arc_ctx* c) {

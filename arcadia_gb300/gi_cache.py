@@ -4,11 +4,14 @@ Both caches learn the same quantity, the one-bounce radiance L(x) at the hit of 
 (sun directional light with a shadow ray + constant sky through one cosine-sampled ray; see
 ``arc_onebounce_dev``), so the comparison is about the caching method alone:
 
-  shared per frame  primary G-buffer (arc_trace_primary_dev) + GI hit points (arc_gi_points_dev)
+  shared per frame  primary G-buffer (arc_trace_primary_dev) + GI hit points (arc_gi_points_dev),
+                    which also compacts the pixels with a GI hit into a device list
   SHARC pipeline    arc_sharc_update_dev (tile-seeded paths, estimator deposits, mode 1) +
-                    arc_sharc_resolve + arc_sharc_query_dev at every GI hit
-  NRC pipeline      arc_nrc_train_samples_dev (65,536 one-bounce samples) + arc_nrc_train_step_dev
-                    (fused forward/backward/Adam) + arc_nrc_query_dev at every GI hit
+                    arc_sharc_resolve + arc_sharc_query_list_dev at every GI hit
+  NRC pipeline      arc_nrc_train_frame_dev (65,536 one-bounce samples drawn from the list, fused
+                    forward/backward + Adam steps) + arc_nrc_query_list_dev at every GI hit
+
+Neither pipeline reads anything back to the host during a frame.
 
 The surfaces are Lambertian with one albedo per material (U[0.1, 0.9] per channel). SHARC caches the
 reflected radiance as the reference does. The network learns the demodulated quantity L / albedo,
@@ -23,7 +26,6 @@ from __future__ import annotations
 
 import ctypes as C
 import statistics
-import time
 
 import numpy as np
 
@@ -61,15 +63,11 @@ class CacheComparison:
         self.nin = torch.zeros((n, 9), dtype=torch.float32, device=dev)
         self.valid = torch.zeros(n, dtype=i32, device=dev)
         self.n_valid = torch.zeros(1, dtype=torch.int64, device=dev)
+        self.list = torch.zeros(n, dtype=i32, device=dev)
         self.sharc_out = torch.zeros((n, 4), dtype=torch.float32, device=dev)
         self.nrc_out = torch.zeros((n, 3), dtype=torch.float32, device=dev)
-        self.train_in = torch.zeros((TRAIN_SAMPLES, 9), dtype=torch.float32, device=dev)
-        self.train_t = torch.zeros((TRAIN_SAMPLES, 3), dtype=torch.float32, device=dev)
-        self.count = torch.zeros(1, dtype=i32, device=dev)
         self.stream = torch.cuda.ExternalStream(tracer.stream())
         self.lib = native.lib()
-        self.frame = 0
-        self.last_valid = n
 
     def camera(self, frame):
         return L.default_camera_for(self.scene, self.w, self.h, quality=self.q, frame_index=frame)
@@ -90,8 +88,8 @@ class CacheComparison:
         self.t.trace_primary_dev(self.w, self.h, self.gdm.data_ptr(), self.gnm.data_ptr(), self.gaa.data_ptr())
         self._ck(self.lib.arc_gi_points_dev(self.t.ctx, self.w, self.h, self.gdm.data_ptr(), self.gnm.data_ptr(),
                                             self.pos.data_ptr(), self.nrm.data_ptr(), self.alb.data_ptr(),
-                                            self.nin.data_ptr(), self.valid.data_ptr(), self.n_valid.data_ptr()),
-                 "arc_gi_points_dev")
+                                            self.nin.data_ptr(), self.valid.data_ptr(), self.n_valid.data_ptr(),
+                                            self.list.data_ptr()), "arc_gi_points_dev")
         b = self._event()
         b.synchronize()
         return a.elapsed_time(b)
@@ -101,35 +99,26 @@ class CacheComparison:
         self._ck(self.lib.arc_sharc_update_dev(self.t.ctx, self.w, self.h, self.gdm.data_ptr(), self.gnm.data_ptr()),
                  "arc_sharc_update_dev")
         self._ck(self.lib.arc_sharc_resolve(self.t.ctx), "arc_sharc_resolve")
-        self._ck(self.lib.arc_sharc_query_dev(self.t.ctx, self.pos.data_ptr(), self.nrm.data_ptr(), None,
-                                              self.w * self.h, self.sharc_out.data_ptr()), "arc_sharc_query_dev")
+        self._ck(self.lib.arc_sharc_query_list_dev(self.t.ctx, self.list.data_ptr(), self.n_valid.data_ptr(), self.w * self.h,
+                                                   self.pos.data_ptr(), self.nrm.data_ptr(), self.sharc_out.data_ptr()),
+                 "arc_sharc_query_list_dev")
         b = self._event()
         b.synchronize()
         return a.elapsed_time(b)
 
     def nrc_frame(self, seed, lr=1e-3, steps=8):
-        """Training samples, `steps` Adam steps on equal slices of them, then inference at every pixel."""
-        n_px = self.w * self.h
-        accept = min(1.0, 1.25 * TRAIN_SAMPLES / max(self.last_valid, 1))
+        """One training frame (TRAIN_SAMPLES samples, `steps` Adam steps on equal slices), then inference at
+        every GI hit; returns its device time in ms."""
         a = self._event()
-        self._ck(self.lib.arc_nrc_train_samples_dev(self.t.ctx, n_px, self.valid.data_ptr(), self.pos.data_ptr(),
-                                                    self.nrm.data_ptr(), self.nin.data_ptr(), C.c_float(accept), seed,
-                                                    TRAIN_SAMPLES, self.train_in.data_ptr(), self.train_t.data_ptr(),
-                                                    self.count.data_ptr()),
-                 "arc_nrc_train_samples_dev")
-        self._event().synchronize()  # the counter is written on the tracer's stream
-        n_train = min(int(self.count.item()), TRAIN_SAMPLES)  # one small read per frame
-        per = n_train // steps
-        for k in range(steps if per else 0):
-            self._ck(self.lib.arc_nrc_train_step_dev(self.t.ctx, self.train_in[k * per:].data_ptr(),
-                                                     self.train_t[k * per:].data_ptr(), per, C.c_float(lr), None),
-                     "arc_nrc_train_step_dev")
-        self._ck(self.lib.arc_nrc_query_dev(self.t.ctx, self.nin.data_ptr(), self.alb.data_ptr(), n_px,
-                                            self.nrc_out.data_ptr()), "arc_nrc_query_dev")
+        self._ck(self.lib.arc_nrc_train_frame_dev(self.t.ctx, self.list.data_ptr(), self.n_valid.data_ptr(),
+                                                  self.pos.data_ptr(), self.nrm.data_ptr(), self.nin.data_ptr(), seed,
+                                                  TRAIN_SAMPLES, steps, C.c_float(lr)), "arc_nrc_train_frame_dev")
+        self._ck(self.lib.arc_nrc_query_list_dev(self.t.ctx, self.list.data_ptr(), self.n_valid.data_ptr(), self.w * self.h,
+                                                 self.nin.data_ptr(), self.alb.data_ptr(), self.nrc_out.data_ptr()),
+                 "arc_nrc_query_list_dev")
         b = self._event()
         b.synchronize()
-        self.last_valid = int(self.n_valid.item())
-        return a.elapsed_time(b), n_train
+        return a.elapsed_time(b)
 
     def reference(self, idx: np.ndarray, seed=12345):
         """4096-spp one-bounce reference at pixels idx (FP32 launches, FP64 host accumulation)."""
@@ -172,7 +161,7 @@ def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920
     for f in range(frames):
         shared_ms.append(cc.shared(f))
         sharc_ms.append(cc.sharc_frame())
-        nrc_ms.append(cc.nrc_frame(seed * 1000003 + f, lr=lr, steps=steps_per_frame)[0])
+        nrc_ms.append(cc.nrc_frame(seed * 1000003 + f, lr=lr, steps=steps_per_frame))
         if f + 1 in curve and f + 1 < frames:
             cand = np.nonzero(cc.valid.cpu().numpy().astype(bool))[0]
             ci = cand[np.linspace(0, len(cand) - 1, min(8192, len(cand))).astype(np.int64)]
@@ -189,8 +178,8 @@ def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920
     sharc_hit = sharc[:, 3] > 0.5
     # untrained network, same points (the method without the learned part)
     cc._ck(lib.arc_nrc_init(tracer.ctx, seed), "arc_nrc_init")
-    cc._ck(lib.arc_nrc_query_dev(tracer.ctx, cc.nin.data_ptr(), cc.alb.data_ptr(), width * height, cc.nrc_out.data_ptr()),
-           "query")
+    cc._ck(lib.arc_nrc_query_list_dev(tracer.ctx, cc.list.data_ptr(), cc.n_valid.data_ptr(), width * height,
+                                      cc.nin.data_ptr(), cc.alb.data_ptr(), cc.nrc_out.data_ptr()), "query")
     tracer.synchronize()
     untrained = cc.nrc_out.cpu().numpy()[idx]
     cc._ck(lib.arc_sharc_set_mode(tracer.ctx, 0), "arc_sharc_set_mode")

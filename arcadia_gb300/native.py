@@ -73,14 +73,16 @@ SIGNATURES = {
     "arc_sharc_upload": [_vp, _vp, _vp, _vp],
     "arc_sharc_deposit_dev": [_vp, _vp, _vp, _vp, _vp, _u32],
     "arc_sharc_set_mode": [_vp, _u32],
-    "arc_gi_points_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "arc_gi_points_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "arc_onebounce_dev": [_vp, _vp, _u32, _vp, _vp, _vp, _u32, _u32, _i32, _vp],
-    "arc_nrc_train_samples_dev": [_vp, _u32, _vp, _vp, _vp, _vp, _f32, _u32, _u32, _vp, _vp, _vp],
     "arc_nrc_init": [_vp, _u32],
     "arc_nrc_set_weights": [_vp, _vp],
     "arc_nrc_get_weights": [_vp, _vp],
     "arc_nrc_set_ema_decay": [_vp, _f32],
     "arc_nrc_get_ema_weights": [_vp, _vp],
+    "arc_nrc_query_list_dev": [_vp, _vp, _vp, _u32, _vp, _vp, _vp],
+    "arc_nrc_train_frame_dev": [_vp, _vp, _vp, _vp, _vp, _vp, _u32, _u32, _u32, _f32],
+    "arc_sharc_query_list_dev": [_vp, _vp, _vp, _u32, _vp, _vp, _vp],
     "arc_nrc_query_dev": [_vp, _vp, _vp, _u32, _vp],
     "arc_nrc_grad_dev": [_vp, _vp, _vp, _u32, _vp],
     "arc_nrc_train_step_dev": [_vp, _vp, _vp, _u32, _f32, _vp],

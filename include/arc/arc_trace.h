@@ -180,15 +180,18 @@ int arc_sharc_set_mode(arc_ctx* ctx, uint32_t mode);
  * is the comparison's Lambertian albedo per material id, each channel from U[0.1, 0.9]. */
 int arc_gi_points_dev(arc_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* gbuf_depth_mat,
                       const uint32_t* gbuf_norm_motion, float* pos, float* normal, float* albedo, float* nrc_in,
-                      uint32_t* valid, uint64_t* n_valid);
+                      uint32_t* valid, uint64_t* n_valid, uint32_t* list);
+/* list (optional, width*height entries): the pixel indices of the points with valid = 1, compacted to
+ * list[0 .. *n_valid) in no particular order. */
 /* Mean of spp one-bounce samples at points idx[i] (idx may be NULL = identity); accumulate adds. */
 int arc_onebounce_dev(arc_ctx* ctx, const uint32_t* idx, uint32_t n, const float* pos, const float* normal,
                       const float* albedo, uint32_t spp, uint32_t seed, int accumulate, float* out);
-/* NRC training samples: each valid point taken with probability accept, up to max_n, 1-spp targets
- * demodulated by the albedo (the estimator with albedo 1). */
-int arc_nrc_train_samples_dev(arc_ctx* ctx, uint32_t n_px, const uint32_t* valid, const float* pos,
-                              const float* normal, const float* nrc_in, float accept, uint32_t seed,
-                              uint32_t max_n, float* train_in, float* train_t, uint32_t* count);
+
+/* query_sharc at the points list[0 .. min(*n_dev, max_n)) (as from arc_gi_points_dev): out[list[j]]
+ * (float4: RGB, 1 if a cached entry was found) from pos/normal[list[j]]. No counterpart in the reference
+ * beyond query_sharc itself. */
+int arc_sharc_query_list_dev(arc_ctx* ctx, const uint32_t* list, const uint64_t* n_dev, uint32_t max_n,
+                             const float* pos, const float* normal, float* out);
 
 /* Neural radiance cache (no reference counterpart: it stands in for query_sharc at secondary hits).
  * 9 inputs per query: position normalised to [0,1]^3, normal, view direction; 3 outputs (RGB).
@@ -203,6 +206,16 @@ int arc_nrc_set_ema_decay(arc_ctx* ctx, float decay);
 int arc_nrc_get_ema_weights(arc_ctx* ctx, float* weights);
 /* out_rgb[i] = albedo[i] * network(inputs[i]) per channel; albedo may be NULL (network output only). */
 int arc_nrc_query_dev(arc_ctx* ctx, const float* inputs, const float* albedo, uint32_t n, float* out_rgb);
+/* arc_nrc_query_dev at the points list[0 .. min(*n_dev, max_n)): out[list[j]] from inputs/albedo[list[j]]. */
+int arc_nrc_query_list_dev(arc_ctx* ctx, const uint32_t* list, const uint64_t* n_dev, uint32_t max_n,
+                           const float* inputs, const float* albedo, float* out_rgb);
+/* One frame of online training with no host synchronisation (graph-capturable after the first call,
+ * which allocates the batch): n_samples points drawn with replacement from list[0 .. *n_valid), their
+ * demodulated 1-spp one-bounce targets, then `steps` Adam steps on equal slices of the batch. A frame
+ * with *n_valid = 0 leaves the weights unchanged. */
+int arc_nrc_train_frame_dev(arc_ctx* ctx, const uint32_t* list, const uint64_t* n_valid, const float* pos,
+                            const float* normal, const float* nrc_in, uint32_t seed, uint32_t n_samples,
+                            uint32_t steps, float lr);
 /* Loss-scaled (x128) weight gradient of the mean relative-L2 loss of one batch (device output). */
 int arc_nrc_grad_dev(arc_ctx* ctx, const float* inputs, const float* targets, uint32_t n, float* grad_out);
 /* One Adam step (lr; beta 0.9/0.99) on a batch; loss_host (optional) receives the batch loss. */

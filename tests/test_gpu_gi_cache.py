@@ -27,3 +27,96 @@ def test_trained_nrc_beats_untrained_and_sharc(native_lib):
     assert r["rel_mse_nrc"] < 0.8 * r["rel_mse_untrained_nrc"]
     assert r["rel_mse_nrc"] < r["rel_mse_sharc"]
     assert 0.0 < r["sharc_hit_fraction"] <= 1.0
+
+
+def _points(native_lib, w=320, h=180):
+    """c1_256 frame: G-buffer, GI hit points and their compacted list on the GPU."""
+    import torch
+    from arcadia_gb300 import gi_cache, layout as L
+
+    scene = L.SCENES["c1_256"]
+    roots, nodes, bricks, _ = native_lib.build_world(scene)
+    t = native_lib.Tracer(0)
+    t.upload_world(scene.grid, roots, nodes, bricks, native_lib.default_palette())
+    cc = gi_cache.CacheComparison(t, scene, w, h)
+    cc.shared(3)
+    return t, cc
+
+
+def test_gi_points_list_is_the_valid_set(native_lib):
+    import numpy as np
+
+    t, cc = _points(native_lib)
+    try:
+        valid = cc.valid.cpu().numpy()
+        n = int(cc.n_valid.item())
+        lst = cc.list.cpu().numpy()[:n]
+        assert n == int(valid.sum()) > 100
+        assert np.array_equal(np.sort(lst), np.nonzero(valid)[0])
+    finally:
+        t.close()
+
+
+def test_list_queries_match_dense_queries(native_lib):
+    """NRC and SHARC queries over the compacted list write exactly the listed pixels, with the dense
+    query's values there."""
+    import numpy as np
+    import torch
+    from arcadia_gb300.native import lib
+
+    t, cc = _points(native_lib)
+    try:
+        L_ = lib()
+        n_px = cc.w * cc.h
+        assert L_.arc_nrc_init(t.ctx, 5) == 0
+        assert L_.arc_sharc_set_mode(t.ctx, 1) == 0
+        t.sharc_reset()
+        assert L_.arc_sharc_update_dev(t.ctx, cc.w, cc.h, cc.gdm.data_ptr(), cc.gnm.data_ptr()) == 0
+        assert L_.arc_sharc_resolve(t.ctx) == 0
+        dense_n = torch.zeros((n_px, 3), dtype=torch.float32, device="cuda")
+        dense_s = torch.zeros((n_px, 4), dtype=torch.float32, device="cuda")
+        assert L_.arc_nrc_query_dev(t.ctx, cc.nin.data_ptr(), cc.alb.data_ptr(), n_px, dense_n.data_ptr()) == 0
+        assert L_.arc_sharc_query_dev(t.ctx, cc.pos.data_ptr(), cc.nrm.data_ptr(), None, n_px, dense_s.data_ptr()) == 0
+        list_n = torch.full((n_px, 3), -7.0, dtype=torch.float32, device="cuda")
+        list_s = torch.full((n_px, 4), -7.0, dtype=torch.float32, device="cuda")
+        assert L_.arc_nrc_query_list_dev(t.ctx, cc.list.data_ptr(), cc.n_valid.data_ptr(), n_px, cc.nin.data_ptr(),
+                                         cc.alb.data_ptr(), list_n.data_ptr()) == 0
+        assert L_.arc_sharc_query_list_dev(t.ctx, cc.list.data_ptr(), cc.n_valid.data_ptr(), n_px, cc.pos.data_ptr(),
+                                           cc.nrm.data_ptr(), list_s.data_ptr()) == 0
+        t.synchronize()
+        v = cc.valid.cpu().numpy().astype(bool)
+        for got, want in ((list_n, dense_n), (list_s, dense_s)):
+            g, w_ = got.cpu().numpy(), want.cpu().numpy()
+            np.testing.assert_array_equal(g[v], w_[v])
+            assert (g[~v] == -7.0).all()
+        assert (dense_s.cpu().numpy()[v][:, 3] > 0.5).any()  # some cached entries found
+        assert L_.arc_sharc_set_mode(t.ctx, 0) == 0
+    finally:
+        t.close()
+
+
+def test_train_frame_updates_weights_and_skips_empty_frames(native_lib):
+    import numpy as np
+    import torch
+    from arcadia_gb300.native import lib
+
+    t, cc = _points(native_lib)
+    try:
+        L_ = lib()
+        assert L_.arc_nrc_init(t.ctx, 5) == 0
+        w0 = np.zeros(30400, np.float32)
+        assert L_.arc_nrc_get_weights(t.ctx, w0.ctypes.data) == 0
+        zero = torch.zeros(1, dtype=torch.int64, device="cuda")
+        args = (cc.list.data_ptr(), zero.data_ptr(), cc.pos.data_ptr(), cc.nrm.data_ptr(), cc.nin.data_ptr(), 11, 4096, 2, 1e-3)
+        assert L_.arc_nrc_train_frame_dev(t.ctx, *args) == 0
+        w1 = np.zeros(30400, np.float32)
+        assert L_.arc_nrc_get_weights(t.ctx, w1.ctypes.data) == 0
+        assert np.array_equal(w0, w1)  # no GI hit: nothing to learn
+        args = (cc.list.data_ptr(), cc.n_valid.data_ptr()) + args[2:]
+        assert L_.arc_nrc_train_frame_dev(t.ctx, *args) == 0
+        assert L_.arc_nrc_get_weights(t.ctx, w1.ctypes.data) == 0
+        assert np.isfinite(w1).all() and np.abs(w1 - w0).max() > 1e-4
+        bad = args[:7] + (0,) + args[8:]
+        assert L_.arc_nrc_train_frame_dev(t.ctx, *bad) != 0  # steps = 0
+    finally:
+        t.close()
