@@ -109,7 +109,9 @@ int arc_ctx_finish(arc_ctx* c) {
     c->last_status = st;
     if (st) {
         char b[128];
-        snprintf(b, sizeof b, "device range check failed (status 0x%x): pool index out of range", st);
+        snprintf(b, sizeof b, (st & 0x80000000u) ? "tensor-core pipeline wait timed out (status 0x%x)"
+                                                 : "device range check failed (status 0x%x): pool index out of range",
+                 st);
         cudaMemsetAsync(c->d_status, 0, sizeof(uint32_t), c->stream);
         cudaStreamSynchronize(c->stream);
         return set_err(c, ARC_E_DEVICE_CHECK, b);
@@ -213,6 +215,7 @@ int arc_destroy(arc_ctx* c) {
     cudaFree(c->d_nrc_w32);
     cudaFree(c->d_nrc_w16);
     cudaFree(c->d_nrc_w16_ema);
+    cudaFree(c->d_nrc_wu_ema);
     cudaFree(c->d_nrc_batch);
     cudaFree(c->d_nrc_gate);
     cudaFree(c->d_nrc_loss);

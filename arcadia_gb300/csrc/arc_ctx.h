@@ -72,7 +72,9 @@ struct arc_ctx {
     float* d_nrc_grad = nullptr;
     void* d_nrc_w16 = nullptr;
     float* d_nrc_ema = nullptr;       // exponential moving average of the weights (inference)
-    void* d_nrc_w16_ema = nullptr;    // its FP16 forward layout
+    void* d_nrc_w16_ema = nullptr;    // its FP16 forward layout (mma.sync kernels)
+    void* d_nrc_wu_ema = nullptr;     // its FP16 tensor-core operand layout (tcgen05 kernels)
+    int nrc_infer_path = 1;           // 1 = tcgen05 inference, 0 = mma.sync inference
     float nrc_ema_decay = 0.99f;
     float* d_nrc_loss = nullptr;
     uint32_t nrc_step = 0;

@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "arc_ctx.h"
+#include "arc_tc.cuh"
 
 namespace nrc {
 
@@ -55,6 +56,19 @@ constexpr int kActHalves = kDZ + 2 * 64 * kSS;
 
 __host__ __device__ constexpr int fwd_off(int l) { return l == 1 ? kF1 : (l <= 5 ? kF2 + (l - 2) * 64 * kS : kF6); }
 __host__ __device__ constexpr int fwd_stride(int l) { return l == 1 ? kS1 : kS; }
+
+// FP16 tensor-core operand layout (tcgen05 kernels): per layer an N_l x K_l K-major block in the
+// canonical no-swizzle layout, element (n, k) at u_index(l, n, k) (halves): 8 x 8 core matrices of
+// 128 B, K-adjacent core matrices 128 B apart, 8-row groups K_l/8 core matrices apart. Layer 1 is
+// 64 x 224 (features 216..223 zero), layers 2..5 64 x 64, layer 6 16 x 64 (outputs 3..15 zero).
+constexpr int kU2 = 64 * kEncPad;
+constexpr int kU6 = kU2 + 4 * 64 * 64;
+constexpr int kUHalves = kU6 + 16 * 64;  // 31744 halves = 63,488 B
+__host__ __device__ constexpr int u_off(int l) { return l == 1 ? 0 : (l <= 5 ? kU2 + (l - 2) * 4096 : kU6); }
+__host__ __device__ constexpr int u_k(int l) { return l == 1 ? kEncPad : kW; }
+__host__ __device__ constexpr int u_index(int l, int n, int k) {
+    return u_off(l) + (n >> 3) * (u_k(l) >> 3) * 64 + (k >> 3) * 64 + (n & 7) * 8 + (k & 7);
+}
 
 __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
     asm volatile(
@@ -376,8 +390,8 @@ __global__ void __launch_bounds__(128) train_kernel(const __half* __restrict__ w
 // layout, which inference reads) follows: ema = decay * ema + (1 - decay) * w.
 __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
                             const float* __restrict__ g, __half* __restrict__ w16, float* __restrict__ ema,
-                            __half* __restrict__ w16_ema, float decay, float lr, float c1, float c2, float inv_scale,
-                            const uint32_t* __restrict__ gate) {
+                            __half* __restrict__ w16_ema, __half* __restrict__ wu_ema, float decay, float lr, float c1,
+                            float c2, float inv_scale, const uint32_t* __restrict__ gate) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams || (gate && *gate == 0u)) return;
     const float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
@@ -397,13 +411,15 @@ __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float*
     if (l == 5) w16[kT6 + k * kST6 + o] = h;
     const float e = decay * ema[i] + (1.0f - decay) * wi;
     ema[i] = e;
-    w16_ema[fwd_off(l + 1) + o * fwd_stride(l + 1) + k] = __float2half_rn(e);
+    const __half he = __float2half_rn(e);
+    w16_ema[fwd_off(l + 1) + o * fwd_stride(l + 1) + k] = he;
+    wu_ema[u_index(l + 1, o, k)] = he;
 }
 
 // FP16 layouts from the masters (used after init / set_weights; padding stays zero); the EMA restarts
 // from the same weights.
 __global__ void pack_kernel(const float* __restrict__ w, __half* __restrict__ w16, float* __restrict__ ema,
-                            __half* __restrict__ w16_ema) {
+                            __half* __restrict__ w16_ema, __half* __restrict__ wu_ema) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams) return;
     int l = 0;
@@ -415,6 +431,182 @@ __global__ void pack_kernel(const float* __restrict__ w, __half* __restrict__ w1
     if (l == 5) w16[kT6 + k * kST6 + o] = h;
     ema[i] = w[i];
     w16_ema[fwd_off(l + 1) + o * fwd_stride(l + 1) + k] = h;
+    wu_ema[u_index(l + 1, o, k)] = h;
+}
+
+
+// ---- tcgen05 inference --------------------------------------------------------------------------
+// A CTA of 128 threads evaluates 128 queries per tile, thread m owning row m. The elected thread 0
+// issues tcgen05.mma (M = 128, N = 64 or 16, K = 16 per instruction) from shared-memory operands into
+// a TMEM accumulator (128 lanes x 64 + 16 columns); every thread reads its lane back with tcgen05.ld,
+// applies ReLU, packs FP16 and writes the next layer's A operand. The weights (63.5 KB) arrive once per
+// CTA through one bulk copy. The A buffer (28 KB) holds half of the 224 encoded features or one hidden
+// layer, so layer 1 runs as two accumulating passes; two CTAs fit on an SM.
+constexpr int kTcA = 128 * 112;  // halves
+constexpr uint32_t kTcSmem = kUHalves * 2 + kTcA * 2 + 64;
+constexpr long long kTcBudget = 2000000000ll;  // cycles (about one second) per wait
+
+// sin/cos(2^k pi x), k = 0..11, as 12 packed (sin, cos) FP16 pairs: sincospif at k = 0 and k = 6 and
+// five angle doublings after each (s' = 2 s c, c' = (c - s)(c + s)), which add a few ulp of FP32.
+__device__ __forceinline__ void enc_input(float x, uint32_t (&h)[12]) {
+    float s, c;
+#pragma unroll
+    for (int base = 0; base < 12; base += 6) {
+        sincospif(base ? x * 64.0f : x, &s, &c);
+        h[base] = pack_h2(s, c);
+#pragma unroll
+        for (int k = 1; k < 6; ++k) {
+            const float s2 = 2.0f * s * c, c2 = (c - s) * (c + s);
+            s = s2;
+            c = c2;
+            h[base + k] = pack_h2(s, c);
+        }
+    }
+}
+
+// 16-byte chunk lc (8 halves along K) of row m in an A buffer of kbc chunks per row.
+__device__ __forceinline__ void st_chunk(uint8_t* sa, int kbc, int m, int lc, uint4 v) {
+    *reinterpret_cast<uint4*>(sa + 2 * ((m >> 3) * kbc * 64 + lc * 64 + (m & 7) * 8)) = v;
+}
+
+__global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restrict__ wu, const float* __restrict__ in,
+                                                          const float* __restrict__ albedo, uint32_t n,
+                                                          float* __restrict__ out, const uint32_t* __restrict__ list,
+                                                          const unsigned long long* __restrict__ n_dev,
+                                                          uint32_t* __restrict__ status) {
+    extern __shared__ __align__(128) uint8_t smem_raw[];
+    uint8_t* sw = smem_raw;
+    uint8_t* sa = smem_raw + kUHalves * 2;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + kUHalves * 2 + kTcA * 2);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
+    if (n_dev) {
+        const unsigned long long nd = *n_dev;
+        n = nd < n ? (uint32_t)nd : n;
+    }
+    const uint32_t tiles = (n + 127u) / 128u;
+    if (blockIdx.x >= tiles) return;  // uniform over the CTA, before any TMEM allocation
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t bar_w = tc::smem_u32(&bars[0]), bar_m = tc::smem_u32(&bars[1]);
+    const uint32_t sa_u = tc::smem_u32(sa), sw_u = tc::smem_u32(sw);
+    if (tid == 0) {
+        tc::mbar_init(bar_w, 1);
+        tc::mbar_init(bar_m, 1);
+        tc::fence_mbar_init();
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(tc::smem_u32(tslot), 128);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t d_hid = tmem, d_out = tmem + 64u, lane_off = (warp * 32u) << 16;
+    if (tid == 0) {
+        tc::mbar_expect_tx(bar_w, kUHalves * 2);
+        tc::bulk_g2s(sw_u, wu, kUHalves * 2, bar_w);
+    }
+    bool ok = tc::mbar_wait(bar_w, 0, kTcBudget);
+    bool fail = __syncthreads_or(!ok);
+    uint32_t phase = 0;
+    constexpr uint32_t kId64 = tc::idesc_f16(128, 64, false, false), kId16 = tc::idesc_f16(128, 16, false, false);
+    // one MMA pass: D (+)= A[sa] * W^T, `steps` K-steps; A has a_sbo bytes per 8-row group
+    auto issue = [&](uint32_t d, uint32_t w_byte, uint32_t w_sbo, uint32_t a_sbo, int steps, uint32_t idesc, bool acc) {
+        if (tid == 0) {
+            tc::fence_after();
+            for (int st = 0; st < steps; ++st)
+                tc::mma_f16(d, tc::sdesc(sa_u + 256u * st, 128u, a_sbo), tc::sdesc(sw_u + w_byte + 256u * st, 128u, w_sbo),
+                            idesc, (acc || st) ? 1u : 0u);
+            tc::commit(bar_m);
+        }
+        ok = tc::mbar_wait(bar_m, phase, kTcBudget);
+        if (ok) phase ^= 1u;
+        tc::fence_after();
+    };
+    for (uint32_t tile = blockIdx.x; !fail && tile < tiles; tile += gridDim.x) {
+        const uint32_t j = tile * 128u + tid;
+        const bool valid = j < n;
+        const uint32_t p = valid ? (list ? __ldg(&list[j]) : j) : 0u;
+        float v[kIn];
+#pragma unroll
+        for (int i = 0; i < kIn; ++i) v[i] = valid ? __ldg(&in[(size_t)p * kIn + i]) : 0.0f;
+        // layer 1, first half: features 0..111 = inputs 0..3 and the first 16 features of input 4
+        uint32_t h[12];
+        uint4 keep;
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+            enc_input(v[i], h);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const uint4 ch = make_uint4(h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
+                if (3 * i + q < 14) st_chunk(sa, 14, tid, 3 * i + q, ch);
+                else keep = ch;
+            }
+        }
+        tc::fence_async_smem();
+        tc::fence_before();
+        if ((fail = __syncthreads_or(!ok))) break;
+        issue(d_hid, 2u * u_off(1), 3584u, 1792u, 7, kId64, false);
+        // second half: features 112..223 (the rest of input 4, inputs 5..8, 8 zero features)
+        if ((fail = __syncthreads_or(!ok))) break;
+        st_chunk(sa, 14, tid, 0, keep);
+#pragma unroll
+        for (int i = 5; i < kIn; ++i) {
+            enc_input(v[i], h);
+#pragma unroll
+            for (int q = 0; q < 3; ++q)
+                st_chunk(sa, 14, tid, 3 * i + q - 14, make_uint4(h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]));
+        }
+        st_chunk(sa, 14, tid, 13, make_uint4(0u, 0u, 0u, 0u));
+        tc::fence_async_smem();
+        tc::fence_before();
+        if ((fail = __syncthreads_or(!ok))) break;
+        issue(d_hid, 2u * u_off(1) + 14u * 128u, 3584u, 1792u, 7, kId64, true);
+        // layers 2..6: ReLU of the accumulator -> FP16 A operand -> next MMA
+        for (int l = 2; l <= 6 && !fail; ++l) {
+            uint32_t r[4][16];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) tc::tmem_ld16(d_hid + lane_off + 16u * q, r[q]);
+            tc::tmem_wait_ld();
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+#pragma unroll
+                for (int c2 = 0; c2 < 2; ++c2) {
+                    uint32_t pk[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        pk[e] = pack_h2(fmaxf(__uint_as_float(r[q][8 * c2 + 2 * e]), 0.0f),
+                                        fmaxf(__uint_as_float(r[q][8 * c2 + 2 * e + 1]), 0.0f));
+                    st_chunk(sa, 8, tid, 2 * q + c2, make_uint4(pk[0], pk[1], pk[2], pk[3]));
+                }
+            }
+            tc::fence_async_smem();
+            tc::fence_before();
+            if ((fail = __syncthreads_or(!ok))) break;
+            issue(l < 6 ? d_hid : d_out, 2u * u_off(l), 1024u, 1024u, 4, l < 6 ? kId64 : kId16, false);
+        }
+        if ((fail = __syncthreads_or(!ok))) break;
+        uint32_t y[16];
+        tc::tmem_ld16(d_out + lane_off, y);
+        tc::tmem_wait_ld();
+        if (valid) {
+#pragma unroll
+            for (int c = 0; c < kOut; ++c) {
+                const size_t o = (size_t)p * 3 + c;
+                const float val = __uint_as_float(y[c]);
+                out[o] = albedo ? val * __ldg(&albedo[o]) : val;
+            }
+        }
+        tc::fence_before();
+    }
+    if (fail && tid == 0) {
+        atomicOr(status, 0x80000000u);
+        tc::mbar_wait(bar_m, phase, kTcBudget);  // an MMA still in flight finishes before TMEM is released
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 0) tc::tmem_dealloc(tmem, 128);
 }
 
 }  // namespace nrc
@@ -449,10 +641,13 @@ int ensure_nrc(arc_ctx* c) {
     c->d_nrc_ema = c->d_nrc_grad + nrc::kParams;
     NRC_CK(cudaMalloc(&c->d_nrc_w16, sizeof(__half) * nrc::kAllHalves));
     NRC_CK(cudaMalloc(&c->d_nrc_w16_ema, sizeof(__half) * nrc::kFwdHalves));
+    NRC_CK(cudaMalloc(&c->d_nrc_wu_ema, sizeof(__half) * nrc::kUHalves));
     NRC_CK(cudaMalloc((void**)&c->d_nrc_loss, sizeof(float)));
     NRC_CK(cudaMemsetAsync(c->d_nrc_w32, 0, sizeof(float) * nrc::kParams * 5, c->stream));
     NRC_CK(cudaMemsetAsync(c->d_nrc_w16, 0, sizeof(__half) * nrc::kAllHalves, c->stream));
     NRC_CK(cudaMemsetAsync(c->d_nrc_w16_ema, 0, sizeof(__half) * nrc::kFwdHalves, c->stream));
+    NRC_CK(cudaMemsetAsync(c->d_nrc_wu_ema, 0, sizeof(__half) * nrc::kUHalves, c->stream));
+    NRC_CK(cudaFuncSetAttribute(nrc::infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nrc::kTcSmem));
     NRC_CK(cudaFuncSetAttribute(nrc::infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 nrc::kFwdHalves * (int)sizeof(__half)));
     NRC_CK(cudaFuncSetAttribute(nrc::train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -484,6 +679,13 @@ void init_weights(std::vector<float>& w, uint32_t seed) {
 
 int launch_infer(arc_ctx* c, const float* inputs, const float* albedo, uint32_t n, float* out, const uint32_t* list,
                  const unsigned long long* n_dev) {
+    if (c->nrc_infer_path == 1) {
+        const uint32_t blocks = std::min<uint32_t>((n + 127u) / 128u, (uint32_t)c->n_sm * 2u);
+        nrc::infer_tc_kernel<<<blocks, 128, nrc::kTcSmem, c->stream>>>(static_cast<const __half*>(c->d_nrc_wu_ema), inputs,
+                                                                        albedo, n, out, list, n_dev, c->d_status);
+        NRC_CK(cudaGetLastError());
+        return ARC_OK;
+    }
     const uint32_t tiles = (n + 15u) / 16u;
     const uint32_t blocks = std::min<uint32_t>((tiles + 3u) / 4u, (uint32_t)c->n_sm * 3u);
     nrc::infer_kernel<<<blocks, 128, nrc::kFwdHalves * sizeof(__half), c->stream>>>(
@@ -510,7 +712,8 @@ int launch_adam(arc_ctx* c, float lr, const uint32_t* gate) {
     const float c1 = 1.0f - std::pow(0.9f, (float)c->nrc_step), c2 = 1.0f - std::pow(0.99f, (float)c->nrc_step);
     nrc::adam_kernel<<<(nrc::kParams + 255) / 256, 256, 0, c->stream>>>(
         c->d_nrc_w32, c->d_nrc_m, c->d_nrc_v, c->d_nrc_grad, static_cast<__half*>(c->d_nrc_w16), c->d_nrc_ema,
-        static_cast<__half*>(c->d_nrc_w16_ema), c->nrc_ema_decay, lr, c1, c2, 1.0f / nrc::kLossScale, gate);
+        static_cast<__half*>(c->d_nrc_w16_ema), static_cast<__half*>(c->d_nrc_wu_ema), c->nrc_ema_decay, lr, c1, c2,
+        1.0f / nrc::kLossScale, gate);
     NRC_CK(cudaGetLastError());
     return ARC_OK;
 }
@@ -535,7 +738,8 @@ int arc_nrc_set_weights(arc_ctx* c, const float* w) {
     NRC_CK(cudaMemcpyAsync(c->d_nrc_w32, w, sizeof(float) * nrc::kParams, cudaMemcpyHostToDevice, c->stream));
     NRC_CK(cudaMemsetAsync(c->d_nrc_m, 0, sizeof(float) * nrc::kParams * 2, c->stream));
     nrc::pack_kernel<<<(nrc::kParams + 255) / 256, 256, 0, c->stream>>>(c->d_nrc_w32, static_cast<__half*>(c->d_nrc_w16),
-                                                                       c->d_nrc_ema, static_cast<__half*>(c->d_nrc_w16_ema));
+                                                                       c->d_nrc_ema, static_cast<__half*>(c->d_nrc_w16_ema),
+                                                                       static_cast<__half*>(c->d_nrc_wu_ema));
     NRC_CK(cudaGetLastError());
     c->nrc_step = 0;
     return arc_ctx_finish(c);
@@ -555,6 +759,12 @@ int arc_nrc_get_ema_weights(arc_ctx* c, float* w) {
     if (rc) return rc;
     NRC_CK(cudaMemcpyAsync(w, c->d_nrc_ema, sizeof(float) * nrc::kParams, cudaMemcpyDeviceToHost, c->stream));
     return arc_ctx_finish(c);
+}
+
+int arc_nrc_set_infer_path(arc_ctx* c, int path) {
+    if (!c || (path != 0 && path != 1)) return ARC_E_INVALID_ARG;
+    c->nrc_infer_path = path;
+    return ARC_OK;
 }
 
 int arc_nrc_set_ema_decay(arc_ctx* c, float decay) {

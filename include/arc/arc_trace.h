@@ -64,7 +64,8 @@ typedef struct arc_launch_config {
 typedef struct arc_stats {
     float last_kernel_ms;      /* device time of the last traversal launch (CUDA events) */
     uint64_t rays_traced;      /* primary + secondary rays of the last launch */
-    uint32_t device_status;    /* bit mask of device-side range check failures */
+    uint32_t device_status;    /* bit mask of device-side range check failures; bit 31 = a tensor-core
+                                  pipeline wait ran out of its time budget */
     uint32_t n_sm;
 } arc_stats;
 
@@ -203,6 +204,9 @@ int arc_nrc_get_weights(arc_ctx* ctx, float* weights);
  * after every Adam step (decay 0.99 by default; 0 = the latest weights). set_weights / init restart
  * it from the given weights. */
 int arc_nrc_set_ema_decay(arc_ctx* ctx, float decay);
+/* Inference kernel: 1 = tcgen05 tensor cores with TMEM accumulators (default), 0 = the warp-level
+ * mma.sync kernel (kept as the comparison point). */
+int arc_nrc_set_infer_path(arc_ctx* ctx, int path);
 int arc_nrc_get_ema_weights(arc_ctx* ctx, float* weights);
 /* out_rgb[i] = albedo[i] * network(inputs[i]) per channel; albedo may be NULL (network output only). */
 int arc_nrc_query_dev(arc_ctx* ctx, const float* inputs, const float* albedo, uint32_t n, float* out_rgb);

@@ -242,3 +242,45 @@ def test_gpu_weight_ema_feeds_inference(orc, tracer):
         assert lib().arc_nrc_set_ema_decay(tracer.ctx, 1.0) != 0  # outside [0, 1)
     finally:
         assert lib().arc_nrc_set_ema_decay(tracer.ctx, 0.99) == 0
+
+
+@pytest.mark.gpu
+def test_gpu_tcgen05_and_mma_sync_inference_agree(orc, tracer):
+    """The tcgen05 (TMEM accumulator) kernel and the mma.sync kernel evaluate the same network; both stay
+    within the FP16 tolerance of the FP64 oracle, including a ragged last tile and a compacted list."""
+    import torch
+    from arcadia_gb300.native import lib
+
+    x, _ = _data(70001, 17)  # 547 tiles of 128, the last one ragged
+    w = _weights(18)
+    _set(tracer, w)
+    dx = torch.from_numpy(x).cuda()
+    outs = []
+    try:
+        for path in (1, 0):
+            assert lib().arc_nrc_set_infer_path(tracer.ctx, path) == 0
+            dy = torch.zeros((len(x), 3), dtype=torch.float32, device="cuda")
+            assert lib().arc_nrc_query_dev(tracer.ctx, dx.data_ptr(), None, len(x), dy.data_ptr()) == 0
+            tracer.synchronize()
+            outs.append(dy.cpu().numpy())
+        ref = orc.nrc_forward(w, x[:4096])
+        for y in outs:
+            assert np.all(np.abs(y[:4096] - ref) <= 2e-2 * np.abs(ref) + 2e-3), np.max(np.abs(y[:4096] - ref))
+        assert np.max(np.abs(outs[0] - outs[1])) <= 1e-2 * np.max(np.abs(outs[1])) + 1e-3
+        # compacted list on the tcgen05 path: every third point, in reverse order
+        assert lib().arc_nrc_set_infer_path(tracer.ctx, 1) == 0
+        idx = np.arange(len(x) - 1, -1, -3, dtype=np.int32)
+        dl = torch.from_numpy(idx).cuda()
+        nd = torch.tensor([len(idx)], dtype=torch.int64, device="cuda")
+        dz = torch.full((len(x), 3), -5.0, dtype=torch.float32, device="cuda")
+        assert lib().arc_nrc_query_list_dev(tracer.ctx, dl.data_ptr(), nd.data_ptr(), len(x), dx.data_ptr(), None,
+                                            dz.data_ptr()) == 0
+        tracer.synchronize()
+        z = dz.cpu().numpy()
+        mask = np.zeros(len(x), bool)
+        mask[idx] = True
+        np.testing.assert_array_equal(z[mask], outs[0][mask])
+        assert (z[~mask] == -5.0).all()
+        assert tracer.stats().device_status == 0
+    finally:
+        assert lib().arc_nrc_set_infer_path(tracer.ctx, 1) == 0
