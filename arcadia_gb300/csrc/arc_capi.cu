@@ -216,6 +216,7 @@ int arc_destroy(arc_ctx* c) {
     cudaFree(c->d_nrc_w16);
     cudaFree(c->d_nrc_w16_ema);
     cudaFree(c->d_nrc_wu_ema);
+    cudaFree(c->d_nrc_wu);
     cudaFree(c->d_nrc_batch);
     cudaFree(c->d_nrc_gate);
     cudaFree(c->d_nrc_loss);

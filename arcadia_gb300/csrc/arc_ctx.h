@@ -74,7 +74,9 @@ struct arc_ctx {
     float* d_nrc_ema = nullptr;       // exponential moving average of the weights (inference)
     void* d_nrc_w16_ema = nullptr;    // its FP16 forward layout (mma.sync kernels)
     void* d_nrc_wu_ema = nullptr;     // its FP16 tensor-core operand layout (tcgen05 kernels)
+    void* d_nrc_wu = nullptr;         // the latest weights in the tensor-core layout (tcgen05 training)
     int nrc_infer_path = 1;           // 1 = tcgen05 inference, 0 = mma.sync inference
+    int nrc_train_path = 1;           // 1 = tcgen05 training, 0 = mma.sync training
     float nrc_ema_decay = 0.99f;
     float* d_nrc_loss = nullptr;
     uint32_t nrc_step = 0;
@@ -97,10 +99,12 @@ struct arc_ctx {
 int arc_ctx_check_ready(arc_ctx* c, bool need_cam);
 int arc_ctx_finish(arc_ctx* c);
 // NRC training samples drawn from a compacted list of GI hit points (defined with the estimator in
-// arc_sharc.cu): sample i takes list[hash(i, seed) mod *n_valid] and its demodulated 1-spp target;
-// gate receives n_samples, or 0 when *n_valid is 0.
+// arc_sharc.cu): stratified over list[0 .. *n_valid) with a seeded phase, demodulated 1-spp targets,
+// interleaved into `steps` slices (n_samples a multiple of steps); gate receives n_samples, or 0
+// when *n_valid is 0.
 extern "C" int arc_launch_train_samples_list(arc_ctx* c, const uint32_t* list, const unsigned long long* n_valid,
                                              const float* pos, const float* nrm, const float* nrc_in, uint32_t seed,
-                                             uint32_t n_samples, float* train_in, float* train_t, uint32_t* gate);
+                                             uint32_t n_samples, uint32_t steps, float* train_in, float* train_t,
+                                             uint32_t* gate);
 int arc_ctx_stage(arc_ctx* c, size_t bytes, void** out);
 int arc_ctx_sync_world_table(arc_ctx* c);

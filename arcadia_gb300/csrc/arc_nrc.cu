@@ -390,8 +390,8 @@ __global__ void __launch_bounds__(128) train_kernel(const __half* __restrict__ w
 // layout, which inference reads) follows: ema = decay * ema + (1 - decay) * w.
 __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
                             const float* __restrict__ g, __half* __restrict__ w16, float* __restrict__ ema,
-                            __half* __restrict__ w16_ema, __half* __restrict__ wu_ema, float decay, float lr, float c1,
-                            float c2, float inv_scale, const uint32_t* __restrict__ gate) {
+                            __half* __restrict__ w16_ema, __half* __restrict__ wu, __half* __restrict__ wu_ema, float decay,
+                            float lr, float c1, float c2, float inv_scale, const uint32_t* __restrict__ gate) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams || (gate && *gate == 0u)) return;
     const float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
@@ -409,6 +409,7 @@ __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float*
     w16[fwd_off(l + 1) + o * fwd_stride(l + 1) + k] = h;
     if (l >= 1 && l <= 4) w16[kT2 + (l - 1) * 64 * kS + k * kS + o] = h;
     if (l == 5) w16[kT6 + k * kST6 + o] = h;
+    wu[u_index(l + 1, o, k)] = h;
     const float e = decay * ema[i] + (1.0f - decay) * wi;
     ema[i] = e;
     const __half he = __float2half_rn(e);
@@ -419,7 +420,7 @@ __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float*
 // FP16 layouts from the masters (used after init / set_weights; padding stays zero); the EMA restarts
 // from the same weights.
 __global__ void pack_kernel(const float* __restrict__ w, __half* __restrict__ w16, float* __restrict__ ema,
-                            __half* __restrict__ w16_ema, __half* __restrict__ wu_ema) {
+                            __half* __restrict__ w16_ema, __half* __restrict__ wu, __half* __restrict__ wu_ema) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams) return;
     int l = 0;
@@ -431,6 +432,7 @@ __global__ void pack_kernel(const float* __restrict__ w, __half* __restrict__ w1
     if (l == 5) w16[kT6 + k * kST6 + o] = h;
     ema[i] = w[i];
     w16_ema[fwd_off(l + 1) + o * fwd_stride(l + 1) + k] = h;
+    wu[u_index(l + 1, o, k)] = h;
     wu_ema[u_index(l + 1, o, k)] = h;
 }
 
@@ -609,6 +611,259 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
     if (warp == 0) tc::tmem_dealloc(tmem, 128);
 }
 
+// ---- tcgen05 training -----------------------------------------------------------------------------
+// One CTA per SM takes 128-sample tiles of the batch (thread m = sample m of the tile):
+//   forward   layers 1..6 as in inference, keeping the FP16 operands: the encoding A0 (128 x 256,
+//             features 216..255 zero) in region R, then H1..H4 in R (A0 is dead after layer 1) and H5
+//   output    dY = 2 (y - t) / (y^2 + 0.01) / n * 128 (loss scale) -> dZ6 (128 x 16)
+//   backward  dA_{l-1} = dZ_l W_l (B = W_l read MN-major from the forward layout), masked by H_{l-1} > 0
+//   gradients dW_l^T += H_{l-1}^T dZ_l in TMEM (A and B MN-major views of the activation buffers; M 64
+//             rows of H features, or 2 x M 128 over the re-encoded A0 for layer 1), accumulated over all
+//             of the CTA's tiles and added to the FP32 gradient once at the end.
+// TMEM columns: 0..63 layer accumulator, 64..79 output, 80..95 dW6^T, 128..255 dW1^T (two M-halves),
+// 256..511 dW2^T..dW5^T. An M = 64 accumulator keeps row r in lane 32 (r / 16) + r % 16.
+constexpr uint32_t kTtR = kUHalves * 2;         // region R: A0, then H1..H4 (64 KB)
+constexpr uint32_t kTtH5 = kTtR + 65536;        // H5 (16 KB)
+constexpr uint32_t kTtDZ = kTtH5 + 16384;       // dZ (16 KB)
+constexpr uint32_t kTtBar = kTtDZ + 16384;
+constexpr uint32_t kTtSmem = kTtBar + 64;       // 161,856 B
+
+__device__ __forceinline__ uint32_t tt_h(int l) { return l <= 4 ? kTtR + 16384u * (l - 1) : kTtH5; }  // H_l, l = 1..5
+
+// red.add of one TMEM row (64 FP32 columns, loss-scaled) of a transposed weight gradient: g[o * din + f].
+__device__ __forceinline__ void red_row(float* __restrict__ g, int din, int f, int ncols, const uint32_t (&r)[4][16]) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int e = 0; e < 16; ++e)
+            if (16 * q + e < ncols) atomicAdd(&g[(16 * q + e) * din + f], __uint_as_float(r[q][e]));
+}
+
+__global__ void __launch_bounds__(128, 1) train_tc_kernel(const __half* __restrict__ wu, const float* __restrict__ in,
+                                                          const float* __restrict__ target, uint32_t n, float inv_norm,
+                                                          float* __restrict__ grad, float* __restrict__ loss_sum,
+                                                          const uint32_t* __restrict__ gate, uint32_t* __restrict__ status) {
+    extern __shared__ __align__(128) uint8_t smem_raw[];
+    if (gate && *gate == 0u) return;  // empty frame batch (uniform over the grid)
+    const uint32_t tiles = (n + 127u) / 128u;
+    if (blockIdx.x >= tiles) return;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + kTtBar);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    const uint32_t bar_w = tc::smem_u32(&bars[0]), bar_m = tc::smem_u32(&bars[1]);
+    const uint32_t s0 = tc::smem_u32(smem_raw);
+    if (tid == 0) {
+        tc::mbar_init(bar_w, 1);
+        tc::mbar_init(bar_m, 1);
+        tc::fence_mbar_init();
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(tc::smem_u32(tslot), 512);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = *tslot, lane_off = (warp * 32u) << 16;
+    const uint32_t d_hid = tmem, d_out = tmem + 64u, d_w6 = tmem + 80u, d_w1 = tmem + 128u;
+    auto d_wl = [&](int l) { return tmem + 256u + 64u * (uint32_t)(l - 2); };  // dW_l^T, l = 2..5
+    if (tid == 0) {
+        tc::mbar_expect_tx(bar_w, kUHalves * 2);
+        tc::bulk_g2s(s0, wu, kUHalves * 2, bar_w);
+    }
+    bool ok = tc::mbar_wait(bar_w, 0, kTcBudget);
+    bool fail = __syncthreads_or(!ok);
+    uint32_t phase = 0;
+    float my_loss = 0.0f;
+    bool first = true;  // first tile of this CTA: weight-gradient accumulators start from zero
+    constexpr uint32_t kF64 = tc::idesc_f16(128, 64, false, false), kF16 = tc::idesc_f16(128, 16, false, false);
+    constexpr uint32_t kBwd = tc::idesc_f16(128, 64, false, true);   // dZ (K-major) x W (MN-major)
+    constexpr uint32_t kG64 = tc::idesc_f16(64, 64, true, true), kG16 = tc::idesc_f16(64, 16, true, true);
+    constexpr uint32_t kG1 = tc::idesc_f16(128, 64, true, true);
+    auto wait_mma = [&]() {
+        if (tid == 0) tc::commit(bar_m);
+        ok = tc::mbar_wait(bar_m, phase, kTcBudget);
+        if (ok) phase ^= 1u;
+        tc::fence_after();
+    };
+    auto fwd_layer = [&](uint32_t d, uint32_t a_off, uint32_t a_sbo, int l, int steps, uint32_t idesc) {
+        if (tid == 0) {
+            tc::fence_after();
+            const uint32_t w_sbo = (uint32_t)(u_k(l) / 8) * 128u;
+            for (int st = 0; st < steps; ++st)
+                tc::mma_f16(d, tc::sdesc(s0 + a_off + 256u * st, 128u, a_sbo), tc::sdesc(s0 + 2u * u_off(l) + 256u * st, 128u, w_sbo),
+                            idesc, st ? 1u : 0u);
+        }
+        wait_mma();
+    };
+    // FP16 row of 64 features from the accumulator (ReLU optional) into a K-major buffer
+    auto store_row64 = [&](const uint32_t (&r)[4][16], uint32_t buf, bool relu) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            uint32_t pk[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                float a = __uint_as_float(r[c >> 1][8 * (c & 1) + 2 * e]), b = __uint_as_float(r[c >> 1][8 * (c & 1) + 2 * e + 1]);
+                if (relu) {
+                    a = fmaxf(a, 0.0f);
+                    b = fmaxf(b, 0.0f);
+                }
+                pk[e] = pack_h2(a, b);
+            }
+            st_chunk(smem_raw + buf, 8, tid, c, make_uint4(pk[0], pk[1], pk[2], pk[3]));
+        }
+    };
+    auto ld64 = [&](uint32_t d, uint32_t (&r)[4][16]) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) tc::tmem_ld16(d + lane_off + 16u * q, r[q]);
+        tc::tmem_wait_ld();
+    };
+    auto encode_a0 = [&](const float (&v)[kIn]) {
+        uint32_t h[12];
+#pragma unroll
+        for (int i = 0; i < kIn; ++i) {
+            enc_input(v[i], h);
+#pragma unroll
+            for (int q = 0; q < 3; ++q)
+                st_chunk(smem_raw + kTtR, 32, tid, 3 * i + q, make_uint4(h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]));
+        }
+#pragma unroll
+        for (int c = 27; c < 32; ++c) st_chunk(smem_raw + kTtR, 32, tid, c, make_uint4(0u, 0u, 0u, 0u));
+    };
+    for (uint32_t tile = blockIdx.x; !fail && tile < tiles; tile += gridDim.x) {
+        const uint32_t j = tile * 128u + tid;
+        const bool valid = j < n;
+        float v[kIn], t[kOut];
+#pragma unroll
+        for (int i = 0; i < kIn; ++i) v[i] = valid ? __ldg(&in[(size_t)j * kIn + i]) : 0.0f;
+#pragma unroll
+        for (int c = 0; c < kOut; ++c) t[c] = valid ? __ldg(&target[(size_t)j * kOut + c]) : 0.0f;
+        // ---- forward
+        encode_a0(v);
+        tc::fence_async_smem();
+        tc::fence_before();
+        if ((fail = __syncthreads_or(!ok))) break;
+        fwd_layer(d_hid, kTtR, 4096u, 1, 14, kF64);
+        uint32_t r[4][16];
+        for (int l = 2; l <= 6 && !fail; ++l) {
+            ld64(d_hid, r);
+            store_row64(r, tt_h(l - 1), true);
+            tc::fence_async_smem();
+            tc::fence_before();
+            if ((fail = __syncthreads_or(!ok))) break;
+            fwd_layer(l < 6 ? d_hid : d_out, tt_h(l - 1), 1024u, l, 4, l < 6 ? kF64 : kF16);
+        }
+        if ((fail = __syncthreads_or(!ok))) break;
+        // ---- output gradient
+        uint32_t y[16];
+        tc::tmem_ld16(d_out + lane_off, y);
+        tc::tmem_wait_ld();
+        float dy[kOut];
+#pragma unroll
+        for (int c = 0; c < kOut; ++c) {
+            const float yc = __uint_as_float(y[c]);
+            const float den = yc * yc + 0.01f;
+            dy[c] = valid ? 2.0f * (yc - t[c]) / den * inv_norm * kLossScale : 0.0f;
+            if (valid) my_loss += (yc - t[c]) * (yc - t[c]) / den;
+        }
+        st_chunk(smem_raw + kTtDZ, 8, tid, 0, make_uint4(pack_h2(dy[0], dy[1]), pack_h2(dy[2], 0.0f), 0u, 0u));
+        st_chunk(smem_raw + kTtDZ, 8, tid, 1, make_uint4(0u, 0u, 0u, 0u));
+        tc::fence_async_smem();
+        tc::fence_before();
+        if ((fail = __syncthreads_or(!ok))) break;
+        if (tid == 0) {
+            tc::fence_after();
+            // dA5 = dZ6 W6 (K = 16 outputs)
+            tc::mma_f16(d_hid, tc::sdesc(s0 + kTtDZ, 128u, 1024u), tc::sdesc(s0 + 2u * u_off(6), 1024u, 128u), kBwd, 0u);
+            // dW6^T += H5^T dZ6 (K = 128 samples)
+            for (int st = 0; st < 8; ++st)
+                tc::mma_f16(d_w6, tc::sdesc(s0 + kTtH5 + 2048u * st, 1024u, 128u), tc::sdesc(s0 + kTtDZ + 2048u * st, 1024u, 128u),
+                            kG16, (!first || st) ? 1u : 0u);
+        }
+        wait_mma();
+        // ---- backward through layers 5..1
+        for (int l = 5; l >= 1 && !fail; --l) {
+            ld64(d_hid, r);  // dA_l
+            const uint8_t* hrow = smem_raw + tt_h(l) + 2 * ((tid >> 3) * 8 * 64 + (tid & 7) * 8);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const uint4 hv = *reinterpret_cast<const uint4*>(hrow + 2 * 64 * c);
+                const uint32_t hw[4] = {hv.x, hv.y, hv.z, hv.w};
+                uint32_t pk[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const __half2 hh = *reinterpret_cast<const __half2*>(&hw[e]);
+                    const float a = __half2float(hh.x) > 0.0f ? __uint_as_float(r[c >> 1][8 * (c & 1) + 2 * e]) : 0.0f;
+                    const float b = __half2float(hh.y) > 0.0f ? __uint_as_float(r[c >> 1][8 * (c & 1) + 2 * e + 1]) : 0.0f;
+                    pk[e] = pack_h2(a, b);
+                }
+                st_chunk(smem_raw + kTtDZ, 8, tid, c, make_uint4(pk[0], pk[1], pk[2], pk[3]));
+            }
+            if (l == 1) {  // H1..H4 are consumed (every thread has read its H1 mask row): A0 again for dW1
+                __syncthreads();
+                encode_a0(v);
+            }
+            tc::fence_async_smem();
+            tc::fence_before();
+            if ((fail = __syncthreads_or(!ok))) break;
+            if (tid == 0) {
+                tc::fence_after();
+                if (l >= 2) {
+                    // dA_{l-1} = dZ_l W_l
+                    for (int st = 0; st < 4; ++st)
+                        tc::mma_f16(d_hid, tc::sdesc(s0 + kTtDZ + 256u * st, 128u, 1024u),
+                                    tc::sdesc(s0 + 2u * u_off(l) + 2048u * st, 1024u, 128u), kBwd, st ? 1u : 0u);
+                    // dW_l^T += H_{l-1}^T dZ_l
+                    for (int st = 0; st < 8; ++st)
+                        tc::mma_f16(d_wl(l), tc::sdesc(s0 + tt_h(l - 1) + 2048u * st, 1024u, 128u),
+                                    tc::sdesc(s0 + kTtDZ + 2048u * st, 1024u, 128u), kG64, (!first || st) ? 1u : 0u);
+                } else {
+                    // dW1^T += A0^T dZ1, features 0..127 and 128..255
+                    for (int half = 0; half < 2; ++half)
+                        for (int st = 0; st < 8; ++st)
+                            tc::mma_f16(d_w1 + 64u * half, tc::sdesc(s0 + kTtR + 2048u * half + 8192u * st, 4096u, 128u),
+                                        tc::sdesc(s0 + kTtDZ + 2048u * st, 1024u, 128u), kG1, (!first || st) ? 1u : 0u);
+                }
+            }
+            wait_mma();
+        }
+        first = false;
+    }
+    if (!fail) fail = __syncthreads_or(!ok);
+    if (!fail) {
+        // weight gradients out of TMEM (every warp runs the collective loads; lanes pick their rows)
+        uint32_t r[4][16];
+        for (int half = 0; half < 2; ++half) {  // layer 1: lane = feature
+            ld64(d_w1 + 64u * half, r);
+            const int f = (int)tid + 128 * half;
+            if (f < kEnc) red_row(grad + off(0), kEnc, f, 64, r);
+        }
+        const bool row_lane = lane < 16u;  // M = 64 accumulators: rows 16 warp + lane for lanes 0..15
+        const int f = (int)(16u * warp + lane);
+        for (int l = 2; l <= 5; ++l) {
+            ld64(d_wl(l), r);
+            if (row_lane) red_row(grad + off(l - 1), kW, f, 64, r);
+        }
+        uint32_t r6[16];
+        tc::tmem_ld16(d_w6 + lane_off, r6);
+        tc::tmem_wait_ld();
+        if (row_lane) {
+#pragma unroll
+            for (int o = 0; o < kOut; ++o) atomicAdd(&grad[off(5) + o * kW + f], __uint_as_float(r6[o]));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) my_loss += __shfl_down_sync(0xFFFFFFFFu, my_loss, o);
+        if (lane == 0) atomicAdd(loss_sum, my_loss);
+    } else if (tid == 0) {
+        atomicOr(status, 0x80000000u);
+        tc::mbar_wait(bar_m, phase, kTcBudget);  // an MMA still in flight finishes before TMEM is released
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 0) tc::tmem_dealloc(tmem, 512);
+}
+
 }  // namespace nrc
 
 // ------------------------------------------------------------------------------------------------
@@ -642,11 +897,14 @@ int ensure_nrc(arc_ctx* c) {
     NRC_CK(cudaMalloc(&c->d_nrc_w16, sizeof(__half) * nrc::kAllHalves));
     NRC_CK(cudaMalloc(&c->d_nrc_w16_ema, sizeof(__half) * nrc::kFwdHalves));
     NRC_CK(cudaMalloc(&c->d_nrc_wu_ema, sizeof(__half) * nrc::kUHalves));
+    NRC_CK(cudaMalloc(&c->d_nrc_wu, sizeof(__half) * nrc::kUHalves));
     NRC_CK(cudaMalloc((void**)&c->d_nrc_loss, sizeof(float)));
     NRC_CK(cudaMemsetAsync(c->d_nrc_w32, 0, sizeof(float) * nrc::kParams * 5, c->stream));
     NRC_CK(cudaMemsetAsync(c->d_nrc_w16, 0, sizeof(__half) * nrc::kAllHalves, c->stream));
     NRC_CK(cudaMemsetAsync(c->d_nrc_w16_ema, 0, sizeof(__half) * nrc::kFwdHalves, c->stream));
     NRC_CK(cudaMemsetAsync(c->d_nrc_wu_ema, 0, sizeof(__half) * nrc::kUHalves, c->stream));
+    NRC_CK(cudaMemsetAsync(c->d_nrc_wu, 0, sizeof(__half) * nrc::kUHalves, c->stream));
+    NRC_CK(cudaFuncSetAttribute(nrc::train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nrc::kTtSmem));
     NRC_CK(cudaFuncSetAttribute(nrc::infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nrc::kTcSmem));
     NRC_CK(cudaFuncSetAttribute(nrc::infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 nrc::kFwdHalves * (int)sizeof(__half)));
@@ -698,6 +956,14 @@ int launch_infer(arc_ctx* c, const float* inputs, const float* albedo, uint32_t 
 int launch_grad(arc_ctx* c, const float* inputs, const float* targets, uint32_t n, const uint32_t* gate) {
     NRC_CK(cudaMemsetAsync(c->d_nrc_grad, 0, sizeof(float) * nrc::kParams, c->stream));
     NRC_CK(cudaMemsetAsync(c->d_nrc_loss, 0, sizeof(float), c->stream));
+    if (c->nrc_train_path == 1) {
+        const uint32_t blocks = std::min<uint32_t>((n + 127u) / 128u, (uint32_t)c->n_sm);
+        nrc::train_tc_kernel<<<blocks, 128, nrc::kTtSmem, c->stream>>>(static_cast<const __half*>(c->d_nrc_wu), inputs, targets, n,
+                                                                         1.0f / (float)n, c->d_nrc_grad, c->d_nrc_loss, gate,
+                                                                         c->d_status);
+        NRC_CK(cudaGetLastError());
+        return ARC_OK;
+    }
     const uint32_t tiles = (n + 63u) / 64u;
     const uint32_t blocks = std::min<uint32_t>(tiles, (uint32_t)c->n_sm);
     nrc::train_kernel<<<blocks, 128, (nrc::kAllHalves + nrc::kActHalves) * sizeof(__half), c->stream>>>(
@@ -712,8 +978,8 @@ int launch_adam(arc_ctx* c, float lr, const uint32_t* gate) {
     const float c1 = 1.0f - std::pow(0.9f, (float)c->nrc_step), c2 = 1.0f - std::pow(0.99f, (float)c->nrc_step);
     nrc::adam_kernel<<<(nrc::kParams + 255) / 256, 256, 0, c->stream>>>(
         c->d_nrc_w32, c->d_nrc_m, c->d_nrc_v, c->d_nrc_grad, static_cast<__half*>(c->d_nrc_w16), c->d_nrc_ema,
-        static_cast<__half*>(c->d_nrc_w16_ema), static_cast<__half*>(c->d_nrc_wu_ema), c->nrc_ema_decay, lr, c1, c2,
-        1.0f / nrc::kLossScale, gate);
+        static_cast<__half*>(c->d_nrc_w16_ema), static_cast<__half*>(c->d_nrc_wu), static_cast<__half*>(c->d_nrc_wu_ema),
+        c->nrc_ema_decay, lr, c1, c2, 1.0f / nrc::kLossScale, gate);
     NRC_CK(cudaGetLastError());
     return ARC_OK;
 }
@@ -739,6 +1005,7 @@ int arc_nrc_set_weights(arc_ctx* c, const float* w) {
     NRC_CK(cudaMemsetAsync(c->d_nrc_m, 0, sizeof(float) * nrc::kParams * 2, c->stream));
     nrc::pack_kernel<<<(nrc::kParams + 255) / 256, 256, 0, c->stream>>>(c->d_nrc_w32, static_cast<__half*>(c->d_nrc_w16),
                                                                        c->d_nrc_ema, static_cast<__half*>(c->d_nrc_w16_ema),
+                                                                       static_cast<__half*>(c->d_nrc_wu),
                                                                        static_cast<__half*>(c->d_nrc_wu_ema));
     NRC_CK(cudaGetLastError());
     c->nrc_step = 0;
@@ -764,6 +1031,12 @@ int arc_nrc_get_ema_weights(arc_ctx* c, float* w) {
 int arc_nrc_set_infer_path(arc_ctx* c, int path) {
     if (!c || (path != 0 && path != 1)) return ARC_E_INVALID_ARG;
     c->nrc_infer_path = path;
+    return ARC_OK;
+}
+
+int arc_nrc_set_train_path(arc_ctx* c, int path) {
+    if (!c || (path != 0 && path != 1)) return ARC_E_INVALID_ARG;
+    c->nrc_train_path = path;
     return ARC_OK;
 }
 
@@ -824,7 +1097,8 @@ int arc_nrc_train_frame_dev(arc_ctx* c, const uint32_t* list, const uint64_t* n_
     int rc = arc_ctx_check_ready(c, true);
     if (rc) return rc;
     if (!list || !n_valid || !pos || !normal || !nrc_in) return nrc_err(c, ARC_E_INVALID_ARG, "null buffer");
-    if (steps == 0 || n_samples < steps) return nrc_err(c, ARC_E_INVALID_ARG, "need 1 <= steps <= n_samples");
+    if (steps == 0 || n_samples < steps || n_samples % steps)
+        return nrc_err(c, ARC_E_INVALID_ARG, "n_samples must be a non-zero multiple of steps");
     if ((rc = ensure_nrc(c))) return rc;
     if (c->nrc_batch_cap < n_samples) {
         cudaFree(c->d_nrc_batch);
@@ -837,7 +1111,7 @@ int arc_nrc_train_frame_dev(arc_ctx* c, const uint32_t* list, const uint64_t* n_
     float* train_in = c->d_nrc_batch;
     float* train_t = c->d_nrc_batch + 9u * (size_t)n_samples;
     if ((rc = arc_launch_train_samples_list(c, list, reinterpret_cast<const unsigned long long*>(n_valid), pos, normal,
-                                            nrc_in, seed, n_samples, train_in, train_t, c->d_nrc_gate)))
+                                            nrc_in, seed, n_samples, steps, train_in, train_t, c->d_nrc_gate)))
         return rc;
     const uint32_t per = n_samples / steps;
     for (uint32_t k = 0; k < steps; ++k) {

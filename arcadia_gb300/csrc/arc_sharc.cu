@@ -416,28 +416,33 @@ __global__ void onebounce_kernel(const World w, const __grid_constant__ arc_came
     }
 }
 
-// NRC training samples from the compacted GI hit list: sample i takes list[j], j = hash(i, seed) scaled
-// to [0, n_valid) (with replacement), and the 1-spp estimator with albedo 1 at that point.
+// NRC training samples from the compacted GI hit list, stratified: sample i takes list entry
+// floor((i + phase) n_valid / n_samples) (phase in [0, 1) from the seed), so the threads of a warp trace
+// neighbouring points (the list is in screen-tile order) and every point is covered evenly. Sample i is
+// stored at slot (i mod steps) * (n_samples / steps) + i / steps: each of the `steps` training slices
+// spans the whole frame. Target: the 1-spp estimator with albedo 1.
 __global__ void train_samples_list_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam,
                                           const uint32_t* __restrict__ list, const unsigned long long* __restrict__ n_valid,
                                           const float* __restrict__ pos, const float* __restrict__ nrm,
-                                          const float* __restrict__ nrc_in, uint32_t seed, uint32_t n_samples,
+                                          const float* __restrict__ nrc_in, uint32_t seed, uint32_t n_samples, uint32_t steps,
                                           float* __restrict__ train_in, float* __restrict__ train_t, uint32_t* __restrict__ gate) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_samples) return;
     const unsigned long long nv = *n_valid;
     if (i == 0) *gate = nv ? n_samples : 0u;
     if (!nv) return;
-    const uint32_t h = pcg_hash(i ^ pcg_hash(seed));
-    const uint32_t j = (uint32_t)(((unsigned long long)h * nv) >> 32);
+    const unsigned long long phase = ((unsigned long long)pcg_hash(seed) * nv) >> 32;  // < nv
+    const uint32_t j = (uint32_t)(((unsigned long long)i * nv + phase) / n_samples);  // < nv
     const uint32_t p = __ldg(&list[j]);
     const f3 l = onebounce(w, cam, f3{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]}, f3{nrm[3 * p], nrm[3 * p + 1], nrm[3 * p + 2]},
-                           f3{1.0f, 1.0f, 1.0f}, pcg_hash(h ^ 0xB5297A4Du));
+                           f3{1.0f, 1.0f, 1.0f}, pcg_hash(i ^ pcg_hash(seed ^ 0xB5297A4Du)));
+    const uint32_t per = n_samples / steps;
+    const size_t slot = (size_t)(i % steps) * per + i / steps;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) train_in[(size_t)i * 9 + k] = nrc_in[(size_t)p * 9 + k];
-    train_t[3 * (size_t)i] = l.x;
-    train_t[3 * (size_t)i + 1] = l.y;
-    train_t[3 * (size_t)i + 2] = l.z;
+    for (int k = 0; k < 9; ++k) train_in[slot * 9 + k] = nrc_in[(size_t)p * 9 + k];
+    train_t[3 * slot] = l.x;
+    train_t[3 * slot + 1] = l.y;
+    train_t[3 * slot + 2] = l.z;
 }
 
 __global__ void sharc_query_list_kernel(const uint4* __restrict__ res, const uint32_t* __restrict__ list,
@@ -535,10 +540,10 @@ int arc_gi_points_dev(arc_ctx* c, uint32_t width, uint32_t height, const uint32_
 }
 
 int arc_launch_train_samples_list(arc_ctx* c, const uint32_t* list, const unsigned long long* n_valid, const float* pos,
-                                  const float* nrm, const float* nrc_in, uint32_t seed, uint32_t n_samples,
+                                  const float* nrm, const float* nrc_in, uint32_t seed, uint32_t n_samples, uint32_t steps,
                                   float* train_in, float* train_t, uint32_t* gate) {
     arc::train_samples_list_kernel<<<(n_samples + 127u) / 128u, 128, 0, c->stream>>>(
-        c->world(), c->cam, list, n_valid, pos, nrm, nrc_in, seed, n_samples, train_in, train_t, gate);
+        c->world(), c->cam, list, n_valid, pos, nrm, nrc_in, seed, n_samples, steps, train_in, train_t, gate);
     return launch_check(c, "train_samples_list_kernel");
 }
 

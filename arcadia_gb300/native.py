@@ -80,6 +80,7 @@ SIGNATURES = {
     "arc_nrc_get_weights": [_vp, _vp],
     "arc_nrc_set_ema_decay": [_vp, _f32],
     "arc_nrc_set_infer_path": [_vp, C.c_int],
+    "arc_nrc_set_train_path": [_vp, C.c_int],
     "arc_nrc_get_ema_weights": [_vp, _vp],
     "arc_nrc_query_list_dev": [_vp, _vp, _vp, _u32, _vp, _vp, _vp],
     "arc_nrc_train_frame_dev": [_vp, _vp, _vp, _vp, _vp, _vp, _u32, _u32, _u32, _f32],

@@ -207,6 +207,8 @@ int arc_nrc_set_ema_decay(arc_ctx* ctx, float decay);
 /* Inference kernel: 1 = tcgen05 tensor cores with TMEM accumulators (default), 0 = the warp-level
  * mma.sync kernel (kept as the comparison point). */
 int arc_nrc_set_infer_path(arc_ctx* ctx, int path);
+/* Training kernel (gradients): 1 = tcgen05 (default), 0 = the mma.sync kernel. */
+int arc_nrc_set_train_path(arc_ctx* ctx, int path);
 int arc_nrc_get_ema_weights(arc_ctx* ctx, float* weights);
 /* out_rgb[i] = albedo[i] * network(inputs[i]) per channel; albedo may be NULL (network output only). */
 int arc_nrc_query_dev(arc_ctx* ctx, const float* inputs, const float* albedo, uint32_t n, float* out_rgb);
@@ -214,9 +216,10 @@ int arc_nrc_query_dev(arc_ctx* ctx, const float* inputs, const float* albedo, ui
 int arc_nrc_query_list_dev(arc_ctx* ctx, const uint32_t* list, const uint64_t* n_dev, uint32_t max_n,
                            const float* inputs, const float* albedo, float* out_rgb);
 /* One frame of online training with no host synchronisation (graph-capturable after the first call,
- * which allocates the batch): n_samples points drawn with replacement from list[0 .. *n_valid), their
- * demodulated 1-spp one-bounce targets, then `steps` Adam steps on equal slices of the batch. A frame
- * with *n_valid = 0 leaves the weights unchanged. */
+ * which allocates the batch): n_samples points stratified over list[0 .. *n_valid) with a seeded
+ * phase, their demodulated 1-spp one-bounce targets, then `steps` Adam steps on interleaved slices of
+ * the batch (each slice spans the frame; n_samples must be a multiple of steps). A frame with
+ * *n_valid = 0 leaves the weights unchanged. */
 int arc_nrc_train_frame_dev(arc_ctx* ctx, const uint32_t* list, const uint64_t* n_valid, const float* pos,
                             const float* normal, const float* nrc_in, uint32_t seed, uint32_t n_samples,
                             uint32_t steps, float lr);

@@ -284,3 +284,40 @@ def test_gpu_tcgen05_and_mma_sync_inference_agree(orc, tracer):
         assert tracer.stats().device_status == 0
     finally:
         assert lib().arc_nrc_set_infer_path(tracer.ctx, 1) == 0
+
+
+@pytest.mark.gpu
+def test_gpu_tcgen05_and_mma_sync_gradients_agree(orc, tracer):
+    """The tcgen05 training kernel (TMEM weight-gradient accumulators over several tiles per CTA, ragged
+    last tile) and the mma.sync kernel give the same loss-scaled gradient and loss."""
+    import ctypes
+    import torch
+    from arcadia_gb300.native import lib
+
+    x, t = _data(40001, 19)
+    w = _weights(20)
+    _set(tracer, w)
+    dx, dt = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
+    grads = []
+    try:
+        for path in (1, 0):
+            assert lib().arc_nrc_set_train_path(tracer.ctx, path) == 0
+            dg = torch.zeros(30400, dtype=torch.float32, device="cuda")
+            assert lib().arc_nrc_grad_dev(tracer.ctx, dx.data_ptr(), dt.data_ptr(), len(x), dg.data_ptr()) == 0
+            tracer.synchronize()
+            grads.append(dg.cpu().numpy().astype(np.float64))
+    finally:
+        assert lib().arc_nrc_set_train_path(tracer.ctx, 1) == 0
+    o = 0
+    for a, b in zip(DIMS[:-1], DIMS[1:]):
+        g1, g0 = grads[0][o:o + a * b], grads[1][o:o + a * b]
+        assert np.linalg.norm(g1 - g0) <= 2e-2 * np.linalg.norm(g0) + 1e-6, (a, b, np.linalg.norm(g1 - g0) / np.linalg.norm(g0))
+        o += a * b
+    # and the first 2048 samples against the FP64 oracle
+    dg = torch.zeros(30400, dtype=torch.float32, device="cuda")
+    assert lib().arc_nrc_grad_dev(tracer.ctx, dx.data_ptr(), dt.data_ptr(), 2048, dg.data_ptr()) == 0
+    tracer.synchronize()
+    g = dg.cpu().numpy().astype(np.float64) / LOSS_SCALE
+    _, ref = orc.nrc_grad(w, x[:2048], t[:2048])
+    assert np.linalg.norm(g - ref) <= 3e-2 * np.linalg.norm(ref)
+    assert tracer.stats().device_status == 0
