@@ -206,3 +206,52 @@ def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920
         "rel_mse_untrained_nrc": rel_mse(untrained, ref),
         "convergence": conv,
     }
+
+
+NRC_FLOPS_PER_QUERY = 2 * (216 * 64 + 4 * 64 * 64 + 3 * 64)  # 60,800
+
+
+def kernel_timing(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920, height=1080, reps=5):
+    """Device times (CUDA events, median of reps) of the NRC stages on one frame's GI hits, for the
+    tcgen05 kernels and the mma.sync kernels: inference over the hit list, one training frame with
+    1 Adam step, and the extra cost of each further step."""
+    import torch
+
+    scene = L.SCENES[scene_name]
+    cc = CacheComparison(tracer, scene, width, height)
+    cc.shared(5)
+    lib = cc.lib
+    cc._ck(lib.arc_nrc_init(tracer.ctx, 3), "arc_nrc_init")
+    n_px = width * height
+    n_hits = int(cc.n_valid.item())
+
+    def timed(fn):
+        ms = []
+        for _ in range(reps):
+            a = cc._event()
+            fn()
+            b = cc._event()
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        return statistics.median(ms)
+
+    def query():
+        cc._ck(lib.arc_nrc_query_list_dev(tracer.ctx, cc.list.data_ptr(), cc.n_valid.data_ptr(), n_px, cc.nin.data_ptr(),
+                                          cc.alb.data_ptr(), cc.nrc_out.data_ptr()), "query")
+
+    def train(steps):
+        return lambda: cc._ck(lib.arc_nrc_train_frame_dev(tracer.ctx, cc.list.data_ptr(), cc.n_valid.data_ptr(),
+                                                          cc.pos.data_ptr(), cc.nrm.data_ptr(), cc.nin.data_ptr(), 9,
+                                                          TRAIN_SAMPLES, steps, C.c_float(1e-3)), "train")
+
+    out = {"gi_hits": n_hits, "train_samples": TRAIN_SAMPLES, "flops_per_query": NRC_FLOPS_PER_QUERY}
+    for name, path in (("tcgen05", 1), ("mma_sync", 0)):
+        cc._ck(lib.arc_nrc_set_infer_path(tracer.ctx, path), "path")
+        cc._ck(lib.arc_nrc_set_train_path(tracer.ctx, path), "path")
+        q = timed(query)
+        t1, t8 = timed(train(1)), timed(train(8))
+        out[name] = {"query_ms": round(q, 4), "query_tflops": round(n_hits * NRC_FLOPS_PER_QUERY / (q * 1e-3) / 1e12, 1),
+                     "train_frame_1step_ms": round(t1, 4), "per_extra_step_ms": round((t8 - t1) / 7, 4)}
+    cc._ck(lib.arc_nrc_set_infer_path(tracer.ctx, 1), "path")
+    cc._ck(lib.arc_nrc_set_train_path(tracer.ctx, 1), "path")
+    return out

@@ -141,6 +141,14 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+def _peaks_all():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+
 def _profile_traffic(kernel: str):
     """DRAM bytes per launch of `kernel` from a committed ncu summary (profiles/*.txt), if any."""
     d = os.path.join(ROOT, "profiles")
@@ -352,9 +360,21 @@ def run_ours(args):
         from arcadia_gb300 import gi_cache
 
         t.set_launch_config(variant=cfg.variant)
-        nrc = gi_cache.run_comparison(t, SCENE, W_, H_, frames=args.nrc_frames)
+        nrc = gi_cache.run_comparison(t, SCENE, W_, H_, frames=args.nrc_frames, steps_per_frame=8)
         nrc["unit"] = "ms/frame"
-        nrc["network"] = "216-64x5-3 FP16 weights, FP32 accumulation, mma.sync m16n8k16"
+        nrc["network"] = ("216-64x5-3, FP16 weights and activations, FP32 accumulation; tcgen05.mma with TMEM "
+                          "accumulators for inference and training")
+        nrc["pareto"] = []
+        for steps in (1, 4, 16):
+            r = gi_cache.run_comparison(t, SCENE, W_, H_, frames=args.nrc_frames, steps_per_frame=steps, curve=())
+            nrc["pareto"].append({"train_steps_per_frame": steps, "nrc_ms_per_frame": r["nrc_ms_per_frame"],
+                                  "rel_mse_nrc": round(r["rel_mse_nrc"], 4)})
+        kt = gi_cache.kernel_timing(t, SCENE, W_, H_)
+        bf16_peak = _peaks_all().get("bf16_tflops")
+        kt["roofline_query"] = {"bound": "tensor", "achieved": kt["tcgen05"]["query_tflops"], "peak": bf16_peak,
+                                "unit": "TFLOP/s", "peak_kind": "measured cuBLAS bf16 burst",
+                                "frac": round(kt["tcgen05"]["query_tflops"] / bf16_peak, 4) if bf16_peak else None}
+        nrc["kernels"] = kt
 
     # many views over several worlds in one persistent launch replayed from a CUDA graph
     batched = None
