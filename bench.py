@@ -199,6 +199,21 @@ def bytes_per_pixel(world, cam, threads):
     return r[4] / r[1]
 
 
+def aggregate_ranks(total_ms: float, rays: float, device):
+    """Whole-job figures of a replicas run: the slowest rank's time and the rays of all ranks (no-op
+    without an initialised process group of more than one rank)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return total_ms, rays
+    tt = torch.tensor([total_ms, float(rays)], dtype=torch.float64, device=device)
+    mx = tt.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    dist.all_reduce(tt, op=dist.ReduceOp.SUM)
+    return float(mx[0]), float(tt[1])
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
@@ -298,12 +313,7 @@ def run_ours(args):
     ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = sum(ms)
     rays = args.steps * npx + int(n_gi.sum().item())
-    if ws > 1:
-        tt = torch.tensor([total_ms, float(rays)], dtype=torch.float64, device=dev)
-        mx = tt.clone()
-        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.SUM)
-        total_ms, rays = float(mx[0]), float(tt[1])
+    total_ms, rays = aggregate_ranks(total_ms, rays, dev)
     value = rays / (total_ms * 1e-3) / 1e6
     cfg = t.launch_config()
     if args.frame_only:
