@@ -162,18 +162,18 @@ __device__ __forceinline__ Surface trace_surface(const World& w, const arc_camer
 
 // One-bounce radiance estimator of the cache comparison (sun directional light + constant sky, Lambertian):
 // L = albedo * (c_sun max(n.l, 0) V(x, l) + L_sky [cosine-sampled ray from x escapes within 64 m]),
-// c_sun = sun_power * (1, 0.9, 0.75) * 0.55 as in sharc_shade_surface. One sample per call.
-__device__ __forceinline__ f3 onebounce(const World& w, const arc_camera_uniforms& cam, f3 pos, f3 n, f3 albedo,
-                                        uint32_t seed) {
+// c_sun = sun_power * (1, 0.9, 0.75) * 0.55 as in sharc_shade_surface. One sample per call. The two
+// terms are independent and traced separately by onebounce_sun / onebounce_sky.
+__device__ __forceinline__ f3 onebounce_sun(const World& w, const arc_camera_uniforms& cam, f3 pos, f3 n) {
     const f3 sun{cam.sun_dir_intensity[0], cam.sun_dir_intensity[1], cam.sun_dir_intensity[2]};
     const float sun_power = cam.sun_dir_intensity[3];
-    const f3 o = add3(pos, mul3s(n, 0.10f));
-    f3 l{0.0f, 0.0f, 0.0f};
     const float ndl = fmaxf(dot3(n, sun), 0.0f);
-    if (ndl > 0.001f && sun_power > 0.01f) {
-        const float k = ((sun_power * ndl) * shadow_vis(w, cam, o, sun, 32.0f)) * 0.55f;
-        l = f3{1.0f * k, 0.90f * k, 0.75f * k};
-    }
+    if (!(ndl > 0.001f && sun_power > 0.01f)) return f3{0.0f, 0.0f, 0.0f};
+    const float k = ((sun_power * ndl) * shadow_vis(w, cam, add3(pos, mul3s(n, 0.10f)), sun, 32.0f)) * 0.55f;
+    return f3{1.0f * k, 0.90f * k, 0.75f * k};
+}
+
+__device__ __forceinline__ f3 onebounce_sky(const World& w, const arc_camera_uniforms& cam, f3 pos, f3 n, uint32_t seed) {
     const uint32_t h1 = pcg_hash(seed), h2 = pcg_hash(h1 ^ 0x68E31DA4u);
     const float u1 = (float)(h1 >> 8) * (1.0f / 16777216.0f), u2 = (float)(h2 >> 8) * (1.0f / 16777216.0f);
     f3 t, b;
@@ -182,17 +182,18 @@ __device__ __forceinline__ f3 onebounce(const World& w, const arc_camera_uniform
     RayState s;
     HitInfo hh;
     StepResult r = kMiss;
-    if (ray_begin(s, cam, o, d, 0.0f, 64.0f, 2u, true)) {
+    if (ray_begin(s, cam, add3(pos, mul3s(n, 0.10f)), d, 0.0f, 64.0f, 2u, true)) {
         do {
             r = ray_advance(s, w, cam, hh);
         } while (r == kContinue);
     }
-    if (r != kHit) {
-        l.x += 0.30f;
-        l.y += 0.42f;
-        l.z += 0.60f;
-    }
-    return f3{albedo.x * l.x, albedo.y * l.y, albedo.z * l.z};
+    return r != kHit ? f3{0.30f, 0.42f, 0.60f} : f3{0.0f, 0.0f, 0.0f};
+}
+
+__device__ __forceinline__ f3 onebounce(const World& w, const arc_camera_uniforms& cam, f3 pos, f3 n, f3 albedo,
+                                        uint32_t seed) {
+    const f3 a = onebounce_sun(w, cam, pos, n), c = onebounce_sky(w, cam, pos, n, seed);
+    return f3{albedo.x * (a.x + c.x), albedo.y * (a.y + c.y), albedo.z * (a.z + c.z)};
 }
 
 __global__ void sharc_update_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, const SharcBuffers S,
@@ -418,24 +419,34 @@ __global__ void onebounce_kernel(const World w, const __grid_constant__ arc_came
 
 // NRC training samples from the compacted GI hit list, stratified: sample i takes list entry
 // floor((i + phase) n_valid / n_samples) (phase in [0, 1) from the seed), so the threads of a warp trace
-// neighbouring points (the list is in screen-tile order) and every point is covered evenly. Sample i is
-// stored at slot (i mod steps) * (n_samples / steps) + i / steps: each of the `steps` training slices
-// spans the whole frame. Target: the 1-spp estimator with albedo 1.
+// neighbouring points (the list is in screen-tile order) and every point is covered evenly. Two adjacent
+// lanes share a sample: the even lane traces the sun term, the odd lane the sky term, and a shuffle
+// sums them. Sample i is stored at slot (i mod steps) * (n_samples / steps) + i / steps, so each of the
+// `steps` training slices spans the whole frame. Target: the 1-spp estimator with albedo 1.
 __global__ void train_samples_list_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam,
                                           const uint32_t* __restrict__ list, const unsigned long long* __restrict__ n_valid,
                                           const float* __restrict__ pos, const float* __restrict__ nrm,
                                           const float* __restrict__ nrc_in, uint32_t seed, uint32_t n_samples, uint32_t steps,
                                           float* __restrict__ train_in, float* __restrict__ train_t, uint32_t* __restrict__ gate) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_samples) return;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = tid >> 1, part = tid & 1u;
     const unsigned long long nv = *n_valid;
-    if (i == 0) *gate = nv ? n_samples : 0u;
-    if (!nv) return;
-    const unsigned long long phase = ((unsigned long long)pcg_hash(seed) * nv) >> 32;  // < nv
-    const uint32_t j = (uint32_t)(((unsigned long long)i * nv + phase) / n_samples);  // < nv
-    const uint32_t p = __ldg(&list[j]);
-    const f3 l = onebounce(w, cam, f3{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]}, f3{nrm[3 * p], nrm[3 * p + 1], nrm[3 * p + 2]},
-                           f3{1.0f, 1.0f, 1.0f}, pcg_hash(i ^ pcg_hash(seed ^ 0xB5297A4Du)));
+    if (tid == 0) *gate = nv ? n_samples : 0u;
+    if (!nv) return;  // uniform over the grid
+    const bool valid = i < n_samples;
+    f3 l{0.0f, 0.0f, 0.0f};
+    uint32_t p = 0;
+    if (valid) {
+        const unsigned long long phase = ((unsigned long long)pcg_hash(seed) * nv) >> 32;  // < nv
+        const uint32_t j = (uint32_t)(((unsigned long long)i * nv + phase) / n_samples);  // < nv
+        p = __ldg(&list[j]);
+        const f3 x{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]}, n{nrm[3 * p], nrm[3 * p + 1], nrm[3 * p + 2]};
+        l = part ? onebounce_sky(w, cam, x, n, pcg_hash(i ^ pcg_hash(seed ^ 0xB5297A4Du))) : onebounce_sun(w, cam, x, n);
+    }
+    l.x += __shfl_xor_sync(0xFFFFFFFFu, l.x, 1);
+    l.y += __shfl_xor_sync(0xFFFFFFFFu, l.y, 1);
+    l.z += __shfl_xor_sync(0xFFFFFFFFu, l.z, 1);
+    if (!valid || part) return;
     const uint32_t per = n_samples / steps;
     const size_t slot = (size_t)(i % steps) * per + i / steps;
 #pragma unroll
@@ -542,7 +553,7 @@ int arc_gi_points_dev(arc_ctx* c, uint32_t width, uint32_t height, const uint32_
 int arc_launch_train_samples_list(arc_ctx* c, const uint32_t* list, const unsigned long long* n_valid, const float* pos,
                                   const float* nrm, const float* nrc_in, uint32_t seed, uint32_t n_samples, uint32_t steps,
                                   float* train_in, float* train_t, uint32_t* gate) {
-    arc::train_samples_list_kernel<<<(n_samples + 127u) / 128u, 128, 0, c->stream>>>(
+    arc::train_samples_list_kernel<<<(2u * n_samples + 127u) / 128u, 128, 0, c->stream>>>(
         c->world(), c->cam, list, n_valid, pos, nrm, nrc_in, seed, n_samples, steps, train_in, train_t, gate);
     return launch_check(c, "train_samples_list_kernel");
 }

@@ -375,7 +375,7 @@ def run_ours(args):
         nrc["network"] = ("216-64x5-3, FP16 weights and activations, FP32 accumulation; tcgen05.mma with TMEM "
                           "accumulators for inference and training")
         nrc["pareto"] = []
-        for steps in (1, 4, 16):
+        for steps in (1, 2, 4, 16):
             r = gi_cache.run_comparison(t, SCENE, W_, H_, frames=args.nrc_frames, steps_per_frame=steps, curve=())
             nrc["pareto"].append({"train_steps_per_frame": steps, "nrc_ms_per_frame": r["nrc_ms_per_frame"],
                                   "rel_mse_nrc": round(r["rel_mse_nrc"], 4)})
