@@ -124,8 +124,9 @@ struct Scene {
     uint32_t voxel(uint32_t x, uint32_t y, uint32_t z) const {
         const float hh = h[(size_t)z * wx + x];
         if (!((float)y < hh)) return ARC_MAT_AIR;
-        if (d.caves && cave(x, y, z) > d.cave_threshold) return ARC_MAT_AIR;
         const int32_t depth = (int32_t)hh - 1 - (int32_t)y;
+        if (d.caves && (d.cave_depth == 0u || depth < (int32_t)d.cave_depth) && cave(x, y, z) > d.cave_threshold)
+            return ARC_MAT_AIR;
         if (depth < 3) return 1u + (hash3((int32_t)x, (int32_t)y, (int32_t)z, d.seed ^ kSoilSeed) & 15u);
         return 1u + (hash3((int32_t)(x >> 4), (int32_t)(y >> 4), (int32_t)(z >> 4), d.seed ^ kRockSeed) & 15u);
     }
@@ -140,7 +141,9 @@ struct Scene {
         const float mx = hmax[lvl][bi], mn = hmin[lvl][bi];
         if ((float)y0 >= mx) return kAir;
         if (!((float)(y0 + size + 3u) <= mn)) return kNone;
-        if (d.caves) {
+        // every voxel of the region deeper than the cave band: no cave can reach it
+        const bool below_band = d.cave_depth && (mn - (float)(y0 + size)) >= (float)d.cave_depth;
+        if (d.caves && !below_band) {
             if (size > 16u) return kNone;
             float ca[8], cb[8];
             lattice_corners(x0, y0, z0, 5u, d.seed ^ kCaveSeedA, ca);
@@ -148,7 +151,9 @@ struct Scene {
             const float amax = *std::max_element(ca, ca + 8), amin = *std::min_element(ca, ca + 8);
             const float bmax = *std::max_element(cb, cb + 8), bmin = *std::min_element(cb, cb + 8);
             const float hi = (amax + bmax) * 0.5f, lo = (amin + bmin) * 0.5f;
-            if (lo > d.cave_threshold + 1e-5f) return kAir;
+            // all empty only if every voxel also lies inside the band
+            const bool in_band = !d.cave_depth || (mx - 1.0f - (float)y0) < (float)d.cave_depth;
+            if (lo > d.cave_threshold + 1e-5f && in_band) return kAir;
             if (!(hi <= d.cave_threshold - 1e-5f)) return kNone;
         }
         if (size > 16u) return kNone;

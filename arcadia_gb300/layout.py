@@ -215,6 +215,7 @@ class SceneParams:
     cave_threshold: float = 0.6
     height_lo: float = 0.25
     height_hi: float = 0.75
+    cave_depth: int = 0  # caves only within this many voxels below the surface (0 = at any depth)
 
 
 SCENES = {
@@ -226,6 +227,11 @@ SCENES = {
     "c2_1024_caves": SceneParams(grid=(4, 4, 4), seed=3, caves=True),
     # 1024^3 heightfield only
     "s1024": SceneParams(grid=(4, 4, 4), seed=4, caves=False),
+    # 512^3 with caves in a 40-voxel band under the surface (small case of the 4096^3 scene's structure)
+    "band512": SceneParams(grid=(2, 2, 2), seed=6, caves=True, cave_depth=40),
+    # 4096^3 = 16^3 chunks (6-level 64-tree), sparse: terrain between 20 % and 35 % of the height,
+    # caves in a 48-voxel band under the surface
+    "c5_4096": SceneParams(grid=(16, 16, 16), seed=5, caves=True, height_lo=0.20, height_hi=0.35, cave_depth=48),
 }
 
 

@@ -123,7 +123,7 @@ class Stats(C.Structure):
 
 class SceneDesc(C.Structure):
     _fields_ = [("grid", C.c_uint32 * 3), ("seed", C.c_uint32), ("caves", C.c_uint32), ("cave_threshold", C.c_float),
-                ("height_lo", C.c_float), ("height_hi", C.c_float)]
+                ("height_lo", C.c_float), ("height_hi", C.c_float), ("cave_depth", C.c_uint32)]
 
 
 def lib() -> C.CDLL:
@@ -162,7 +162,7 @@ def default_palette() -> np.ndarray:
 def build_world(scene: SceneParams, palette: np.ndarray | None = None, threads: int = 0):
     """Native world build: returns (roots, nodes, bricks, solid_voxels)."""
     d = SceneDesc((C.c_uint32 * 3)(*scene.grid), scene.seed, int(scene.caves), scene.cave_threshold, scene.height_lo,
-                  scene.height_hi)
+                  scene.height_hi, scene.cave_depth)
     h = C.c_void_p()
     pal = None if palette is None else np.ascontiguousarray(palette).view(MATERIAL_DTYPE)
     rc = lib().arc_world_build(C.byref(d), _p(pal), threads, C.byref(h))

@@ -27,6 +27,7 @@ typedef struct arc_scene_desc {
     float cave_threshold; /* voxel empty where cave noise > threshold */
     float height_lo;      /* terrain height range, fraction of world height */
     float height_hi;
+    uint32_t cave_depth;  /* caves only within this many voxels below the surface (0 = at any depth) */
 } arc_scene_desc;
 
 typedef struct arc_world_pools arc_world_pools;

@@ -38,6 +38,7 @@ typedef struct orc_scene_params {
     float cave_threshold;  /* empty where cave noise > threshold (0.6) */
     float height_lo;       /* terrain height range as a fraction of world height */
     float height_hi;
+    uint32_t cave_depth;   /* caves only within this many voxels below the surface (0 = at any depth) */
 } orc_scene_params;
 
 typedef struct orc_pools {

@@ -171,8 +171,10 @@ uint32_t orc_scene_voxel(const orc_scene_params* p, const float* hm, uint32_t x,
     uint32_t wx = p->grid[0] * 256u;
     float h = hm[(size_t)z * wx + x];
     if (!((float)y < h)) return ARC_MAT_AIR;
-    if (p->caves && cave_noise(x, y, z, p->seed) > p->cave_threshold) return ARC_MAT_AIR;
     int32_t depth = (int32_t)h - 1 - (int32_t)y;
+    if (p->caves && (p->cave_depth == 0u || depth < (int32_t)p->cave_depth) &&
+        cave_noise(x, y, z, p->seed) > p->cave_threshold)
+        return ARC_MAT_AIR;
     if (depth < 3) return 1u + (hash3u((int32_t)x, (int32_t)y, (int32_t)z, p->seed ^ 0xA511E9B3u) & 15u);
     return 1u + (hash3u((int32_t)(x >> 4), (int32_t)(y >> 4), (int32_t)(z >> 4), p->seed ^ 0x63D83595u) & 15u);
 }

@@ -43,6 +43,7 @@ class _Scene(C.Structure):
         ("cave_threshold", C.c_float),
         ("height_lo", C.c_float),
         ("height_hi", C.c_float),
+        ("cave_depth", C.c_uint32),
     ]
 
 
@@ -146,7 +147,7 @@ class World:
 
 def build_world(scene: SceneParams) -> World:
     s = _Scene((C.c_uint32 * 3)(*scene.grid), scene.seed, int(scene.caves), scene.cave_threshold, scene.height_lo,
-               scene.height_hi)
+               scene.height_hi, scene.cave_depth)
     p = _Pools()
     lib().orc_build_world(C.byref(s), C.byref(p))
     n_ch = p.n_chunks
@@ -342,7 +343,7 @@ def powi(x: np.ndarray, e: int) -> np.ndarray:
 def scene_volume(scene: SceneParams, chunk=(0, 0, 0)) -> np.ndarray:
     """Dense (z, y, x) u8 materials of one chunk of a synthetic scene (per-voxel evaluation)."""
     s = _Scene((C.c_uint32 * 3)(*scene.grid), scene.seed, int(scene.caves), scene.cave_threshold, scene.height_lo,
-               scene.height_hi)
+               scene.height_hi, scene.cave_depth)
     vol = np.zeros((256, 256, 256), np.uint8)
     lib().orc_test_scene_volume(C.byref(s), chunk[0], chunk[1], chunk[2], _p(vol))
     return vol

@@ -38,6 +38,15 @@ def test_native_builder_caves_small(orc, native_lib):
     _same(orc.build_world(s), native_lib.build_world(s, orc.default_palette()))
 
 
+def test_native_builder_cave_band(orc, native_lib):
+    """Caves limited to a band under the surface: the native builder's region classification (band
+    bounds from the per-block height minima and maxima) gives the oracle's per-voxel pools."""
+    s = SceneParams(grid=(2, 2, 2), seed=12, caves=True, cave_depth=24)
+    _same(orc.build_world(s), native_lib.build_world(s, orc.default_palette()))
+    full = orc.build_world(dataclasses.replace(s, cave_depth=0))
+    assert orc.build_world(s).solid_voxels > full.solid_voxels  # the band carves less
+
+
 @pytest.mark.slow
 def test_native_builder_caves_1024(orc, native_lib, world_cache):
     _same(world_cache("c2_1024_caves"), native_lib.build_world(SCENES["c2_1024_caves"], orc.default_palette()))
