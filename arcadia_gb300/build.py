@@ -25,6 +25,7 @@ CU_UNITS = {
     "arc_sharc.cu": CANONICAL,
     "arc_nrc.cu": [],
     "arc_noalloc.cu": CANONICAL,
+    "arc_edit.cu": CANONICAL,
 }
 CPP_UNITS = ["arc_world.cpp"]
 

@@ -217,6 +217,9 @@ int arc_destroy(arc_ctx* c) {
     cudaFree(c->d_nrc_w16_ema);
     cudaFree(c->d_nrc_wu_ema);
     cudaFree(c->d_nrc_wu);
+    cudaFree(c->d_edit);
+    cudaFree(c->d_edit_stage);
+    cudaFreeHost(c->h_edit_stage);
     cudaFree(c->d_nrc_batch);
     cudaFree(c->d_nrc_gate);
     cudaFree(c->d_nrc_loss);
@@ -309,6 +312,12 @@ int arc_upload_world(arc_ctx* c, const uint32_t grid[3], const uint32_t* roots, 
     ARC_CK(c, cudaMemcpyAsync(c->d_nodes, nodes, sizeof(arc_node64) * n_nodes, cudaMemcpyHostToDevice, c->stream));
     if (n_bricks) ARC_CK(c, cudaMemcpyAsync(c->d_bricks, bricks, sizeof(arc_brick64) * n_bricks, cudaMemcpyHostToDevice, c->stream));
     else ARC_CK(c, cudaMemsetAsync(c->d_bricks, 0, sizeof(arc_brick64), c->stream));
+    // headroom starts empty: growth from patches or in-place edits lands here
+    if (cap_nodes > n_nodes)
+        ARC_CK(c, cudaMemsetAsync(c->d_nodes + n_nodes, 0, sizeof(arc_node64) * (cap_nodes - n_nodes), c->stream));
+    const uint32_t nb0 = std::max<uint32_t>(n_bricks, 1u);
+    if (cap_bricks > nb0)
+        ARC_CK(c, cudaMemsetAsync(c->d_bricks + nb0, 0, sizeof(arc_brick64) * (cap_bricks - nb0), c->stream));
     ARC_CK(c, cudaMemcpyAsync(c->d_palette, palette, sizeof(arc_material) * 256, cudaMemcpyHostToDevice, c->stream));
     ARC_CK(c, cudaStreamSynchronize(c->stream));
     c->grid[0] = grid[0];
@@ -320,6 +329,7 @@ int arc_upload_world(arc_ctx* c, const uint32_t grid[3], const uint32_t* roots, 
     c->n_bricks = std::max<uint32_t>(n_bricks, 1u);
     c->cap_bricks = (uint32_t)cap_bricks;
     c->have_world = true;
+    if ((rc = arc_edit_reset(c))) return rc;
     return arc_ctx_sync_world_table(c);
 }
 
@@ -380,10 +390,11 @@ int arc_apply_patch(arc_ctx* c, uint32_t chunk, uint32_t new_root, uint32_t node
     if (n_nodes) ARC_CK(c, cudaMemcpyAsync(c->d_nodes + node_offset, nodes, sizeof(arc_node64) * n_nodes, cudaMemcpyHostToDevice, c->stream));
     if (n_bricks) ARC_CK(c, cudaMemcpyAsync(c->d_bricks + brick_offset, bricks, sizeof(arc_brick64) * n_bricks, cudaMemcpyHostToDevice, c->stream));
     ARC_CK(c, cudaMemcpyAsync(c->d_roots + chunk, &new_root, sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
+    if ((rc = arc_edit_raise_floor(c, node_offset + n_nodes, brick_offset + n_bricks))) return rc;
     ARC_CK(c, cudaStreamSynchronize(c->stream));
     c->n_nodes = node_limit;
     c->n_bricks = brick_limit;
-    return ARC_OK;
+    return arc_ctx_sync_world_table(c);
 }
 
 int arc_set_camera(arc_ctx* c, const arc_camera_uniforms* cam) {

@@ -80,6 +80,12 @@ struct arc_ctx {
     float nrc_ema_decay = 0.99f;
     float* d_nrc_loss = nullptr;
     uint32_t nrc_step = 0;
+    // in-place edits: device counters [next node, next brick, bricks rewritten, overflow] and staging
+    uint32_t* d_edit = nullptr;
+    void* d_edit_stage = nullptr;
+    void* h_edit_stage = nullptr;
+    size_t edit_stage_bytes = 0;
+
     // per-frame training batch of arc_nrc_train_frame_dev: inputs (9 floats) + targets (3), and the
     // gate word (the batch size, 0 when the frame has no GI hit) that the training kernels read
     float* d_nrc_batch = nullptr;
@@ -98,6 +104,9 @@ struct arc_ctx {
 
 int arc_ctx_check_ready(arc_ctx* c, bool need_cam);
 int arc_ctx_finish(arc_ctx* c);
+// edit allocator (arc_edit.cu): restart growth at the end of the uploaded pools / keep it above a patch
+int arc_edit_reset(arc_ctx* c);
+int arc_edit_raise_floor(arc_ctx* c, uint32_t node_floor, uint32_t brick_floor);
 // NRC training samples drawn from a compacted list of GI hit points (defined with the estimator in
 // arc_sharc.cu): stratified over list[0 .. *n_valid) with a seeded phase, demodulated 1-spp targets,
 // interleaved into `steps` slices (n_samples a multiple of steps); gate receives n_samples, or 0

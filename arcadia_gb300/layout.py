@@ -60,6 +60,13 @@ VIEW_DTYPE = np.dtype(
         ("gi_hits", "<u8"),
     ]
 )
+EDIT_CARVE = 0
+EDIT_RECOLOR = 1
+EDIT_DTYPE = np.dtype(
+    [("kind", "<u4"), ("material", "<u4"), ("brick", "<u4", (3,)), ("center", "<f4", (3,)), ("radius", "<f4"),
+     ("pad", "<u4")]
+)
+assert EDIT_DTYPE.itemsize == 40
 assert VIEW_DTYPE.itemsize == 536
 assert NODE_DTYPE.itemsize == 16 and BRICK_DTYPE.itemsize == 64 and MATERIAL_DTYPE.itemsize == 32
 assert CAMERA_DTYPE.itemsize == 480 and SHARC_SLOT_DTYPE.itemsize == 16

@@ -15,6 +15,7 @@ import numpy as np
 from .layout import (
     BRICK_DTYPE,
     CAMERA_DTYPE,
+    EDIT_DTYPE,
     HIT_DTYPE,
     MATERIAL_DTYPE,
     NODE_DTYPE,
@@ -75,6 +76,9 @@ SIGNATURES = {
     "arc_sharc_set_mode": [_vp, _u32],
     "arc_gi_points_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "arc_onebounce_dev": [_vp, _vp, _u32, _vp, _vp, _vp, _u32, _u32, _i32, _vp],
+    "arc_apply_edits": [_vp, _vp, _u32, _vp],
+    "arc_edit_stats": [_vp, _vp, _vp, _vp, _vp],
+    "arc_download_world": [_vp, _vp, _vp, _u32, _vp, _u32, _vp, _vp],
     "arc_nrc_init": [_vp, _u32],
     "arc_nrc_set_weights": [_vp, _vp],
     "arc_nrc_get_weights": [_vp, _vp],
@@ -229,6 +233,31 @@ class Tracer:
         self._check(lib().arc_apply_patch(self._ctx, chunk, new_root, node_offset, _p(nodes) if len(nodes) else None,
                                           len(nodes), brick_offset, _p(bricks) if len(bricks) else None, len(bricks)),
                     "arc_apply_patch")
+
+    def apply_edits(self, ops: np.ndarray, sync: bool = False):
+        """In-place edits (layout.EDIT_DTYPE records, applied in order) on the device; with sync=True
+        returns the running count of rewritten bricks."""
+        ops = np.ascontiguousarray(ops).view(EDIT_DTYPE)
+        out = C.c_uint32(0)
+        self._check(lib().arc_apply_edits(self._ctx, _p(ops) if len(ops) else None, len(ops),
+                                          C.byref(out) if sync else None), "arc_apply_edits")
+        return out.value if sync else None
+
+    def download_world(self):
+        """(roots, nodes, bricks) as the device holds them, up to the last written node and brick."""
+        nn, nb = C.c_uint32(0), C.c_uint32(0)
+        self._check(lib().arc_download_world(self._ctx, None, None, 0, None, 0, C.byref(nn), C.byref(nb)), "arc_download_world")
+        roots = np.zeros(len(self._roots), np.uint32)
+        nodes = np.zeros(nn.value, NODE_DTYPE)
+        bricks = np.zeros(nb.value, BRICK_DTYPE)
+        self._check(lib().arc_download_world(self._ctx, _p(roots), _p(nodes), nn.value, _p(bricks), nb.value, None, None),
+                    "arc_download_world")
+        return roots, nodes, bricks
+
+    def edit_stats(self):
+        v = [C.c_uint32(0) for _ in range(4)]
+        self._check(lib().arc_edit_stats(self._ctx, *[C.byref(x) for x in v]), "arc_edit_stats")
+        return {"next_node": v[0].value, "next_brick": v[1].value, "bricks_rewritten": v[2].value, "overflow": v[3].value}
 
     def set_camera(self, cam: np.ndarray):
         cam = np.ascontiguousarray(cam).view(CAMERA_DTYPE)

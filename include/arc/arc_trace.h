@@ -194,6 +194,26 @@ int arc_onebounce_dev(arc_ctx* ctx, const uint32_t* idx, uint32_t n, const float
 int arc_sharc_query_list_dev(arc_ctx* ctx, const uint32_t* list, const uint64_t* n_dev, uint32_t max_n,
                              const float* pos, const float* normal, float* out);
 
+/* In-place world edits on the device (replaces the CPU edit + GpuPatch round trip:
+ * ChunkTree64::carve_sphere_tracked, crates/arcadia-core/src/chunk_tree/edit/carve.rs:39-176,
+ * mutate_brick_in_place, edit/set.rs:244-569, then Renderer::apply_world_patches,
+ * crates/arcadia-render/src/renderer.rs:147-315). The records (include/arc/layout.h) apply in order to
+ * the world of arc_upload_world; the tree afterwards equals the reference's sequential edit node for
+ * node (only the pool positions of grown nodes and bricks differ), and the next trace on the context's
+ * stream sees it. Growth (uncollapsed nodes, new bricks) comes from the upload headroom. Carve radius
+ * in (0, 16] voxels. bricks_rewritten (optional) synchronises and receives the running count of
+ * rewritten bricks; an exhausted headroom is reported there as ARC_E_CAPACITY. */
+int arc_apply_edits(arc_ctx* ctx, const arc_edit_op* ops, uint32_t n_ops, uint32_t* bricks_rewritten);
+/* Copies the device pools back (pool dumps, checks after edits): the roots, and the first
+ * min(cap, used) nodes and bricks, where used covers every node and brick the uploads, patches and
+ * edits have written; n_nodes / n_bricks receive `used`. Any output pointer may be NULL. No reference
+ * counterpart (the reference keeps the CPU copy authoritative). */
+int arc_download_world(arc_ctx* ctx, uint32_t* roots, arc_node64* nodes, uint32_t node_cap, arc_brick64* bricks,
+                       uint32_t brick_cap, uint32_t* n_nodes, uint32_t* n_bricks);
+/* Edit allocator state: next free node and brick, bricks rewritten since the upload, overflow flags. */
+int arc_edit_stats(arc_ctx* ctx, uint32_t* next_node, uint32_t* next_brick, uint32_t* bricks_rewritten,
+                   uint32_t* overflow);
+
 /* Neural radiance cache (no reference counterpart: it stands in for query_sharc at secondary hits).
  * 9 inputs per query: position normalised to [0,1]^3, normal, view direction; 3 outputs (RGB).
  * 30,400 FP32 master weights: W1[64][216], W2..W5[64][64], W6[3][64], row-major, no biases. */

@@ -144,6 +144,24 @@ ARC_STATIC_ASSERT(sizeof(arc_sharc_slot) == 16, "SharcResolvedSlot is 16 B");
 ARC_STATIC_ASSERT(sizeof(arc_ray) == 24, "ray is 24 B");
 ARC_STATIC_ASSERT(sizeof(arc_hit_record) == 20, "hit record is 20 B");
 
+/* One in-place world edit. The reference has no edit record: its callers invoke
+ * ChunkTree64::carve_sphere_tracked (crates/arcadia-core/src/chunk_tree/edit/carve.rs:39-176) and
+ * mutate_brick_in_place (edit/set.rs:244-319) directly; this record names those two operations.
+ *   ARC_EDIT_CARVE    clear every solid voxel whose centre lies within `radius` of `center` (world
+ *                     voxel units; voxel v spans [v, v + 1)); no scorch rim
+ *   ARC_EDIT_RECOLOR  set every solid voxel of world brick `brick` (voxel coordinates >> 2) to `material` */
+#define ARC_EDIT_CARVE 0u
+#define ARC_EDIT_RECOLOR 1u
+typedef struct arc_edit_op {
+    uint32_t kind;
+    uint32_t material;
+    uint32_t brick[3];
+    float center[3];
+    float radius;
+    uint32_t pad;
+} arc_edit_op;
+ARC_STATIC_ASSERT(sizeof(arc_edit_op) == 40, "edit record is 40 B");
+
 #ifdef __cplusplus
 }
 #endif

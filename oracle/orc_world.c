@@ -69,6 +69,9 @@ static uint32_t pack_lod_payload(const arc_material* m, uint32_t mat) {
     return (mat << 24) | (b << 16) | (g << 8) | r;
 }
 
+uint32_t orc_pack_lod_payload(const arc_material* m, uint32_t mat) { return pack_lod_payload(m, mat); }
+int orc_mat_is_emissive(const arc_material* m) { return mat_is_emissive(m); }
+
 /* pack_rgb_and_mat (builder.rs:72-78). */
 static uint32_t pack_rgb_and_mat(float r, float g, float b, uint32_t mat) {
     uint32_t ru = orc_f2u(orc_clamp(r, 0.0f, 1.0f) * 255.0f);
@@ -76,6 +79,8 @@ static uint32_t pack_rgb_and_mat(float r, float g, float b, uint32_t mat) {
     uint32_t bu = orc_f2u(orc_clamp(b, 0.0f, 1.0f) * 255.0f);
     return (mat << 24) | (bu << 16) | (gu << 8) | ru;
 }
+
+uint32_t orc_pack_rgb_and_mat(float r, float g, float b, uint32_t mat) { return pack_rgb_and_mat(r, g, b, mat); }
 
 /* ------------------------------------------------------------------------------------------ */
 /* Synthetic scene: seeded 2D value-noise heightfield + 3D value-noise caves.                  */

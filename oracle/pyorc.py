@@ -14,6 +14,7 @@ import numpy as np
 from arcadia_gb300.layout import (
     BRICK_DTYPE,
     CAMERA_DTYPE,
+    EDIT_DTYPE,
     HIT_DTYPE,
     MATERIAL_DTYPE,
     NODE_DTYPE,
@@ -114,6 +115,10 @@ def lib():
         _lib.orc_nrc_grad.argtypes = [vp, vp, vp, u32, vp]
         _lib.orc_nrc_grad.restype = C.c_double
         _lib.orc_nrc_adam.argtypes = [vp, vp, vp, vp, u32, u32, f32]
+        _lib.orc_apply_edits.argtypes = [vp, vp, vp, C.POINTER(u32), u32, vp, C.POINTER(u32), u32, vp, vp, u32]
+        _lib.orc_pool_chunk_volume.argtypes = [vp, vp, vp, vp, u32, u32, u32, vp]
+        _lib.orc_tree_compare.argtypes = [u32, vp, vp, u32, vp, vp, C.c_int]
+        _lib.orc_tree_compare.restype = C.c_uint64
     return _lib
 
 
@@ -159,6 +164,41 @@ def build_world(scene: SceneParams) -> World:
     w = World(scene.grid, roots, nodes, bricks)
     w.solid_voxels = solid
     return w
+
+
+def apply_edits(world: World, ops: np.ndarray, node_headroom: int = 1 << 20, brick_headroom: int = 1 << 18) -> World:
+    """A copy of `world` with the edit records `ops` (layout.EDIT_DTYPE) applied in order by the
+    sequential restatement of the reference edit path (orc_edit.c)."""
+    ops = np.ascontiguousarray(ops).view(EDIT_DTYPE)
+    nodes = np.zeros(len(world.nodes) + node_headroom, NODE_DTYPE)
+    nodes[: len(world.nodes)] = world.nodes
+    bricks = np.zeros(len(world.bricks) + brick_headroom, BRICK_DTYPE)
+    bricks[: len(world.bricks)] = world.bricks
+    nn, nb = C.c_uint32(len(world.nodes)), C.c_uint32(len(world.bricks))
+    grid = np.array(world.grid, np.uint32)
+    rc = lib().orc_apply_edits(_p(grid), _p(world.roots), _p(nodes), C.byref(nn), len(nodes), _p(bricks), C.byref(nb),
+                               len(bricks), _p(world.palette), _p(ops), len(ops))
+    if rc:
+        raise RuntimeError("orc_apply_edits: pool headroom exhausted")
+    return World(world.grid, world.roots.copy(), nodes[: nn.value].copy(), bricks[: nb.value].copy(), world.palette)
+
+
+def chunk_volume(grid, roots, nodes, bricks, chunk) -> np.ndarray:
+    """Dense (z, y, x) u8 materials of one chunk of a flattened pool, by point descent."""
+    vol = np.zeros((256, 256, 256), np.uint8)
+    g = np.array(grid, np.uint32)
+    lib().orc_pool_chunk_volume(_p(g), _p(np.ascontiguousarray(roots, np.uint32)), _p(np.ascontiguousarray(nodes)),
+                                _p(np.ascontiguousarray(bricks)), chunk[0], chunk[1], chunk[2], _p(vol))
+    return vol
+
+
+def tree_compare(root_a, nodes_a, bricks_a, root_b, nodes_b, bricks_b, leaf_form: bool = True) -> int:
+    """0 when two chunk trees are equal node by node in child order (masks, flags, lod payloads, voxel
+    materials under leaf masks), wherever their nodes sit; else the position of the first difference.
+    leaf_form=False lets a brick leaf equal a uniform leaf with the same voxels."""
+    return int(lib().orc_tree_compare(int(root_a), _p(np.ascontiguousarray(nodes_a)), _p(np.ascontiguousarray(bricks_a)),
+                                      int(root_b), _p(np.ascontiguousarray(nodes_b)), _p(np.ascontiguousarray(bricks_b)),
+                                      1 if leaf_form else 0))
 
 
 def build_chunk_dense(vol: np.ndarray, palette: np.ndarray | None = None):
