@@ -389,6 +389,82 @@ __global__ void gi_points_kernel(const World w, const __grid_constant__ arc_came
     if (ok && list) list[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)k;
 }
 
+// GI hit points from the frame kernel's GI hit records, without tracing again: the point is the centre
+// of the entry face of the hit cell (LOD cells included), the normal that face's, the albedo the hit
+// material's, and the view direction points from the point back to the GI ray's origin (the primary
+// hit + 0.10 m along its normal, from the G-buffer). Outputs as gi_points_kernel, list included.
+__global__ void gi_points_hits_kernel(const __grid_constant__ arc_camera_uniforms cam, const uint32_t* __restrict__ gdm,
+                                      const uint32_t* __restrict__ gnm, const arc_hit_record* __restrict__ gi_hits,
+                                      uint32_t W, uint32_t H, float* __restrict__ pos, float* __restrict__ nrm,
+                                      float* __restrict__ alb, float* __restrict__ nrc_in, uint32_t* __restrict__ valid,
+                                      unsigned long long* __restrict__ n_valid, uint32_t* __restrict__ list) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const size_t k = (size_t)y * W + x;
+    const arc_hit_record h = gi_hits[k];
+    const float hit_dist = __uint_as_float(gdm[2 * k]);
+    uint32_t ok = (h.flags & ARC_HIT_FLAG_HIT) && h.face < 6u && hit_dist < 1e4f ? 1u : 0u;
+    if (ok) {
+        const int32_t span_i = 1 << (2u * ((h.flags >> 1) & 7u));  // LOD cell of the hit (1 voxel at level 0)
+        const float span = (float)span_i;
+        const float c0 = (float)(h.voxel[0] & ~(span_i - 1)), c1 = (float)(h.voxel[1] & ~(span_i - 1)),
+                    c2 = (float)(h.voxel[2] & ~(span_i - 1));
+        const float axis_sign = (h.face & 1u) ? -1.0f : 1.0f;  // +X, -X, +Y, -Y, +Z, -Z
+        const uint32_t axis = h.face >> 1;
+        f3 n{0.0f, 0.0f, 0.0f};
+        f3 p{c0 + 0.5f * span, c1 + 0.5f * span, c2 + 0.5f * span};
+        if (axis == 0) {
+            n.x = axis_sign;
+            p.x = c0 + (axis_sign > 0.0f ? span : 0.0f);
+        } else if (axis == 1) {
+            n.y = axis_sign;
+            p.y = c1 + (axis_sign > 0.0f ? span : 0.0f);
+        } else {
+            n.z = axis_sign;
+            p.z = c2 + (axis_sign > 0.0f ? span : 0.0f);
+        }
+        p = mul3s(p, ARC_VOXEL_SIZE);
+        const f3 eye{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]};
+        const f3 hp = add3(eye, mul3s(camera_dir(cam, x, y, W, H), hit_dist));
+        float ox, oy;
+        unpack2x16snorm(gnm[2 * k], &ox, &oy);
+        const f3 o = add3(hp, mul3s(oct_decode(ox, oy), 0.10f));
+        const f3 v = sub3(o, p);
+        const float len = length3(v);
+        const f3 view = len > 0.0f ? mul3s(v, __fdiv_rn(1.0f, len)) : n;
+        const f3 a = cmp_albedo(h.mat);
+        pos[3 * k] = p.x;
+        pos[3 * k + 1] = p.y;
+        pos[3 * k + 2] = p.z;
+        nrm[3 * k] = n.x;
+        nrm[3 * k + 1] = n.y;
+        nrm[3 * k + 2] = n.z;
+        alb[3 * k] = a.x;
+        alb[3 * k + 1] = a.y;
+        alb[3 * k + 2] = a.z;
+        const float ex = (float)cam.world_grid_dims[0] * 16.0f, ey = (float)cam.world_grid_dims[1] * 16.0f,
+                    ez = (float)cam.world_grid_dims[2] * 16.0f;
+        float* q = nrc_in + 9 * k;
+        q[0] = __fdiv_rn(p.x, ex);
+        q[1] = __fdiv_rn(p.y, ey);
+        q[2] = __fdiv_rn(p.z, ez);
+        q[3] = n.x;
+        q[4] = n.y;
+        q[5] = n.z;
+        q[6] = view.x;
+        q[7] = view.y;
+        q[8] = view.z;
+    }
+    valid[k] = ok;
+    const uint32_t act = __activemask();
+    const uint32_t m = __ballot_sync(act, ok != 0u);
+    const uint32_t lane = (threadIdx.x + threadIdx.y * blockDim.x) & 31u;
+    unsigned long long base = 0ull;
+    if (m && lane == (uint32_t)(__ffs(m) - 1)) base = atomicAdd(n_valid, (unsigned long long)__popc(m));
+    if (m) base = __shfl_sync(act, base, __ffs(m) - 1);
+    if (ok && list) list[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)k;
+}
+
 __global__ void onebounce_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, const uint32_t* __restrict__ idx,
                                  uint32_t n, const float* __restrict__ pos, const float* __restrict__ nrm,
                                  const float* __restrict__ alb, uint32_t spp, uint32_t seed, uint32_t accumulate,
@@ -534,6 +610,23 @@ int arc_sharc_set_mode(arc_ctx* c, uint32_t mode) {
     if (!c || mode > 1u) return ARC_E_INVALID_ARG;
     c->sharc_mode = mode;
     return ARC_OK;
+}
+
+int arc_gi_points_from_hits_dev(arc_ctx* c, uint32_t width, uint32_t height, const uint32_t* gdm, const uint32_t* gnm,
+                                const arc_hit_record* gi_hits, float* pos, float* nrm, float* albedo, float* nrc_in,
+                                uint32_t* valid, uint64_t* n_valid, uint32_t* list) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if (!gdm || !gnm || !gi_hits || !pos || !nrm || !albedo || !nrc_in || !valid || !n_valid)
+        return sharc_err(c, ARC_E_INVALID_ARG, "null buffer");
+    if ((c->cam.world_grid_dims[3] & 0xFFFFu) != width || (c->cam.world_grid_dims[3] >> 16) != height)
+        return sharc_err(c, ARC_E_INVALID_ARG, "frame size differs from camera world_grid_dims.w");
+    cudaMemsetAsync(n_valid, 0, sizeof(uint64_t), c->stream);
+    dim3 block(8, 8), grid((width + 7u) / 8u, (height + 7u) / 8u);
+    arc::gi_points_hits_kernel<<<grid, block, 0, c->stream>>>(c->cam, gdm, gnm, gi_hits, width, height, pos, nrm, albedo,
+                                                              nrc_in, valid, reinterpret_cast<unsigned long long*>(n_valid),
+                                                              list);
+    return launch_check(c, "gi_points_hits_kernel");
 }
 
 int arc_gi_points_dev(arc_ctx* c, uint32_t width, uint32_t height, const uint32_t* gdm, const uint32_t* gnm, float* pos,

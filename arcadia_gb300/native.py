@@ -74,6 +74,7 @@ SIGNATURES = {
     "arc_sharc_upload": [_vp, _vp, _vp, _vp],
     "arc_sharc_deposit_dev": [_vp, _vp, _vp, _vp, _vp, _u32],
     "arc_sharc_set_mode": [_vp, _u32],
+    "arc_gi_points_from_hits_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "arc_gi_points_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "arc_onebounce_dev": [_vp, _vp, _u32, _vp, _vp, _vp, _u32, _u32, _i32, _vp],
     "arc_apply_edits": [_vp, _vp, _u32, _vp],

@@ -58,6 +58,10 @@ def _args():
     p.add_argument("--no-batched", action="store_true", help="skip the multi-view batch section")
     p.add_argument("--no-nrc", action="store_true", help="skip the radiance-cache comparison section")
     p.add_argument("--nrc-frames", type=int, default=300)
+    p.add_argument("--no-c5", action="store_true", help="skip the 4096^3 edit + trace + NRC pipeline section")
+    p.add_argument("--c5-frames", type=int, default=300)
+    p.add_argument("--c5-width", type=int, default=3840)
+    p.add_argument("--c5-height", type=int, default=2160)
     return p.parse_args()
 
 
@@ -410,6 +414,25 @@ def run_ours(args):
                    "launch": {"block_threads": best.block_threads, "reg_blocks": best.reg_blocks,
                               "refill_threshold": best.refill_threshold, "tile": [best.tile_w, best.tile_h]}}
     t.close()
+
+    # full pipeline on the 4096^3 sparse world: in-place edits (1 % of the leaf bricks per frame), 4K
+    # primary + GI, NRC training + query at the secondary hits, along a 300-frame camera path
+    c5 = None
+    if not args.no_c5:
+        from arcadia_gb300.pipeline import FullPipeline
+
+        sc5 = L.SCENES["c5_4096"]
+        r5, n5, b5, _ = native.build_world(sc5)
+        t5 = native.Tracer(local)
+        t5.upload_world(sc5.grid, r5, n5, b5, pal, node_headroom=1 << 25, brick_headroom=1 << 22)
+        p5 = FullPipeline(t5, sc5, args.c5_width, args.c5_height, n_bricks=len(b5), n_frames=args.c5_frames)
+        c5 = p5.run(warmup=3)
+        c5.update({"workload": "4096^3 sparse world (16^3 chunks: heightfield at 20-35 % of the height, caves in a "
+                               "48-voxel band), edits + primary + GI + NRC per frame, camera path",
+                   "scene": "c5_4096", "world_nodes": len(n5), "world_bricks": len(b5),
+                   "quality": "high_quality preset (LOD on)", "unit_trace": "Mrays/s"})
+        t5.close()
+        del r5, n5, b5
     clk = clocks.stop() if clocks else None
 
     if rank != 0:
@@ -451,6 +474,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "nrc": nrc,
         "batched": batched,
+        "c5": c5,
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)

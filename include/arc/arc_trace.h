@@ -184,6 +184,13 @@ int arc_gi_points_dev(arc_ctx* ctx, uint32_t width, uint32_t height, const uint3
                       uint32_t* valid, uint64_t* n_valid, uint32_t* list);
 /* list (optional, width*height entries): the pixel indices of the points with valid = 1, compacted to
  * list[0 .. *n_valid) in no particular order. */
+/* arc_gi_points_dev from the GI hit records of arc_trace_frame_dev instead of tracing the GI rays again:
+ * the point is the centre of the hit cell's entry face, the normal that face's, the view direction
+ * from the point to the GI ray's origin (primary hit + 0.10 m along its normal). */
+int arc_gi_points_from_hits_dev(arc_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* gbuf_depth_mat,
+                                const uint32_t* gbuf_norm_motion, const arc_hit_record* gi_hits, float* pos,
+                                float* normal, float* albedo, float* nrc_in, uint32_t* valid, uint64_t* n_valid,
+                                uint32_t* list);
 /* Mean of spp one-bounce samples at points idx[i] (idx may be NULL = identity); accumulate adds. */
 int arc_onebounce_dev(arc_ctx* ctx, const uint32_t* idx, uint32_t n, const float* pos, const float* normal,
                       const float* albedo, uint32_t spp, uint32_t seed, int accumulate, float* out);

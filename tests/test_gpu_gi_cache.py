@@ -120,3 +120,49 @@ def test_train_frame_updates_weights_and_skips_empty_frames(native_lib):
         assert L_.arc_nrc_train_frame_dev(t.ctx, *bad) != 0  # steps = 0
     finally:
         t.close()
+
+
+def test_gi_points_from_hit_records(native_lib):
+    """Points from the frame kernel's GI hit records: the same hit pixels as re-tracing the GI rays, the
+    same normals and albedos, positions on the hit cell's entry face."""
+    import numpy as np
+    import torch
+    from arcadia_gb300 import gi_cache, layout as L
+    from arcadia_gb300.native import lib
+
+    scene = L.SCENES["c1_256"]
+    roots, nodes, bricks, _ = native_lib.build_world(scene)
+    t = native_lib.Tracer(0)
+    try:
+        t.upload_world(scene.grid, roots, nodes, bricks, native_lib.default_palette())
+        w, h = 320, 180
+        cc = gi_cache.CacheComparison(t, scene, w, h)
+        t.set_camera(cc.camera(4))
+        hits = torch.zeros(w * h * 5, dtype=torch.int32, device="cuda")
+        gi = torch.zeros(w * h * 5, dtype=torch.int32, device="cuda")
+        t.trace_frame_dev(w, h, cc.gdm.data_ptr(), cc.gnm.data_ptr(), cc.gaa.data_ptr(), hits.data_ptr(), gi.data_ptr())
+        assert lib().arc_gi_points_dev(t.ctx, w, h, cc.gdm.data_ptr(), cc.gnm.data_ptr(), cc.pos.data_ptr(), cc.nrm.data_ptr(),
+                                       cc.alb.data_ptr(), cc.nin.data_ptr(), cc.valid.data_ptr(), cc.n_valid.data_ptr(),
+                                       cc.list.data_ptr()) == 0
+        t.synchronize()
+        ref = [x.cpu().numpy().copy() for x in (cc.pos, cc.nrm, cc.alb, cc.valid)]
+        assert lib().arc_gi_points_from_hits_dev(t.ctx, w, h, cc.gdm.data_ptr(), cc.gnm.data_ptr(), gi.data_ptr(),
+                                                 cc.pos.data_ptr(), cc.nrm.data_ptr(), cc.alb.data_ptr(), cc.nin.data_ptr(),
+                                                 cc.valid.data_ptr(), cc.n_valid.data_ptr(), cc.list.data_ptr()) == 0
+        t.synchronize()
+        pos, nrm, alb, valid = [x.cpu().numpy() for x in (cc.pos, cc.nrm, cc.alb, cc.valid)]
+        v = ref[3].astype(bool)
+        assert v.sum() > 1000 and np.array_equal(valid.astype(bool), v)
+        assert int(cc.n_valid.item()) == int(v.sum())
+        np.testing.assert_array_equal(nrm[v], ref[1][v])
+        np.testing.assert_array_equal(alb[v], ref[2][v])
+        span = 1 << (2 * ((gi.cpu().numpy().view(L.HIT_DTYPE)["flags"][v] >> 1) & 7))
+        # on the entry face: within half a cell of its centre per axis; a GI ray that starts inside a
+        # solid voxel hits at its own origin, off the face (a few points)
+        d = np.abs(pos[v] - ref[0][v]).max(1)
+        assert np.mean(d <= 0.0625 * span * 0.5 + 1e-4) >= 0.99, np.mean(d <= 0.0625 * span * 0.5 + 1e-4)
+        assert np.all(d <= 0.0625 * span * 2.0), d.max()
+        nin = cc.nin.cpu().numpy()[v]
+        np.testing.assert_allclose(np.linalg.norm(nin[:, 6:9], axis=1), 1.0, atol=1e-5)
+    finally:
+        t.close()
