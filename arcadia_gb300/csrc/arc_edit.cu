@@ -5,17 +5,23 @@
 // edit/set.rs:244-569) and ships the changed node and brick ranges to the GPU as patches
 // (crates/arcadia-world/src/world_map.rs:319-383). Here the tree is updated where it lives.
 //
-// One CTA per touched chunk applies that chunk's edits in order. For each edit:
-//   candidates   the bricks the edit changes (sphere-brick test, brick solid mask, voxel-centre
-//                distance, tree.rs:109-166 semantics) with their 64-bit entry masks
-//   uncollapse   top-down, root / L1 / L2: a collapsed ancestor of a candidate is expanded into full
-//                uniform children (uncollapse_if_needed, set.rs:404-428); one thread per node
-//   leaves       one thread per candidate applies the entries to its leaf in ascending voxel order
-//                (apply_voxel_entries_to_leaf, set.rs:431-515), allocating a brick when a uniform leaf
-//                turns mixed, and refreshes the leaf's LOD payload (compute_leaf_lod, set.rs:573-618)
-//   bottom-up    L2, L1, root: each touched node drops its emptied children, compacting its child slice
-//                as remove_child does (set.rs:322-354), and refreshes its LOD payload
-//                (refresh_internal_lod, set.rs:518-569); one thread per node
+// Three launches per batch:
+//   root uncollapse  one thread per touched chunk: a collapsed root (the whole chunk one uniform solid)
+//                    expands when an edit rewrites a voxel of it (uncollapse_if_needed, set.rs:404-428)
+//   regions          one CTA per (chunk, 64^3 region) with edits: the CTA owns the region's L1 node and
+//                    everything below it and applies the region's edits in order. For each edit:
+//       candidates   the bricks it changes (sphere-brick test, brick solid mask, voxel-centre distance,
+//                    tree.rs:109-166 semantics) with their 64-bit entry masks
+//       uncollapse   the L1 node, then the L2 nodes on candidate paths (one thread per node)
+//       leaves       one thread per candidate applies the entries in ascending voxel order
+//                    (apply_voxel_entries_to_leaf, set.rs:431-515), allocating a brick when a uniform
+//                    leaf turns mixed, and refreshes the leaf's LOD (compute_leaf_lod, set.rs:573-618)
+//       bottom-up    touched L2 nodes, then the L1 node: drop emptied children, compacting the child
+//                    slice as remove_child does (set.rs:322-354), and refresh the LOD payload
+//                    (refresh_internal_lod, set.rs:518-569)
+//   root refresh     one thread per chunk with rewritten leaves: the same for its root
+// Edits in different regions touch disjoint nodes below the root, so regions run in parallel; the
+// root's child slice stays put until the root pass.
 // The result equals the reference's sequential edit node for node (masks, flags, LOD payloads, brick
 // materials); only the pool positions of grown nodes and bricks differ. Growth comes from the pools'
 // upload headroom through atomic counters; exhausted headroom skips the growth and raises an overflow
@@ -275,54 +281,68 @@ __device__ void compact_refresh(const Params& P, uint32_t idx) {
     P.nodes[idx] = n;
 }
 
-__global__ void __launch_bounds__(kThreads) edit_chunks_kernel(const Params P, const uint32_t grid_x, const uint32_t grid_y) {
-    __shared__ uint32_t s_cand[kMaxCand];        // bx | by << 6 | bz << 12
+// Work item: one 64^3 L1 region of one chunk with the edits touching it (op_idx[op_start[i] ..
+// op_start[i + 1]), in edit order). The CTA owns the region's L1 node and everything below it.
+__global__ void __launch_bounds__(kThreads) edit_regions_kernel(const Params P, const uint32_t* __restrict__ item_chunk,
+                                                               const uint32_t* __restrict__ item_region,
+                                                               const uint32_t* __restrict__ item_slot,
+                                                               uint32_t* __restrict__ chunk_touched, uint32_t grid_x,
+                                                               uint32_t grid_y) {
+    __shared__ uint32_t s_cand[kMaxCand];        // bx | by << 6 | bz << 12 (chunk-local bricks)
     __shared__ unsigned long long s_entries[kMaxCand];
-    __shared__ uint32_t s_l1[2], s_l2[128];      // touched / claimed bitmaps
-    __shared__ uint32_t s_u1[2], s_u2[128];
-    __shared__ uint32_t s_n_cand, s_root_touched;
+    __shared__ uint32_t s_l2[2], s_u2[2];        // touched / claimed L2 nodes of the region (64 bits)
+    __shared__ uint32_t s_n_cand, s_touched;
     const uint32_t tid = threadIdx.x;
-    const uint32_t chunk = P.chunk_list[blockIdx.x];
+    const uint32_t chunk = item_chunk[blockIdx.x], b0 = item_region[blockIdx.x];
     const uint32_t root = P.roots[chunk];
-    if (root == ARC_EMPTY_CHUNK) return;  // nothing to edit (uniform over the CTA)
+    if (root == ARC_EMPTY_CHUNK) return;  // uniform over the CTA
+    {
+        const uint4 rn = P.nodes[root];
+        if (nleaf(rn) || !(nmask(rn) & (1ull << b0))) return;  // empty region (or growth refused): nothing to edit
+    }
+    const uint32_t l1 = nslot(P.nodes[root], b0);  // the root's slice is stable until the root pass
+    const uint32_t r0x = (b0 & 3u) * 16u, r0y = ((b0 >> 2) & 3u) * 16u, r0z = (b0 >> 4) * 16u;  // region bricks
     const float ox = (float)((chunk % grid_x) * 256u), oy = (float)(((chunk / grid_x) % grid_y) * 256u),
                 oz = (float)((chunk / (grid_x * grid_y)) * 256u);
+    if (tid == 0) s_touched = 0u;
     for (uint32_t e = P.op_start[blockIdx.x]; e < P.op_start[blockIdx.x + 1]; ++e) {
         const arc_edit_op op = P.ops[P.op_idx[e]];
-        if (tid == 0) {
-            s_n_cand = 0;
-            s_root_touched = 0;
-        }
-        for (uint32_t i = tid; i < 128; i += kThreads) s_l2[i] = s_u2[i] = 0u;
-        if (tid < 2) s_l1[tid] = s_u1[tid] = 0u;
+        if (tid == 0) s_n_cand = 0;
+        if (tid < 2) s_l2[tid] = s_u2[tid] = 0u;
         __syncthreads();
-        if (nmask(P.nodes[root]) == 0ull) break;  // empty chunk: nothing to carve or recolour (uniform)
-        // ---- candidates
+        if (nmask(P.nodes[l1]) == 0ull) break;  // region emptied by an earlier edit (uniform)
+        // ---- candidates inside this region
         const bool carve = op.kind == ARC_EDIT_CARVE;
         const uint32_t mat = carve ? ARC_MAT_AIR : op.material;
         const float cx = op.center[0] - ox, cy = op.center[1] - oy, cz = op.center[2] - oz, rr = op.radius;
-        uint32_t x0, x1, y0, y1, z0, z1;
-        bool any = true;
+        int32_t x0, x1, y0, y1, z0, z1;
         if (carve) {
             const float kx = clampf(cx, 0.0f, 256.0f), ky = clampf(cy, 0.0f, 256.0f), kz = clampf(cz, 0.0f, 256.0f);
             const float sx0 = fmaxf(floorf(cx - rr), 0.0f), sy0 = fmaxf(floorf(cy - rr), 0.0f), sz0 = fmaxf(floorf(cz - rr), 0.0f);
             const float sx1 = fminf(ceilf(cx + rr), 255.0f), sy1 = fminf(ceilf(cy + rr), 255.0f), sz1 = fminf(ceilf(cz + rr), 255.0f);
-            any = !(dist2(cx, cy, cz, kx, ky, kz) > rr * rr) && !(sx0 > sx1 || sy0 > sy1 || sz0 > sz1);
-            x0 = any ? (uint32_t)sx0 >> 2 : 1u;
-            x1 = any ? (uint32_t)sx1 >> 2 : 0u;
-            y0 = any ? (uint32_t)sy0 >> 2 : 1u;
-            y1 = any ? (uint32_t)sy1 >> 2 : 0u;
-            z0 = any ? (uint32_t)sz0 >> 2 : 1u;
-            z1 = any ? (uint32_t)sz1 >> 2 : 0u;
+            const bool any = !(dist2(cx, cy, cz, kx, ky, kz) > rr * rr) && !(sx0 > sx1 || sy0 > sy1 || sz0 > sz1);
+            x0 = any ? (int32_t)((uint32_t)sx0 >> 2) : 1;
+            x1 = any ? (int32_t)((uint32_t)sx1 >> 2) : 0;
+            y0 = any ? (int32_t)((uint32_t)sy0 >> 2) : 1;
+            y1 = any ? (int32_t)((uint32_t)sy1 >> 2) : 0;
+            z0 = any ? (int32_t)((uint32_t)sz0 >> 2) : 1;
+            z1 = any ? (int32_t)((uint32_t)sz1 >> 2) : 0;
         } else {
-            x0 = x1 = op.brick[0] & 63u;
-            y0 = y1 = op.brick[1] & 63u;
-            z0 = z1 = op.brick[2] & 63u;
+            x0 = x1 = (int32_t)(op.brick[0] & 63u);
+            y0 = y1 = (int32_t)(op.brick[1] & 63u);
+            z0 = z1 = (int32_t)(op.brick[2] & 63u);
         }
-        const uint32_t nx = x1 >= x0 ? x1 - x0 + 1u : 0u, ny = y1 >= y0 ? y1 - y0 + 1u : 0u, nz = z1 >= z0 ? z1 - z0 + 1u : 0u;
+        x0 = max(x0, (int32_t)r0x);
+        x1 = min(x1, (int32_t)r0x + 15);
+        y0 = max(y0, (int32_t)r0y);
+        y1 = min(y1, (int32_t)r0y + 15);
+        z0 = max(z0, (int32_t)r0z);
+        z1 = min(z1, (int32_t)r0z + 15);
+        const uint32_t nx = x1 >= x0 ? (uint32_t)(x1 - x0 + 1) : 0u, ny = y1 >= y0 ? (uint32_t)(y1 - y0 + 1) : 0u,
+                       nz = z1 >= z0 ? (uint32_t)(z1 - z0 + 1) : 0u;
         const float r2 = rr * rr;
         for (uint32_t i = tid; i < nx * ny * nz; i += kThreads) {
-            const uint32_t bx = x0 + i % nx, by = y0 + (i / nx) % ny, bz = z0 + i / (nx * ny);
+            const uint32_t bx = (uint32_t)x0 + i % nx, by = (uint32_t)y0 + (i / nx) % ny, bz = (uint32_t)z0 + i / (nx * ny);
             if (carve) {
                 const float mnx = (float)(bx * 4u), mny = (float)(by * 4u), mnz = (float)(bz * 4u);
                 if (dist2(cx, cy, cz, clampf(cx, mnx, mnx + 4.0f), clampf(cy, mny, mny + 4.0f), clampf(cz, mnz, mnz + 4.0f)) > r2)
@@ -352,62 +372,77 @@ __global__ void __launch_bounds__(kThreads) edit_chunks_kernel(const Params P, c
         if (tid == 0 && s_n_cand > (uint32_t)kMaxCand) atomicOr(&P.counters[3], 2u);
         const uint32_t n_cand = min(s_n_cand, (uint32_t)kMaxCand);
         if (n_cand == 0) continue;  // uniform over the CTA
-        // ---- uncollapse top-down
-        if (tid == 0) uncollapse(P, root);
+        // ---- uncollapse top-down: the region's L1 node, then its L2 nodes
+        if (tid == 0) uncollapse(P, l1);
         __syncthreads();
         for (uint32_t c = tid; c < n_cand; c += kThreads) {
             const uint32_t bx = s_cand[c] & 63u, by = (s_cand[c] >> 6) & 63u, bz = s_cand[c] >> 12;
-            const uint32_t b0 = cbit((bx >> 4) & 3u, (by >> 4) & 3u, (bz >> 4) & 3u);
-            const uint4 rn = P.nodes[root];
-            if (nleaf(rn) || !(nmask(rn) & (1ull << b0))) continue;
-            if (!(atomicOr(&s_u1[b0 >> 5], 1u << (b0 & 31u)) & (1u << (b0 & 31u)))) uncollapse(P, nslot(rn, b0));
-        }
-        __syncthreads();
-        for (uint32_t c = tid; c < n_cand; c += kThreads) {
-            const uint32_t bx = s_cand[c] & 63u, by = (s_cand[c] >> 6) & 63u, bz = s_cand[c] >> 12;
-            const uint32_t b0 = cbit((bx >> 4) & 3u, (by >> 4) & 3u, (bz >> 4) & 3u);
             const uint32_t b1 = cbit((bx >> 2) & 3u, (by >> 2) & 3u, (bz >> 2) & 3u);
-            const uint4 rn = P.nodes[root];
-            if (nleaf(rn) || !(nmask(rn) & (1ull << b0))) continue;
-            const uint4 l1 = P.nodes[nslot(rn, b0)];
-            if (nleaf(l1) || !(nmask(l1) & (1ull << b1))) continue;
-            const uint32_t key = b0 * 64u + b1;
-            if (!(atomicOr(&s_u2[key >> 5], 1u << (key & 31u)) & (1u << (key & 31u)))) uncollapse(P, nslot(l1, b1));
+            const uint4 n1 = P.nodes[l1];
+            if (nleaf(n1) || !(nmask(n1) & (1ull << b1))) continue;
+            if (!(atomicOr(&s_u2[b1 >> 5], 1u << (b1 & 31u)) & (1u << (b1 & 31u)))) uncollapse(P, nslot(n1, b1));
         }
         __syncthreads();
         // ---- leaves
         for (uint32_t c = tid; c < n_cand; c += kThreads) {
             const uint32_t bx = s_cand[c] & 63u, by = (s_cand[c] >> 6) & 63u, bz = s_cand[c] >> 12;
-            const uint32_t b0 = cbit((bx >> 4) & 3u, (by >> 4) & 3u, (bz >> 4) & 3u);
             const uint32_t b1 = cbit((bx >> 2) & 3u, (by >> 2) & 3u, (bz >> 2) & 3u);
             const uint32_t b2 = cbit(bx & 3u, by & 3u, bz & 3u);
-            const uint4 rn = P.nodes[root];
-            if (nleaf(rn) || !(nmask(rn) & (1ull << b0))) continue;  // growth was refused
-            const uint4 l1 = P.nodes[nslot(rn, b0)];
-            if (nleaf(l1) || !(nmask(l1) & (1ull << b1))) continue;
-            const uint4 l2 = P.nodes[nslot(l1, b1)];
-            if (nleaf(l2) || !(nmask(l2) & (1ull << b2))) continue;
-            apply_leaf(P, nslot(l2, b2), s_entries[c], mat);
-            const uint32_t key = b0 * 64u + b1;
-            atomicOr(&s_l2[key >> 5], 1u << (key & 31u));
-            atomicOr(&s_l1[b0 >> 5], 1u << (b0 & 31u));
-            s_root_touched = 1u;
+            const uint4 n1 = P.nodes[l1];
+            if (nleaf(n1) || !(nmask(n1) & (1ull << b1))) continue;  // growth was refused
+            const uint4 n2 = P.nodes[nslot(n1, b1)];
+            if (nleaf(n2) || !(nmask(n2) & (1ull << b2))) continue;
+            apply_leaf(P, nslot(n2, b2), s_entries[c], mat);
+            atomicOr(&s_l2[b1 >> 5], 1u << (b1 & 31u));
+            s_touched = 1u;
             atomicAdd(&P.counters[2], 1u);
         }
         __syncthreads();
-        // ---- bottom-up: L2, L1, root
-        for (uint32_t key = tid; key < 4096u; key += kThreads) {
-            if (!(s_l2[key >> 5] & (1u << (key & 31u)))) continue;
-            const uint4 rn = P.nodes[root];
-            const uint4 l1 = P.nodes[nslot(rn, key >> 6)];
-            compact_refresh(P, nslot(l1, key & 63u));
-        }
+        // ---- bottom-up: the touched L2 nodes, then the L1 node (the root waits for the root pass)
+        if (tid < 64 && (s_l2[tid >> 5] & (1u << (tid & 31u)))) compact_refresh(P, nslot(P.nodes[l1], tid));
         __syncthreads();
-        if (tid < 64 && (s_l1[tid >> 5] & (1u << (tid & 31u)))) compact_refresh(P, nslot(P.nodes[root], tid));
-        __syncthreads();
-        if (tid == 0 && s_root_touched) compact_refresh(P, root);
+        if (tid == 0 && (s_l2[0] | s_l2[1])) compact_refresh(P, l1);
         __syncthreads();
     }
+    if (tid == 0 && s_touched) chunk_touched[item_slot[blockIdx.x]] = 1u;
+}
+
+// Before the region pass: a chunk whose root is collapsed (the whole chunk one uniform solid) expands
+// when one of its edits rewrites a voxel, as ensure_child does on the first mutated brick. For a full
+// chunk that is: any recolour, or a carve whose nearest voxel centre lies within the radius.
+__global__ void edit_root_uncollapse_kernel(const Params P, uint32_t grid_x, uint32_t grid_y, uint32_t n_chunks) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_chunks) return;
+    const uint32_t chunk = P.chunk_list[i];
+    const uint32_t root = P.roots[chunk];
+    if (root == ARC_EMPTY_CHUNK || !nleaf(P.nodes[root]) || nmask(P.nodes[root]) == 0ull) return;
+    const uint32_t m = nprimary(P.nodes[root]);
+    if (m == ARC_MAT_AIR || m == kMatWater) return;  // not solid: no edit rewrites it
+    const float ox = (float)((chunk % grid_x) * 256u), oy = (float)(((chunk / grid_x) % grid_y) * 256u),
+                oz = (float)((chunk / (grid_x * grid_y)) * 256u);
+    for (uint32_t e = P.op_start[i]; e < P.op_start[i + 1]; ++e) {
+        const arc_edit_op op = P.ops[P.op_idx[e]];
+        bool hit = op.kind == ARC_EDIT_RECOLOR;
+        if (!hit) {
+            const float cx = op.center[0] - ox, cy = op.center[1] - oy, cz = op.center[2] - oz;
+            const float vx = clampf(floorf(cx), 0.0f, 255.0f) + 0.5f, vy = clampf(floorf(cy), 0.0f, 255.0f) + 0.5f,
+                        vz = clampf(floorf(cz), 0.0f, 255.0f) + 0.5f;
+            hit = dist2(cx, cy, cz, vx, vy, vz) <= op.radius * op.radius;
+        }
+        if (hit) {
+            uncollapse(P, root);
+            return;
+        }
+    }
+}
+
+// After the region pass: roots of chunks with rewritten leaves drop emptied L1 nodes and refresh LOD.
+__global__ void edit_root_refresh_kernel(const Params P, const uint32_t* __restrict__ chunks,
+                                         const uint32_t* __restrict__ touched, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !touched[i]) return;
+    const uint32_t root = P.roots[chunks[i]];
+    if (root != ARC_EMPTY_CHUNK && !nleaf(P.nodes[root])) compact_refresh(P, root);
 }
 
 // Raises the allocator floors to cover host-written patch ranges.
@@ -480,7 +515,8 @@ int arc_apply_edits(arc_ctx* c, const arc_edit_op* ops, uint32_t n_ops, uint32_t
     }
     if (!c->d_edit && (rc = arc_edit_reset(c))) return rc;
     if (!pairs.empty()) {
-        std::stable_sort(pairs.begin(), pairs.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+        std::stable_sort(pairs.begin(), pairs.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+        // per touched chunk: its edits in order (root passes)
         std::vector<uint32_t> chunks, start, idx;
         for (size_t i = 0; i < pairs.size(); ++i) {
             if (i == 0 || pairs[i].first != pairs[i - 1].first) {
@@ -490,9 +526,55 @@ int arc_apply_edits(arc_ctx* c, const arc_edit_op* ops, uint32_t n_ops, uint32_t
             idx.push_back(pairs[i].second);
         }
         start.push_back((uint32_t)pairs.size());
-        // one staged upload: ops | chunk list | starts | op indices
-        const size_t b_ops = sizeof(arc_edit_op) * n_ops, b_ch = 4 * chunks.size(), b_st = 4 * start.size(), b_ix = 4 * idx.size();
-        const size_t total = b_ops + b_ch + b_st + b_ix;
+        // per (chunk, 64^3 region): the edits whose voxel bounds reach the region, in order (region pass)
+        std::vector<uint64_t> trip;  // chunk slot << 40 | region << 32 | op
+        for (uint32_t ci = 0; ci < (uint32_t)chunks.size(); ++ci) {
+            const uint32_t ch = chunks[ci];
+            const float ox = (float)((ch % gx) * 256u), oy = (float)(((ch / gx) % gy) * 256u), oz = (float)((ch / (gx * gy)) * 256u);
+            for (uint32_t e = start[ci]; e < start[ci + 1]; ++e) {
+                const arc_edit_op& op = ops[idx[e]];
+                uint32_t lo[3], hi[3];
+                if (op.kind == ARC_EDIT_RECOLOR) {
+                    for (int a = 0; a < 3; ++a) lo[a] = hi[a] = (op.brick[a] & 63u) >> 4;
+                } else {
+                    const float l[3] = {op.center[0] - ox, op.center[1] - oy, op.center[2] - oz};
+                    bool empty = false;
+                    for (int a = 0; a < 3; ++a) {
+                        const float s0 = std::max(std::floor(l[a] - op.radius), 0.0f), s1 = std::min(std::ceil(l[a] + op.radius), 255.0f);
+                        if (s0 > s1) empty = true;
+                        lo[a] = empty ? 1u : (uint32_t)s0 >> 6;
+                        hi[a] = empty ? 0u : (uint32_t)s1 >> 6;
+                    }
+                    if (empty) continue;
+                }
+                for (uint32_t z = lo[2]; z <= hi[2]; ++z)
+                    for (uint32_t y = lo[1]; y <= hi[1]; ++y)
+                        for (uint32_t x = lo[0]; x <= hi[0]; ++x)
+                            trip.push_back(((uint64_t)ci << 40) | ((uint64_t)(x | (y << 2) | (z << 4)) << 32) | idx[e]);
+            }
+        }
+        // edit order inside a (chunk, region) group: op index order
+        std::sort(trip.begin(), trip.end());
+        std::vector<uint32_t> it_chunk, it_region, it_slot, it_start, it_idx;
+        for (size_t i = 0; i < trip.size(); ++i) {
+            const uint64_t key = trip[i] >> 32;
+            if (i == 0 || key != (trip[i - 1] >> 32)) {
+                it_slot.push_back((uint32_t)(trip[i] >> 40));
+                it_chunk.push_back(chunks[trip[i] >> 40]);
+                it_region.push_back((uint32_t)(key & 63u));
+                it_start.push_back((uint32_t)i);
+            }
+            it_idx.push_back((uint32_t)trip[i]);
+        }
+        it_start.push_back((uint32_t)trip.size());
+        const uint32_t n_items = (uint32_t)it_chunk.size(), n_ch = (uint32_t)chunks.size();
+        // one staged upload
+        const size_t parts[11] = {sizeof(arc_edit_op) * n_ops, 4 * chunks.size(), 4 * start.size(), 4 * idx.size(),
+                                  4 * it_chunk.size(), 4 * it_region.size(), 4 * it_slot.size(), 4 * it_start.size(),
+                                  4 * it_idx.size(), 4 * (size_t)n_ch, 0};
+        size_t off[11] = {0};
+        for (int k = 1; k < 11; ++k) off[k] = (off[k - 1] + parts[k - 1] + 15) & ~(size_t)15;
+        const size_t total = off[10];
         if (c->edit_stage_bytes < total) {
             cudaFree(c->d_edit_stage);
             cudaFreeHost(c->h_edit_stage);
@@ -506,18 +588,19 @@ int arc_apply_edits(arc_ctx* c, const arc_edit_op* ops, uint32_t n_ops, uint32_t
         // the pinned block may still feed the previous batch's copy
         if (cudaStreamSynchronize(c->stream) != cudaSuccess) return edit_err(c, ARC_E_CUDA, "edit staging sync");
         uint8_t* h = static_cast<uint8_t*>(c->h_edit_stage);
-        std::memcpy(h, ops, b_ops);
-        std::memcpy(h + b_ops, chunks.data(), b_ch);
-        std::memcpy(h + b_ops + b_ch, start.data(), b_st);
-        std::memcpy(h + b_ops + b_ch + b_st, idx.data(), b_ix);
+        const void* src[10] = {ops, chunks.data(), start.data(), idx.data(), it_chunk.data(), it_region.data(),
+                               it_slot.data(), it_start.data(), it_idx.data(), nullptr};
+        for (int k = 0; k < 9; ++k) std::memcpy(h + off[k], src[k], parts[k]);
+        std::memset(h + off[9], 0, parts[9]);
         if (cudaMemcpyAsync(c->d_edit_stage, h, total, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
             return edit_err(c, ARC_E_CUDA, "edit upload");
-        const uint8_t* d = static_cast<const uint8_t*>(c->d_edit_stage);
+        uint8_t* d = static_cast<uint8_t*>(c->d_edit_stage);
+        auto dptr = [&](int k) { return reinterpret_cast<uint32_t*>(d + off[k]); };
         arc::edit::Params P;
         P.ops = reinterpret_cast<const arc_edit_op*>(d);
-        P.chunk_list = reinterpret_cast<const uint32_t*>(d + b_ops);
-        P.op_start = reinterpret_cast<const uint32_t*>(d + b_ops + b_ch);
-        P.op_idx = reinterpret_cast<const uint32_t*>(d + b_ops + b_ch + b_st);
+        P.chunk_list = dptr(1);
+        P.op_start = dptr(2);
+        P.op_idx = dptr(3);
         P.roots = c->d_roots;
         P.nodes = reinterpret_cast<uint4*>(c->d_nodes);
         P.bricks = reinterpret_cast<uint32_t*>(c->d_bricks);
@@ -525,8 +608,16 @@ int arc_apply_edits(arc_ctx* c, const arc_edit_op* ops, uint32_t n_ops, uint32_t
         P.counters = c->d_edit;
         P.node_cap = c->cap_nodes;
         P.brick_cap = c->cap_bricks;
-        arc::edit::edit_chunks_kernel<<<(uint32_t)chunks.size(), arc::edit::kThreads, 0, c->stream>>>(P, gx, gy);
-        if (cudaGetLastError() != cudaSuccess) return edit_err(c, ARC_E_CUDA, "edit_chunks_kernel launch");
+        arc::edit::edit_root_uncollapse_kernel<<<(n_ch + 127u) / 128u, 128, 0, c->stream>>>(P, gx, gy, n_ch);
+        if (n_items) {
+            arc::edit::Params R = P;
+            R.op_start = dptr(7);
+            R.op_idx = dptr(8);
+            arc::edit::edit_regions_kernel<<<n_items, arc::edit::kThreads, 0, c->stream>>>(R, dptr(4), dptr(5), dptr(6),
+                                                                                            dptr(9), gx, gy);
+        }
+        arc::edit::edit_root_refresh_kernel<<<(n_ch + 127u) / 128u, 128, 0, c->stream>>>(P, dptr(1), dptr(9), n_ch);
+        if (cudaGetLastError() != cudaSuccess) return edit_err(c, ARC_E_CUDA, "edit kernels launch");
         // traversal range checks now cover the whole pools: grown nodes live in the headroom
         if (c->n_nodes != c->cap_nodes || c->n_bricks != c->cap_bricks) {
             c->n_nodes = c->cap_nodes;
