@@ -120,31 +120,31 @@ __global__ void __launch_bounds__(256, MINB) frame_plain_kernel(const FrameParam
     const bool underwater = (cam.point_light_count[1] & 0xFFFFu) != 0u;
     RayState s;
     HitInfo h;
-    StepResult r = kMiss;
-    if (ray_begin(s, cam, eye, dir, 0.0f, 250.0f, 0u, underwater)) {
-        do {
-            r = ray_advance(s, w, cam, h);
-        } while (r == kContinue);
-    }
-    if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
-    uint32_t dw, nw;
-    primary_store(P, w.palette, cam, x, y, dir, r == kHit, h, &dw, &nw);
-    if (!P.do_gi) return;
+    // One traversal call site for both rays: the primary ray, then (for a hit) the GI ray continues in
+    // the same loop, so lanes in either phase run the same instructions together.
+    bool active = ray_begin(s, cam, eye, dir, 0.0f, 250.0f, 0u, underwater);
+    bool gi_phase = false;
     const size_t k = (size_t)y * P.width + x;
-    f3 go, gd;
-    if (!gi_setup(w, cam, x, y, P.width, P.height, dw, nw, &go, &gd)) {
-        if (P.gi_hits) store_no_ray(&P.gi_hits[k]);
-        return;
-    }
+    f3 go{0.0f, 0.0f, 0.0f}, gd{0.0f, 0.0f, 1.0f};
     const float gmax = cam.ray_distances[2];
-    StepResult g = kMiss;
-    if (ray_begin(s, cam, go, gd, 0.0f, gmax, 2u, true)) {
-        do {
-            g = ray_advance(s, w, cam, h);
-        } while (g == kContinue);
+    StepResult r;
+    for (;;) {
+        r = active ? ray_advance(s, w, cam, h) : kMiss;
+        if (r == kContinue) continue;
+        if (gi_phase) break;
+        if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
+        uint32_t dw, nw;
+        primary_store(P, w.palette, cam, x, y, dir, r == kHit, h, &dw, &nw);
+        if (!P.do_gi) return;
+        if (!gi_setup(w, cam, x, y, P.width, P.height, dw, nw, &go, &gd)) {
+            if (P.gi_hits) store_no_ray(&P.gi_hits[k]);
+            return;
+        }
+        gi_phase = true;
+        active = ray_begin(s, cam, go, gd, 0.0f, gmax, 2u, true);
     }
-    if (g != kHit) hit_init_miss(h, go, gd, gmax);
-    if (P.gi_hits) store_hit(&P.gi_hits[k], h, g == kHit);
+    if (r != kHit) hit_init_miss(h, go, gd, gmax);
+    if (P.gi_hits) store_hit(&P.gi_hits[k], h, r == kHit);
     // warp-aggregated count of GI rays
     const uint32_t m = __activemask();
     if (((threadIdx.x + threadIdx.y * blockDim.x) & 31u) == (uint32_t)(__ffs(m) - 1)) atomicAdd(&P.scratch->gi_rays, (unsigned long long)__popc(m));
