@@ -382,6 +382,64 @@ __global__ void __launch_bounds__(256, MINB) views_persistent_kernel(const Views
     if (lane == 0 && gi_count) atomicAdd(&V.scratch->gi_rays, (unsigned long long)gi_count);
 }
 
+// One thread per queue slot over many views: the slot's view by binary search, its pixel by the same
+// 32-pixel tile mapping as the persistent kernel (a warp traces one tile), then the single-view plain
+// kernel's work: one traversal call site for the primary ray and the pixel's GI ray.
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) views_plain_kernel(const ViewsParams V) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    bool gi_ray = false;
+    if (q < V.queue_len) {
+        uint32_t lo = 0, hi = V.n_views;  // last view with queue_begin <= q
+        while (hi - lo > 1u) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (V.views[mid].queue_begin <= q) lo = mid; else hi = mid;
+        }
+        const ViewDev& vd = V.views[lo];
+        const uint32_t local = q - vd.queue_begin, tile = local >> 5, within = local & 31u;
+        const uint32_t px = (tile % vd.tiles_x) * V.tile_w + within % V.tile_w;
+        const uint32_t py = (tile / vd.tiles_x) * V.tile_h + within / V.tile_w;
+        if (px < vd.width && py < vd.height) {
+            const arc_camera_uniforms& cam = vd.cam;
+            const World& w = V.worlds[vd.slot];
+            const f3 eye{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]};
+            const f3 dir = camera_dir(cam, px, py, vd.width, vd.height);
+            const bool underwater = (cam.point_light_count[1] & 0xFFFFu) != 0u;
+            const size_t k = (size_t)py * vd.width + px;
+            RayState s;
+            HitInfo h;
+            bool active = ray_begin(s, cam, eye, dir, 0.0f, 250.0f, 0u, underwater);
+            bool gi_phase = false, done = false;
+            f3 go{0.0f, 0.0f, 0.0f}, gd{0.0f, 0.0f, 1.0f};
+            const float gmax = cam.ray_distances[2];
+            StepResult r = kMiss;
+            while (!done) {
+                r = active ? ray_advance(s, w, cam, h) : kMiss;
+                if (r == kContinue) continue;
+                if (gi_phase) {
+                    if (r != kHit) hit_init_miss(h, go, gd, gmax);
+                    if (vd.gi_hits) store_hit(&vd.gi_hits[k], h, r == kHit);
+                    done = true;
+                    continue;
+                }
+                if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
+                uint32_t dw, nw;
+                primary_store(vd, w.palette, cam, px, py, dir, r == kHit, h, &dw, &nw);
+                if (!gi_setup(w, cam, px, py, vd.width, vd.height, dw, nw, &go, &gd)) {
+                    if (vd.gi_hits) store_no_ray(&vd.gi_hits[k]);
+                    done = true;
+                    continue;
+                }
+                gi_ray = true;
+                gi_phase = true;
+                active = ray_begin(s, cam, go, gd, 0.0f, gmax, 2u, true);
+            }
+        }
+    }
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, gi_ray);
+    if ((threadIdx.x & 31u) == 0u && m) atomicAdd(&V.scratch->gi_rays, (unsigned long long)__popc(m));
+}
+
 // ------------------------------------------------------------------------------------------------
 // Host launchers (called by the C ABI on the context's stream)
 // ------------------------------------------------------------------------------------------------
@@ -419,6 +477,10 @@ cudaError_t launch_frame(const FrameParams& P, const arc_camera_uniforms& cam, c
 
 template <int MINB>
 cudaError_t launch_views_t(const ViewsParams& V, const arc_launch_config& cfg, int n_sm, cudaStream_t st) {
+    if (cfg.variant == 0u) {
+        views_plain_kernel<MINB><<<(V.queue_len + cfg.block_threads - 1u) / cfg.block_threads, cfg.block_threads, 0, st>>>(V);
+        return cudaGetLastError();
+    }
     int per_sm = (int)cfg.blocks_per_sm;
     if (per_sm <= 0) {
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, views_persistent_kernel<MINB>,

@@ -411,7 +411,8 @@ def run_ours(args):
                    "views": len(b.views), "scenes": BENCH_SCENES, "pixels_per_frame": b.pixels,
                    "gi_rays_last_frame": n_gi_last, "ms_per_frame": round(statistics.mean(b_ms), 3),
                    "cuda_graph": True, "launches_per_frame": 1,
-                   "launch": {"block_threads": best.block_threads, "reg_blocks": best.reg_blocks,
+                   "launch": {"kernel": "persistent" if best.variant == 1 else "plain",
+                              "block_threads": best.block_threads, "reg_blocks": best.reg_blocks,
                               "refill_threshold": best.refill_threshold, "tile": [best.tile_w, best.tile_h]}}
     t.close()
 
