@@ -807,6 +807,14 @@ int arc_autotune_frame_dev(arc_ctx* c, uint32_t width, uint32_t height, uint32_t
     return arc_ctx_finish(c);
 }
 
+int arc_shadow_rays_di_dev(arc_ctx* c, const arc_ray* rays, const float* max_dist_m, uint32_t n, float* vis) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if (n && (!rays || !max_dist_m || !vis)) return set_err(c, ARC_E_INVALID_ARG, "null buffer");
+    if (n) ARC_CK(c, arc::launch_shadow_di(c->world(), c->cam, rays, max_dist_m, n, vis, c->stream));
+    return ARC_OK;
+}
+
 int arc_shadow_rays_dev(arc_ctx* c, const arc_ray* rays, uint32_t n, float max_dist_m, float* vis) {
     int rc = arc_ctx_check_ready(c, true);
     if (rc) return rc;

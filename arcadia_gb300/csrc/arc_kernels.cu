@@ -287,6 +287,16 @@ __global__ void shadow_kernel(const World w, const __grid_constant__ arc_camera_
     vis[i] = shadow_vis(w, cam, f3{rp[0], rp[1], rp[2]}, f3{rp[3], rp[4], rp[5]}, max_dist_m);
 }
 
+// trace_shadow_vis_di over a batch of rays towards emitters, each with its own target distance.
+__global__ void shadow_di_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam,
+                                 const arc_ray* __restrict__ rays, const float* __restrict__ max_dist_m, uint32_t n,
+                                 float* __restrict__ vis) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* rp = reinterpret_cast<const float*>(&rays[i]);
+    vis[i] = shadow_vis_di(w, cam, f3{rp[0], rp[1], rp[2]}, f3{rp[3], rp[4], rp[5]}, max_dist_m[i]);
+}
+
 // Persistent kernel over many views (several worlds, mixed resolutions) in one launch. The queue is
 // the concatenation of every view's 32-pixel tiles; a lane finds its view by binary search over the
 // views' queue offsets and reads that view's camera block and world from global memory (L1-cached),
@@ -512,6 +522,12 @@ cudaError_t launch_rays(const World& w, const arc_camera_uniforms& cam, const ar
                         uint32_t lod_bias, int ignore_water, arc_hit_record* hits, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     rays_kernel<<<(n + 127u) / 128u, 128, 0, st>>>(w, cam, rays, n, max_dist_m, lod_bias, ignore_water ? 1u : 0u, hits);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shadow_di(const World& w, const arc_camera_uniforms& cam, const arc_ray* rays, const float* max_dist_m,
+                             uint32_t n, float* vis, cudaStream_t st) {
+    shadow_di_kernel<<<(n + 127u) / 128u, 128, 0, st>>>(w, cam, rays, max_dist_m, n, vis);
     return cudaGetLastError();
 }
 

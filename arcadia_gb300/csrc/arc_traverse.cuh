@@ -370,9 +370,17 @@ __device__ __forceinline__ StepResult ray_advance(RayState& s, const World& w, c
     return kContinue;
 }
 
-// trace_shadow_vis (traversal64.wgsl:571-773): 1.0 unoccluded, 0.0 occluded.
-__device__ __forceinline__ float shadow_vis(const World& w, const arc_camera_uniforms& cam, f3 origin_m, f3 dir,
-                                            float max_dist_m) {
+// is_emissive_mat (traversal64.wgsl:775-777)
+__device__ __forceinline__ bool is_emissive_mat(uint32_t m) { return (m >= 19u && m <= 22u) || m == 24u || m == 27u; }
+
+// trace_shadow_vis (traversal64.wgsl:571-773) for kDi = false; trace_shadow_vis_di (781-989), the
+// ReSTIR DI any-hit ray towards an emitter, for kDi = true. 1.0 unoccluded, 0.0 occluded. The DI
+// variant clamps the step budget to [32, 48], coarsens only with distance left to the target, reads
+// brick materials, lets an emissive hit within 16 voxels of the target through, and calls the ray
+// visible only when it ended within 2 voxels of the target.
+template <bool kDi>
+__device__ __forceinline__ float shadow_vis_t(const World& w, const arc_camera_uniforms& cam, f3 origin_m, f3 dir,
+                                              float max_dist_m) {
     const f3 vo = mul3s(origin_m, ARC_VOXELS_PER_METER);
     const float max_t_v = max_dist_m * ARC_VOXELS_PER_METER;
     RayState s;
@@ -393,7 +401,7 @@ __device__ __forceinline__ float shadow_vis(const World& w, const arc_camera_uni
     if (w_exit < fmaxf(w_enter, 0.0f) || w_enter >= max_t_v) return 1.0f;
     s.t = fmaxf(w_enter, 0.0f);
     s.t_limit = fminf(w_exit, max_t_v);
-    const uint32_t max_steps = cam.ray_steps[3];
+    const uint32_t max_steps = kDi ? umin(umax(cam.ray_steps[3], 32u), 48u) : cam.ray_steps[3];
     float st = s.t + 1e-4f;
     s.vx = f2u(clampf(vo.x + dir.x * st, 0.0f, wx - 1e-3f));
     s.vy = f2u(clampf(vo.y + dir.y * st, 0.0f, wy - 1e-3f));
@@ -423,8 +431,14 @@ __device__ __forceinline__ float shadow_vis(const World& w, const arc_camera_uni
             continue;
         }
         uint32_t min_shift = 0u;
-        if (s.t > 48.0f || step > 6u) min_shift = 2u;
-        if (s.t > 192.0f || step > 16u) min_shift = 4u;
+        if (kDi) {
+            const float dist_rem = s.t_limit - s.t;
+            if (s.t > 48.0f && dist_rem > 32.0f && step > 6u) min_shift = 2u;
+            if (s.t > 160.0f && dist_rem > 64.0f && step > 14u) min_shift = 4u;
+        } else {
+            if (s.t > 48.0f || step > 6u) min_shift = 2u;
+            if (s.t > 192.0f || step > 16u) min_shift = 4u;
+        }
         uint4 node;
         uint32_t shift;
         if (diff < 4u && min_shift == 0u && cached_shift == 0u) { node = l3; shift = 0u; }
@@ -446,11 +460,15 @@ __device__ __forceinline__ float shadow_vis(const World& w, const arc_camera_uni
                 step_box(s, bx, by, bz, span);
                 break;
             }
-            if ((node.z & ARC_IS_LEAF_FLAG) != 0u || shift <= min_shift) {
-                if (((node.w >> 24) & 0xFFu) == ARC_MAT_WATER_CRYSTAL) {
+            const bool is_leaf = (node.z & ARC_IS_LEAF_FLAG) != 0u, is_uniform = (node.z & ARC_IS_UNIFORM_FLAG) != 0u;
+            if (is_leaf || (kDi && is_uniform) || shift <= min_shift) {
+                uint32_t mat = (node.w >> 24) & 0xFFu;
+                if (kDi && is_leaf && !is_uniform && shift == 0u) mat = load_brick_mat(w, node.z & ARC_PTR_INDEX_MASK, b);
+                if (mat == ARC_MAT_WATER_CRYSTAL) {
                     step_box(s, bx, by, bz, span);
                     break;
                 }
+                if (kDi && is_emissive_mat(mat) && s.t >= s.t_limit - 16.0f) return 1.0f;
                 return 0.0f;
             }
             node = load_node(w, child_index(node, b));
@@ -461,10 +479,20 @@ __device__ __forceinline__ float shadow_vis(const World& w, const arc_camera_uni
             else if (shift == 0u) l3 = node;
         }
     }
+    if (kDi) return s.t >= s.t_limit - 2.0f ? 1.0f : 0.0f;
     if (s.t < s.t_limit) {
         if ((vo.y + dir.y * s.t) * ARC_VOXEL_SIZE < 32.0f) return 0.0f;
     }
     return 1.0f;
+}
+
+__device__ __forceinline__ float shadow_vis(const World& w, const arc_camera_uniforms& cam, f3 origin_m, f3 dir,
+                                            float max_dist_m) {
+    return shadow_vis_t<false>(w, cam, origin_m, dir, max_dist_m);
+}
+__device__ __forceinline__ float shadow_vis_di(const World& w, const arc_camera_uniforms& cam, f3 origin_m, f3 dir,
+                                               float max_dist_m) {
+    return shadow_vis_t<true>(w, cam, origin_m, dir, max_dist_m);
 }
 
 // Pinhole camera ray (primary_gbuffer.wgsl:103-115, reconstruct_ray_dir types.wgsl:334-345).

@@ -80,6 +80,7 @@ SIGNATURES = {
     "arc_apply_edits": [_vp, _vp, _u32, _vp],
     "arc_edit_stats": [_vp, _vp, _vp, _vp, _vp],
     "arc_download_world": [_vp, _vp, _vp, _u32, _vp, _u32, _vp, _vp],
+    "arc_shadow_rays_di_dev": [_vp, _vp, _vp, _u32, _vp],
     "arc_nrc_init": [_vp, _u32],
     "arc_nrc_set_weights": [_vp, _vp],
     "arc_nrc_get_weights": [_vp, _vp],

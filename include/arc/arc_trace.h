@@ -157,6 +157,11 @@ int arc_trace_rays_dev(arc_ctx* ctx, const arc_ray* rays, uint32_t n, float max_
                        int ignore_water, arc_hit_record* hits);
 /* trace_shadow_vis on a batch (1.0 visible / 0.0 occluded per ray). */
 int arc_shadow_rays_dev(arc_ctx* ctx, const arc_ray* rays, uint32_t n, float max_dist_m, float* vis);
+/* trace_shadow_vis_di (shaders/common/traversal64.wgsl:781-989, called at
+ * shaders/lighting_restir_gi.wgsl:744): the ReSTIR DI any-hit ray towards an emitter at distance
+ * max_dist_m[i] (metres). 1.0 when the ray reaches within 2 voxels of the target or strikes an emissive
+ * voxel within 16 voxels of it, else 0.0. */
+int arc_shadow_rays_di_dev(arc_ctx* ctx, const arc_ray* rays, const float* max_dist_m, uint32_t n, float* vis);
 
 /* SHARC radiance cache, library-owned (keys 512 KB, accumulators 2 MB, resolved slots 2 MB). */
 int arc_sharc_reset(arc_ctx* ctx);

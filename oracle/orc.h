@@ -92,6 +92,8 @@ uint32_t orc_morton3d(uint32_t x, uint32_t y, uint32_t z);
 /* traversal */
 void orc_trace(const orc_world* w, const arc_camera_uniforms* cam, const float origin_m[3], const float dir[3],
                float start_t_m, float max_dist_m, uint32_t lod_bias, int ignore_water, orc_trace_out* out);
+float orc_shadow_vis_di(const orc_world* w, const arc_camera_uniforms* cam, const float origin_m[3], const float dir[3],
+                        float max_dist_m);
 float orc_shadow_vis(const orc_world* w, const arc_camera_uniforms* cam, const float origin_m[3], const float dir[3],
                      float max_dist_m, uint32_t* bytes);
 uint32_t orc_face_id(const float n[3]);

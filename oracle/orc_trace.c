@@ -335,9 +335,15 @@ void orc_trace(const orc_world* w, const arc_camera_uniforms* cam, const float o
     res->bytes = bytes;
 }
 
-/* trace_shadow_vis: traversal64.wgsl:571-773 */
-float orc_shadow_vis(const orc_world* w, const arc_camera_uniforms* cam, const float origin_m[3], const float dir[3],
-                     float max_dist_m, uint32_t* bytes_io) {
+/* is_emissive_mat: traversal64.wgsl:775-777 */
+static int is_emissive_mat(uint32_t m) { return (m >= 19u && m <= 22u) || m == 24u || m == 27u; }
+
+/* trace_shadow_vis: traversal64.wgsl:571-773 (di = 0); trace_shadow_vis_di: traversal64.wgsl:781-989
+ * (di = 1): step budget clamped to [32, 48], LOD only with distance left to the target, uniform nodes
+ * and brick materials read, an emissive hit within 16 voxels of the target visible, and visible at the
+ * end only when within 2 voxels of the target. */
+static float shadow_vis_impl(const orc_world* w, const arc_camera_uniforms* cam, const float origin_m[3], const float dir[3],
+                             float max_dist_m, uint32_t* bytes_io, int di) {
     uint32_t bytes = 0;
     float vo[3], inv[3];
     for (int i = 0; i < 3; ++i) {
@@ -354,7 +360,7 @@ float orc_shadow_vis(const orc_world* w, const arc_camera_uniforms* cam, const f
     if (wy < orc_max(wx, 0.0f) || wx >= max_t_v) { if (bytes_io) *bytes_io += bytes; return 1.0f; }
     float t = orc_max(wx, 0.0f);
     float t_limit = orc_min(wy, max_t_v);
-    uint32_t max_steps = cam->ray_steps[3];
+    uint32_t max_steps = di ? orc_uclamp(cam->ray_steps[3], 32u, 48u) : cam->ray_steps[3];
     int pos[3] = {inv[0] >= 0.0f, inv[1] >= 0.0f, inv[2] >= 0.0f};
     float noi[3] = {-vo[0] * inv[0], -vo[1] * inv[1], -vo[2] * inv[2]};
     uint32_t wmax_vi[3] = {g[0] << 8, g[1] << 8, g[2] << 8};
@@ -389,8 +395,14 @@ float orc_shadow_vis(const orc_world* w, const arc_camera_uniforms* cam, const f
             continue;
         }
         uint32_t min_shift = 0u;
-        if (t > 48.0f || step > 6u) min_shift = 2u;
-        if (t > 192.0f || step > 16u) min_shift = 4u;
+        if (di) {
+            float dist_rem = t_limit - t;
+            if (t > 48.0f && dist_rem > 32.0f && step > 6u) min_shift = 2u;
+            if (t > 160.0f && dist_rem > 64.0f && step > 14u) min_shift = 4u;
+        } else {
+            if (t > 48.0f || step > 6u) min_shift = 2u;
+            if (t > 192.0f || step > 16u) min_shift = 4u;
+        }
         arc_node64 node;
         uint32_t shift;
         if (diff < 4u && min_shift == 0u && cached_shift == 0u) { node = c_l3; shift = 0u; }
@@ -416,8 +428,11 @@ float orc_shadow_vis(const orc_world* w, const arc_camera_uniforms* cam, const f
                 break;
             }
             int is_leaf = (node.child_ptr & ARC_IS_LEAF_FLAG) != 0u;
-            if (is_leaf || shift <= min_shift) {
+            int is_uniform = (node.child_ptr & ARC_IS_UNIFORM_FLAG) != 0u;
+            if (is_leaf || (di && is_uniform) || shift <= min_shift) {
                 uint32_t mat = (node.lod_payload >> 24) & 0xFFu;
+                if (di && is_leaf && !is_uniform && shift == 0u)
+                    mat = brick_get_material(w, node.child_ptr & ARC_PTR_INDEX_MASK, b, &bytes);
                 if (mat == ARC_MAT_WATER_CRYSTAL) {
                     uint32_t span = 1u << shift;
                     u3 cmin = {vi.x & ~(span - 1u), vi.y & ~(span - 1u), vi.z & ~(span - 1u)};
@@ -426,6 +441,7 @@ float orc_shadow_vis(const orc_world* w, const arc_camera_uniforms* cam, const f
                     break;
                 }
                 if (bytes_io) *bytes_io += bytes;
+                if (di && is_emissive_mat(mat) && t >= t_limit - 16.0f) return 1.0f;
                 return 0.0f;
             }
             uint32_t next = node_child_offset(&node, b);
@@ -438,11 +454,22 @@ float orc_shadow_vis(const orc_world* w, const arc_camera_uniforms* cam, const f
         }
     }
     if (bytes_io) *bytes_io += bytes;
+    if (di) return t >= t_limit - 2.0f ? 1.0f : 0.0f;
     if (t < t_limit) {
         float py = vo[1] + dir[1] * t;
         if (py * ARC_VOXEL_SIZE < 32.0f) return 0.0f;
     }
     return 1.0f;
+}
+
+float orc_shadow_vis(const orc_world* w, const arc_camera_uniforms* cam, const float origin_m[3], const float dir[3],
+                     float max_dist_m, uint32_t* bytes_io) {
+    return shadow_vis_impl(w, cam, origin_m, dir, max_dist_m, bytes_io, 0);
+}
+
+float orc_shadow_vis_di(const orc_world* w, const arc_camera_uniforms* cam, const float origin_m[3], const float dir[3],
+                        float max_dist_m) {
+    return shadow_vis_impl(w, cam, origin_m, dir, max_dist_m, NULL, 1);
 }
 
 /* ------------------------------------------------------------------------------------------ */

@@ -103,6 +103,8 @@ def lib():
         _lib.orc_sharc_update.argtypes = [C.POINTER(_World), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         _lib.orc_shadow_vis.argtypes = [C.POINTER(_World), vp, vp, vp, f32, vp]
         _lib.orc_shadow_vis.restype = f32
+        _lib.orc_shadow_vis_di.argtypes = [C.POINTER(_World), vp, vp, vp, f32]
+        _lib.orc_shadow_vis_di.restype = f32
         _lib.orc_test_sincos.argtypes = [vp, u32, vp, vp]
         _lib.orc_test_f16.argtypes = [vp, u32, vp]
         _lib.orc_test_powi.argtypes = [vp, u32, u32, vp]
@@ -315,6 +317,12 @@ def shadow_vis(world: World, cam, origin_m, dir_, max_dist_m) -> float:
     o = np.asarray(origin_m, np.float32)
     d = np.asarray(dir_, np.float32)
     return lib().orc_shadow_vis(world.cw, _p(cam), _p(o), _p(d), max_dist_m, None)
+
+
+def shadow_vis_di(world: World, cam, origin_m, dir_, max_dist_m) -> float:
+    o = np.asarray(origin_m, np.float32)
+    d = np.asarray(dir_, np.float32)
+    return lib().orc_shadow_vis_di(world.cw, _p(cam), _p(o), _p(d), max_dist_m)
 
 
 class Sharc:

@@ -269,3 +269,60 @@ def test_patch_application(orc, tracer, world_cache):
     patched = orc.World(base.grid, roots, patched.nodes, patched.bricks)
     _assert_hits_equal(tracer.trace_rays(rays, 60.0), orc.trace_rays(patched, cam, rays, 60.0, 0, False, threads=THREADS),
                        "after empty patch")
+
+
+def test_shadow_rays_di(orc, tracer, world_cache):
+    """trace_shadow_vis_di: rays between nearby visible surface points, 30 % of the visible bricks
+    recoloured to the emissive ids, each ray with its own target distance. Bit-exact against the
+    oracle; both outcomes occur, and some rays are visible only because their target is emissive
+    (the emitter early-out)."""
+    import torch
+    from arcadia_gb300.layout import EDIT_DTYPE, EDIT_RECOLOR
+    from arcadia_gb300.native import lib
+
+    W, H = 320, 180
+    w = world_cache("c2_1024_caves")
+    cam = L.default_camera_for(L.SCENES["c2_1024_caves"], W, H, quality=L.quality_high())
+    _load(tracer, w, cam)
+    hits = tracer.trace_frame()[3]
+    rng = np.random.default_rng(31)
+    is_hit = (hits["flags"] & 1).astype(bool)
+    vox = hits["voxel"].astype(np.int64)
+    hit_px = np.nonzero(is_hit)[0]
+    emit_px = rng.choice(hit_px, int(0.3 * len(hit_px)), replace=False)
+    ops = np.zeros(len(emit_px), EDIT_DTYPE)
+    ops["kind"] = EDIT_RECOLOR
+    ops["brick"] = (vox[emit_px] >> 2).astype(np.uint32)
+    ops["material"] = rng.choice([19, 20, 21, 22, 24, 27], len(emit_px))
+    ew = orc.apply_edits(w, ops)
+    # ray pairs: a hit pixel and a hit pixel within +-12 pixels of it
+    src = rng.choice(hit_px, 8000)
+    sx, sy = src % W + rng.integers(-12, 13, len(src)), src // W + rng.integers(-12, 13, len(src))
+    ok = (sx >= 0) & (sx < W) & (sy >= 0) & (sy < H)
+    src, dst = src[ok], (sy * W + sx)[ok]
+    ok = is_hit[dst] & (np.abs(vox[src] - vox[dst]).max(1) > 2)
+    src, dst = src[ok], dst[ok]
+    o = (vox[src].astype(np.float32) + np.float32(0.5)) * np.float32(0.0625) + np.array([0, 0.04, 0], np.float32)
+    tgt = (vox[dst].astype(np.float32) + np.float32(0.5)) * np.float32(0.0625)
+    d = tgt - o
+    dist = np.sqrt((d * d).sum(1)).astype(np.float32)
+    d = (d / dist[:, None]).astype(np.float32)
+    rays = np.zeros(len(o), L.RAY_DTYPE)
+    rays["origin_m"] = o
+    rays["dir"] = d
+    d_rays = torch.from_numpy(rays.view(np.uint8).copy()).cuda()
+    d_max = torch.from_numpy(dist.copy()).cuda()
+
+    def gpu_vis(world):
+        _load(tracer, world, cam)
+        out = torch.zeros(len(rays), dtype=torch.float32, device="cuda")
+        assert lib().arc_shadow_rays_di_dev(tracer.ctx, d_rays.data_ptr(), d_max.data_ptr(), len(rays), out.data_ptr()) == 0
+        tracer.synchronize()
+        return out.cpu().numpy()
+
+    vis = gpu_vis(ew)
+    ovis = np.array([orc.shadow_vis_di(ew, cam, r["origin_m"], r["dir"], float(m)) for r, m in zip(rays, dist)], np.float32)
+    np.testing.assert_array_equal(vis, ovis)
+    assert 0.05 < vis.mean() < 0.95, vis.mean()
+    plain = gpu_vis(w)  # same rays, no emitters in the world
+    assert np.all(plain <= vis) and (vis > plain).sum() > 20
