@@ -217,6 +217,17 @@ int arc_destroy(arc_ctx* c) {
     cudaFree(c->d_nrc_w16_ema);
     cudaFree(c->d_nrc_wu_ema);
     cudaFree(c->d_nrc_wu);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamDestroy(c->copy_stream);
+        for (int i = 0; i < arc_ctx::kMaxBands; ++i) {
+            cudaStreamSynchronize(c->band_stream[i]);
+            cudaStreamDestroy(c->band_stream[i]);
+            cudaEventDestroy(c->band_ev[i]);
+        }
+        cudaEventDestroy(c->copies_done);
+        cudaEventDestroy(c->frame_start);
+    }
     cudaFree(c->d_edit);
     cudaFree(c->d_edit_stage);
     cudaFreeHost(c->h_edit_stage);
@@ -421,6 +432,14 @@ static int check_dims(arc_ctx* c, uint32_t width, uint32_t height) {
     return ARC_OK;
 }
 
+// Restricts a frame launch to rows [row0, row_end) (the persistent kernel's queue covers those rows).
+static void frame_rows(arc_ctx* c, arc::FrameParams& P, uint32_t row0, uint32_t row_end) {
+    P.row0 = row0;
+    P.row_end = row_end;
+    const uint32_t tiles_y = (row_end - row0 + c->cfg.tile_h - 1u) / c->cfg.tile_h;
+    P.queue_len = P.tiles_x * tiles_y * 32u;
+}
+
 static arc::FrameParams frame_params(arc_ctx* c, uint32_t width, uint32_t height) {
     arc::FrameParams P;
     memset(&P, 0, sizeof P);
@@ -431,9 +450,8 @@ static arc::FrameParams frame_params(arc_ctx* c, uint32_t width, uint32_t height
     P.tile_w = c->cfg.tile_w;
     P.tile_h = c->cfg.tile_h;
     P.tiles_x = (width + c->cfg.tile_w - 1u) / c->cfg.tile_w;
-    const uint32_t tiles_y = (height + c->cfg.tile_h - 1u) / c->cfg.tile_h;
-    P.queue_len = P.tiles_x * tiles_y * 32u;
     P.refill_threshold = c->cfg.refill_threshold;
+    frame_rows(c, P, 0u, height);
     return P;
 }
 
@@ -508,30 +526,83 @@ int arc_trace_secondary_dev(arc_ctx* c, uint32_t width, uint32_t height, const u
 }
 
 // Host-buffer variants: stage outputs in one context-owned device block.
+static int ensure_band_streams(arc_ctx* c) {
+    if (c->copy_stream) return ARC_OK;
+    ARC_CK(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (int i = 0; i < arc_ctx::kMaxBands; ++i) {
+        ARC_CK(c, cudaStreamCreateWithFlags(&c->band_stream[i], cudaStreamNonBlocking));
+        ARC_CK(c, cudaEventCreateWithFlags(&c->band_ev[i], cudaEventDisableTiming));
+    }
+    ARC_CK(c, cudaEventCreateWithFlags(&c->copies_done, cudaEventDisableTiming));
+    ARC_CK(c, cudaEventCreateWithFlags(&c->frame_start, cudaEventDisableTiming));
+    return ARC_OK;
+}
+
+// Host-buffer frame in horizontal bands: band b traces rows [b H / n, (b + 1) H / n); the copy stream
+// waits for it and copies that band's rows of every output while later bands trace, so only the last
+// band's copies follow the traversal. The plain kernel's bands are launched together on their own
+// streams (the SMs fill with band b + 1 while band b drains: no tail per band); the persistent kernel's
+// bands share its queue head and run one after another on the context's stream.
 int arc_trace_frame(arc_ctx* c, uint32_t width, uint32_t height, uint32_t* gdm, uint32_t* gnm, uint32_t* gaa,
                     arc_hit_record* hits, arc_hit_record* gi_hits, uint64_t* n_gi_out) {
     int rc = arc_ctx_check_ready(c, true);
     if (rc) return rc;
     if ((rc = check_dims(c, width, height))) return rc;
     if (!gdm || !gnm || !gaa) return set_err(c, ARC_E_INVALID_ARG, "null G-buffer");
+    if ((rc = ensure_band_streams(c))) return rc;
     const size_t np = (size_t)width * height;
-    const size_t b_g = np * 20, b_h = hits ? np * 20 : 0, b_gi = gi_hits ? np * 20 : 0;
+    void* host[5] = {gdm, gnm, gaa, hits, gi_hits};
+    const size_t px_bytes[5] = {8, 8, 4, 20, 20};
+    size_t total = 0;
+    size_t off[5];
+    for (int i = 0; i < 5; ++i) {
+        off[i] = total;
+        if (host[i]) total += (np * px_bytes[i] + 255) & ~(size_t)255;
+    }
     void* stage;
-    if ((rc = arc_ctx_stage(c, b_g + b_h + b_gi, &stage))) return rc;
+    if ((rc = arc_ctx_stage(c, total, &stage))) return rc;
     unsigned char* base = static_cast<unsigned char*>(stage);
+    unsigned char* dev[5];
+    for (int i = 0; i < 5; ++i) dev[i] = host[i] ? base + off[i] : nullptr;
     arc::FrameParams P = frame_params(c, width, height);
-    P.gbuf_depth_mat = reinterpret_cast<uint32_t*>(base);
-    P.gbuf_norm_motion = reinterpret_cast<uint32_t*>(base + np * 8);
-    P.gbuf_albedo_ao = reinterpret_cast<uint32_t*>(base + np * 16);
-    P.hits = hits ? reinterpret_cast<arc_hit_record*>(base + b_g) : nullptr;
-    P.gi_hits = gi_hits ? reinterpret_cast<arc_hit_record*>(base + b_g + b_h) : nullptr;
+    P.gbuf_depth_mat = reinterpret_cast<uint32_t*>(dev[0]);
+    P.gbuf_norm_motion = reinterpret_cast<uint32_t*>(dev[1]);
+    P.gbuf_albedo_ao = reinterpret_cast<uint32_t*>(dev[2]);
+    P.hits = reinterpret_cast<arc_hit_record*>(dev[3]);
+    P.gi_hits = reinterpret_cast<arc_hit_record*>(dev[4]);
     P.do_gi = 1;
-    if ((rc = run_frame(c, P))) return rc;
-    ARC_CK(c, cudaMemcpyAsync(gdm, P.gbuf_depth_mat, np * 8, cudaMemcpyDeviceToHost, c->stream));
-    ARC_CK(c, cudaMemcpyAsync(gnm, P.gbuf_norm_motion, np * 8, cudaMemcpyDeviceToHost, c->stream));
-    ARC_CK(c, cudaMemcpyAsync(gaa, P.gbuf_albedo_ao, np * 4, cudaMemcpyDeviceToHost, c->stream));
-    if (hits) ARC_CK(c, cudaMemcpyAsync(hits, P.hits, b_h, cudaMemcpyDeviceToHost, c->stream));
-    if (gi_hits) ARC_CK(c, cudaMemcpyAsync(gi_hits, P.gi_hits, b_gi, cudaMemcpyDeviceToHost, c->stream));
+    const bool concurrent = c->cfg.variant == 0u;
+    const uint32_t n_bands =
+        std::max<uint32_t>(1u, std::min<uint32_t>((uint32_t)arc_ctx::kMaxBands, height / (concurrent ? 128u : 256u)));
+    ARC_CK(c, cudaMemsetAsync(c->d_scratch, 0, sizeof(Scratch), c->stream));
+    ARC_CK(c, cudaEventRecord(c->ev0, c->stream));
+    ARC_CK(c, cudaEventRecord(c->frame_start, c->stream));
+    for (uint32_t b = 0; b < n_bands; ++b) {
+        const uint32_t r0 = (uint32_t)((uint64_t)height * b / n_bands), r1 = (uint32_t)((uint64_t)height * (b + 1) / n_bands);
+        frame_rows(c, P, r0, r1);
+        cudaStream_t st = c->stream;
+        if (concurrent) {
+            st = c->band_stream[b];
+            ARC_CK(c, cudaStreamWaitEvent(st, c->frame_start, 0));
+        } else if (b > 0) {
+            ARC_CK(c, cudaMemsetAsync(&c->d_scratch->queue_head, 0, sizeof(uint32_t), c->stream));
+        }
+        ARC_CK(c, arc::launch_frame(P, c->cam, c->cfg, c->n_sm, st));
+        ARC_CK(c, cudaEventRecord(c->band_ev[b], st));
+        ARC_CK(c, cudaStreamWaitEvent(c->copy_stream, c->band_ev[b], 0));
+        for (int i = 0; i < 5; ++i) {
+            if (!host[i]) continue;
+            const size_t o = (size_t)r0 * width * px_bytes[i], len = (size_t)(r1 - r0) * width * px_bytes[i];
+            ARC_CK(c, cudaMemcpyAsync(static_cast<unsigned char*>(host[i]) + o, dev[i] + o, len, cudaMemcpyDeviceToHost,
+                                      c->copy_stream));
+        }
+    }
+    if (concurrent)
+        for (uint32_t b = 0; b < n_bands; ++b) ARC_CK(c, cudaStreamWaitEvent(c->stream, c->band_ev[b], 0));
+    ARC_CK(c, cudaEventRecord(c->ev1, c->stream));
+    c->timing_pending = true;
+    ARC_CK(c, cudaEventRecord(c->copies_done, c->copy_stream));
+    ARC_CK(c, cudaStreamWaitEvent(c->stream, c->copies_done, 0));
     return collect_frame(c, np, n_gi_out);
 }
 

@@ -94,6 +94,12 @@ struct arc_ctx {
 
     arc_launch_config cfg{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // host-buffer frames: copy stream and per-band events (copies of a band overlap the next band)
+    static constexpr int kMaxBands = 8;
+    cudaStream_t copy_stream = nullptr;
+    cudaStream_t band_stream[kMaxBands] = {};  // the plain kernel's bands run concurrently, one per stream
+    cudaEvent_t band_ev[kMaxBands] = {};
+    cudaEvent_t copies_done = nullptr, frame_start = nullptr;
     bool timing_pending = false;
     float last_ms = 0.0f;
     uint64_t last_rays = 0;

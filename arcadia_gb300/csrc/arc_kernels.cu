@@ -101,7 +101,7 @@ __device__ __forceinline__ void pixel_of(const FrameParams& P, uint32_t q, uint3
     const uint32_t tile = q >> 5, within = q & 31u;
     const uint32_t tx = tile % P.tiles_x, ty = tile / P.tiles_x;
     *x = tx * P.tile_w + within % P.tile_w;
-    *y = ty * P.tile_h + within / P.tile_w;
+    *y = P.row0 + ty * P.tile_h + within / P.tile_w;
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -112,8 +112,8 @@ template <int MINB>
 __global__ void __launch_bounds__(256, MINB) frame_plain_kernel(const FrameParams P,
                                                                    const __grid_constant__ arc_camera_uniforms cam) {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= P.width || y >= P.height) return;
+    const uint32_t y = P.row0 + blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.width || y >= P.row_end) return;
     const World& w = P.world;
     const f3 eye{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]};
     const f3 dir = camera_dir(cam, x, y, P.width, P.height);
@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(256, MINB) frame_persistent_kernel(const Frame
                     uint32_t px, py;
                     pixel_of(P, q, &px, &py);
                     pxy = px | (py << 16);
-                    if (px < P.width && py < P.height) {
+                    if (px < P.width && py < P.row_end) {
                         const f3 dir = camera_dir(cam, px, py, P.width, P.height);
                         if (ray_begin(s, cam, eye, dir, 0.0f, 250.0f, 0u, underwater)) {
                             phase = kPrimary;
@@ -460,7 +460,7 @@ cudaError_t launch_frame_t(const FrameParams& P, const arc_camera_uniforms& cam,
     if (cfg.variant == 0u) {
         const uint32_t bw = 8u, bh = cfg.block_threads / 8u;
         dim3 block(bw, bh);
-        dim3 grid((P.width + bw - 1u) / bw, (P.height + bh - 1u) / bh);
+        dim3 grid((P.width + bw - 1u) / bw, (P.row_end - P.row0 + bh - 1u) / bh);
         frame_plain_kernel<MINB><<<grid, block, 0, st>>>(P, cam);
         return cudaGetLastError();
     }

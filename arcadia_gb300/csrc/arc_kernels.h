@@ -36,6 +36,7 @@ struct FrameParams {
     uint32_t do_gi;
     Scratch* scratch;
     uint32_t tile_w, tile_h, tiles_x, queue_len, refill_threshold;
+    uint32_t row0, row_end;  // rows traced by this launch (a band of the frame; 0, height for all)
 };
 
 // One view of a batched launch: camera block, world slot, resolution, queue offset, outputs.

@@ -101,6 +101,8 @@ extern "C" int arc_trace_frame_noalloc(arc_ctx* c, uint32_t width, uint32_t heig
     P.tiles_x = (width + c->cfg.tile_w - 1u) / c->cfg.tile_w;
     P.queue_len = P.tiles_x * ((height + c->cfg.tile_h - 1u) / c->cfg.tile_h) * 32u;
     P.refill_threshold = c->cfg.refill_threshold;
+    P.row0 = 0u;
+    P.row_end = height;
     e = arc::launch_frame(P, c->cam, c->cfg, c->n_sm, c->stream);
     if (e != cudaSuccess) return fail(c, ARC_E_CUDA, std::string("frame launch: ") + cudaGetErrorString(e));
     if (n_gi_dev) {

@@ -127,7 +127,9 @@ int arc_trace_secondary(arc_ctx* ctx, uint32_t width, uint32_t height, const uin
 int arc_trace_secondary_dev(arc_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* gbuf_depth_mat,
                             const uint32_t* gbuf_norm_motion, arc_hit_record* gi_hits);
 /* Both passes in one launch: writes the G-buffer, primary hits and GI hits (any output may be NULL
- * except the G-buffer). n_gi_out (optional) receives the number of GI rays traced. */
+ * except the G-buffer). n_gi_out (optional) receives the number of GI rays traced. The host-buffer
+ * form traces the frame in horizontal bands and copies each band back while the next one traces
+ * (page-locked host buffers make those copies asynchronous). */
 int arc_trace_frame(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbuf_depth_mat, uint32_t* gbuf_norm_motion,
                     uint32_t* gbuf_albedo_ao, arc_hit_record* hits, arc_hit_record* gi_hits, uint64_t* n_gi_out);
 int arc_trace_frame_dev(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbuf_depth_mat,

@@ -326,3 +326,29 @@ def test_shadow_rays_di(orc, tracer, world_cache):
     assert 0.05 < vis.mean() < 0.95, vis.mean()
     plain = gpu_vis(w)  # same rays, no emitters in the world
     assert np.all(plain <= vis) and (vis > plain).sum() > 20
+
+
+def test_host_frame_into_pinned_buffers(tracer, world_cache):
+    """arc_trace_frame into page-locked host buffers (written by the kernel directly), into pageable
+    buffers (staged copies) and on the device: identical results."""
+    import torch
+
+    w = world_cache("c1_256")
+    W, H = 480, 270
+    cam = L.default_camera_for(L.SCENES["c1_256"], W, H, quality=L.quality_high(), frame_index=5)
+    _load(tracer, w, cam)
+    pageable = tracer.trace_frame()
+    pinned = [torch.zeros(m, dtype=torch.int32).pin_memory() for m in (W * H * 2, W * H * 2, W * H, W * H * 5, W * H * 5)]
+    import ctypes
+
+    from arcadia_gb300.native import lib
+
+    n = ctypes.c_uint64(0)
+    assert lib().arc_trace_frame(tracer.ctx, W, H, *[p.data_ptr() for p in pinned], ctypes.byref(n)) == 0
+    dev = [torch.zeros(m, dtype=torch.int32, device="cuda") for m in (W * H * 2, W * H * 2, W * H, W * H * 5, W * H * 5)]
+    tracer.trace_frame_dev(W, H, *[d.data_ptr() for d in dev])
+    tracer.synchronize()
+    for a, b, c in zip(pageable[:5], pinned, dev):
+        a = np.ascontiguousarray(a).view(np.int32).reshape(-1)
+        assert np.array_equal(a, b.numpy()) and np.array_equal(a, c.cpu().numpy())
+    assert n.value == pageable[5]
