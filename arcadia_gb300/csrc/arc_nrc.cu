@@ -383,19 +383,21 @@ __global__ void __launch_bounds__(128) train_kernel(const __half* __restrict__ w
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) my_loss += __shfl_down_sync(0xFFFFFFFFu, my_loss, o);
-    if (lane == 0) atomicAdd(loss_sum, my_loss);
+    if (lane == 0 && loss_sum) atomicAdd(loss_sum, my_loss);
 }
 
 // Adam on the FP32 masters, then refresh both FP16 layouts; the weight EMA (and its FP16 forward
-// layout, which inference reads) follows: ema = decay * ema + (1 - decay) * w.
+// layout, which inference reads) follows: ema = decay * ema + (1 - decay) * w. The consumed gradient
+// is cleared here, so the next step accumulates into zeros.
 __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
-                            const float* __restrict__ g, __half* __restrict__ w16, float* __restrict__ ema,
+                            float* __restrict__ g, __half* __restrict__ w16, float* __restrict__ ema,
                             __half* __restrict__ w16_ema, __half* __restrict__ wu, __half* __restrict__ wu_ema, float decay,
                             float lr, float c1, float c2, float inv_scale, const uint32_t* __restrict__ gate) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams || (gate && *gate == 0u)) return;
     const float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
     const float gi = g[i] * inv_scale;
+    g[i] = 0.0f;  // the gradient starts from zero for the next step (no separate clear)
     const float mi = b1 * m[i] + (1.0f - b1) * gi;
     const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
     m[i] = mi;
@@ -525,13 +527,25 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
         if (ok) phase ^= 1u;
         tc::fence_after();
     };
-    for (uint32_t tile = blockIdx.x; !fail && tile < tiles; tile += gridDim.x) {
+    // inputs of the CTA's first tile; each iteration then fetches the next tile's before its MMA chain
+    float vn[kIn];
+    uint32_t pn = 0u;
+    bool valid_n = false;
+    auto fetch = [&](uint32_t tile) {
         const uint32_t j = tile * 128u + tid;
-        const bool valid = j < n;
-        const uint32_t p = valid ? (list ? __ldg(&list[j]) : j) : 0u;
+        valid_n = tile < tiles && j < n;
+        pn = valid_n ? (list ? __ldg(&list[j]) : j) : 0u;
+#pragma unroll
+        for (int i = 0; i < kIn; ++i) vn[i] = valid_n ? __ldg(&in[(size_t)pn * kIn + i]) : 0.0f;
+    };
+    fetch(blockIdx.x);
+    for (uint32_t tile = blockIdx.x; !fail && tile < tiles; tile += gridDim.x) {
+        const bool valid = valid_n;
+        const uint32_t p = pn;
         float v[kIn];
 #pragma unroll
-        for (int i = 0; i < kIn; ++i) v[i] = valid ? __ldg(&in[(size_t)p * kIn + i]) : 0.0f;
+        for (int i = 0; i < kIn; ++i) v[i] = vn[i];
+        fetch(tile + gridDim.x);
         // layer 1, first half: features 0..111 = inputs 0..3 and the first 16 features of input 4
         uint32_t h[12];
         uint4 keep;
@@ -853,7 +867,7 @@ __global__ void __launch_bounds__(128, 1) train_tc_kernel(const __half* __restri
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) my_loss += __shfl_down_sync(0xFFFFFFFFu, my_loss, o);
-        if (lane == 0) atomicAdd(loss_sum, my_loss);
+        if (lane == 0 && loss_sum) atomicAdd(loss_sum, my_loss);
     } else if (tid == 0) {
         atomicOr(status, 0x80000000u);
         tc::mbar_wait(bar_m, phase, kTcBudget);  // an MMA still in flight finishes before TMEM is released
@@ -952,14 +966,16 @@ int launch_infer(arc_ctx* c, const float* inputs, const float* albedo, uint32_t 
     return ARC_OK;
 }
 
-// Loss-scaled gradient of one batch into d_nrc_grad (zeroed first) and its loss sum into d_nrc_loss.
-int launch_grad(arc_ctx* c, const float* inputs, const float* targets, uint32_t n, const uint32_t* gate) {
-    NRC_CK(cudaMemsetAsync(c->d_nrc_grad, 0, sizeof(float) * nrc::kParams, c->stream));
-    NRC_CK(cudaMemsetAsync(c->d_nrc_loss, 0, sizeof(float), c->stream));
+// Loss-scaled gradient of one batch added to d_nrc_grad (which the previous Adam step, or the
+// gradient query, left at zero); with want_loss the batch loss sum goes to d_nrc_loss.
+int launch_grad(arc_ctx* c, const float* inputs, const float* targets, uint32_t n, const uint32_t* gate,
+                bool want_loss = false) {
+    float* loss = want_loss ? c->d_nrc_loss : nullptr;
+    if (want_loss) NRC_CK(cudaMemsetAsync(c->d_nrc_loss, 0, sizeof(float), c->stream));
     if (c->nrc_train_path == 1) {
         const uint32_t blocks = std::min<uint32_t>((n + 127u) / 128u, (uint32_t)c->n_sm);
         nrc::train_tc_kernel<<<blocks, 128, nrc::kTtSmem, c->stream>>>(static_cast<const __half*>(c->d_nrc_wu), inputs, targets, n,
-                                                                         1.0f / (float)n, c->d_nrc_grad, c->d_nrc_loss, gate,
+                                                                         1.0f / (float)n, c->d_nrc_grad, loss, gate,
                                                                          c->d_status);
         NRC_CK(cudaGetLastError());
         return ARC_OK;
@@ -967,7 +983,7 @@ int launch_grad(arc_ctx* c, const float* inputs, const float* targets, uint32_t 
     const uint32_t tiles = (n + 63u) / 64u;
     const uint32_t blocks = std::min<uint32_t>(tiles, (uint32_t)c->n_sm);
     nrc::train_kernel<<<blocks, 128, (nrc::kAllHalves + nrc::kActHalves) * sizeof(__half), c->stream>>>(
-        static_cast<const __half*>(c->d_nrc_w16), inputs, targets, n, 1.0f / (float)n, c->d_nrc_grad, c->d_nrc_loss, gate);
+        static_cast<const __half*>(c->d_nrc_w16), inputs, targets, n, 1.0f / (float)n, c->d_nrc_grad, loss, gate);
     NRC_CK(cudaGetLastError());
     return ARC_OK;
 }
@@ -1071,9 +1087,10 @@ int arc_nrc_grad_dev(arc_ctx* c, const float* inputs, const float* targets, uint
     if (!c || !inputs || !targets || n == 0) return ARC_E_INVALID_ARG;
     int rc = ensure_nrc(c);
     if (rc) return rc;
-    if ((rc = launch_grad(c, inputs, targets, n, nullptr))) return rc;
+    if ((rc = launch_grad(c, inputs, targets, n, nullptr, true))) return rc;
     if (grad_out)
         NRC_CK(cudaMemcpyAsync(grad_out, c->d_nrc_grad, sizeof(float) * nrc::kParams, cudaMemcpyDeviceToDevice, c->stream));
+    NRC_CK(cudaMemsetAsync(c->d_nrc_grad, 0, sizeof(float) * nrc::kParams, c->stream));  // no step consumes it
     return ARC_OK;
 }
 
@@ -1081,7 +1098,7 @@ int arc_nrc_train_step_dev(arc_ctx* c, const float* inputs, const float* targets
     if (!c || !inputs || !targets || n == 0) return ARC_E_INVALID_ARG;
     int rc = ensure_nrc(c);
     if (rc) return rc;
-    if ((rc = launch_grad(c, inputs, targets, n, nullptr)) || (rc = launch_adam(c, lr, nullptr))) return rc;
+    if ((rc = launch_grad(c, inputs, targets, n, nullptr, loss_host != nullptr)) || (rc = launch_adam(c, lr, nullptr))) return rc;
     if (loss_host) {
         float l = 0.0f;
         NRC_CK(cudaMemcpyAsync(&l, c->d_nrc_loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));

@@ -494,20 +494,23 @@ __global__ void onebounce_kernel(const World w, const __grid_constant__ arc_came
 }
 
 // NRC training samples from the compacted GI hit list, stratified: sample i takes list entry
-// floor((i + phase) n_valid / n_samples) (phase in [0, 1) from the seed), so the threads of a warp trace
-// neighbouring points (the list is in screen-tile order) and every point is covered evenly. Two adjacent
-// lanes share a sample: the even lane traces the sun term, the odd lane the sky term, and a shuffle
-// sums them. Sample i is stored at slot (i mod steps) * (n_samples / steps) + i / steps, so each of the
+// floor((i + phase) n_valid / n_samples) (phase in [0, 1) from the seed), so neighbouring samples are
+// neighbouring points (the list is in screen-tile order) and every point is covered evenly. A block of
+// 4 warps takes 64 samples: warps 0 and 2 trace the sun term of samples 0..31 and 32..63, warps 1 and 3
+// the sky term of the same samples (each warp follows one traversal path), and shared memory sums
+// them. Sample i is stored at slot (i mod steps) * (n_samples / steps) + i / steps, so each of the
 // `steps` training slices spans the whole frame. Target: the 1-spp estimator with albedo 1.
-__global__ void train_samples_list_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam,
-                                          const uint32_t* __restrict__ list, const unsigned long long* __restrict__ n_valid,
-                                          const float* __restrict__ pos, const float* __restrict__ nrm,
-                                          const float* __restrict__ nrc_in, uint32_t seed, uint32_t n_samples, uint32_t steps,
-                                          float* __restrict__ train_in, float* __restrict__ train_t, uint32_t* __restrict__ gate) {
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t i = tid >> 1, part = tid & 1u;
+__global__ void __launch_bounds__(128) train_samples_list_kernel(
+    const World w, const __grid_constant__ arc_camera_uniforms cam, const uint32_t* __restrict__ list,
+    const unsigned long long* __restrict__ n_valid, const float* __restrict__ pos, const float* __restrict__ nrm,
+    const float* __restrict__ nrc_in, uint32_t seed, uint32_t n_samples, uint32_t steps, float* __restrict__ train_in,
+    float* __restrict__ train_t, uint32_t* __restrict__ gate) {
+    __shared__ float s_sun[64][3];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t pair = warp >> 1, part = warp & 1u;  // part 0: sun, 1: sky
+    const uint32_t i = blockIdx.x * 64u + pair * 32u + lane;
     const unsigned long long nv = *n_valid;
-    if (tid == 0) *gate = nv ? n_samples : 0u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *gate = nv ? n_samples : 0u;
     if (!nv) return;  // uniform over the grid
     const bool valid = i < n_samples;
     f3 l{0.0f, 0.0f, 0.0f};
@@ -519,14 +522,21 @@ __global__ void train_samples_list_kernel(const World w, const __grid_constant__
         const f3 x{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]}, n{nrm[3 * p], nrm[3 * p + 1], nrm[3 * p + 2]};
         l = part ? onebounce_sky(w, cam, x, n, pcg_hash(i ^ pcg_hash(seed ^ 0xB5297A4Du))) : onebounce_sun(w, cam, x, n);
     }
-    l.x += __shfl_xor_sync(0xFFFFFFFFu, l.x, 1);
-    l.y += __shfl_xor_sync(0xFFFFFFFFu, l.y, 1);
-    l.z += __shfl_xor_sync(0xFFFFFFFFu, l.z, 1);
-    if (!valid || part) return;
+    const uint32_t k = pair * 32u + lane;
+    if (part == 0u) {
+        s_sun[k][0] = l.x;
+        s_sun[k][1] = l.y;
+        s_sun[k][2] = l.z;
+    }
+    __syncthreads();
+    if (!valid || part == 0u) return;
+    l.x += s_sun[k][0];
+    l.y += s_sun[k][1];
+    l.z += s_sun[k][2];
     const uint32_t per = n_samples / steps;
     const size_t slot = (size_t)(i % steps) * per + i / steps;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) train_in[slot * 9 + k] = nrc_in[(size_t)p * 9 + k];
+    for (int q = 0; q < 9; ++q) train_in[slot * 9 + q] = nrc_in[(size_t)p * 9 + q];
     train_t[3 * slot] = l.x;
     train_t[3 * slot + 1] = l.y;
     train_t[3 * slot + 2] = l.z;
@@ -646,7 +656,7 @@ int arc_gi_points_dev(arc_ctx* c, uint32_t width, uint32_t height, const uint32_
 int arc_launch_train_samples_list(arc_ctx* c, const uint32_t* list, const unsigned long long* n_valid, const float* pos,
                                   const float* nrm, const float* nrc_in, uint32_t seed, uint32_t n_samples, uint32_t steps,
                                   float* train_in, float* train_t, uint32_t* gate) {
-    arc::train_samples_list_kernel<<<(2u * n_samples + 127u) / 128u, 128, 0, c->stream>>>(
+    arc::train_samples_list_kernel<<<(n_samples + 63u) / 64u, 128, 0, c->stream>>>(
         c->world(), c->cam, list, n_valid, pos, nrm, nrc_in, seed, n_samples, steps, train_in, train_t, gate);
     return launch_check(c, "train_samples_list_kernel");
 }
