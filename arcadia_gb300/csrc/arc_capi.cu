@@ -154,6 +154,33 @@ int arc_ctx_stage(arc_ctx* c, size_t bytes, void** out) {
     return ARC_OK;
 }
 
+int arc_ctx_reserve_surface(arc_ctx* c, size_t entries) {
+    if (c->surf_cap >= entries && c->d_surf_count) return ARC_OK;
+    ARC_CK(c, cudaStreamSynchronize(c->stream));
+    if (c->copy_stream)
+        for (int i = 0; i < arc_ctx::kMaxBands; ++i) ARC_CK(c, cudaStreamSynchronize(c->band_stream[i]));
+    cudaFree(c->d_surf);
+    c->d_surf = nullptr;
+    c->surf_cap = 0;
+    if (!c->d_surf_count) ARC_CK(c, cudaMalloc((void**)&c->d_surf_count, sizeof(uint32_t) * arc_ctx::kMaxBands));
+    ARC_CK(c, cudaMalloc((void**)&c->d_surf, sizeof(arc::SurfaceEntry) * std::max<size_t>(entries, 1)));
+    c->surf_cap = entries;
+    return ARC_OK;
+}
+
+bool arc_pools_have_surface_mats(const arc_node64* nodes, uint32_t n_nodes, const arc_brick64* bricks, uint32_t n_bricks) {
+    for (uint32_t i = 0; i < n_nodes; ++i) {
+        const uint32_t m = nodes[i].lod_payload >> 24;
+        if (m == arc::kMatWaterCrystal || m == arc::kMatMirrorChrome) return true;
+    }
+    // a zero byte in w ^ 0x12121212 (0x1C1C1C1C) is a material-18 (28) voxel
+    auto has_zero_byte = [](uint32_t v) { return ((v - 0x01010101u) & ~v & 0x80808080u) != 0u; };
+    for (uint32_t i = 0; i < n_bricks; ++i)
+        for (uint32_t w : bricks[i].packed_materials)
+            if (has_zero_byte(w ^ 0x12121212u) || has_zero_byte(w ^ 0x1C1C1C1Cu)) return true;
+    return false;
+}
+
 extern "C" {
 
 int arc_create(int device, arc_ctx** out) {
@@ -228,6 +255,8 @@ int arc_destroy(arc_ctx* c) {
         cudaEventDestroy(c->copies_done);
         cudaEventDestroy(c->frame_start);
     }
+    cudaFree(c->d_surf);
+    cudaFree(c->d_surf_count);
     cudaFree(c->d_edit);
     cudaFree(c->d_edit_stage);
     cudaFreeHost(c->h_edit_stage);
@@ -340,6 +369,7 @@ int arc_upload_world(arc_ctx* c, const uint32_t grid[3], const uint32_t* roots, 
     c->n_bricks = std::max<uint32_t>(n_bricks, 1u);
     c->cap_bricks = (uint32_t)cap_bricks;
     c->have_world = true;
+    c->surface_mats[0] = arc_pools_have_surface_mats(nodes, n_nodes, bricks, n_bricks);
     if ((rc = arc_edit_reset(c))) return rc;
     return arc_ctx_sync_world_table(c);
 }
@@ -382,6 +412,7 @@ int arc_upload_world_slot(arc_ctx* c, uint32_t slot, const uint32_t grid[3], con
     sl.n_nodes = n_nodes;
     sl.n_bricks = nb;
     sl.valid = true;
+    c->surface_mats[slot] = arc_pools_have_surface_mats(nodes, n_nodes, bricks, n_bricks);
     return arc_ctx_sync_world_table(c);
 }
 
@@ -405,7 +436,15 @@ int arc_apply_patch(arc_ctx* c, uint32_t chunk, uint32_t new_root, uint32_t node
     ARC_CK(c, cudaStreamSynchronize(c->stream));
     c->n_nodes = node_limit;
     c->n_bricks = brick_limit;
+    if (arc_pools_have_surface_mats(nodes, n_nodes, bricks, n_bricks)) c->surface_mats[0] = true;
     return arc_ctx_sync_world_table(c);
+}
+
+int arc_reserve_surface_list(arc_ctx* c, uint64_t max_pixels) {
+    if (!c) return ARC_E_INVALID_ARG;
+    if (max_pixels == 0 || max_pixels > (1ull << 32)) return set_err(c, ARC_E_INVALID_ARG, "max_pixels must be in [1, 2^32]");
+    ARC_CK(c, cudaSetDevice(c->device));
+    return arc_ctx_reserve_surface(c, (size_t)max_pixels);
 }
 
 int arc_set_camera(arc_ctx* c, const arc_camera_uniforms* cam) {
@@ -455,10 +494,31 @@ static arc::FrameParams frame_params(arc_ctx* c, uint32_t width, uint32_t height
     return P;
 }
 
+static bool cam_underwater(const arc_camera_uniforms& cam) { return (cam.point_light_count[1] & 0xFFFFu) != 0u; }
+
+// Surface list for the rows of P (the listed hits are shaded after the frame kernel): none when the
+// world holds no water or mirror voxel and the camera is above water. `count` is a counter that is
+// zero when the launch starts.
+static int surface_prepare(arc_ctx* c, arc::FrameParams& P, uint32_t* count) {
+    P.surf = nullptr;
+    P.surf_count = nullptr;
+    P.surf_cap = 0;
+    if (!c->surface_mats[0] && !cam_underwater(c->cam)) return ARC_OK;
+    int rc = arc_ctx_reserve_surface(c, (size_t)P.width * P.height);
+    if (rc) return rc;
+    P.surf = c->d_surf + (size_t)P.row0 * P.width;
+    P.surf_cap = (P.row_end - P.row0) * P.width;
+    P.surf_count = count;
+    return ARC_OK;
+}
+
 static int run_frame(arc_ctx* c, arc::FrameParams& P) {
+    int rc = surface_prepare(c, P, &c->d_scratch->surf_count);
+    if (rc) return rc;
     ARC_CK(c, cudaMemsetAsync(c->d_scratch, 0, sizeof(Scratch), c->stream));
     ARC_CK(c, cudaEventRecord(c->ev0, c->stream));
     ARC_CK(c, arc::launch_frame(P, c->cam, c->cfg, c->n_sm, c->stream));
+    ARC_CK(c, arc::launch_surface(P, c->cam, c->n_sm, c->stream));
     ARC_CK(c, cudaEventRecord(c->ev1, c->stream));
     c->timing_pending = true;
     return ARC_OK;
@@ -550,6 +610,8 @@ int arc_trace_frame(arc_ctx* c, uint32_t width, uint32_t height, uint32_t* gdm, 
     if ((rc = check_dims(c, width, height))) return rc;
     if (!gdm || !gnm || !gaa) return set_err(c, ARC_E_INVALID_ARG, "null G-buffer");
     if ((rc = ensure_band_streams(c))) return rc;
+    const bool surf = c->surface_mats[0] || cam_underwater(c->cam);
+    if (surf && (rc = arc_ctx_reserve_surface(c, (size_t)width * height))) return rc;
     const size_t np = (size_t)width * height;
     void* host[5] = {gdm, gnm, gaa, hits, gi_hits};
     const size_t px_bytes[5] = {8, 8, 4, 20, 20};
@@ -575,6 +637,7 @@ int arc_trace_frame(arc_ctx* c, uint32_t width, uint32_t height, uint32_t* gdm, 
     const uint32_t n_bands =
         std::max<uint32_t>(1u, std::min<uint32_t>((uint32_t)arc_ctx::kMaxBands, height / (concurrent ? 128u : 256u)));
     ARC_CK(c, cudaMemsetAsync(c->d_scratch, 0, sizeof(Scratch), c->stream));
+    if (surf) ARC_CK(c, cudaMemsetAsync(c->d_surf_count, 0, sizeof(uint32_t) * arc_ctx::kMaxBands, c->stream));
     ARC_CK(c, cudaEventRecord(c->ev0, c->stream));
     ARC_CK(c, cudaEventRecord(c->frame_start, c->stream));
     for (uint32_t b = 0; b < n_bands; ++b) {
@@ -587,7 +650,9 @@ int arc_trace_frame(arc_ctx* c, uint32_t width, uint32_t height, uint32_t* gdm, 
         } else if (b > 0) {
             ARC_CK(c, cudaMemsetAsync(&c->d_scratch->queue_head, 0, sizeof(uint32_t), c->stream));
         }
+        if ((rc = surface_prepare(c, P, c->d_surf_count + b))) return rc;
         ARC_CK(c, arc::launch_frame(P, c->cam, c->cfg, c->n_sm, st));
+        ARC_CK(c, arc::launch_surface(P, c->cam, c->n_sm, st));
         ARC_CK(c, cudaEventRecord(c->band_ev[b], st));
         ARC_CK(c, cudaStreamWaitEvent(c->copy_stream, c->band_ev[b], 0));
         for (int i = 0; i < 5; ++i) {
@@ -700,6 +765,21 @@ static int views_prepare(arc_ctx* c, const arc_view_desc* views, uint32_t n, uin
         c->views_graph = nullptr;
     }
     ARC_CK(c, cudaStreamSynchronize(c->stream));  // the previous launch has read the mirror
+    // surface list over every view's pixels when a view's world holds water or mirror voxels or a
+    // view's camera is under water
+    bool surf = false;
+    uint64_t n_px = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t slot = views[i].world_slot;
+        if (slot < (uint32_t)arc_ctx::kSlots && (c->surface_mats[slot] || cam_underwater(views[i].cam))) surf = true;
+        n_px += (uint64_t)views[i].width * views[i].height;
+    }
+    if (surf && n_px > 0xFFFFFFFFull) return set_err(c, ARC_E_CAPACITY, "batch above 2^32 pixels");
+    if (surf) {
+        int rc = arc_ctx_reserve_surface(c, (size_t)n_px);
+        if (rc) return rc;
+    }
+    c->views_surf_cap = surf ? (uint32_t)n_px : 0u;
     uint64_t q = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const arc_view_desc& d = views[i];
@@ -726,6 +806,12 @@ static int views_prepare(arc_ctx* c, const arc_view_desc* views, uint32_t n, uin
         v.gbuf_albedo_ao = d.gbuf_albedo_ao;
         v.hits = d.hits;
         v.gi_hits = d.gi_hits;
+        v.view_id = i;
+        if (surf) {
+            v.surf = c->d_surf;
+            v.surf_count = &c->d_scratch->surf_count;
+            v.surf_cap = (uint32_t)n_px;
+        }
         q += (uint64_t)v.tiles_x * ((d.height + c->cfg.tile_h - 1u) / c->cfg.tile_h) * 32u;
         if (q > (1ull << 31)) return set_err(c, ARC_E_CAPACITY, "batch exceeds 2^31 queue entries");
     }
@@ -746,6 +832,8 @@ static int views_enqueue(arc_ctx* c, uint32_t n, uint32_t queue_len, uint64_t* n
     ARC_CK(c, cudaMemsetAsync(c->d_scratch, 0, sizeof(arc::Scratch), c->stream));
     ARC_CK(c, cudaMemcpyAsync(c->d_views, c->h_views, sizeof(arc::ViewDev) * n, cudaMemcpyHostToDevice, c->stream));
     ARC_CK(c, arc::launch_views(V, c->cfg, c->n_sm, c->stream));
+    if (c->views_surf_cap)
+        ARC_CK(c, arc::launch_surface_views(V, c->d_surf, &c->d_scratch->surf_count, c->views_surf_cap, c->n_sm, c->stream));
     if (n_gi_dev)
         ARC_CK(c, cudaMemcpyAsync(n_gi_dev, &c->d_scratch->gi_rays, sizeof(uint64_t), cudaMemcpyDeviceToDevice, c->stream));
     return ARC_OK;
@@ -760,7 +848,8 @@ int arc_trace_views_dev(arc_ctx* c, const arc_view_desc* views, uint32_t n_views
         if ((rc = views_enqueue(c, n_views, queue_len, n_gi_dev))) return rc;
     } else {
         const bool same = c->views_exec && c->graph_n_views == n_views && c->graph_n_gi == n_gi_dev &&
-                          c->graph_queue_len == queue_len && memcmp(&c->graph_cfg, &c->cfg, sizeof c->cfg) == 0;
+                          c->graph_queue_len == queue_len && c->graph_surf_cap == c->views_surf_cap &&
+                          c->graph_surf_list == c->d_surf && memcmp(&c->graph_cfg, &c->cfg, sizeof c->cfg) == 0;
         if (!same) {
             if (c->views_exec) cudaGraphExecDestroy(c->views_exec);
             if (c->views_graph) cudaGraphDestroy(c->views_graph);
@@ -780,6 +869,8 @@ int arc_trace_views_dev(arc_ctx* c, const arc_view_desc* views, uint32_t n_views
             c->graph_n_views = n_views;
             c->graph_n_gi = n_gi_dev;
             c->graph_queue_len = queue_len;
+            c->graph_surf_cap = c->views_surf_cap;
+            c->graph_surf_list = c->d_surf;
             c->graph_cfg = c->cfg;
         }
         ARC_CK(c, cudaGraphLaunch(c->views_exec, c->stream));

@@ -92,6 +92,19 @@ struct arc_ctx {
     uint32_t nrc_batch_cap = 0;
     uint32_t* d_nrc_gate = nullptr;
 
+    // primary-pass surface list: hits that take the underwater / water / mirror branch, listed by the
+    // frame kernels and shaded by the surface kernel (entries for every pixel of the largest frame or
+    // batch so far; kMaxBands counters for the bands of a host-buffer frame). surface_mats[s] is set
+    // when world slot s may hold water or mirror voxels (upload, patch or edit); a frame without them
+    // and with the camera above water skips the list.
+    arc::SurfaceEntry* d_surf = nullptr;
+    uint32_t* d_surf_count = nullptr;
+    size_t surf_cap = 0;
+    bool surface_mats[kSlots] = {};
+    uint32_t views_surf_cap = 0;                   // list entries of the current view batch (0: no list)
+    uint32_t graph_surf_cap = 0;                   // ... and of the captured batch graph
+    arc::SurfaceEntry* graph_surf_list = nullptr;  // the list the captured graph writes
+
     arc_launch_config cfg{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // host-buffer frames: copy stream and per-band events (copies of a band overlap the next band)
@@ -122,4 +135,8 @@ extern "C" int arc_launch_train_samples_list(arc_ctx* c, const uint32_t* list, c
                                              uint32_t n_samples, uint32_t steps, float* train_in, float* train_t,
                                              uint32_t* gate);
 int arc_ctx_stage(arc_ctx* c, size_t bytes, void** out);
+// surface list of at least `entries` entries (frees and reallocates when smaller)
+int arc_ctx_reserve_surface(arc_ctx* c, size_t entries);
+// whether any word of the pools holds material 18 (water) or 28 (mirror) in a brick or a node payload
+bool arc_pools_have_surface_mats(const arc_node64* nodes, uint32_t n_nodes, const arc_brick64* bricks, uint32_t n_bricks);
 int arc_ctx_sync_world_table(arc_ctx* c);

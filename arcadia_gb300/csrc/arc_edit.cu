@@ -496,6 +496,8 @@ int arc_apply_edits(arc_ctx* c, const arc_edit_op* ops, uint32_t n_ops, uint32_t
             if (op.brick[0] >= gx * 64u || op.brick[1] >= gy * 64u || op.brick[2] >= gz * 64u)
                 return edit_err(c, ARC_E_INVALID_ARG, "recolour brick outside the world");
             pairs.emplace_back((op.brick[0] >> 6) + (op.brick[1] >> 6) * gx + (op.brick[2] >> 6) * gx * gy, k);
+            // water and mirror voxels take the primary pass's surface branches from now on
+            if (op.material == 18u || op.material == 28u) c->surface_mats[0] = true;
         } else if (op.kind == ARC_EDIT_CARVE) {
             if (!(op.radius > 0.0f && op.radius <= 16.0f)) return edit_err(c, ARC_E_INVALID_ARG, "carve radius must lie in (0, 16]");
             if (!(std::isfinite(op.center[0]) && std::isfinite(op.center[1]) && std::isfinite(op.center[2])))

@@ -14,7 +14,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cooperative_groups.h>
+
 #include "arc_kernels.h"
+#include "arc_surface.cuh"
 #include "arc_traverse.cuh"
 
 namespace arc {
@@ -44,9 +47,31 @@ __device__ __forceinline__ void store_no_ray(arc_hit_record* p) {
     q[4] = 0u;
 }
 
-// G-buffer words of one pixel (primary_gbuffer.wgsl:138-143 miss, 145-311 hit; no rigid bodies and
-// no water / mirror / underwater shading branches). Returns the packed depth and normal words the
-// GI ray is generated from.
+__device__ __forceinline__ uint32_t view_of(const FrameParams&) { return 0u; }
+__device__ __forceinline__ uint32_t view_of(const ViewDev& v) { return v.view_id; }
+
+// Appends a hit that takes a surface branch to the launch's list; the lanes of a warp that append
+// together claim their slots with one atomic.
+template <class Out>
+__device__ __forceinline__ void surface_append(const Out& P, size_t k, uint32_t x, uint32_t y, const HitInfo& h,
+                                               float hit_dist) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    uint32_t base = 0u;
+    if (g.thread_rank() == 0) base = atomicAdd(P.surf_count, g.size());
+    base = g.shfl(base, 0) + g.thread_rank();
+    if (base >= P.surf_cap) return;
+    uint4* e = reinterpret_cast<uint4*>(&P.surf[base]);
+    e[0] = make_uint4((uint32_t)k, x | (y << 16), (h.mat & 0xFFu) | (face_id(h.normal) << 8) | (view_of(P) << 16),
+                      h.voxel_hash);
+    e[1] = make_uint4(__float_as_uint(hit_dist), __float_as_uint(h.hit_pos_m.x), __float_as_uint(h.hit_pos_m.y),
+                      __float_as_uint(h.hit_pos_m.z));
+}
+
+// G-buffer words of one pixel (primary_gbuffer.wgsl:138-143 miss, 145-311 hit; no rigid bodies).
+// A hit on water under an above-water camera stores the up normal (primary_gbuffer.wgsl:286); hits
+// that take the underwater / water / mirror branch are listed for surface_kernel, which rewrites
+// their albedo. Returns the packed depth and normal words the GI ray is generated from.
 template <class Out>
 __device__ __forceinline__ void primary_store(const Out& P, const float4* __restrict__ palette,
                                               const arc_camera_uniforms& cam, uint32_t x, uint32_t y, f3 dir, bool hit,
@@ -87,8 +112,11 @@ __device__ __forceinline__ void primary_store(const Out& P, const float4* __rest
         mx = (ndx * 0.5f + 0.5f) - pu;
         my = (0.5f - ndy * 0.5f) - pv;
     }
+    const bool underwater = (cam.point_light_count[1] & 0xFFFFu) != 0u;
+    const f3 nrm = (h.mat == kMatWaterCrystal && !underwater) ? f3{0.0f, 1.0f, 0.0f} : h.normal;
+    if (P.surf && surface_special(cam, h.mat)) surface_append(P, k, x, y, h, hit_dist);
     float ox, oy;
-    oct_encode(h.normal, &ox, &oy);
+    oct_encode(nrm, &ox, &oy);
     const uint32_t n0 = pack2x16snorm(ox, oy);
     reinterpret_cast<uint2*>(P.gbuf_depth_mat)[k] = make_uint2(__float_as_uint(hit_dist), h.mat & 0xFFFFu);
     reinterpret_cast<uint2*>(P.gbuf_norm_motion)[k] = make_uint2(n0, pack2x16float(mx, my));
@@ -509,6 +537,76 @@ cudaError_t launch_views(const ViewsParams& V, const arc_launch_config& cfg, int
         case 4: return launch_views_t<4>(V, cfg, n_sm, st);
         default: return launch_views_t<1>(V, cfg, n_sm, st);
     }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Surface branches (primary_gbuffer.wgsl:163-295) over the listed hits
+// ------------------------------------------------------------------------------------------------
+
+__device__ __forceinline__ void surface_store(uint32_t* albedo_ao, uint32_t k, f3 a) {
+    // the AO byte stays; the albedo bytes are replaced
+    const uint32_t old = albedo_ao[k];
+    albedo_ao[k] = (old & 0xFF000000u) | (pack4x8unorm(a.x, a.y, a.z, 0.0f) & 0x00FFFFFFu);
+}
+
+__global__ void __launch_bounds__(128) surface_kernel(const FrameParams P, const __grid_constant__ arc_camera_uniforms cam) {
+    const uint32_t n = umin(*P.surf_count, P.surf_cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        SurfaceEntry e;
+        const uint4 a = reinterpret_cast<const uint4*>(&P.surf[i])[0];
+        const uint4 b = reinterpret_cast<const uint4*>(&P.surf[i])[1];
+        e.k = a.x;
+        e.xy = a.y;
+        e.mat_face_view = a.z;
+        e.hash = a.w;
+        e.hit_dist = __uint_as_float(b.x);
+        e.hp[0] = __uint_as_float(b.y);
+        e.hp[1] = __uint_as_float(b.z);
+        e.hp[2] = __uint_as_float(b.w);
+        const f3 dir = camera_dir(cam, e.xy & 0xFFFFu, e.xy >> 16, P.width, P.height);
+        surface_store(P.gbuf_albedo_ao, e.k, surface_shade(P.world, cam, dir, e));
+    }
+}
+
+__global__ void __launch_bounds__(128) surface_views_kernel(const ViewsParams V, const SurfaceEntry* __restrict__ surf,
+                                                            const uint32_t* __restrict__ count, uint32_t cap) {
+    const uint32_t n = umin(*count, cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        SurfaceEntry e;
+        const uint4 a = reinterpret_cast<const uint4*>(&surf[i])[0];
+        const uint4 b = reinterpret_cast<const uint4*>(&surf[i])[1];
+        e.k = a.x;
+        e.xy = a.y;
+        e.mat_face_view = a.z;
+        e.hash = a.w;
+        e.hit_dist = __uint_as_float(b.x);
+        e.hp[0] = __uint_as_float(b.y);
+        e.hp[1] = __uint_as_float(b.z);
+        e.hp[2] = __uint_as_float(b.w);
+        const uint32_t v = e.mat_face_view >> 16;
+        if (v >= V.n_views) continue;
+        const ViewDev& vd = V.views[v];
+        const f3 dir = camera_dir(vd.cam, e.xy & 0xFFFFu, e.xy >> 16, vd.width, vd.height);
+        surface_store(vd.gbuf_albedo_ao, e.k, surface_shade(V.worlds[vd.slot], vd.cam, dir, e));
+    }
+}
+
+static uint32_t surface_blocks(uint32_t cap, int n_sm) {
+    const uint32_t need = (cap + 127u) / 128u, most = (uint32_t)n_sm * 8u;
+    return need < 1u ? 1u : (need > most ? most : need);
+}
+
+cudaError_t launch_surface(const FrameParams& P, const arc_camera_uniforms& cam, int n_sm, cudaStream_t st) {
+    if (!P.surf || !P.surf_count) return cudaSuccess;
+    surface_kernel<<<surface_blocks(P.surf_cap, n_sm), 128, 0, st>>>(P, cam);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_surface_views(const ViewsParams& V, const SurfaceEntry* surf, const uint32_t* count, uint32_t cap,
+                                 int n_sm, cudaStream_t st) {
+    if (!surf || !count) return cudaSuccess;
+    surface_views_kernel<<<surface_blocks(cap, n_sm), 128, 0, st>>>(V, surf, count, cap);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_secondary(const FrameParams& P, const arc_camera_uniforms& cam, cudaStream_t st) {

@@ -10,10 +10,26 @@ namespace arc {
 
 struct World;  // arc_traverse.cuh
 
+// Materials with primary-pass surface branches (shaders/common/types.wgsl:15,17).
+constexpr uint32_t kMatWaterCrystal = 18u;
+constexpr uint32_t kMatMirrorChrome = 28u;
+
+// One hit that takes a surface branch (32 B): output pixel index, pixel coordinates, material,
+// face and view, voxel hash, hit distance and hit position of the primary ray (arc_surface.cuh).
+struct SurfaceEntry {
+    uint32_t k;
+    uint32_t xy;             // x | y << 16
+    uint32_t mat_face_view;  // mat | face << 8 | view << 16
+    uint32_t hash;
+    float hit_dist;
+    float hp[3];
+};
+static_assert(sizeof(SurfaceEntry) == 32, "SurfaceEntry is 32 B");
+
 // Per-launch scratch in device memory, cleared before every frame launch.
 struct Scratch {
     uint32_t queue_head;          // next queue entry of the persistent kernel
-    uint32_t pad;
+    uint32_t surf_count;          // surface-list entries of a single-band launch
     unsigned long long gi_rays;   // GI rays traced
 };
 
@@ -37,19 +53,25 @@ struct FrameParams {
     Scratch* scratch;
     uint32_t tile_w, tile_h, tiles_x, queue_len, refill_threshold;
     uint32_t row0, row_end;  // rows traced by this launch (a band of the frame; 0, height for all)
+    // Surface list of this launch's rows (null when no hit can take a water / mirror / underwater
+    // branch): hits that take one are appended here and shaded by launch_surface afterwards.
+    SurfaceEntry* surf;
+    uint32_t* surf_count;
+    uint32_t surf_cap;
 };
 
 // One view of a batched launch: camera block, world slot, resolution, queue offset, outputs.
 struct ViewDev {
     arc_camera_uniforms cam;
     uint32_t slot, width, height, tiles_x;
-    uint32_t queue_begin, pad0, pad1, pad2;
+    uint32_t queue_begin, view_id, surf_cap, pad2;
     uint32_t* gbuf_depth_mat;
     uint32_t* gbuf_norm_motion;
     uint32_t* gbuf_albedo_ao;
     arc_hit_record* hits;
     arc_hit_record* gi_hits;
-    void* pad3;
+    SurfaceEntry* surf;      // the batch's surface list (shared by all views; null when unused)
+    uint32_t* surf_count;
 };
 
 struct ViewsParams {
@@ -63,6 +85,10 @@ struct ViewsParams {
 cudaError_t launch_views(const ViewsParams& V, const arc_launch_config& cfg, int n_sm, cudaStream_t st);
 cudaError_t launch_frame(const FrameParams& P, const arc_camera_uniforms& cam, const arc_launch_config& cfg, int n_sm,
                          cudaStream_t st);
+// Surface branches of the hits a frame launch listed (one thread per entry, grid-stride).
+cudaError_t launch_surface(const FrameParams& P, const arc_camera_uniforms& cam, int n_sm, cudaStream_t st);
+cudaError_t launch_surface_views(const ViewsParams& V, const SurfaceEntry* surf, const uint32_t* count, uint32_t cap,
+                                 int n_sm, cudaStream_t st);
 cudaError_t launch_secondary(const FrameParams& P, const arc_camera_uniforms& cam, cudaStream_t st);
 cudaError_t launch_rays(const World& w, const arc_camera_uniforms& cam, const arc_ray* rays, uint32_t n, float max_dist_m,
                         uint32_t lod_bias, int ignore_water, arc_hit_record* hits, cudaStream_t st);

@@ -95,6 +95,55 @@ __device__ __forceinline__ float powi(float x, uint32_t n) {
     return result;
 }
 
+// 2^x: x = k + r with k = rint(x), |r| <= 1/2; 2^r = e^(r ln 2) from its Taylor series to degree 7
+// (remainder below 6e-9 relative) in Horner form; k enters through the exponent field. Arguments
+// below -126 give 0, above 127 are clamped to 127.
+__device__ __forceinline__ float exp2_canon(float x) {
+    if (!(x >= -126.0f)) return 0.0f;
+    x = fminf(x, 127.0f);
+    const float kf = rintf(x);
+    const float t = (x - kf) * 0.693147181f;
+    float p = 1.98412698e-4f;
+    p = p * t + 1.38888889e-3f;
+    p = p * t + 8.33333333e-3f;
+    p = p * t + 4.16666667e-2f;
+    p = p * t + 1.66666667e-1f;
+    p = p * t + 0.5f;
+    p = p * t + 1.0f;
+    p = p * t + 1.0f;
+    return p * __uint_as_float((uint32_t)((int)kf + 127) << 23);
+}
+
+// log2(x) for normal x > 0: x = m 2^e with m in [sqrt(1/2), sqrt(2)); log2 m = (2 / ln 2) atanh(s)
+// with s = (m - 1) / (m + 1), |s| <= 0.1716, and atanh(s) = s (1 + s^2/3 + s^4/5 + ... + s^10/11).
+__device__ __forceinline__ float log2_canon(float x) {
+    const uint32_t b = __float_as_uint(x);
+    int e = (int)((b >> 23) & 0xFFu) - 127;
+    float m = __uint_as_float((b & 0x7FFFFFu) | 0x3F800000u);
+    if (m > 1.41421356f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    const float s = __fdiv_rn(m - 1.0f, m + 1.0f);
+    const float s2 = s * s;
+    float p = 9.09090909e-2f;
+    p = p * s2 + 1.11111111e-1f;
+    p = p * s2 + 1.42857143e-1f;
+    p = p * s2 + 2.0e-1f;
+    p = p * s2 + 3.33333333e-1f;
+    p = p * s2 + 1.0f;
+    return (float)e + (s * p) * 2.88539008f;
+}
+
+// pow(x, y) = 2^(y log2 x) for the non-integer exponents of the shading code; x below the normal
+// range (including 0 and negatives) gives 0.
+__device__ __forceinline__ float pow_canon(float x, float y) {
+    if (!(x >= 1.17549435e-38f)) return 0.0f;
+    return exp2_canon(y * log2_canon(x));
+}
+
+__device__ __forceinline__ float exp_canon(float x) { return exp2_canon(x * 1.44269504f); }
+
 __device__ __forceinline__ int floor_log2(float x) { return (int)((__float_as_uint(x) >> 23) & 0xFFu) - 127; }
 
 __device__ __forceinline__ uint32_t f16_bits(float x) { return (uint32_t)__half_as_ushort(__float2half_rn(x)); }

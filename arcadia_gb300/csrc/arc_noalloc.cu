@@ -19,7 +19,11 @@
 //     and calls whose kernels overlap on the GPU (two streams, two contexts on one device) race on
 //     it, so callers must not run two of these calls concurrently on one device;
 //   - the first call on a device looks up the array's device address (cudaGetSymbolAddress) with
-//     that device current; make that first call before any stream capture.
+//     that device current; make that first call before any stream capture;
+//   - a world with water or mirror voxels, or a camera under water, needs the context's surface
+//     list (the hits that take those shading branches): reserve it beforehand with
+//     arc_reserve_surface_list for at least width x height pixels, else the call fails with
+//     ARC_E_CAPACITY.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -103,8 +107,17 @@ extern "C" int arc_trace_frame_noalloc(arc_ctx* c, uint32_t width, uint32_t heig
     P.refill_threshold = c->cfg.refill_threshold;
     P.row0 = 0u;
     P.row_end = height;
+    if (c->surface_mats[0] || (c->cam.point_light_count[1] & 0xFFFFu) != 0u) {
+        if (c->surf_cap < (size_t)width * height)
+            return fail(c, ARC_E_CAPACITY, "surface list not reserved for this frame size (arc_reserve_surface_list)");
+        P.surf = c->d_surf;
+        P.surf_cap = width * height;
+        P.surf_count = &static_cast<arc::Scratch*>(scratch)->surf_count;
+    }
     e = arc::launch_frame(P, c->cam, c->cfg, c->n_sm, c->stream);
     if (e != cudaSuccess) return fail(c, ARC_E_CUDA, std::string("frame launch: ") + cudaGetErrorString(e));
+    e = arc::launch_surface(P, c->cam, c->n_sm, c->stream);
+    if (e != cudaSuccess) return fail(c, ARC_E_CUDA, std::string("surface launch: ") + cudaGetErrorString(e));
     if (n_gi_dev) {
         e = cudaMemcpyAsync(n_gi_dev, &static_cast<arc::Scratch*>(scratch)->gi_rays, sizeof(uint64_t),
                             cudaMemcpyDeviceToDevice, c->stream);

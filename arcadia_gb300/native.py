@@ -63,6 +63,7 @@ SIGNATURES = {
     "arc_trace_frame": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp],
     "arc_trace_frame_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp],
     "arc_trace_frame_noalloc": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp],
+    "arc_reserve_surface_list": [_vp, _u64],
     "arc_trace_rays": [_vp, _vp, _u32, _f32, _u32, _i32, _vp],
     "arc_trace_rays_dev": [_vp, _vp, _u32, _f32, _u32, _i32, _vp],
     "arc_shadow_rays_dev": [_vp, _vp, _u32, _f32, _vp],
@@ -368,6 +369,10 @@ class Tracer:
     def trace_frame_noalloc(self, w, h, gdm, gnm, gaa, hits=0, gi=0, n_gi=0):
         self._check(lib().arc_trace_frame_noalloc(self._ctx, w, h, gdm, gnm, gaa, hits or None, gi or None,
                                                   n_gi or None), "arc_trace_frame_noalloc")
+
+    def reserve_surface_list(self, max_pixels: int):
+        """Surface list (water / mirror / underwater branches) for frames of up to max_pixels pixels."""
+        self._check(lib().arc_reserve_surface_list(self._ctx, int(max_pixels)), "arc_reserve_surface_list")
 
     def trace_primary_dev(self, w, h, gdm, gnm, gaa, hits=0):
         self._check(lib().arc_trace_primary_dev(self._ctx, w, h, gdm, gnm, gaa, hits or None), "arc_trace_primary_dev")

@@ -115,7 +115,12 @@ typedef struct arc_view_desc {
 
 /* Primary pass: G-buffer (gbuf_depth_mat and gbuf_norm_motion: 2 u32 per pixel, gbuf_albedo_ao:
  * 1 u32 per pixel, row-major width x height) and optional per-pixel hit records. Width and height
- * must match the camera's world_grid_dims.w. */
+ * must match the camera's world_grid_dims.w. As primary_raymarch (shaders/primary_gbuffer.wgsl:93-312)
+ * the G-buffer includes its surface branches: under an underwater camera (point_light_count.y & 0xFFFF)
+ * every hit's albedo takes caustics and absorption; above water, a water hit (material 18) traces a
+ * refraction ray (ray_distances.x) and, at grazing angles, a reflection ray, and stores the up normal;
+ * a mirror hit (material 28) traces a reflection ray (ray_distances.y). Those hits are shaded by a
+ * second kernel after the traversal kernel, in the same call. */
 int arc_trace_primary(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbuf_depth_mat,
                       uint32_t* gbuf_norm_motion, uint32_t* gbuf_albedo_ao, arc_hit_record* hits);
 int arc_trace_primary_dev(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbuf_depth_mat,
@@ -144,6 +149,11 @@ int arc_trace_frame_dev(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t*
 int arc_trace_frame_noalloc(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbuf_depth_mat,
                             uint32_t* gbuf_norm_motion, uint32_t* gbuf_albedo_ao, arc_hit_record* hits,
                             arc_hit_record* gi_hits, uint64_t* n_gi_dev);
+/* Reserves the surface list (32 B per pixel) of the water / mirror / underwater branches for frames
+ * (or view batches) of up to max_pixels pixels. The other entry points allocate it on first need;
+ * arc_trace_frame_noalloc requires it when the world holds water or mirror voxels or the camera is
+ * under water. No counterpart in the reference. */
+int arc_reserve_surface_list(arc_ctx* ctx, uint64_t max_pixels);
 /* Primary + GI rays of many views (several worlds, mixed resolutions) in one persistent launch; with
  * use_graph the launch is captured once into a CUDA graph and replayed (re-captured when the view
  * count, n_gi_dev or the launch configuration changes). Outputs per view as arc_trace_frame_dev.

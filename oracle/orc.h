@@ -97,6 +97,11 @@ float orc_shadow_vis_di(const orc_world* w, const arc_camera_uniforms* cam, cons
 float orc_shadow_vis(const orc_world* w, const arc_camera_uniforms* cam, const float origin_m[3], const float dir[3],
                      float max_dist_m, uint32_t* bytes);
 uint32_t orc_face_id(const float n[3]);
+/* primary-pass surface branches (orc_surface.c): 1 when the hit takes one (underwater camera, water,
+ * mirror); orc_surface_shade rewrites albedo (and, for water, the normal) of that hit. */
+int orc_surface_special(const arc_camera_uniforms* cam, uint32_t mat);
+void orc_surface_shade(const orc_world* w, const arc_camera_uniforms* cam, const float ray_dir[3],
+                       const orc_trace_out* p, float albedo[3], float normal[3], uint32_t* bytes);
 
 /* batch entry points (OpenMP over rays when threads > 1) */
 void orc_trace_rays(const orc_world* w, const arc_camera_uniforms* cam, const arc_ray* rays, uint32_t n, float max_dist_m,

@@ -115,6 +115,54 @@ static inline float orc_powi(float x, uint32_t n) {
     return result;
 }
 
+/* 2^x: x = k + r with k = rint(x), |r| <= 1/2; 2^r = e^(r ln 2) by its Taylor series to degree 7
+ * in Horner form; k enters through the exponent field. Below -126: 0; above 127: clamped. */
+static inline float orc_exp2(float x) {
+    if (!(x >= -126.0f)) return 0.0f;
+    x = fminf(x, 127.0f);
+    float kf = rintf(x);
+    float t = (x - kf) * 0.693147181f;
+    float p = 1.98412698e-4f;
+    p = p * t + 1.38888889e-3f;
+    p = p * t + 8.33333333e-3f;
+    p = p * t + 4.16666667e-2f;
+    p = p * t + 1.66666667e-1f;
+    p = p * t + 0.5f;
+    p = p * t + 1.0f;
+    p = p * t + 1.0f;
+    return p * orc_bitsf((uint32_t)((int32_t)kf + 127) << 23);
+}
+
+/* log2(x), normal x > 0: x = m 2^e, m in [sqrt(1/2), sqrt(2)); log2 m = (2/ln 2) atanh(s),
+ * s = (m-1)/(m+1), atanh(s) = s (1 + s^2/3 + ... + s^10/11). */
+static inline float orc_log2(float x) {
+    uint32_t b = orc_fbits(x);
+    int32_t e = (int32_t)((b >> 23) & 0xFFu) - 127;
+    float m = orc_bitsf((b & 0x7FFFFFu) | 0x3F800000u);
+    if (m > 1.41421356f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    float s = (m - 1.0f) / (m + 1.0f);
+    float s2 = s * s;
+    float p = 9.09090909e-2f;
+    p = p * s2 + 1.11111111e-1f;
+    p = p * s2 + 1.42857143e-1f;
+    p = p * s2 + 2.0e-1f;
+    p = p * s2 + 3.33333333e-1f;
+    p = p * s2 + 1.0f;
+    return (float)e + (s * p) * 2.88539008f;
+}
+
+/* pow(x, y) for the non-integer exponents of the shading code: 2^(y log2 x); x below the normal
+ * range (0, negatives) gives 0. */
+static inline float orc_pow(float x, float y) {
+    if (!(x >= 1.17549435e-38f)) return 0.0f;
+    return orc_exp2(y * orc_log2(x));
+}
+
+static inline float orc_exp(float x) { return orc_exp2(x * 1.44269504f); }
+
 /* floor(log2(x)) for normal x > 0, as the unbiased binary exponent. */
 static inline int32_t orc_floor_log2(float x) {
     uint32_t b = orc_fbits(x);

@@ -18,6 +18,17 @@ void orc_test_powi(const float* x, uint32_t n, uint32_t e, float* out) {
     for (uint32_t i = 0; i < n; ++i) out[i] = orc_powi(x[i], e);
 }
 
+void orc_test_exp2_log2(const float* x, uint32_t n, float* e2, float* l2) {
+    for (uint32_t i = 0; i < n; ++i) {
+        e2[i] = orc_exp2(x[i]);
+        l2[i] = x[i] > 0.0f ? orc_log2(x[i]) : 0.0f;
+    }
+}
+
+void orc_test_pow(const float* x, uint32_t n, float y, float* out) {
+    for (uint32_t i = 0; i < n; ++i) out[i] = orc_pow(x[i], y);
+}
+
 /* Dense (z, y, x) material volume of one chunk of a synthetic scene, by per-voxel evaluation. */
 void orc_test_scene_volume(const orc_scene_params* p, uint32_t cx, uint32_t cy, uint32_t cz, uint8_t* vol) {
     uint32_t wx = p->grid[0] * 256u, wz = p->grid[2] * 256u;

@@ -531,8 +531,8 @@ static void fill_hit_record(const orc_trace_out* r, float t_scale_m, arc_hit_rec
     h->depth_m = r->t_voxels * t_scale_m;
 }
 
-/* primary_raymarch (primary_gbuffer.wgsl:93-312) for pixels [x0,x1) x [y0,y1); no rigid bodies,
- * no water/mirror/underwater shading branches. */
+/* primary_raymarch (primary_gbuffer.wgsl:93-312) for pixels [x0,x1) x [y0,y1); no rigid bodies.
+ * The underwater / water / mirror shading branches are orc_surface_shade (orc_surface.c). */
 static void primary_pixel(const orc_world* w, const arc_camera_uniforms* cam, uint32_t x, uint32_t y, uint32_t W,
                           uint32_t H, uint32_t out[5], arc_hit_record* hit, uint32_t* bytes) {
     float d[3];
@@ -572,8 +572,10 @@ static void primary_pixel(const orc_world* w, const arc_camera_uniforms* cam, ui
         mx = (ndx * 0.5f + 0.5f) - pu;
         my = (0.5f - ndy * 0.5f) - pv;
     }
+    float nrm[3] = {r.normal[0], r.normal[1], r.normal[2]};
+    if (orc_surface_special(cam, r.mat_id)) orc_surface_shade(w, cam, d, &r, alb, nrm, bytes);
     float p[2];
-    oct_encode(r.normal, p);
+    oct_encode(nrm, p);
     out[0] = orc_fbits(hit_dist);
     out[1] = (r.mat_id & 0xFFFFu);
     out[2] = orc_pack2x16snorm(p[0], p[1]);

@@ -108,6 +108,8 @@ def lib():
         _lib.orc_test_sincos.argtypes = [vp, u32, vp, vp]
         _lib.orc_test_f16.argtypes = [vp, u32, vp]
         _lib.orc_test_powi.argtypes = [vp, u32, u32, vp]
+        _lib.orc_test_exp2_log2.argtypes = [vp, u32, vp, vp]
+        _lib.orc_test_pow.argtypes = [vp, u32, C.c_float, vp]
         _lib.orc_scene_heightmap.argtypes = [C.POINTER(_Scene), vp]
         _lib.orc_scene_voxel.argtypes = [C.POINTER(_Scene), vp, u32, u32, u32]
         _lib.orc_scene_voxel.restype = u32
@@ -385,6 +387,21 @@ def powi(x: np.ndarray, e: int) -> np.ndarray:
     x = np.ascontiguousarray(x, np.float32)
     out = np.zeros_like(x)
     lib().orc_test_powi(_p(x), len(x), e, _p(out))
+    return out
+
+
+def exp2_log2(x: np.ndarray):
+    """Canonical 2^x and log2(x) (log2 only where x > 0, else 0)."""
+    x = np.ascontiguousarray(x, np.float32)
+    e2, l2 = np.zeros_like(x), np.zeros_like(x)
+    lib().orc_test_exp2_log2(_p(x), len(x), _p(e2), _p(l2))
+    return e2, l2
+
+
+def pow_canon(x: np.ndarray, y: float) -> np.ndarray:
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros_like(x)
+    lib().orc_test_pow(_p(x), len(x), float(y), _p(out))
     return out
 
 

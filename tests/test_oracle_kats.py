@@ -210,6 +210,25 @@ def test_canonical_sincos_error_bound(orc):
     assert np.max(np.abs(c - np.cos(xd))) < 4e-7
 
 
+def test_canonical_exp2_log2_pow_error_bounds(orc):
+    x = np.linspace(-40.0, 40.0, 200001, dtype=np.float32)
+    e2, _ = orc.exp2_log2(x)
+    ref = np.exp2(x.astype(np.float64))
+    assert np.max(np.abs(e2 / ref - 1.0)) < 4e-7
+    assert orc.exp2_log2(np.float32([-127.0, -200.0]))[0].tolist() == [0.0, 0.0]
+    y = np.concatenate([np.linspace(1e-6, 4.0, 200001, dtype=np.float32), np.float32([1.0, 2.0, 0.5, 1e-30, 3e38])])
+    _, l2 = orc.exp2_log2(y)
+    err = np.abs(l2 - np.log2(y.astype(np.float64)))
+    assert np.max(err / np.maximum(np.abs(np.log2(y.astype(np.float64))), 1.0)) < 4e-7
+    assert l2[-5] == 0.0 and l2[-4] == 1.0 and l2[-3] == -1.0
+    p = np.linspace(0.0, 1.0, 100001, dtype=np.float32)
+    for e in (2.2, 2.5):
+        got = orc.pow_canon(p, e)
+        want = p.astype(np.float64) ** e
+        assert np.max(np.abs(got - want)) < 2e-6
+    assert orc.pow_canon(np.float32([0.0, -1.0]), 2.2).tolist() == [0.0, 0.0]
+
+
 def test_f16_packing_matches_ieee_rne(orc):
     rng = np.random.default_rng(7)
     x = np.concatenate([
