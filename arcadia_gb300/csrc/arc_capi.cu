@@ -829,6 +829,7 @@ static int views_enqueue(arc_ctx* c, uint32_t n, uint32_t queue_len, uint64_t* n
     V.tile_w = c->cfg.tile_w;
     V.tile_h = c->cfg.tile_h;
     V.refill_threshold = c->cfg.refill_threshold;
+    V.surf = c->views_surf_cap ? 1u : 0u;
     ARC_CK(c, cudaMemsetAsync(c->d_scratch, 0, sizeof(arc::Scratch), c->stream));
     ARC_CK(c, cudaMemcpyAsync(c->d_views, c->h_views, sizeof(arc::ViewDev) * n, cudaMemcpyHostToDevice, c->stream));
     ARC_CK(c, arc::launch_views(V, c->cfg, c->n_sm, c->stream));

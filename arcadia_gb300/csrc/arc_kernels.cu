@@ -69,10 +69,13 @@ __device__ __forceinline__ void surface_append(const Out& P, size_t k, uint32_t 
 }
 
 // G-buffer words of one pixel (primary_gbuffer.wgsl:138-143 miss, 145-311 hit; no rigid bodies).
-// A hit on water under an above-water camera stores the up normal (primary_gbuffer.wgsl:286); hits
-// that take the underwater / water / mirror branch are listed for surface_kernel, which rewrites
-// their albedo. Returns the packed depth and normal words the GI ray is generated from.
-template <class Out>
+// With SURF (the launch has a surface list: the world may hold water or mirror voxels, or the camera
+// is under water), a hit on water under an above-water camera stores the up normal
+// (primary_gbuffer.wgsl:286) and hits that take the underwater / water / mirror branch are listed
+// for surface_kernel, which rewrites their albedo. Without SURF no hit can take a branch and the
+// kernels carry none of that code. Returns the packed depth and normal words the GI ray is
+// generated from.
+template <bool SURF, class Out>
 __device__ __forceinline__ void primary_store(const Out& P, const float4* __restrict__ palette,
                                               const arc_camera_uniforms& cam, uint32_t x, uint32_t y, f3 dir, bool hit,
                                               const HitInfo& h, uint32_t* depth_word, uint32_t* normal_word) {
@@ -112,9 +115,11 @@ __device__ __forceinline__ void primary_store(const Out& P, const float4* __rest
         mx = (ndx * 0.5f + 0.5f) - pu;
         my = (0.5f - ndy * 0.5f) - pv;
     }
-    const bool underwater = (cam.point_light_count[1] & 0xFFFFu) != 0u;
-    const f3 nrm = (h.mat == kMatWaterCrystal && !underwater) ? f3{0.0f, 1.0f, 0.0f} : h.normal;
-    if (P.surf && surface_special(cam, h.mat)) surface_append(P, k, x, y, h, hit_dist);
+    f3 nrm = h.normal;
+    if constexpr (SURF) {
+        if (h.mat == kMatWaterCrystal && (cam.point_light_count[1] & 0xFFFFu) == 0u) nrm = f3{0.0f, 1.0f, 0.0f};
+        if (surface_special(cam, h.mat)) surface_append(P, k, x, y, h, hit_dist);
+    }
     float ox, oy;
     oct_encode(nrm, &ox, &oy);
     const uint32_t n0 = pack2x16snorm(ox, oy);
@@ -136,7 +141,7 @@ __device__ __forceinline__ void pixel_of(const FrameParams& P, uint32_t q, uint3
 // Frame kernels
 // ------------------------------------------------------------------------------------------------
 
-template <int MINB>
+template <int MINB, bool SURF>
 __global__ void __launch_bounds__(256, MINB) frame_plain_kernel(const FrameParams P,
                                                                    const __grid_constant__ arc_camera_uniforms cam) {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -162,7 +167,7 @@ __global__ void __launch_bounds__(256, MINB) frame_plain_kernel(const FrameParam
         if (gi_phase) break;
         if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
         uint32_t dw, nw;
-        primary_store(P, w.palette, cam, x, y, dir, r == kHit, h, &dw, &nw);
+        primary_store<SURF>(P, w.palette, cam, x, y, dir, r == kHit, h, &dw, &nw);
         if (!P.do_gi) return;
         if (!gi_setup(w, cam, x, y, P.width, P.height, dw, nw, &go, &gd)) {
             if (P.gi_hits) store_no_ray(&P.gi_hits[k]);
@@ -180,7 +185,7 @@ __global__ void __launch_bounds__(256, MINB) frame_plain_kernel(const FrameParam
 
 enum : uint32_t { kIdle = 0u, kPrimary = 1u, kGi = 2u };
 
-template <int MINB>
+template <int MINB, bool SURF>
 __global__ void __launch_bounds__(256, MINB) frame_persistent_kernel(const FrameParams P,
                                                                      const __grid_constant__ arc_camera_uniforms cam) {
     const World& w = P.world;
@@ -217,7 +222,7 @@ __global__ void __launch_bounds__(256, MINB) frame_persistent_kernel(const Frame
                         } else {
                             hit_init_miss(h, eye, dir, 250.0f);
                             uint32_t dw, nw;
-                            primary_store(P, w.palette, cam, px, py, dir, false, h, &dw, &nw);
+                            primary_store<SURF>(P, w.palette, cam, px, py, dir, false, h, &dw, &nw);
                             if (P.do_gi && P.gi_hits) store_no_ray(&P.gi_hits[(size_t)py * P.width + px]);
                         }
                     }
@@ -236,7 +241,7 @@ __global__ void __launch_bounds__(256, MINB) frame_persistent_kernel(const Frame
             const f3 dir = s.dir;
             if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
             uint32_t dw, nw;
-            primary_store(P, w.palette, cam, px, py, dir, r == kHit, h, &dw, &nw);
+            primary_store<SURF>(P, w.palette, cam, px, py, dir, r == kHit, h, &dw, &nw);
             phase = kIdle;
             if (P.do_gi) {
                 f3 go, gd;
@@ -329,7 +334,7 @@ __global__ void shadow_di_kernel(const World w, const __grid_constant__ arc_came
 // the concatenation of every view's 32-pixel tiles; a lane finds its view by binary search over the
 // views' queue offsets and reads that view's camera block and world from global memory (L1-cached),
 // so the per-ray work is exactly the single-view kernel's.
-template <int MINB>
+template <int MINB, bool SURF>
 __global__ void __launch_bounds__(256, MINB) views_persistent_kernel(const ViewsParams V) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt_mask = (1u << lane) - 1u;
@@ -370,7 +375,7 @@ __global__ void __launch_bounds__(256, MINB) views_persistent_kernel(const Views
                         } else {
                             hit_init_miss(h, eye, dir, 250.0f);
                             uint32_t dw, nw;
-                            primary_store(vd, V.worlds[vd.slot].palette, cam, px, py, dir, false, h, &dw, &nw);
+                            primary_store<SURF>(vd, V.worlds[vd.slot].palette, cam, px, py, dir, false, h, &dw, &nw);
                             if (vd.gi_hits) store_no_ray(&vd.gi_hits[(size_t)py * vd.width + px]);
                         }
                     }
@@ -394,7 +399,7 @@ __global__ void __launch_bounds__(256, MINB) views_persistent_kernel(const Views
             const f3 dir = s.dir;
             if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
             uint32_t dw, nw;
-            primary_store(vd, w.palette, cam, px, py, dir, r == kHit, h, &dw, &nw);
+            primary_store<SURF>(vd, w.palette, cam, px, py, dir, r == kHit, h, &dw, &nw);
             phase = kIdle;
             f3 go, gd;
             if (gi_setup(w, cam, px, py, vd.width, vd.height, dw, nw, &go, &gd)) {
@@ -423,7 +428,7 @@ __global__ void __launch_bounds__(256, MINB) views_persistent_kernel(const Views
 // One thread per queue slot over many views: the slot's view by binary search, its pixel by the same
 // 32-pixel tile mapping as the persistent kernel (a warp traces one tile), then the single-view plain
 // kernel's work: one traversal call site for the primary ray and the pixel's GI ray.
-template <int MINB>
+template <int MINB, bool SURF>
 __global__ void __launch_bounds__(256, MINB) views_plain_kernel(const ViewsParams V) {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     bool gi_ray = false;
@@ -462,7 +467,7 @@ __global__ void __launch_bounds__(256, MINB) views_plain_kernel(const ViewsParam
                 }
                 if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
                 uint32_t dw, nw;
-                primary_store(vd, w.palette, cam, px, py, dir, r == kHit, h, &dw, &nw);
+                primary_store<SURF>(vd, w.palette, cam, px, py, dir, r == kHit, h, &dw, &nw);
                 if (!gi_setup(w, cam, px, py, vd.width, vd.height, dw, nw, &go, &gd)) {
                     if (vd.gi_hits) store_no_ray(&vd.gi_hits[k]);
                     done = true;
@@ -489,17 +494,21 @@ cudaError_t launch_frame_t(const FrameParams& P, const arc_camera_uniforms& cam,
         const uint32_t bw = 8u, bh = cfg.block_threads / 8u;
         dim3 block(bw, bh);
         dim3 grid((P.width + bw - 1u) / bw, (P.row_end - P.row0 + bh - 1u) / bh);
-        frame_plain_kernel<MINB><<<grid, block, 0, st>>>(P, cam);
+        if (P.surf) frame_plain_kernel<MINB, true><<<grid, block, 0, st>>>(P, cam);
+        else frame_plain_kernel<MINB, false><<<grid, block, 0, st>>>(P, cam);
         return cudaGetLastError();
     }
     int per_sm = (int)cfg.blocks_per_sm;
     if (per_sm <= 0) {
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, frame_persistent_kernel<MINB>,
-                                                                      (int)cfg.block_threads, 0);
+        cudaError_t e = P.surf ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, frame_persistent_kernel<MINB, true>,
+                                                                               (int)cfg.block_threads, 0)
+                               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, frame_persistent_kernel<MINB, false>,
+                                                                               (int)cfg.block_threads, 0);
         if (e != cudaSuccess) return e;
         if (per_sm <= 0) per_sm = 1;
     }
-    frame_persistent_kernel<MINB><<<n_sm * per_sm, cfg.block_threads, 0, st>>>(P, cam);
+    if (P.surf) frame_persistent_kernel<MINB, true><<<n_sm * per_sm, cfg.block_threads, 0, st>>>(P, cam);
+    else frame_persistent_kernel<MINB, false><<<n_sm * per_sm, cfg.block_threads, 0, st>>>(P, cam);
     return cudaGetLastError();
 }
 
@@ -516,17 +525,22 @@ cudaError_t launch_frame(const FrameParams& P, const arc_camera_uniforms& cam, c
 template <int MINB>
 cudaError_t launch_views_t(const ViewsParams& V, const arc_launch_config& cfg, int n_sm, cudaStream_t st) {
     if (cfg.variant == 0u) {
-        views_plain_kernel<MINB><<<(V.queue_len + cfg.block_threads - 1u) / cfg.block_threads, cfg.block_threads, 0, st>>>(V);
+        const uint32_t blocks = (V.queue_len + cfg.block_threads - 1u) / cfg.block_threads;
+        if (V.surf) views_plain_kernel<MINB, true><<<blocks, cfg.block_threads, 0, st>>>(V);
+        else views_plain_kernel<MINB, false><<<blocks, cfg.block_threads, 0, st>>>(V);
         return cudaGetLastError();
     }
     int per_sm = (int)cfg.blocks_per_sm;
     if (per_sm <= 0) {
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, views_persistent_kernel<MINB>,
-                                                                      (int)cfg.block_threads, 0);
+        cudaError_t e = V.surf ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, views_persistent_kernel<MINB, true>,
+                                                                               (int)cfg.block_threads, 0)
+                               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, views_persistent_kernel<MINB, false>,
+                                                                               (int)cfg.block_threads, 0);
         if (e != cudaSuccess) return e;
         if (per_sm <= 0) per_sm = 1;
     }
-    views_persistent_kernel<MINB><<<n_sm * per_sm, cfg.block_threads, 0, st>>>(V);
+    if (V.surf) views_persistent_kernel<MINB, true><<<n_sm * per_sm, cfg.block_threads, 0, st>>>(V);
+    else views_persistent_kernel<MINB, false><<<n_sm * per_sm, cfg.block_threads, 0, st>>>(V);
     return cudaGetLastError();
 }
 

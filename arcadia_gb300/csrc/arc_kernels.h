@@ -80,6 +80,7 @@ struct ViewsParams {
     const World* worlds;
     Scratch* scratch;
     uint32_t queue_len, tile_w, tile_h, refill_threshold;
+    uint32_t surf;  // 1 when the views carry a surface list (the kernels list surface-branch hits)
 };
 
 cudaError_t launch_views(const ViewsParams& V, const arc_launch_config& cfg, int n_sm, cudaStream_t st);
