@@ -26,6 +26,7 @@ CU_UNITS = {
     "arc_nrc.cu": [],
     "arc_noalloc.cu": CANONICAL,
     "arc_edit.cu": CANONICAL,
+    "arc_restir.cu": CANONICAL,
 }
 CPP_UNITS = ["arc_world.cpp"]
 

@@ -535,10 +535,20 @@ __device__ __forceinline__ float probe_emissive(const World& w, const arc_camera
     return (em.x * 0.333f + em.y * 0.333f) + em.z * 0.333f;
 }
 
+// What the GI ray setup of a hit pixel also yields for the temporal pass: primary hit point and
+// normal, the smoothed hemisphere normal, the noise pair and whether the emissive probe chose the
+// candidate direction.
+struct GiSetup {
+    float hit_dist;
+    f3 hit_pos, normal, smooth_n;
+    float u1, u2;
+    bool guided;
+};
+
 // GI secondary ray of a hit pixel from its G-buffer words (lighting_restir_gi.wgsl:69-87, 195-209).
-__device__ __forceinline__ bool gi_setup(const World& w, const arc_camera_uniforms& cam, uint32_t x, uint32_t y,
-                                         uint32_t W, uint32_t H, uint32_t depth_word, uint32_t normal_word, f3* origin,
-                                         f3* dir) {
+__device__ __forceinline__ bool gi_setup_full(const World& w, const arc_camera_uniforms& cam, uint32_t x, uint32_t y,
+                                              uint32_t W, uint32_t H, uint32_t depth_word, uint32_t normal_word,
+                                              f3* origin, f3* dir, GiSetup* g) {
     const float hit_dist = __uint_as_float(depth_word);
     if (hit_dist >= 1e4f) return false;
     const f3 rd = camera_dir(cam, x, y, W, H);
@@ -556,10 +566,43 @@ __device__ __forceinline__ bool gi_setup(const World& w, const arc_camera_unifor
     const f3 cd = cosine_sample(fractf(u1 + 0.5f), fractf(u2 + 0.381966f), sn, bt, bb);
     const float em_near = probe_emissive(w, cam, hp, cd, 1.25f);
     const float em_mid = probe_emissive(w, cam, hp, cd, 3.0f);
-    if (fmaxf(em_near, em_mid) > 0.25f) bd = cd;
+    const bool guided = fmaxf(em_near, em_mid) > 0.25f;
+    if (guided) bd = cd;
     *origin = add3(hp, mul3s(n, 0.10f));
     *dir = bd;
+    g->hit_dist = hit_dist;
+    g->hit_pos = hp;
+    g->normal = n;
+    g->smooth_n = sn;
+    g->u1 = u1;
+    g->u2 = u2;
+    g->guided = guided;
     return true;
+}
+
+__device__ __forceinline__ bool gi_setup(const World& w, const arc_camera_uniforms& cam, uint32_t x, uint32_t y,
+                                         uint32_t W, uint32_t H, uint32_t depth_word, uint32_t normal_word, f3* origin,
+                                         f3* dir) {
+    GiSetup g;
+    return gi_setup_full(w, cam, x, y, W, H, depth_word, normal_word, origin, dir, &g);
+}
+
+// lod_payload of the node whose child cells have span 1 << shift on the way from the chunk root to
+// voxel (vx, vy, vz): the node a traversal hit at that cell read its payload from (leaf, uniform
+// leaf or LOD cell). The voxel must lie in a non-empty chunk.
+__device__ __forceinline__ uint32_t lod_payload_at(const World& w, const arc_camera_uniforms& cam, uint32_t vx, uint32_t vy,
+                                                   uint32_t vz, uint32_t shift) {
+    const uint32_t gx = cam.world_grid_dims[0], gy = cam.world_grid_dims[1];
+    const uint32_t root_idx = load_root(w, (vx >> 8) + (vy >> 8) * gx + (vz >> 8) * gx * gy);
+    if (root_idx == ARC_EMPTY_CHUNK) return 0u;
+    uint4 node = load_node(w, root_idx);
+    const uint32_t lx = vx & 255u, ly = vy & 255u, lz = vz & 255u;
+    for (uint32_t s = 6u; s > shift && !(node.z & ARC_IS_LEAF_FLAG); s -= 2u) {
+        const uint32_t b = (((lz >> s) & 3u) << 4) | (((ly >> s) & 3u) << 2) | ((lx >> s) & 3u);
+        if (!has_child(node.x, node.y, b)) break;
+        node = load_node(w, child_index(node, b));
+    }
+    return node.w;
 }
 
 }  // namespace arc

@@ -60,13 +60,26 @@ VIEW_DTYPE = np.dtype(
         ("gi_hits", "<u8"),
     ]
 )
+RESERVOIR_DTYPE = np.dtype(
+    [("sample_pos", "<f4", (3,)), ("norm_m_flags", "<u4"), ("lo_rg", "<u4"), ("lo_b_w", "<u4"), ("primary_depth", "<f4"),
+     ("shadow_vis_m", "<u4")]
+)
+
+
+def empty_reservoirs(n: int) -> np.ndarray:
+    """create_empty_reservoir (types.wgsl:187-196) for n pixels."""
+    r = np.zeros(n, RESERVOIR_DTYPE)
+    r["primary_depth"] = 1e5
+    return r
+
+
 EDIT_CARVE = 0
 EDIT_RECOLOR = 1
 EDIT_DTYPE = np.dtype(
     [("kind", "<u4"), ("material", "<u4"), ("brick", "<u4", (3,)), ("center", "<f4", (3,)), ("radius", "<f4"),
      ("pad", "<u4")]
 )
-assert EDIT_DTYPE.itemsize == 40
+assert EDIT_DTYPE.itemsize == 40 and RESERVOIR_DTYPE.itemsize == 32
 assert VIEW_DTYPE.itemsize == 536
 assert NODE_DTYPE.itemsize == 16 and BRICK_DTYPE.itemsize == 64 and MATERIAL_DTYPE.itemsize == 32
 assert CAMERA_DTYPE.itemsize == 480 and SHARC_SLOT_DTYPE.itemsize == 16

@@ -64,6 +64,7 @@ SIGNATURES = {
     "arc_trace_frame_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp],
     "arc_trace_frame_noalloc": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp],
     "arc_reserve_surface_list": [_vp, _u64],
+    "arc_restir_gi_temporal_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp],
     "arc_trace_rays": [_vp, _vp, _u32, _f32, _u32, _i32, _vp],
     "arc_trace_rays_dev": [_vp, _vp, _u32, _f32, _u32, _i32, _vp],
     "arc_shadow_rays_dev": [_vp, _vp, _u32, _f32, _vp],
@@ -369,6 +370,11 @@ class Tracer:
     def trace_frame_noalloc(self, w, h, gdm, gnm, gaa, hits=0, gi=0, n_gi=0):
         self._check(lib().arc_trace_frame_noalloc(self._ctx, w, h, gdm, gnm, gaa, hits or None, gi or None,
                                                   n_gi or None), "arc_trace_frame_noalloc")
+
+    def restir_gi_temporal_dev(self, w, h, gdm, gnm, gi_hits, res_in, res_out, radiance=0):
+        """ReSTIR GI temporal pass over a traced frame (device pointers; reservoirs of layout.RESERVOIR_DTYPE)."""
+        self._check(lib().arc_restir_gi_temporal_dev(self._ctx, w, h, gdm, gnm, gi_hits, res_in, res_out, radiance or None),
+                    "arc_restir_gi_temporal_dev")
 
     def reserve_surface_list(self, max_pixels: int):
         """Surface list (water / mirror / underwater branches) for frames of up to max_pixels pixels."""

@@ -218,6 +218,20 @@ int arc_onebounce_dev(arc_ctx* ctx, const uint32_t* idx, uint32_t n, const float
 int arc_sharc_query_list_dev(arc_ctx* ctx, const uint32_t* list, const uint64_t* n_dev, uint32_t max_n,
                              const float* pos, const float* normal, float* out);
 
+/* ReSTIR GI temporal pass: the GI part of temporal_main (shaders/lighting_restir_gi.wgsl:61-336) for
+ * every pixel of a frame traced by arc_trace_frame_dev (its G-buffer and GI hit records, which the
+ * pass consumes instead of tracing the GI ray again). reservoir_in holds the previous frame's
+ * reservoirs (all empty on the first frame: primary_depth 1e5, the rest 0), reservoir_out receives
+ * this frame's; the camera's prev_cam_pos and the G-buffer motion vectors locate the history. The
+ * radiance at a secondary hit is query_sharc's (the context's resolved SHARC cache), or, with
+ * gi_radiance non-NULL, gi_radiance[3 p .. 3 p + 2] (e.g. arc_nrc_query_list_dev's output). The
+ * emissive-light ReSTIR DI half of the reference pass is not part of this call (no emissive light
+ * list: its DI reservoirs would be empty). */
+int arc_restir_gi_temporal_dev(arc_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* gbuf_depth_mat,
+                               const uint32_t* gbuf_norm_motion, const arc_hit_record* gi_hits,
+                               const arc_gi_reservoir* reservoir_in, arc_gi_reservoir* reservoir_out,
+                               const float* gi_radiance);
+
 /* In-place world edits on the device (replaces the CPU edit + GpuPatch round trip:
  * ChunkTree64::carve_sphere_tracked, crates/arcadia-core/src/chunk_tree/edit/carve.rs:39-176,
  * mutate_brick_in_place, edit/set.rs:244-569, then Renderer::apply_world_patches,

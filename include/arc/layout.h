@@ -10,6 +10,7 @@
  *   arc_material          crates/arcadia-core/src/material.rs:42-47, shaders/common/types.wgsl:76-79
  *   arc_camera_uniforms   crates/arcadia-render/src/camera.rs:11-38, shaders/common/types.wgsl:19-63
  *   arc_sharc_slot        crates/arcadia-render/src/sharc.rs:49-54, shaders/common/sharc.wgsl:16-21
+ *   arc_gi_reservoir      shaders/common/types.wgsl:90-106 (GiReservoir, 32 B)
  *   G-buffer words        shaders/common/types.wgsl:292-332 (20 B per pixel in three arrays)
  *
  * Two records have no buffer counterpart in the reference and are this library's own:
@@ -117,6 +118,19 @@ typedef struct arc_sharc_slot {
     uint32_t pad;
 } arc_sharc_slot;
 
+/* ReSTIR GI reservoir of one pixel. norm_m_flags: bits 0..15 octahedral normal of the sample
+ * (2 x 8 bit), 16..23 M, 24..30 sample age, 31 sample is sky; lo_rg / lo_b_w: f16 outgoing radiance
+ * of the sample and f16 RIS weight W; primary_depth: the pixel's primary hit distance (1e5 when the
+ * reservoir is empty); shadow_vis_m: f16 temporal sun visibility and its sample count. */
+typedef struct arc_gi_reservoir {
+    float sample_pos[3];
+    uint32_t norm_m_flags;
+    uint32_t lo_rg;
+    uint32_t lo_b_w;
+    float primary_depth;
+    uint32_t shadow_vis_m;
+} arc_gi_reservoir;
+
 /* A ray in world meters: origin xyz, unit direction xyz. */
 typedef struct arc_ray {
     float origin_m[3];
@@ -143,6 +157,7 @@ ARC_STATIC_ASSERT(sizeof(arc_camera_uniforms) == 480, "CameraUniforms is 480 B")
 ARC_STATIC_ASSERT(sizeof(arc_sharc_slot) == 16, "SharcResolvedSlot is 16 B");
 ARC_STATIC_ASSERT(sizeof(arc_ray) == 24, "ray is 24 B");
 ARC_STATIC_ASSERT(sizeof(arc_hit_record) == 20, "hit record is 20 B");
+ARC_STATIC_ASSERT(sizeof(arc_gi_reservoir) == 32, "GiReservoir is 32 B");
 
 /* One in-place world edit. The reference has no edit record: its callers invoke
  * ChunkTree64::carve_sphere_tracked (crates/arcadia-core/src/chunk_tree/edit/carve.rs:39-176) and

@@ -97,6 +97,30 @@ float orc_shadow_vis_di(const orc_world* w, const arc_camera_uniforms* cam, cons
 float orc_shadow_vis(const orc_world* w, const arc_camera_uniforms* cam, const float origin_m[3], const float dir[3],
                      float max_dist_m, uint32_t* bytes);
 uint32_t orc_face_id(const float n[3]);
+/* GI ray of a hit pixel from its G-buffer words and what temporal_main reuses of its setup. */
+typedef struct orc_gi_ray {
+    float hit_dist;
+    float ray_dir[3];
+    float hit_pos[3];
+    float normal[3];
+    float smooth_n[3];
+    float xi[2];
+    int guided;
+    float origin[3];
+    float dir[3];
+} orc_gi_ray;
+int orc_gi_setup(const orc_world* w, const arc_camera_uniforms* cam, uint32_t x, uint32_t y, uint32_t W, uint32_t H,
+                 uint32_t gd0, uint32_t gn0, orc_gi_ray* g, uint32_t* bytes);
+void orc_ign(float px, float py, uint32_t frame, float out[2]);
+void orc_oct_decode_packed(uint32_t packed, float n[3]);
+void orc_sky_radiance(const float dir[3], const float sun[3], float out[3]);
+
+/* ReSTIR GI temporal pass (orc_restir.c): res_in is the previous frame's reservoirs, res_out this
+ * frame's; radiance (3 floats per pixel, may be NULL) replaces the SHARC query at secondary hits. */
+void orc_restir_gi_temporal(const orc_world* w, const arc_camera_uniforms* cam, const arc_sharc_slot* resolved,
+                            const float* radiance, const uint32_t* gdm, const uint32_t* gnm, const arc_gi_reservoir* res_in,
+                            arc_gi_reservoir* res_out, int threads);
+
 /* primary-pass surface branches (orc_surface.c): 1 when the hit takes one (underwater camera, water,
  * mirror); orc_surface_shade rewrites albedo (and, for water, the normal) of that hit. */
 int orc_surface_special(const arc_camera_uniforms* cam, uint32_t mat);

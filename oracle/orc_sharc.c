@@ -178,6 +178,8 @@ static void eval_sky(const float dir[3], const float sun[3], float out[3]) {
     memcpy(out, sky, sizeof(sky));
 }
 
+void orc_sky_radiance(const float dir[3], const float sun[3], float out[3]) { eval_sky(dir, sun, out); }
+
 typedef struct surf { int hit; float t_m; float pos[3]; float normal[3]; float albedo[3]; float emission[3]; } surf;
 
 static void trace_surface(const orc_world* w, const arc_camera_uniforms* cam, const float o[3], const float d[3],

@@ -665,35 +665,52 @@ static float probe_emissive(const orc_world* w, const arc_camera_uniforms* cam, 
     return (em[0] * 0.333f + em[1] * 0.333f) + em[2] * 0.333f;
 }
 
-/* GI secondary ray of pixel (x, y) from the G-buffer (lighting_restir_gi.wgsl:69-87,195-209).
- * Returns 0 when the pixel has no primary hit. */
-static int gi_ray_for_pixel(const orc_world* w, const arc_camera_uniforms* cam, uint32_t x, uint32_t y, uint32_t W,
-                            uint32_t H, uint32_t gd0, uint32_t gn0, float origin[3], float dir[3], uint32_t* bytes) {
+/* GI secondary ray of pixel (x, y) from the G-buffer (lighting_restir_gi.wgsl:69-87,195-209), with
+ * the quantities temporal_main goes on to use. Returns 0 when the pixel has no primary hit. */
+int orc_gi_setup(const orc_world* w, const arc_camera_uniforms* cam, uint32_t x, uint32_t y, uint32_t W, uint32_t H,
+                 uint32_t gd0, uint32_t gn0, orc_gi_ray* g, uint32_t* bytes) {
     float hit_dist = orc_bitsf(gd0);
     if (hit_dist >= 1e4f) return 0;
-    float rd[3];
-    camera_ray_dir(cam, x, y, W, H, rd);
-    float hp[3];
-    for (int i = 0; i < 3; ++i) hp[i] = cam->cam_pos_time[i] + rd[i] * hit_dist;
-    float oc[2], n[3];
+    g->hit_dist = hit_dist;
+    camera_ray_dir(cam, x, y, W, H, g->ray_dir);
+    for (int i = 0; i < 3; ++i) g->hit_pos[i] = cam->cam_pos_time[i] + g->ray_dir[i] * hit_dist;
+    float oc[2];
     orc_unpack2x16snorm(gn0, oc);
-    oct_decode(oc, n);
+    oct_decode(oc, g->normal);
+    const float* n = g->normal;
     uint32_t frame = orc_fbits(cam->cam_up_frame[3]);
-    float xi[2];
-    ign((float)x, (float)y, frame, xi);
+    ign((float)x, (float)y, frame, g->xi);
     float sn_in[3] = {n[0] + 0.0f, n[1] + 0.22f, n[2] + 0.0f};
-    float sn[3], bt[3], bb[3];
-    orc_normalize3(sn_in, sn);
-    make_basis(sn, bt, bb);
+    float bt[3], bb[3];
+    orc_normalize3(sn_in, g->smooth_n);
+    make_basis(g->smooth_n, bt, bb);
     float bd[3], cd[3];
-    sample_cosine_hemisphere(xi[0], xi[1], sn, bt, bb, bd);
-    sample_cosine_hemisphere(orc_fract(xi[0] + 0.5f), orc_fract(xi[1] + 0.381966f), sn, bt, bb, cd);
-    float em_near = probe_emissive(w, cam, hp, cd, 1.25f, bytes);
-    float em_mid = probe_emissive(w, cam, hp, cd, 3.0f, bytes);
-    if (orc_max(em_near, em_mid) > 0.25f) memcpy(bd, cd, sizeof(bd));
-    for (int i = 0; i < 3; ++i) origin[i] = hp[i] + n[i] * 0.10f;
-    memcpy(dir, bd, sizeof(bd));
+    sample_cosine_hemisphere(g->xi[0], g->xi[1], g->smooth_n, bt, bb, bd);
+    sample_cosine_hemisphere(orc_fract(g->xi[0] + 0.5f), orc_fract(g->xi[1] + 0.381966f), g->smooth_n, bt, bb, cd);
+    float em_near = probe_emissive(w, cam, g->hit_pos, cd, 1.25f, bytes);
+    float em_mid = probe_emissive(w, cam, g->hit_pos, cd, 3.0f, bytes);
+    g->guided = orc_max(em_near, em_mid) > 0.25f;
+    if (g->guided) memcpy(bd, cd, sizeof(bd));
+    for (int i = 0; i < 3; ++i) g->origin[i] = g->hit_pos[i] + n[i] * 0.10f;
+    memcpy(g->dir, bd, sizeof(bd));
     return 1;
+}
+
+static int gi_ray_for_pixel(const orc_world* w, const arc_camera_uniforms* cam, uint32_t x, uint32_t y, uint32_t W,
+                            uint32_t H, uint32_t gd0, uint32_t gn0, float origin[3], float dir[3], uint32_t* bytes) {
+    orc_gi_ray g;
+    if (!orc_gi_setup(w, cam, x, y, W, H, gd0, gn0, &g, bytes)) return 0;
+    memcpy(origin, g.origin, sizeof(g.origin));
+    memcpy(dir, g.dir, sizeof(g.dir));
+    return 1;
+}
+
+void orc_ign(float px, float py, uint32_t frame, float out[2]) { ign(px, py, frame, out); }
+
+void orc_oct_decode_packed(uint32_t packed, float n[3]) {
+    float oc[2];
+    orc_unpack2x16snorm(packed, oc);
+    oct_decode(oc, n);
 }
 
 void orc_gi_rays(const orc_world* w, const arc_camera_uniforms* cam, uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1,

@@ -86,6 +86,7 @@ def lib():
         _lib.orc_trace_rays.argtypes = [C.POINTER(_World), vp, vp, u32, f32, u32, i32, vp, vp, i32]
         _lib.orc_primary.argtypes = [C.POINTER(_World), vp, u32, u32, u32, u32, vp, vp, vp, vp, vp, i32]
         _lib.orc_gi_rays.argtypes = [C.POINTER(_World), vp, u32, u32, u32, u32, vp, vp, vp, vp, vp, i32]
+        _lib.orc_restir_gi_temporal.argtypes = [C.POINTER(_World), vp, vp, vp, vp, vp, vp, vp, i32]
         _lib.orc_frame_sample.argtypes = [C.POINTER(_World), vp, u32, i32, vp, vp, vp]
         _lib.orc_frame_sample.restype = C.c_uint64
         _lib.orc_cpu_frame_sample.argtypes = [C.POINTER(_World), vp, u32, i32, vp, vp, vp]
@@ -272,6 +273,23 @@ def gi_rays(world: World, cam: np.ndarray, gdm, gnm, rect=None, threads: int = 8
     by = np.zeros(h * w, np.uint32)
     lib().orc_gi_rays(world.cw, _p(cam), x0, y0, x1, y1, _p(gdm), _p(gnm), _p(rays), _p(hits), _p(by), threads)
     return rays, hits, by
+
+
+def restir_gi_temporal(world: World, cam: np.ndarray, resolved: np.ndarray, gdm, gnm, res_in: np.ndarray,
+                       radiance=None, threads: int = 8) -> np.ndarray:
+    """GI part of temporal_main for every pixel: this frame's reservoirs from the previous frame's
+    (``res_in``), the G-buffer and the resolved SHARC slots (or a per-pixel radiance buffer)."""
+    from arcadia_gb300.layout import RESERVOIR_DTYPE
+
+    w = int(cam["world_grid_dims"][0][3] & 0xFFFF)
+    h = int(cam["world_grid_dims"][0][3] >> 16)
+    res_in = np.ascontiguousarray(res_in).view(RESERVOIR_DTYPE)
+    out = np.zeros(h * w, RESERVOIR_DTYPE)
+    rad = None if radiance is None else np.ascontiguousarray(radiance, np.float32)
+    lib().orc_restir_gi_temporal(world.cw, _p(cam), _p(np.ascontiguousarray(resolved)), _p(rad),
+                                 _p(np.ascontiguousarray(gdm, np.uint32)), _p(np.ascontiguousarray(gnm, np.uint32)),
+                                 _p(res_in), _p(out), threads)
+    return out
 
 
 def frame_sample(world: World, cam: np.ndarray, stride: int, threads: int, cpu_query: bool = False):
