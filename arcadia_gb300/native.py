@@ -152,11 +152,14 @@ def lib() -> C.CDLL:
 
 
 def _p(a):
+    """Pointer argument: None, a device address (int) or a host array. The array's pointer object
+    keeps the array alive, so a temporary made by a dtype conversion in the call expression outlives
+    the C call."""
     if a is None:
         return None
     if isinstance(a, int):
         return a
-    return a.ctypes.data
+    return a.ctypes.data_as(C.c_void_p)
 
 
 def default_palette() -> np.ndarray:

@@ -128,7 +128,9 @@ def lib():
 
 
 def _p(a: np.ndarray | None):
-    return None if a is None else a.ctypes.data
+    """Pointer to the array's data that keeps the array alive (a temporary made by a dtype
+    conversion in the call expression must outlive the C call)."""
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
 
 
 def default_palette() -> np.ndarray:
