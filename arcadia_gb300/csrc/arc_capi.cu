@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -85,6 +86,8 @@ arc::World arc_ctx::world() const {
     w.n_bricks = n_bricks;
     w.n_roots = n_roots;
     w.status = d_status;
+    w.bodies = d_bodies;
+    w.n_bodies = n_bodies;
     return w;
 }
 
@@ -257,6 +260,7 @@ int arc_destroy(arc_ctx* c) {
     }
     cudaFree(c->d_surf);
     cudaFree(c->d_surf_count);
+    cudaFree(c->d_bodies);
     cudaFree(c->d_edit);
     cudaFree(c->d_edit_stage);
     cudaFreeHost(c->h_edit_stage);
@@ -793,6 +797,8 @@ static int views_prepare(arc_ctx* c, const arc_view_desc* views, uint32_t n, uin
             (d.cam.world_grid_dims[3] >> 16) != d.height)
             return set_err(c, ARC_E_INVALID_ARG, "view size differs from its camera world_grid_dims.w");
         if (!d.gbuf_depth_mat || !d.gbuf_norm_motion || !d.gbuf_albedo_ao) return set_err(c, ARC_E_INVALID_ARG, "null G-buffer");
+        if (slot == 0 && c->n_bodies && ((d.cam.point_light_count[1] >> 16) & 0xFFFFu))
+            return set_err(c, ARC_E_INVALID_ARG, "batched views do not trace rigid bodies (use arc_trace_frame_dev)");
         arc::ViewDev& v = c->h_views[i];
         memset(&v, 0, sizeof v);
         v.cam = d.cam;
@@ -975,6 +981,45 @@ int arc_shadow_rays_di_dev(arc_ctx* c, const arc_ray* rays, const float* max_dis
     if (rc) return rc;
     if (n && (!rays || !max_dist_m || !vis)) return set_err(c, ARC_E_INVALID_ARG, "null buffer");
     if (n) ARC_CK(c, arc::launch_shadow_di(c->world(), c->cam, rays, max_dist_m, n, vis, c->stream));
+    return ARC_OK;
+}
+
+int arc_set_rigid_bodies(arc_ctx* c, const arc_rigid_body* bodies, uint32_t n) {
+    int rc = arc_ctx_check_ready(c, false);
+    if (rc) return rc;
+    if (n > ARC_MAX_RIGID_BODIES) return set_err(c, ARC_E_INVALID_ARG, "more than 32 rigid bodies");
+    if (n && !bodies) return set_err(c, ARC_E_INVALID_ARG, "null body table");
+    for (uint32_t i = 0; i < n; ++i) {
+        const arc_rigid_body& b = bodies[i];
+        uint32_t root;
+        memcpy(&root, &b.local_bounds_and_root[3], 4);
+        bool ok = root == ARC_EMPTY_CHUNK || root < c->n_nodes;
+        for (int k = 0; k < 3; ++k)
+            ok = ok && std::isfinite(b.local_bounds_and_root[k]) && b.local_bounds_and_root[k] > 0.0f &&
+                 b.local_bounds_and_root[k] <= 16.0f;
+        for (int k = 0; k < 16; ++k)
+            ok = ok && std::isfinite(b.world_to_local[k]) && std::isfinite(b.local_to_world[k]) &&
+                 std::isfinite(b.prev_local_to_world[k]);
+        for (int k = 0; k < 4; ++k) ok = ok && std::isfinite(b.world_sphere[k]);
+        if (!ok) {
+            char m[160];
+            snprintf(m, sizeof m, "rigid body %u: root out of the node pool, local bounds outside (0, 16] m or a non-finite value", i);
+            return set_err(c, ARC_E_INVALID_ARG, m);
+        }
+    }
+    if (!c->d_bodies) ARC_CK(c, cudaMalloc((void**)&c->d_bodies, sizeof(arc_rigid_body) * ARC_MAX_RIGID_BODIES));
+    ARC_CK(c, cudaStreamSynchronize(c->stream));
+    if (n) ARC_CK(c, cudaMemcpy(c->d_bodies, bodies, sizeof(arc_rigid_body) * n, cudaMemcpyHostToDevice));
+    c->n_bodies = n;
+    return arc_ctx_sync_world_table(c);
+}
+
+int arc_trace_rigid_bodies_dev(arc_ctx* c, const arc_ray* rays, uint32_t n, float max_dist_m, arc_hit_record* hits,
+                               float* detail) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if (n && (!rays || !hits)) return set_err(c, ARC_E_INVALID_ARG, "null buffer");
+    if (n) ARC_CK(c, arc::launch_rigid_rays(c->world(), c->cam, rays, n, max_dist_m, hits, detail, c->stream));
     return ARC_OK;
 }
 

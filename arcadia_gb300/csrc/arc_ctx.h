@@ -26,6 +26,10 @@ struct arc_ctx {
     arc_camera_uniforms cam{};
     bool have_cam = false;
 
+    // rigid voxel bodies (GpuRigidBodyInstance table; their trees live in the node pool above)
+    arc_rigid_body* d_bodies = nullptr;
+    uint32_t n_bodies = 0;
+
     // extra worlds for batched multi-view launches (slot 0 is the world above)
     static constexpr int kSlots = 8;
     struct Slot {

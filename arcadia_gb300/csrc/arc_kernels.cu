@@ -330,6 +330,110 @@ __global__ void shadow_di_kernel(const World w, const __grid_constant__ arc_came
     vis[i] = shadow_vis_di(w, cam, f3{rp[0], rp[1], rp[2]}, f3{rp[3], rp[4], rp[5]}, max_dist_m[i]);
 }
 
+// Frame with rigid bodies (the camera's point_light_count.y >> 16 > 0 and a body table uploaded):
+// one thread per pixel of the launch's rows. The primary ray is the world trace followed by the
+// bodies in front of its hit (primary_gbuffer.wgsl:121-136): a body hit replaces distance, point,
+// normal, material, voxel hash and contact AO, puts its previous-frame point into the motion vector
+// and sets the G-buffer flag. Surface branches are shaded inline with the bodies in every surface
+// ray; the GI ray is the world trace followed by the bodies in front of its hit
+// (lighting_restir_gi.wgsl:209-224). Hit records of body hits carry ARC_HIT_FLAG_RIGID, the body
+// index and the body-local voxel.
+__device__ __forceinline__ void mark_rigid(arc_hit_record* p, uint32_t body) {
+    reinterpret_cast<uint32_t*>(p)[3] |= (ARC_HIT_FLAG_RIGID | (body << 8)) << 16;
+}
+
+__device__ __forceinline__ void take_rigid(HitInfo& h, const RigidHit& rb) {
+    h.t_voxels = rb.t_voxels;
+    h.hit_pos_m = rb.pos;
+    h.normal = rb.normal;
+    h.mat = rb.mat;
+    h.voxel_hash = rb.hash;
+    h.contact_ao = rb.ao;
+    h.vx = rb.vx;
+    h.vy = rb.vy;
+    h.vz = rb.vz;
+    h.shift = rb.shift;
+}
+
+__global__ void __launch_bounds__(128) frame_rigid_kernel(const FrameParams P, const __grid_constant__ arc_camera_uniforms cam) {
+    const uint32_t x = blockIdx.x * 16u + (threadIdx.x & 15u);
+    const uint32_t y = P.row0 + blockIdx.y * 8u + (threadIdx.x >> 4);
+    if (x >= P.width || y >= P.row_end) return;
+    const World& w = P.world;
+    const f3 eye{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]};
+    const f3 dir = camera_dir(cam, x, y, P.width, P.height);
+    const bool underwater = (cam.point_light_count[1] & 0xFFFFu) != 0u;
+    const size_t k = (size_t)y * P.width + x;
+    HitInfo h;
+    bool hit = trace_full(w, cam, eye, dir, 250.0f, 0u, underwater, h);
+    f3 prev = h.hit_pos_m;
+    const RigidHit rb = trace_rigid_bodies(w, cam, eye, dir, hit ? h.t_voxels * ARC_VOXEL_SIZE : 250.0f);
+    if (rb.hit) {
+        hit = true;
+        take_rigid(h, rb);
+        prev = rb.prev_pos;
+    }
+    if (P.hits) {
+        store_hit(&P.hits[k], h, hit);
+        if (rb.hit) mark_rigid(&P.hits[k], rb.body);
+    }
+    uint32_t dw, nw;
+    if (!hit) {
+        float ox, oy;
+        oct_encode(dir, &ox, &oy);
+        nw = pack2x16snorm(ox, oy);
+        dw = __float_as_uint(1e5f);
+        reinterpret_cast<uint2*>(P.gbuf_depth_mat)[k] = make_uint2(dw, 0u);
+        reinterpret_cast<uint2*>(P.gbuf_norm_motion)[k] = make_uint2(nw, pack2x16float(0.0f, 0.0f));
+        P.gbuf_albedo_ao[k] = pack4x8unorm(0.0f, 0.0f, 0.0f, 1.0f);
+    } else {
+        const float hit_dist = h.t_voxels * ARC_VOXEL_SIZE;
+        f3 alb = varied_albedo(w.palette, h.mat, h.voxel_hash, 1.0f - smoothstepf(18.0f, 48.0f, hit_dist));
+        const float pu = __fdiv_rn((float)x + 0.5f, (float)P.width), pv = __fdiv_rn((float)y + 0.5f, (float)P.height);
+        const float* M = cam.prev_view_proj;
+        float clip[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) clip[r] = ((M[r] * prev.x + M[4 + r] * prev.y) + M[8 + r] * prev.z) + M[12 + r] * 1.0f;
+        float mx = -2.0f, my = -2.0f;
+        if (clip[3] > 0.001f) {
+            const float ndx = __fdiv_rn(clip[0], clip[3]), ndy = __fdiv_rn(clip[1], clip[3]);
+            mx = (ndx * 0.5f + 0.5f) - pu;
+            my = (0.5f - ndy * 0.5f) - pv;
+        }
+        f3 nrm = h.normal;
+        if (surface_special(cam, h.mat)) {
+            alb = surface_shade<true>(w, cam, dir, h.mat, h.normal, h.voxel_hash, hit_dist, h.hit_pos_m);
+            if (h.mat == kMatWaterCrystal && !underwater) nrm = f3{0.0f, 1.0f, 0.0f};
+        }
+        float ox, oy;
+        oct_encode(nrm, &ox, &oy);
+        nw = pack2x16snorm(ox, oy);
+        dw = __float_as_uint(hit_dist);
+        reinterpret_cast<uint2*>(P.gbuf_depth_mat)[k] = make_uint2(dw, (h.mat & 0xFFFFu) | (rb.hit ? 1u << 16 : 0u));
+        reinterpret_cast<uint2*>(P.gbuf_norm_motion)[k] = make_uint2(nw, pack2x16float(mx, my));
+        P.gbuf_albedo_ao[k] = pack4x8unorm(alb.x, alb.y, alb.z, clampf(h.contact_ao, 0.0f, 1.0f));
+    }
+    if (!P.do_gi) return;
+    f3 go, gd;
+    if (!gi_setup(w, cam, x, y, P.width, P.height, dw, nw, &go, &gd)) {
+        if (P.gi_hits) store_no_ray(&P.gi_hits[k]);
+        return;
+    }
+    const float gmax = cam.ray_distances[2];
+    HitInfo g;
+    bool gh = trace_full(w, cam, go, gd, gmax, 2u, true, g);
+    const RigidHit rg = trace_rigid_bodies(w, cam, go, gd, gh ? g.t_voxels * ARC_VOXEL_SIZE : gmax);
+    if (rg.hit) {
+        gh = true;
+        take_rigid(g, rg);
+    }
+    if (P.gi_hits) {
+        store_hit(&P.gi_hits[k], g, gh);
+        if (rg.hit) mark_rigid(&P.gi_hits[k], rg.body);
+    }
+    atomicAdd(&P.scratch->gi_rays, 1ull);
+}
+
 // Persistent kernel over many views (several worlds, mixed resolutions) in one launch. The queue is
 // the concatenation of every view's 32-pixel tiles; a lane finds its view by binary search over the
 // views' queue offsets and reads that view's camera block and world from global memory (L1-cached),
@@ -490,6 +594,11 @@ __global__ void __launch_bounds__(256, MINB) views_plain_kernel(const ViewsParam
 template <int MINB>
 cudaError_t launch_frame_t(const FrameParams& P, const arc_camera_uniforms& cam, const arc_launch_config& cfg, int n_sm,
                            cudaStream_t st) {
+    if (P.world.n_bodies && ((cam.point_light_count[1] >> 16) & 0xFFFFu)) {
+        dim3 grid((P.width + 15u) / 16u, (P.row_end - P.row0 + 7u) / 8u);
+        frame_rigid_kernel<<<grid, 128, 0, st>>>(P, cam);
+        return cudaGetLastError();
+    }
     if (cfg.variant == 0u) {
         const uint32_t bw = 8u, bh = cfg.block_threads / 8u;
         dim3 block(bw, bh);
@@ -578,7 +687,9 @@ __global__ void __launch_bounds__(128) surface_kernel(const FrameParams P, const
         e.hp[1] = __uint_as_float(b.z);
         e.hp[2] = __uint_as_float(b.w);
         const f3 dir = camera_dir(cam, e.xy & 0xFFFFu, e.xy >> 16, P.width, P.height);
-        surface_store(P.gbuf_albedo_ao, e.k, surface_shade(P.world, cam, dir, e));
+        surface_store(P.gbuf_albedo_ao, e.k,
+                      surface_shade<false>(P.world, cam, dir, e.mat_face_view & 0xFFu, face_normal((e.mat_face_view >> 8) & 0xFFu),
+                                           e.hash, e.hit_dist, f3{e.hp[0], e.hp[1], e.hp[2]}));
     }
 }
 
@@ -601,7 +712,10 @@ __global__ void __launch_bounds__(128) surface_views_kernel(const ViewsParams V,
         if (v >= V.n_views) continue;
         const ViewDev& vd = V.views[v];
         const f3 dir = camera_dir(vd.cam, e.xy & 0xFFFFu, e.xy >> 16, vd.width, vd.height);
-        surface_store(vd.gbuf_albedo_ao, e.k, surface_shade(V.worlds[vd.slot], vd.cam, dir, e));
+        surface_store(vd.gbuf_albedo_ao, e.k,
+                      surface_shade<false>(V.worlds[vd.slot], vd.cam, dir, e.mat_face_view & 0xFFu,
+                                           face_normal((e.mat_face_view >> 8) & 0xFFu), e.hash, e.hit_dist,
+                                           f3{e.hp[0], e.hp[1], e.hp[2]}));
     }
 }
 
@@ -634,6 +748,41 @@ cudaError_t launch_rays(const World& w, const arc_camera_uniforms& cam, const ar
                         uint32_t lod_bias, int ignore_water, arc_hit_record* hits, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     rays_kernel<<<(n + 127u) / 128u, 128, 0, st>>>(w, cam, rays, n, max_dist_m, lod_bias, ignore_water ? 1u : 0u, hits);
+    return cudaGetLastError();
+}
+
+// trace_rigid_bodies over a ray batch: hit records (body hits flagged) and optional per-ray detail
+// (world hit point, previous-frame hit point, world normal).
+__global__ void rigid_rays_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, const arc_ray* __restrict__ rays,
+                                  uint32_t n, float max_dist_m, arc_hit_record* __restrict__ hits, float* __restrict__ detail) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* rp = reinterpret_cast<const float*>(&rays[i]);
+    const f3 o{rp[0], rp[1], rp[2]}, d{rp[3], rp[4], rp[5]};
+    const RigidHit rb = trace_rigid_bodies(w, cam, o, d, max_dist_m);
+    HitInfo h;
+    hit_init_miss(h, o, d, max_dist_m);
+    if (rb.hit) take_rigid(h, rb);
+    store_hit(&hits[i], h, rb.hit);
+    if (rb.hit) mark_rigid(&hits[i], rb.body);
+    if (detail) {
+        const f3 pp = rb.hit ? rb.prev_pos : h.hit_pos_m;
+        float* q = detail + 9u * (size_t)i;
+        q[0] = h.hit_pos_m.x;
+        q[1] = h.hit_pos_m.y;
+        q[2] = h.hit_pos_m.z;
+        q[3] = pp.x;
+        q[4] = pp.y;
+        q[5] = pp.z;
+        q[6] = h.normal.x;
+        q[7] = h.normal.y;
+        q[8] = h.normal.z;
+    }
+}
+
+cudaError_t launch_rigid_rays(const World& w, const arc_camera_uniforms& cam, const arc_ray* rays, uint32_t n, float max_dist_m,
+                              arc_hit_record* hits, float* detail, cudaStream_t st) {
+    rigid_rays_kernel<<<(n + 127u) / 128u, 128, 0, st>>>(w, cam, rays, n, max_dist_m, hits, detail);
     return cudaGetLastError();
 }
 

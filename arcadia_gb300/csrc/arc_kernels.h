@@ -93,6 +93,8 @@ cudaError_t launch_surface_views(const ViewsParams& V, const SurfaceEntry* surf,
 cudaError_t launch_secondary(const FrameParams& P, const arc_camera_uniforms& cam, cudaStream_t st);
 cudaError_t launch_rays(const World& w, const arc_camera_uniforms& cam, const arc_ray* rays, uint32_t n, float max_dist_m,
                         uint32_t lod_bias, int ignore_water, arc_hit_record* hits, cudaStream_t st);
+cudaError_t launch_rigid_rays(const World& w, const arc_camera_uniforms& cam, const arc_ray* rays, uint32_t n, float max_dist_m,
+                              arc_hit_record* hits, float* detail, cudaStream_t st);
 cudaError_t launch_shadow_di(const World& w, const arc_camera_uniforms& cam, const arc_ray* rays, const float* max_dist_m,
                              uint32_t n, float* vis, cudaStream_t st);
 cudaError_t launch_shadow(const World& w, const arc_camera_uniforms& cam, const arc_ray* rays, uint32_t n, float max_dist_m,

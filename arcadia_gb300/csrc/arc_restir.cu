@@ -5,7 +5,8 @@
 //                              with its temporal average (checkerboard half rate in low-tap mode),
 //                              one GI candidate, temporal RIS, the 32 B reservoir.
 //
-// The GI candidate is the secondary ray the frame kernel already traced: its hit record (hit flag,
+// The GI candidate is the secondary ray the frame kernel already traced (traced again here only
+// when rigid bodies are in the frame, whose hits a record cannot give back): its hit record (hit flag,
 // material, face, depth, voxel, cell level) gives back the secondary hit exactly (the hit point is
 // (origin * 16 + dir * depth * 16) / 16, the same operations as the traversal's; the node payload
 // for the LOD colour is a four-load point query), so the pass traces only the sun shadow ray and,
@@ -21,6 +22,7 @@
 
 #include "arc_ctx.h"
 #include "arc_sharc.cuh"
+#include "arc_surface.cuh"
 
 namespace arc {
 
@@ -168,33 +170,61 @@ __global__ void __launch_bounds__(128) restir_gi_temporal_kernel(const RestirPar
         shadow_m = 1.0f;
     }
 
-    // GI candidate from the frame's secondary hit (195-284)
-    const uint32_t* hr = reinterpret_cast<const uint32_t*>(&P.gi_hits[p]);
-    const uint32_t w3 = hr[3];
-    const bool gi_hit = ((w3 >> 16) & ARC_HIT_FLAG_HIT) != 0u;
+    // GI candidate (195-284): the frame's secondary hit from its record, or, with rigid bodies, the GI
+    // ray traced again (world, then the bodies in front of its hit)
+    bool gi_hit;
+    uint32_t mat = 0u;
+    float gd_m = 0.0f;
+    f3 gpos{0.0f, 0.0f, 0.0f}, gnrm{0.0f, 1.0f, 0.0f}, lod{0.0f, 0.0f, 0.0f};
+    if (rigid_count(w, cam)) {
+        HitInfo gh;
+        gi_hit = trace_full(w, cam, gi_o, gi_d, cam.ray_distances[2], 2u, true, gh);
+        const RigidHit rb = trace_rigid_bodies(w, cam, gi_o, gi_d, gi_hit ? gh.t_voxels * ARC_VOXEL_SIZE : cam.ray_distances[2]);
+        if (rb.hit) {
+            gi_hit = true;
+            mat = rb.mat;
+            gd_m = rb.t_voxels * ARC_VOXEL_SIZE;
+            gpos = rb.pos;
+            gnrm = rb.normal;
+            const float4 ra = __ldg(&w.palette[2u * rb.mat]);
+            lod = f3{ra.x, ra.y, ra.z};
+        } else if (gi_hit) {
+            mat = gh.mat;
+            gd_m = gh.t_voxels * ARC_VOXEL_SIZE;
+            gpos = gh.hit_pos_m;
+            gnrm = gh.normal;
+            lod = f3{__fdiv_rn((float)(gh.lod_payload & 0xFFu), 255.0f), __fdiv_rn((float)((gh.lod_payload >> 8) & 0xFFu), 255.0f),
+                     __fdiv_rn((float)((gh.lod_payload >> 16) & 0xFFu), 255.0f)};
+        }
+    } else {
+        const uint32_t* hr = reinterpret_cast<const uint32_t*>(&P.gi_hits[p]);
+        const uint32_t w3 = hr[3];
+        gi_hit = ((w3 >> 16) & ARC_HIT_FLAG_HIT) != 0u;
+        if (gi_hit) {
+            mat = (w3 >> 8) & 0xFFu;
+            const uint32_t face = w3 & 0xFFu;
+            const uint32_t shift = ((w3 >> 17) & 7u) << 1;
+            gd_m = __uint_as_float(hr[4]);
+            const float t = gd_m * ARC_VOXELS_PER_METER;
+            const f3 vo = mul3s(gi_o, ARC_VOXELS_PER_METER);
+            gpos = mul3s(add3(vo, mul3s(gi_d, t)), ARC_VOXEL_SIZE);
+            gnrm = face_normal(face);
+            const uint32_t payload = lod_payload_at(w, cam, hr[0], hr[1], hr[2], shift);
+            lod = f3{__fdiv_rn((float)(payload & 0xFFu), 255.0f), __fdiv_rn((float)((payload >> 8) & 0xFFu), 255.0f),
+                     __fdiv_rn((float)((payload >> 16) & 0xFFu), 255.0f)};
+        }
+    }
     f3 cand_pos = add3(hp, mul3s(gi_d, 500.0f));
     f3 cand_norm{-gi_d.x, -gi_d.y, -gi_d.z};
     bool cand_sky = true;
     f3 lo{0.0f, 0.0f, 0.0f};
     if (gi_hit) {
-        const uint32_t mat = (w3 >> 8) & 0xFFu;
-        const uint32_t face = w3 & 0xFFu;
-        const uint32_t shift = ((w3 >> 17) & 7u) << 1;
-        const float gd_m = __uint_as_float(hr[4]);
-        const float t = gd_m * ARC_VOXELS_PER_METER;
-        const f3 vo = mul3s(gi_o, ARC_VOXELS_PER_METER);
-        const f3 gpos = mul3s(add3(vo, mul3s(gi_d, t)), ARC_VOXEL_SIZE);
-        const float s_ = (face & 1u) ? -1.0f : 1.0f;
-        const f3 gnrm{face < 2u ? s_ : 0.0f, (face >> 1) == 1u ? s_ : 0.0f, (face >> 1) == 2u ? s_ : 0.0f};
         cand_pos = gpos;
         cand_norm = gnrm;
         cand_sky = false;
-        const uint32_t payload = lod_payload_at(w, cam, hr[0], hr[1], hr[2], shift);
         const float4 a = __ldg(&w.palette[2u * mat]);
         const float4 em = __ldg(&w.palette[2u * mat + 1u]);
-        const f3 alb{mixf(a.x, __fdiv_rn((float)(payload & 0xFFu), 255.0f), 0.55f),
-                     mixf(a.y, __fdiv_rn((float)((payload >> 8) & 0xFFu), 255.0f), 0.55f),
-                     mixf(a.z, __fdiv_rn((float)((payload >> 16) & 0xFFu), 255.0f), 0.55f)};
+        const f3 alb{mixf(a.x, lod.x, 0.55f), mixf(a.y, lod.y, 0.55f), mixf(a.z, lod.z, 0.55f)};
         const float att = __fdiv_rn(1.0f, (1.0f + gd_m * 0.06f) + (gd_m * gd_m) * 0.025f);
         const float gw = g.guided ? 0.55f : 1.0f;
         lo = f3{((em.x * att) * gw) * 1.0f, ((em.y * att) * gw) * 1.0f, ((em.z * att) * gw) * 1.0f};

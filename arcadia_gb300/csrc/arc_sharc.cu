@@ -14,6 +14,7 @@
 #include <string>
 
 #include "arc_ctx.h"
+#include "arc_rigid.cuh"
 #include "arc_sharc.cuh"
 
 namespace arc {
@@ -58,7 +59,8 @@ __device__ __forceinline__ f3 cmp_albedo(uint32_t mat) {
     return f3{0.1f + (float)(h0 >> 8) * s, 0.1f + (float)(h1 >> 8) * s, 0.1f + (float)(h2 >> 8) * s};
 }
 
-// sharc_trace_surface (shaders/sharc_update.wgsl:32-64) without rigid bodies.
+// sharc_trace_surface (shaders/sharc_update.wgsl:32-64): the static world, then the rigid bodies in
+// front of its hit (a body hit's LOD colour is its material's albedo).
 __device__ __forceinline__ Surface trace_surface(const World& w, const arc_camera_uniforms& cam, f3 o, f3 d, float max_dist) {
     Surface out;
     out.hit = false;
@@ -70,12 +72,27 @@ __device__ __forceinline__ Surface trace_surface(const World& w, const arc_camer
             r = ray_advance(s, w, cam, h);
         } while (r == kContinue);
     }
+    if (r != kHit) h.lod_payload = 0u;
+    float lr = __fdiv_rn((float)(h.lod_payload & 0xFFu), 255.0f);
+    float lg = __fdiv_rn((float)((h.lod_payload >> 8) & 0xFFu), 255.0f);
+    float lb = __fdiv_rn((float)((h.lod_payload >> 16) & 0xFFu), 255.0f);
+    if (rigid_count(w, cam)) {
+        const RigidHit rb = trace_rigid_bodies(w, cam, o, d, r == kHit ? h.t_voxels * ARC_VOXEL_SIZE : max_dist);
+        if (rb.hit) {
+            r = kHit;
+            h.t_voxels = rb.t_voxels;
+            h.hit_pos_m = rb.pos;
+            h.normal = rb.normal;
+            h.mat = rb.mat;
+            const float4 ra = __ldg(&w.palette[2u * rb.mat]);
+            lr = ra.x;
+            lg = ra.y;
+            lb = ra.z;
+        }
+    }
     if (r != kHit) return out;
     const float4 alb = __ldg(&w.palette[2u * h.mat]);
     const float4 em = __ldg(&w.palette[2u * h.mat + 1u]);
-    const float lr = __fdiv_rn((float)(h.lod_payload & 0xFFu), 255.0f);
-    const float lg = __fdiv_rn((float)((h.lod_payload >> 8) & 0xFFu), 255.0f);
-    const float lb = __fdiv_rn((float)((h.lod_payload >> 16) & 0xFFu), 255.0f);
     out.hit = true;
     out.mat = h.mat;
     out.t_m = h.t_voxels * ARC_VOXEL_SIZE;

@@ -7,10 +7,11 @@
 // append every hit that takes a branch to a compacted list; surface_kernel shades the list after
 // the frame kernel and rewrites the albedo bytes of those pixels. The arithmetic is the canonical
 // one of arc_math.cuh (WGSL expressions evaluated left to right, pow with an integer exponent by
-// powi, with a non-integer exponent by pow_canon, exp by exp_canon). Rigid bodies are absent
-// (rb_count = 0 makes trace_rigid_bodies a no-op, traversal64.wgsl:1230-1233).
+// powi, with a non-integer exponent by pow_canon, exp by exp_canon). Frames with rigid bodies shade
+// their surface hits inline (frame_rigid_kernel), with the bodies in front of every surface ray.
 #pragma once
 
+#include "arc_rigid.cuh"
 #include "arc_traverse.cuh"
 
 namespace arc {
@@ -204,20 +205,21 @@ static __device__ __noinline__ bool trace_full(const World& w, const arc_camera_
     return r == kHit;
 }
 
-// Albedo of one listed hit after its branch (primary_gbuffer.wgsl:167-295).
-__device__ __forceinline__ f3 surface_shade(const World& w, const arc_camera_uniforms& cam, f3 dir, const SurfaceEntry& e) {
-    const uint32_t mat = e.mat_face_view & 0xFFu;
-    const f3 n = face_normal((e.mat_face_view >> 8) & 0xFFu);
-    const f3 hp{e.hp[0], e.hp[1], e.hp[2]};
+// Albedo of a primary hit after its branch (primary_gbuffer.wgsl:167-295): material, normal, voxel
+// hash, hit distance and point of the hit, primary ray direction. With RB every surface ray is
+// followed by the rigid bodies in front of its world hit, as the reference's trace_rigid_bodies calls.
+template <bool RB>
+__device__ __forceinline__ f3 surface_shade(const World& w, const arc_camera_uniforms& cam, f3 dir, uint32_t mat, f3 n,
+                                            uint32_t hash, float hit_dist, f3 hp) {
     const f3 sun{cam.sun_dir_intensity[0], cam.sun_dir_intensity[1], cam.sun_dir_intensity[2]};
     const float sun_power = cam.sun_dir_intensity[3];
     const float t_sec = cam.cam_pos_time[3];
     HitInfo r;
     if ((cam.point_light_count[1] & 0xFFFFu) != 0u) {
-        const f3 alb = varied_albedo(w.palette, mat, e.hash, 1.0f - smoothstepf(18.0f, 48.0f, e.hit_dist));
+        const f3 alb = varied_albedo(w.palette, mat, hash, 1.0f - smoothstepf(18.0f, 48.0f, hit_dist));
         const float water_y = fmaxf(11.25f, cam.cam_pos_time[1] + 0.35f);
         const f3 cau = water_caustics(hp, water_y, n, sun, t_sec);
-        const float dd = fminf(e.hit_dist, 24.0f);
+        const float dd = fminf(hit_dist, 24.0f);
         return f3{mixf(0.02f, alb.x * cau.x, exp_canon(-0.16f * dd)), mixf(0.14f, alb.y * cau.y, exp_canon(-0.045f * dd)),
                   mixf(0.22f, alb.z * cau.z, exp_canon(-0.020f * dd))};
     }
@@ -225,7 +227,21 @@ __device__ __forceinline__ f3 surface_shade(const World& w, const arc_camera_uni
         const f3 wave = surface_water_normal(hp.x, hp.z, t_sec);
         const f3 refr_dir = normalize3(f3{dir.x - wave.x * 0.38f, dir.y - 0.0f * 0.38f, dir.z - wave.z * 0.38f});
         f3 water_col{0.03f, 0.16f, 0.24f};
-        if (trace_full(w, cam, add3(hp, mul3s(dir, 0.12f)), refr_dir, cam.ray_distances[0], 1u, true, r)) {
+        const f3 ro = add3(hp, mul3s(dir, 0.12f));
+        bool refr_hit = trace_full(w, cam, ro, refr_dir, cam.ray_distances[0], 1u, true, r);
+        if constexpr (RB) {
+            const RigidHit rb =
+                trace_rigid_bodies(w, cam, ro, refr_dir, refr_hit ? r.t_voxels * ARC_VOXEL_SIZE : cam.ray_distances[0]);
+            if (rb.hit) {
+                refr_hit = true;
+                r.t_voxels = rb.t_voxels;
+                r.hit_pos_m = rb.pos;
+                r.normal = rb.normal;
+                r.mat = rb.mat;
+                r.voxel_hash = rb.hash;
+            }
+        }
+        if (refr_hit) {
             const float4 em = __ldg(&w.palette[2u * r.mat + 1u]);
             const f3 bed0 = varied_albedo(w.palette, r.mat, r.voxel_hash, 1.0f);
             const f3 cau = water_caustics(r.hit_pos_m, hp.y, n, sun, t_sec);
@@ -242,7 +258,16 @@ __device__ __forceinline__ f3 surface_shade(const World& w, const arc_camera_uni
         f3 refl_col = reflection_sky(refl_dir, sun);
         const bool low = cam.quality_flags[2] != 0u || (cam.quality_flags[3] & 0xFFu) <= 12u;
         if (fresnel > (low ? 0.22f : 0.08f)) {
-            if (trace_full(w, cam, f3{hp.x + 0.0f, hp.y + 0.08f, hp.z + 0.0f}, refl_dir, 36.0f, 2u, true, r)) {
+            const f3 o2{hp.x + 0.0f, hp.y + 0.08f, hp.z + 0.0f};
+            bool refl_hit = trace_full(w, cam, o2, refl_dir, 36.0f, 2u, true, r);
+            if constexpr (RB) {
+                const RigidHit rb = trace_rigid_bodies(w, cam, o2, refl_dir, refl_hit ? r.t_voxels * ARC_VOXEL_SIZE : 36.0f);
+                if (rb.hit) {
+                    refl_hit = true;
+                    r.mat = rb.mat;
+                }
+            }
+            if (refl_hit) {
                 const float4 a = __ldg(&w.palette[2u * r.mat]);
                 const float4 em = __ldg(&w.palette[2u * r.mat + 1u]);
                 refl_col = f3{a.x * day_factor + em.x * 0.35f, a.y * day_factor + em.y * 0.35f, a.z * day_factor + em.z * 0.35f};
@@ -255,13 +280,25 @@ __device__ __forceinline__ f3 surface_shade(const World& w, const arc_camera_uni
     // mirror chrome
     const float dn = dot3(n, dir);
     const f3 refl_dir{dir.x - (2.0f * dn) * n.x, dir.y - (2.0f * dn) * n.y, dir.z - (2.0f * dn) * n.z};
-    bool hit = trace_full(w, cam, add3(hp, mul3s(n, 0.04f)), refl_dir, cam.ray_distances[1], 1u, false, r);
+    const f3 mo = add3(hp, mul3s(n, 0.04f));
+    bool hit = trace_full(w, cam, mo, refl_dir, cam.ray_distances[1], 1u, false, r);
     f3 mirror_col = reflection_sky(refl_dir, sun);
     if (hit && r.mat == kMatMirrorChrome && r.t_voxels * ARC_VOXEL_SIZE < 0.12f) {
         HitInfo re;
         if (trace_full(w, cam, add3(r.hit_pos_m, mul3s(refl_dir, 0.08f)), refl_dir, cam.ray_distances[1], 1u, false, re)) r = re;
     }
     const bool self = hit && r.mat == kMatMirrorChrome && r.t_voxels * ARC_VOXEL_SIZE < 0.12f;
+    if constexpr (RB) {
+        const RigidHit rb = trace_rigid_bodies(w, cam, mo, refl_dir, (hit && !self) ? r.t_voxels * ARC_VOXEL_SIZE : cam.ray_distances[1]);
+        if (rb.hit) {
+            hit = true;
+            r.t_voxels = rb.t_voxels;
+            r.hit_pos_m = rb.pos;
+            r.normal = rb.normal;
+            r.mat = rb.mat;
+            r.voxel_hash = rb.hash;
+        }
+    }
     if (hit && !self) {
         const f3 ra = varied_albedo(w.palette, r.mat, r.voxel_hash, 1.0f);
         const float4 em = __ldg(&w.palette[2u * r.mat + 1u]);

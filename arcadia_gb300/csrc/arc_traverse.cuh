@@ -36,6 +36,8 @@ struct World {
     uint32_t n_bricks;
     uint32_t n_roots;
     uint32_t* status;
+    const arc_rigid_body* bodies;  // rigid bodies whose trees live in this node pool (may be null)
+    uint32_t n_bodies;
 };
 
 __device__ __forceinline__ uint4 load_node(const World& w, uint32_t idx) {

@@ -73,13 +73,18 @@ def empty_reservoirs(n: int) -> np.ndarray:
     return r
 
 
+RIGID_BODY_DTYPE = np.dtype(
+    [("world_to_local", "<f4", (16,)), ("local_to_world", "<f4", (16,)), ("prev_local_to_world", "<f4", (16,)),
+     ("local_bounds_and_root", "<f4", (4,)), ("world_sphere", "<f4", (4,))]
+)
+
 EDIT_CARVE = 0
 EDIT_RECOLOR = 1
 EDIT_DTYPE = np.dtype(
     [("kind", "<u4"), ("material", "<u4"), ("brick", "<u4", (3,)), ("center", "<f4", (3,)), ("radius", "<f4"),
      ("pad", "<u4")]
 )
-assert EDIT_DTYPE.itemsize == 40 and RESERVOIR_DTYPE.itemsize == 32
+assert EDIT_DTYPE.itemsize == 40 and RESERVOIR_DTYPE.itemsize == 32 and RIGID_BODY_DTYPE.itemsize == 224
 assert VIEW_DTYPE.itemsize == 536
 assert NODE_DTYPE.itemsize == 16 and BRICK_DTYPE.itemsize == 64 and MATERIAL_DTYPE.itemsize == 32
 assert CAMERA_DTYPE.itemsize == 480 and SHARC_SLOT_DTYPE.itemsize == 16

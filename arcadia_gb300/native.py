@@ -64,6 +64,8 @@ SIGNATURES = {
     "arc_trace_frame_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp],
     "arc_trace_frame_noalloc": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp],
     "arc_reserve_surface_list": [_vp, _u64],
+    "arc_set_rigid_bodies": [_vp, _vp, _u32],
+    "arc_trace_rigid_bodies_dev": [_vp, _vp, _u32, _f32, _vp, _vp],
     "arc_restir_gi_temporal_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _vp],
     "arc_trace_rays": [_vp, _vp, _u32, _f32, _u32, _i32, _vp],
     "arc_trace_rays_dev": [_vp, _vp, _u32, _f32, _u32, _i32, _vp],
@@ -378,6 +380,18 @@ class Tracer:
         """ReSTIR GI temporal pass over a traced frame (device pointers; reservoirs of layout.RESERVOIR_DTYPE)."""
         self._check(lib().arc_restir_gi_temporal_dev(self._ctx, w, h, gdm, gnm, gi_hits, res_in, res_out, radiance or None),
                     "arc_restir_gi_temporal_dev")
+
+    def set_rigid_bodies(self, bodies):
+        """Rigid-body table (layout.RIGID_BODY_DTYPE records; their trees must be in the node pool)."""
+        from .layout import RIGID_BODY_DTYPE
+
+        self._bodies = np.ascontiguousarray(bodies).view(RIGID_BODY_DTYPE)
+        self._check(lib().arc_set_rigid_bodies(self._ctx, _p(self._bodies) if len(self._bodies) else None,
+                                               len(self._bodies)), "arc_set_rigid_bodies")
+
+    def trace_rigid_bodies_dev(self, rays, n, max_dist_m, hits, detail=0):
+        self._check(lib().arc_trace_rigid_bodies_dev(self._ctx, rays, n, max_dist_m, hits, detail or None),
+                    "arc_trace_rigid_bodies_dev")
 
     def reserve_surface_list(self, max_pixels: int):
         """Surface list (water / mirror / underwater branches) for frames of up to max_pixels pixels."""

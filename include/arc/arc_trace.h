@@ -218,6 +218,20 @@ int arc_onebounce_dev(arc_ctx* ctx, const uint32_t* idx, uint32_t n, const float
 int arc_sharc_query_list_dev(arc_ctx* ctx, const uint32_t* list, const uint64_t* n_dev, uint32_t max_n,
                              const float* pos, const float* normal, float* out);
 
+/* Rigid voxel bodies (the rigid_bodies buffer, crates/arcadia-render/src/gpu_pools.rs:228-247 and
+ * renderer.rs:567-602): up to ARC_MAX_RIGID_BODIES bodies whose trees are already in the node pool
+ * (uploaded with the world or patched in). The camera's point_light_count.y >> 16 says how many are
+ * traced (the reference's rb_count); frames whose camera names bodies trace them after the world on
+ * the primary, surface and GI rays (primary_gbuffer.wgsl:121-136, lighting_restir_gi.wgsl:209-224),
+ * and so do SHARC updates and the ReSTIR temporal pass. Batched views do not trace bodies (a view of
+ * world slot 0 whose camera names bodies is rejected). n = 0 clears the table. */
+int arc_set_rigid_bodies(arc_ctx* ctx, const arc_rigid_body* bodies, uint32_t n);
+/* trace_rigid_bodies (traversal64.wgsl:1224-1244) over a ray batch (device pointers): hit records
+ * (a body hit has ARC_HIT_FLAG_RIGID, the body index in flags bits 8..12 and the body-local voxel),
+ * and, with detail non-NULL, 9 floats per ray: world hit point, previous-frame hit point, normal. */
+int arc_trace_rigid_bodies_dev(arc_ctx* ctx, const arc_ray* rays, uint32_t n, float max_dist_m, arc_hit_record* hits,
+                               float* detail);
+
 /* ReSTIR GI temporal pass: the GI part of temporal_main (shaders/lighting_restir_gi.wgsl:61-336) for
  * every pixel of a frame traced by arc_trace_frame_dev (its G-buffer and GI hit records, which the
  * pass consumes instead of tracing the GI ray again). reservoir_in holds the previous frame's

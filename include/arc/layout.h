@@ -11,6 +11,7 @@
  *   arc_camera_uniforms   crates/arcadia-render/src/camera.rs:11-38, shaders/common/types.wgsl:19-63
  *   arc_sharc_slot        crates/arcadia-render/src/sharc.rs:49-54, shaders/common/sharc.wgsl:16-21
  *   arc_gi_reservoir      shaders/common/types.wgsl:90-106 (GiReservoir, 32 B)
+ *   arc_rigid_body        crates/arcadia-physics/src/rigid_voxel/types.rs:20-31, shaders/common/types.wgsl:220-226
  *   G-buffer words        shaders/common/types.wgsl:292-332 (20 B per pixel in three arrays)
  *
  * Two records have no buffer counterpart in the reference and are this library's own:
@@ -131,6 +132,20 @@ typedef struct arc_gi_reservoir {
     uint32_t shadow_vis_m;
 } arc_gi_reservoir;
 
+/* One rigid voxel body (GpuRigidBodyInstance, 224 B): column-major 4x4 matrices world -> body-local
+ * meters, body-local -> world meters now and in the previous frame; local_bounds_and_root.xyz the
+ * body's local box in meters (at most 16 m: its tree is one 256^3 chunk tree in the node pool) and .w
+ * the bit pattern of its root node index; world_sphere its bounding sphere (centre, radius) in
+ * meters. The camera's point_light_count.y >> 16 says how many of the uploaded bodies are traced. */
+#define ARC_MAX_RIGID_BODIES 32u
+typedef struct arc_rigid_body {
+    float world_to_local[16];
+    float local_to_world[16];
+    float prev_local_to_world[16];
+    float local_bounds_and_root[4];
+    float world_sphere[4];
+} arc_rigid_body;
+
 /* A ray in world meters: origin xyz, unit direction xyz. */
 typedef struct arc_ray {
     float origin_m[3];
@@ -149,6 +164,9 @@ typedef struct arc_hit_record {
 } arc_hit_record;
 
 #define ARC_HIT_FLAG_HIT 1u
+/* A hit on a rigid body: voxel is the body-local voxel, face the dominant axis of the world normal,
+ * flags bits 8..12 the body index. */
+#define ARC_HIT_FLAG_RIGID 0x10u
 
 ARC_STATIC_ASSERT(sizeof(arc_node64) == 16, "Node64 is 16 B");
 ARC_STATIC_ASSERT(sizeof(arc_brick64) == 64, "LeafBrick64 is 64 B");
@@ -158,6 +176,7 @@ ARC_STATIC_ASSERT(sizeof(arc_sharc_slot) == 16, "SharcResolvedSlot is 16 B");
 ARC_STATIC_ASSERT(sizeof(arc_ray) == 24, "ray is 24 B");
 ARC_STATIC_ASSERT(sizeof(arc_hit_record) == 20, "hit record is 20 B");
 ARC_STATIC_ASSERT(sizeof(arc_gi_reservoir) == 32, "GiReservoir is 32 B");
+ARC_STATIC_ASSERT(sizeof(arc_rigid_body) == 224, "GpuRigidBodyInstance is 224 B");
 
 /* One in-place world edit. The reference has no edit record: its callers invoke
  * ChunkTree64::carve_sphere_tracked (crates/arcadia-core/src/chunk_tree/edit/carve.rs:39-176) and

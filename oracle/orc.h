@@ -59,6 +59,8 @@ typedef struct orc_world {
     const arc_brick64* bricks;
     uint32_t n_bricks;
     const arc_material* palette; /* 256 entries */
+    const arc_rigid_body* bodies; /* rigid bodies (their trees live in the node pool), may be NULL */
+    uint32_t n_bodies;
 } orc_world;
 
 /* Per-ray outcome in the form the CUDA kernels report it. */
@@ -97,6 +99,28 @@ float orc_shadow_vis_di(const orc_world* w, const arc_camera_uniforms* cam, cons
 float orc_shadow_vis(const orc_world* w, const arc_camera_uniforms* cam, const float origin_m[3], const float dir[3],
                      float max_dist_m, uint32_t* bytes);
 uint32_t orc_face_id(const float n[3]);
+
+/* Rigid-body hit (RigidTraceResult) with the body-local voxel, its cell level and the body index. */
+typedef struct orc_rigid_out {
+    uint32_t hit;
+    float t_voxels;
+    float hit_pos_m[3];
+    float prev_hit_pos_m[3];
+    float normal[3];
+    uint32_t mat_id;
+    uint32_t voxel_hash;
+    float contact_ao;
+    uint32_t vi[3];
+    uint32_t shift;
+    uint32_t body;
+} orc_rigid_out;
+void orc_trace_rigid_bodies(const orc_world* w, const arc_camera_uniforms* cam, const float origin_m[3],
+                            const float dir[3], float max_dist_m, orc_rigid_out* best);
+uint32_t orc_rigid_count(const orc_world* w, const arc_camera_uniforms* cam);
+void orc_trace_rigid_rays(const orc_world* w, const arc_camera_uniforms* cam, const arc_ray* rays, uint32_t n,
+                          float max_dist_m, arc_hit_record* hits, float* detail, int threads);
+int orc_trace_scene(const orc_world* w, const arc_camera_uniforms* cam, const float o[3], const float d[3],
+                    float max_dist_m, uint32_t lod_bias, int ignore_water, orc_trace_out* r);
 /* GI ray of a hit pixel from its G-buffer words and what temporal_main reuses of its setup. */
 typedef struct orc_gi_ray {
     float hit_dist;

@@ -174,7 +174,7 @@ static void restir_pixel(const orc_world* w, const arc_camera_uniforms* cam, con
 
     /* GI candidate (195-284) */
     orc_trace_out gi;
-    orc_trace(w, cam, g.origin, g.dir, 0.0f, cam->ray_distances[2], 2u, 1, &gi);
+    orc_trace_scene(w, cam, g.origin, g.dir, cam->ray_distances[2], 2u, 1, &gi);
     const float* bd = g.dir;
     float cand_pos[3], cand_norm[3], lo[3] = {0.0f, 0.0f, 0.0f};
     int cand_sky = 1;

@@ -186,7 +186,7 @@ static void trace_surface(const orc_world* w, const arc_camera_uniforms* cam, co
                           float max_dist, surf* s) {
     memset(s, 0, sizeof(*s));
     orc_trace_out tr;
-    orc_trace(w, cam, o, d, 0.0f, max_dist, 2u, 1, &tr);
+    orc_trace_scene(w, cam, o, d, max_dist, 2u, 1, &tr);
     if (!tr.hit) return;
     const arc_material* m = &w->palette[tr.mat_id];
     s->hit = 1;

@@ -9,8 +9,8 @@
  *
  * Arithmetic is the oracle's canonical one (orc_math.h): expressions are evaluated left to right
  * as written in WGSL, vector operations component by component, pow with an integer exponent by
- * orc_powi and with a non-integer exponent by orc_pow, exp by orc_exp. Rigid bodies are absent
- * (rb_count = 0 makes trace_rigid_bodies a no-op, traversal64.wgsl:1230-1233).
+ * orc_powi and with a non-integer exponent by orc_pow, exp by orc_exp. Every surface ray is followed
+ * by the rigid bodies in front of its world hit, as the reference's trace_rigid_bodies calls.
  */
 #include <string.h>
 
@@ -205,6 +205,14 @@ static void varied_albedo(const arc_material* m, uint32_t hash, float weight, fl
     for (int i = 0; i < 3; ++i) out[i] = orc_clamp(m->albedo_roughness[i] * (1.0f + r * m->emission_meta[3]), 0.01f, 1.0f);
 }
 
+/* trace_rigid_bodies in front of a surface ray's world hit (1 when a body was hit) */
+static int rigid_in_front(const orc_world* w, const arc_camera_uniforms* cam, const float o[3], const float d[3],
+                          float max_dist_m, orc_rigid_out* rb) {
+    if (orc_rigid_count(w, cam) == 0u) return 0;
+    orc_trace_rigid_bodies(w, cam, o, d, max_dist_m, rb);
+    return rb->hit != 0u;
+}
+
 int orc_surface_special(const arc_camera_uniforms* cam, uint32_t mat) {
     if ((cam->point_light_count[1] & 0xFFFFu) != 0u) return 1;
     return mat == MAT_WATER_CRYSTAL || mat == MAT_MIRROR_CHROME;
@@ -237,6 +245,15 @@ void orc_surface_shade(const orc_world* w, const arc_camera_uniforms* cam, const
         for (int i = 0; i < 3; ++i) ro[i] = hp[i] + ray_dir[i] * 0.12f;
         orc_trace(w, cam, ro, refr_dir, 0.0f, cam->ray_distances[0], 1u, 1, &r);
         *bytes += r.bytes;
+        orc_rigid_out rb;
+        if (rigid_in_front(w, cam, ro, refr_dir, r.hit ? r.t_voxels * ARC_VOXEL_SIZE : cam->ray_distances[0], &rb)) {
+            r.hit = 1;
+            r.t_voxels = rb.t_voxels;
+            memcpy(r.hit_pos_m, rb.hit_pos_m, sizeof(r.hit_pos_m));
+            memcpy(r.normal, rb.normal, sizeof(r.normal));
+            r.mat_id = rb.mat_id;
+            r.voxel_hash = rb.voxel_hash;
+        }
         float water_col[3] = {0.03f, 0.16f, 0.24f};
         if (r.hit) {
             const arc_material* bm = &w->palette[r.mat_id];
@@ -265,6 +282,11 @@ void orc_surface_shade(const orc_world* w, const arc_camera_uniforms* cam, const
             float o2[3] = {hp[0] + 0.0f, hp[1] + 0.08f, hp[2] + 0.0f};
             orc_trace(w, cam, o2, refl_dir, 0.0f, 36.0f, 2u, 1, &r);
             *bytes += r.bytes;
+            orc_rigid_out rb2;
+            if (rigid_in_front(w, cam, o2, refl_dir, r.hit ? r.t_voxels * ARC_VOXEL_SIZE : 36.0f, &rb2)) {
+                r.hit = 1;
+                r.mat_id = rb2.mat_id;
+            }
             if (r.hit) {
                 const arc_material* rm = &w->palette[r.mat_id];
                 for (int i = 0; i < 3; ++i) refl_col[i] = rm->albedo_roughness[i] * day_factor + rm->emission_meta[i] * 0.35f;
@@ -294,6 +316,15 @@ void orc_surface_shade(const orc_world* w, const arc_camera_uniforms* cam, const
             if (re.hit) r = re;
         }
         int self = r.hit && r.mat_id == MAT_MIRROR_CHROME && r.t_voxels * ARC_VOXEL_SIZE < 0.12f;
+        orc_rigid_out rb;
+        if (rigid_in_front(w, cam, ro, refl_dir, (r.hit && !self) ? r.t_voxels * ARC_VOXEL_SIZE : cam->ray_distances[1], &rb)) {
+            r.hit = 1;
+            r.t_voxels = rb.t_voxels;
+            memcpy(r.hit_pos_m, rb.hit_pos_m, sizeof(r.hit_pos_m));
+            memcpy(r.normal, rb.normal, sizeof(r.normal));
+            r.mat_id = rb.mat_id;
+            r.voxel_hash = rb.voxel_hash;
+        }
         if (r.hit && !self) {
             const arc_material* rm = &w->palette[r.mat_id];
             float ra[3], sky[3], light[3];

@@ -336,6 +336,227 @@ void orc_trace(const orc_world* w, const arc_camera_uniforms* cam, const float o
 }
 
 /* is_emissive_mat: traversal64.wgsl:775-777 */
+static void fill_hit_record(const orc_trace_out* r, float t_scale_m, arc_hit_record* h);
+
+/* mat4x4 (column-major) * vec4(v, w): ((c0 x + c1 y) + c2 z) + c3 w per row */
+static void xform4(const float* M, const float v[3], float wc, float out[3]) {
+    for (int r = 0; r < 3; ++r) out[r] = ((M[r] * v[0] + M[4 + r] * v[1]) + M[8 + r] * v[2]) + M[12 + r] * wc;
+}
+
+/* trace_single_rigid_body: traversal64.wgsl:1006-1222 */
+static void trace_single_rigid(const orc_world* w, uint32_t body, const float origin_m[3], const float dir[3],
+                               float max_dist_m, orc_rigid_out* res) {
+    memset(res, 0, sizeof(*res));
+    res->t_voxels = max_dist_m * ARC_VOXELS_PER_METER;
+    res->normal[1] = 1.0f;
+    res->contact_ao = 1.0f;
+    res->body = body;
+    const arc_rigid_body* rb = &w->bodies[body];
+    uint32_t root_idx = orc_fbits(rb->local_bounds_and_root[3]);
+    if (root_idx == ARC_EMPTY_CHUNK) return;
+    /* bounding-sphere pre-reject */
+    float oc[3] = {origin_m[0] - rb->world_sphere[0], origin_m[1] - rb->world_sphere[1], origin_m[2] - rb->world_sphere[2]};
+    float bp = orc_dot3(oc, dir);
+    float cd = orc_dot3(oc, oc) - rb->world_sphere[3] * rb->world_sphere[3];
+    if (cd > 0.0f && bp > 0.0f) return;
+    float disc = bp * bp - cd;
+    if (disc < 0.0f) return;
+    float near = orc_max(-bp - sqrtf(disc), 0.0f);
+    if (near >= max_dist_m) return;
+    /* body-local voxel space */
+    float lo_m[3], ld[3], vo[3], lmax[3], sd[3], inv[3], noi[3];
+    xform4(rb->world_to_local, origin_m, 1.0f, lo_m);
+    xform4(rb->world_to_local, dir, 0.0f, ld);
+    for (int i = 0; i < 3; ++i) {
+        vo[i] = lo_m[i] * ARC_VOXELS_PER_METER;
+        lmax[i] = rb->local_bounds_and_root[i] * ARC_VOXELS_PER_METER;
+        sd[i] = fabsf(ld[i]) < 1e-7f ? 1e-7f : ld[i];
+        inv[i] = 1.0f / sd[i];
+    }
+    float max_t_v = max_dist_m * ARC_VOXELS_PER_METER;
+    const float zero[3] = {0.0f, 0.0f, 0.0f};
+    float b0, b1;
+    intersect_aabb(vo, inv, zero, lmax, &b0, &b1);
+    float t_enter = orc_max(b0, 0.0f);
+    if (b1 < t_enter || t_enter >= max_t_v) return;
+    float t = t_enter;
+    float t_limit = orc_min(b1, max_t_v);
+    int pos[3];
+    uint32_t maxi[3];
+    for (int i = 0; i < 3; ++i) {
+        pos[i] = inv[i] >= 0.0f;
+        noi[i] = -vo[i] * inv[i];
+        maxi[i] = orc_f2u(lmax[i] + 0.5f);
+    }
+    u3 vi;
+    {
+        float p[3];
+        for (int i = 0; i < 3; ++i) p[i] = orc_clamp(vo[i] + ld[i] * (t + 1e-4f), 0.0f, lmax[i] - 1e-3f);
+        vi.x = orc_f2u(p[0]);
+        vi.y = orc_f2u(p[1]);
+        vi.z = orc_f2u(p[2]);
+    }
+    u3 prev = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+    uint32_t cached_shift = 6u, bytes = 0;
+    arc_node64 c1, c2, c3;
+    memset(&c1, 0, sizeof(c1));
+    memset(&c2, 0, sizeof(c2));
+    memset(&c3, 0, sizeof(c3));
+    for (uint32_t step = 0; step < 64u; ++step) {
+        if (t >= t_limit) break;
+        if (vi.x >= maxi[0] || vi.y >= maxi[1] || vi.z >= maxi[2]) break;
+        uint32_t diff = (prev.x ^ vi.x) | (prev.y ^ vi.y) | (prev.z ^ vi.z);
+        prev = vi;
+        arc_node64 node;
+        uint32_t shift;
+        if (diff < 4u && cached_shift == 0u) {
+            node = c3;
+            shift = 0u;
+        } else if (diff < 16u && cached_shift <= 2u) {
+            node = c2;
+            shift = 2u;
+        } else if (diff < 64u && cached_shift <= 4u) {
+            node = c1;
+            shift = 4u;
+        } else {
+            node = load_node(w, root_idx, &bytes);
+            shift = 6u;
+        }
+        cached_shift = shift;
+        uint32_t l[3] = {vi.x & 255u, vi.y & 255u, vi.z & 255u};
+        for (;;) {
+            uint32_t cx = (l[0] >> shift) & 3u, cy = (l[1] >> shift) & 3u, cz = (l[2] >> shift) & 3u;
+            uint32_t b = (cz << 4) | (cy << 2) | cx;
+            uint32_t span = 1u << shift;
+            u3 cmin = {vi.x & ~(span - 1u), vi.y & ~(span - 1u), vi.z & ~(span - 1u)};
+            u3 cmax = {cmin.x + span, cmin.y + span, cmin.z + span};
+            if (!node_has_child(node.mask_low, node.mask_high, b)) {
+                step_dda_box(vo, ld, inv, noi, pos, cmin, cmax, t, &t, &vi);
+                break;
+            }
+            if (node.child_ptr & ARC_IS_LEAF_FLAG) {
+                uint32_t mat = (node.lod_payload >> 24) & 0xFFu;
+                if (!(node.child_ptr & ARC_IS_UNIFORM_FLAG)) mat = brick_get_material(w, node.child_ptr & ARC_PTR_INDEX_MASK, b, &bytes);
+                if (mat != ARC_MAT_AIR) {
+                    uint32_t ec[3] = {pos[0] ? cmin.x : cmax.x, pos[1] ? cmin.y : cmax.y, pos[2] ? cmin.z : cmax.z};
+                    float tm[3];
+                    for (int i = 0; i < 3; ++i) tm[i] = (float)ec[i] * inv[i] + noi[i];
+                    float enter = orc_max(orc_max(tm[0], tm[1]), tm[2]);
+                    float et = orc_max(enter, 0.0f);
+                    float hpv[3], hpm[3];
+                    for (int i = 0; i < 3; ++i) {
+                        hpv[i] = vo[i] + ld[i] * et;
+                        hpm[i] = hpv[i] * ARC_VOXEL_SIZE;
+                    }
+                    res->hit = 1;
+                    res->t_voxels = et;
+                    xform4(rb->local_to_world, hpm, 1.0f, res->hit_pos_m);
+                    xform4(rb->prev_local_to_world, hpm, 1.0f, res->prev_hit_pos_m);
+                    float ln[3] = {0.0f, 0.0f, 0.0f};
+                    if (tm[0] >= tm[1] && tm[0] >= tm[2]) ln[0] = -orc_sign(ld[0]);
+                    else if (tm[1] >= tm[2]) ln[1] = -orc_sign(ld[1]);
+                    else ln[2] = -orc_sign(ld[2]);
+                    float wn[3];
+                    xform4(rb->local_to_world, ln, 0.0f, wn);
+                    orc_normalize3(wn, res->normal);
+                    res->mat_id = mat;
+                    res->voxel_hash = orc_pcg_hash((vi.x * 73856093u) ^ (vi.y * 19349663u) ^ (vi.z * 83492791u));
+                    res->vi[0] = vi.x;
+                    res->vi[1] = vi.y;
+                    res->vi[2] = vi.z;
+                    res->shift = shift;
+                    if (shift == 0u) res->contact_ao = eval_leaf_bitwise_ao(node.mask_low, node.mask_high, cx, cy, cz, ln, hpv);
+                    return;
+                }
+                step_dda_box(vo, ld, inv, noi, pos, cmin, cmax, t, &t, &vi);
+                break;
+            }
+            node = load_node(w, node_child_offset(&node, b), &bytes);
+            shift -= 2u;
+            cached_shift = shift;
+            if (shift == 4u) c1 = node;
+            else if (shift == 2u) c2 = node;
+            else if (shift == 0u) c3 = node;
+        }
+    }
+}
+
+/* trace_rigid_bodies: traversal64.wgsl:1224-1244 (bodies min(cam count, table size, 32)) */
+void orc_trace_rigid_bodies(const orc_world* w, const arc_camera_uniforms* cam, const float origin_m[3],
+                            const float dir[3], float max_dist_m, orc_rigid_out* best) {
+    memset(best, 0, sizeof(*best));
+    best->t_voxels = max_dist_m * ARC_VOXELS_PER_METER;
+    best->normal[1] = 1.0f;
+    best->contact_ao = 1.0f;
+    uint32_t n = orc_umin(orc_umin((cam->point_light_count[1] >> 16) & 0xFFFFu, ARC_MAX_RIGID_BODIES), w->n_bodies);
+    float cur = max_dist_m;
+    for (uint32_t i = 0; i < n; ++i) {
+        orc_rigid_out c;
+        trace_single_rigid(w, i, origin_m, dir, cur, &c);
+        if (c.hit && c.t_voxels < best->t_voxels) {
+            *best = c;
+            cur = c.t_voxels * ARC_VOXEL_SIZE;
+        }
+    }
+}
+
+/* A secondary-ray trace of the static world followed by the rigid bodies in front of its hit, as
+ * the GI ray (lighting_restir_gi.wgsl:209-224) and sharc_trace_surface (sharc_update.wgsl:32-52) do:
+ * a rigid hit replaces hit, distance, point, normal and material, and its LOD colour is the
+ * material's albedo. Returns the body index of a rigid hit, -1 otherwise. */
+int orc_trace_scene(const orc_world* w, const arc_camera_uniforms* cam, const float o[3], const float d[3],
+                    float max_dist_m, uint32_t lod_bias, int ignore_water, orc_trace_out* r) {
+    orc_trace(w, cam, o, d, 0.0f, max_dist_m, lod_bias, ignore_water, r);
+    if (orc_rigid_count(w, cam) == 0u) return -1;
+    orc_rigid_out rb;
+    orc_trace_rigid_bodies(w, cam, o, d, r->hit ? r->t_voxels * ARC_VOXEL_SIZE : max_dist_m, &rb);
+    if (!rb.hit) return -1;
+    r->hit = 1;
+    r->t_voxels = rb.t_voxels;
+    memcpy(r->hit_pos_m, rb.hit_pos_m, sizeof(r->hit_pos_m));
+    memcpy(r->normal, rb.normal, sizeof(r->normal));
+    r->mat_id = rb.mat_id;
+    memcpy(r->lod_rgb, w->palette[rb.mat_id].albedo_roughness, sizeof(r->lod_rgb));
+    memcpy(r->vi, rb.vi, sizeof(r->vi));
+    r->shift = rb.shift;
+    return (int)rb.body;
+}
+
+/* trace_rigid_bodies over a ray batch: hit records as the GPU writes them (body hits flagged, the
+ * body index in flags bits 8..12) and 9 floats per ray (hit point, previous hit point, normal). */
+void orc_trace_rigid_rays(const orc_world* w, const arc_camera_uniforms* cam, const arc_ray* rays, uint32_t n,
+                          float max_dist_m, arc_hit_record* hits, float* detail, int threads) {
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads > 0 ? threads : 1)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        orc_rigid_out rb;
+        orc_trace_rigid_bodies(w, cam, rays[i].origin_m, rays[i].dir, max_dist_m, &rb);
+        orc_trace_out r;
+        memset(&r, 0, sizeof(r));
+        r.hit = rb.hit;
+        r.t_voxels = rb.t_voxels;
+        memcpy(r.normal, rb.normal, sizeof(r.normal));
+        r.mat_id = rb.mat_id;
+        memcpy(r.vi, rb.vi, sizeof(r.vi));
+        r.shift = rb.shift;
+        fill_hit_record(&r, ARC_VOXEL_SIZE, &hits[i]);
+        if (rb.hit) hits[i].flags = (uint16_t)(hits[i].flags | ARC_HIT_FLAG_RIGID | (rb.body << 8));
+        if (detail) {
+            float* q = detail + 9 * i;
+            if (rb.hit) {
+                memcpy(q, rb.hit_pos_m, 12);
+                memcpy(q + 3, rb.prev_hit_pos_m, 12);
+            } else {
+                for (int k = 0; k < 3; ++k) q[k] = q[3 + k] = rays[i].origin_m[k] + rays[i].dir[k] * max_dist_m;
+            }
+            memcpy(q + 6, rb.normal, 12);
+        }
+    }
+}
+
+uint32_t orc_rigid_count(const orc_world* w, const arc_camera_uniforms* cam) {
+    return orc_umin(orc_umin((cam->point_light_count[1] >> 16) & 0xFFFFu, ARC_MAX_RIGID_BODIES), w->n_bodies);
+}
+
 static int is_emissive_mat(uint32_t m) { return (m >= 19u && m <= 22u) || m == 24u || m == 27u; }
 
 /* trace_shadow_vis: traversal64.wgsl:571-773 (di = 0); trace_shadow_vis_di: traversal64.wgsl:781-989
@@ -542,7 +763,32 @@ static void primary_pixel(const orc_world* w, const arc_camera_uniforms* cam, ui
     orc_trace_out r;
     orc_trace(w, cam, eye, d, 0.0f, 250.0f, 0u, underwater, &r);
     *bytes += r.bytes + 20u + 20u;
-    if (hit) fill_hit_record(&r, ARC_VOXEL_SIZE, hit);
+    /* rigid bodies in front of the world hit (primary_gbuffer.wgsl:123-136) */
+    float prev_pos[3] = {r.hit_pos_m[0], r.hit_pos_m[1], r.hit_pos_m[2]};
+    int rigid = 0;
+    uint32_t body = 0;
+    if (orc_rigid_count(w, cam) > 0u) {
+        orc_rigid_out rb;
+        orc_trace_rigid_bodies(w, cam, eye, d, r.hit ? r.t_voxels * ARC_VOXEL_SIZE : 250.0f, &rb);
+        if (rb.hit) {
+            r.hit = 1;
+            r.t_voxels = rb.t_voxels;
+            memcpy(r.hit_pos_m, rb.hit_pos_m, sizeof(r.hit_pos_m));
+            memcpy(r.normal, rb.normal, sizeof(r.normal));
+            r.mat_id = rb.mat_id;
+            r.voxel_hash = rb.voxel_hash;
+            r.contact_ao = rb.contact_ao;
+            memcpy(r.vi, rb.vi, sizeof(r.vi));
+            r.shift = rb.shift;
+            memcpy(prev_pos, rb.prev_hit_pos_m, sizeof(prev_pos));
+            rigid = 1;
+            body = rb.body;
+        }
+    }
+    if (hit) {
+        fill_hit_record(&r, ARC_VOXEL_SIZE, hit);
+        if (rigid) hit->flags = (uint16_t)(hit->flags | ARC_HIT_FLAG_RIGID | (body << 8));
+    }
     if (!r.hit) {
         float p[2];
         oct_encode(d, p);
@@ -562,7 +808,7 @@ static void primary_pixel(const orc_world* w, const arc_camera_uniforms* cam, ui
     /* motion: primary_gbuffer.wgsl:298-305 */
     float pu = ((float)x + 0.5f) / (float)W, pv = ((float)y + 0.5f) / (float)H;
     const float* M = cam->prev_view_proj;
-    float hp[4] = {r.hit_pos_m[0], r.hit_pos_m[1], r.hit_pos_m[2], 1.0f};
+    float hp[4] = {prev_pos[0], prev_pos[1], prev_pos[2], 1.0f};
     float clip[4];
     for (int row = 0; row < 4; ++row)
         clip[row] = ((M[0 * 4 + row] * hp[0] + M[1 * 4 + row] * hp[1]) + M[2 * 4 + row] * hp[2]) + M[3 * 4 + row] * hp[3];
@@ -577,7 +823,7 @@ static void primary_pixel(const orc_world* w, const arc_camera_uniforms* cam, ui
     float p[2];
     oct_encode(nrm, p);
     out[0] = orc_fbits(hit_dist);
-    out[1] = (r.mat_id & 0xFFFFu);
+    out[1] = (r.mat_id & 0xFFFFu) | ((uint32_t)rigid << 16);
     out[2] = orc_pack2x16snorm(p[0], p[1]);
     out[3] = orc_pack2x16float(mx, my);
     out[4] = orc_pack4x8unorm(alb[0], alb[1], alb[2], orc_clamp(r.contact_ao, 0.0f, 1.0f));
@@ -728,9 +974,10 @@ void orc_gi_rays(const orc_world* w, const arc_camera_uniforms* cam, uint32_t x0
         arc_hit_record hr;
         if (gi_ray_for_pixel(w, cam, x, y, W, H, gdm[2 * k], gnm[2 * k], o, d, &b)) {
             orc_trace_out r;
-            orc_trace(w, cam, o, d, 0.0f, cam->ray_distances[2], 2u, 1, &r);
+            int body = orc_trace_scene(w, cam, o, d, cam->ray_distances[2], 2u, 1, &r);
             b += r.bytes + 20u;
             fill_hit_record(&r, ARC_VOXEL_SIZE, &hr);
+            if (body >= 0) hr.flags = (uint16_t)(hr.flags | ARC_HIT_FLAG_RIGID | ((uint32_t)body << 8));
             if (gi_rays_out) {
                 memcpy(gi_rays_out[k].origin_m, o, sizeof(o));
                 memcpy(gi_rays_out[k].dir, d, sizeof(d));

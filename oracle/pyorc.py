@@ -69,6 +69,8 @@ class _World(C.Structure):
         ("bricks", C.c_void_p),
         ("n_bricks", C.c_uint32),
         ("palette", C.c_void_p),
+        ("bodies", C.c_void_p),
+        ("n_bodies", C.c_uint32),
     ]
 
 
@@ -87,6 +89,7 @@ def lib():
         _lib.orc_primary.argtypes = [C.POINTER(_World), vp, u32, u32, u32, u32, vp, vp, vp, vp, vp, i32]
         _lib.orc_gi_rays.argtypes = [C.POINTER(_World), vp, u32, u32, u32, u32, vp, vp, vp, vp, vp, i32]
         _lib.orc_restir_gi_temporal.argtypes = [C.POINTER(_World), vp, vp, vp, vp, vp, vp, vp, i32]
+        _lib.orc_trace_rigid_rays.argtypes = [C.POINTER(_World), vp, vp, u32, f32, vp, vp, i32]
         _lib.orc_frame_sample.argtypes = [C.POINTER(_World), vp, u32, i32, vp, vp, vp]
         _lib.orc_frame_sample.restype = C.c_uint64
         _lib.orc_cpu_frame_sample.argtypes = [C.POINTER(_World), vp, u32, i32, vp, vp, vp]
@@ -142,15 +145,23 @@ def default_palette() -> np.ndarray:
 class World:
     """Flat GPU-ready pools (chunk roots, Node64 pool, LeafBrick64 pool, palette)."""
 
-    def __init__(self, grid, roots, nodes, bricks, palette=None):
+    def __init__(self, grid, roots, nodes, bricks, palette=None, bodies=None):
+        from arcadia_gb300.layout import RIGID_BODY_DTYPE
+
         self.grid = tuple(int(g) for g in grid)
         self.roots = np.ascontiguousarray(roots, np.uint32)
         self.nodes = np.ascontiguousarray(nodes).view(NODE_DTYPE)
         self.bricks = np.ascontiguousarray(bricks).view(BRICK_DTYPE)
         self.palette = default_palette() if palette is None else np.ascontiguousarray(palette).view(MATERIAL_DTYPE)
+        self.bodies = np.zeros(0, RIGID_BODY_DTYPE) if bodies is None else np.ascontiguousarray(bodies).view(RIGID_BODY_DTYPE)
         self._w = _World(
-            _p(self.roots), _p(self.nodes), len(self.nodes), _p(self.bricks), len(self.bricks), _p(self.palette)
+            _p(self.roots), _p(self.nodes), len(self.nodes), _p(self.bricks), len(self.bricks), _p(self.palette),
+            _p(self.bodies) if len(self.bodies) else None, len(self.bodies)
         )
+
+    def with_bodies(self, bodies) -> "World":
+        """The same pools with a rigid-body table."""
+        return World(self.grid, self.roots, self.nodes, self.bricks, self.palette, bodies)
 
     @property
     def cw(self):
@@ -275,6 +286,15 @@ def gi_rays(world: World, cam: np.ndarray, gdm, gnm, rect=None, threads: int = 8
     by = np.zeros(h * w, np.uint32)
     lib().orc_gi_rays(world.cw, _p(cam), x0, y0, x1, y1, _p(gdm), _p(gnm), _p(rays), _p(hits), _p(by), threads)
     return rays, hits, by
+
+
+def trace_rigid_rays(world: World, cam: np.ndarray, rays: np.ndarray, max_dist_m: float, threads: int = 8):
+    """trace_rigid_bodies over a ray batch: (hit records, (n, 9) hit point / previous point / normal)."""
+    rays = np.ascontiguousarray(rays).view(RAY_DTYPE)
+    hits = np.zeros(len(rays), HIT_DTYPE)
+    detail = np.zeros((len(rays), 9), np.float32)
+    lib().orc_trace_rigid_rays(world.cw, _p(cam), _p(rays), len(rays), max_dist_m, _p(hits), _p(detail), threads)
+    return hits, detail
 
 
 def restir_gi_temporal(world: World, cam: np.ndarray, resolved: np.ndarray, gdm, gnm, res_in: np.ndarray,
