@@ -429,6 +429,12 @@ def run_ours(args):
                                 "frac": round(kt["tcgen05"]["query_tflops"] / bf16_peak, 4) if bf16_peak else None}
         nrc["kernels"] = kt
 
+    # ReSTIR GI temporal pass on this world's frames (before the batch replaces world slot 0)
+    restir = None
+    if not args.no_restir:
+        t.set_launch_config(variant=cfg.variant)
+        restir = restir_section(t, scene, W_, H_, dev, (gdm, gnm, gaa, hits, gi))
+
     # many views over several worlds in one persistent launch replayed from a CUDA graph
     batched = None
     if not args.no_batched:
@@ -453,10 +459,6 @@ def run_ours(args):
                    "launch": {"kernel": "persistent" if best.variant == 1 else "plain",
                               "block_threads": best.block_threads, "reg_blocks": best.reg_blocks,
                               "refill_threshold": best.refill_threshold, "tile": [best.tile_w, best.tile_h]}}
-    restir = None
-    if not args.no_restir:
-        t.set_launch_config(variant=cfg.variant)
-        restir = restir_section(t, scene, W_, H_, dev, (gdm, gnm, gaa, hits, gi))
     t.close()
 
     # full pipeline on the 4096^3 sparse world: in-place edits (1 % of the leaf bricks per frame), 4K
