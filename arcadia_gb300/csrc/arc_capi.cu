@@ -157,6 +157,29 @@ int arc_ctx_stage(arc_ctx* c, size_t bytes, void** out) {
     return ARC_OK;
 }
 
+int arc_ctx_side_begin(arc_ctx* c) {
+    if (!c->side_stream) {
+        ARC_CK(c, cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking));
+        ARC_CK(c, cudaEventCreateWithFlags(&c->side_fork, cudaEventDisableTiming));
+        ARC_CK(c, cudaEventCreateWithFlags(&c->side_join, cudaEventDisableTiming));
+    }
+    ARC_CK(c, cudaEventRecord(c->side_fork, c->stream));
+    ARC_CK(c, cudaStreamWaitEvent(c->side_stream, c->side_fork, 0));
+    std::swap(c->stream, c->side_stream);
+    return ARC_OK;
+}
+
+int arc_ctx_side_end(arc_ctx* c) {
+    std::swap(c->stream, c->side_stream);
+    ARC_CK(c, cudaEventRecord(c->side_join, c->side_stream));
+    return ARC_OK;
+}
+
+int arc_ctx_side_join(arc_ctx* c) {
+    ARC_CK(c, cudaStreamWaitEvent(c->stream, c->side_join, 0));
+    return ARC_OK;
+}
+
 int arc_ctx_reserve_surface(arc_ctx* c, size_t entries) {
     if (c->surf_cap >= entries && c->d_surf_count) return ARC_OK;
     ARC_CK(c, cudaStreamSynchronize(c->stream));
@@ -267,6 +290,12 @@ int arc_destroy(arc_ctx* c) {
     cudaFree(c->d_nrc_batch);
     cudaFree(c->d_nrc_gate);
     cudaFree(c->d_nrc_loss);
+    if (c->side_stream) {
+        cudaStreamSynchronize(c->side_stream);
+        cudaStreamDestroy(c->side_stream);
+        cudaEventDestroy(c->side_fork);
+        cudaEventDestroy(c->side_join);
+    }
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);

@@ -117,6 +117,10 @@ struct arc_ctx {
     cudaStream_t band_stream[kMaxBands] = {};  // the plain kernel's bands run concurrently, one per stream
     cudaEvent_t band_ev[kMaxBands] = {};
     cudaEvent_t copies_done = nullptr, frame_start = nullptr;
+    // side stream for a cache query that overlaps the cache's own update (arc_nrc_frame_dev,
+    // arc_sharc_frame_dev): forked from and joined back into `stream` with two events
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t side_fork = nullptr, side_join = nullptr;
     bool timing_pending = false;
     float last_ms = 0.0f;
     uint64_t last_rays = 0;
@@ -139,6 +143,12 @@ extern "C" int arc_launch_train_samples_list(arc_ctx* c, const uint32_t* list, c
                                              uint32_t n_samples, uint32_t steps, float* train_in, float* train_t,
                                              uint32_t* gate);
 int arc_ctx_stage(arc_ctx* c, size_t bytes, void** out);
+// Work enqueued between arc_ctx_side_begin and arc_ctx_side_end goes to the side stream, which first
+// waits for everything enqueued on the context's stream so far; arc_ctx_side_join makes the context's
+// stream wait for that side work. Between begin and end, c->stream is the side stream.
+int arc_ctx_side_begin(arc_ctx* c);
+int arc_ctx_side_end(arc_ctx* c);
+int arc_ctx_side_join(arc_ctx* c);
 // surface list of at least `entries` entries (frees and reallocates when smaller)
 int arc_ctx_reserve_surface(arc_ctx* c, size_t entries);
 // whether any word of the pools holds material 18 (water) or 28 (mirror) in a brick or a node payload

@@ -1002,6 +1002,11 @@ int launch_adam(arc_ctx* c, float lr, const uint32_t* gate) {
 
 }  // namespace
 
+// One training frame: samples from the hit list, then `steps` Adam steps (join_side: the context's
+// stream waits for the side-stream query before the first step).
+static int train_frame(arc_ctx* c, const uint32_t* list, const uint64_t* n_valid, const float* pos, const float* normal,
+                       const float* nrc_in, uint32_t seed, uint32_t n_samples, uint32_t steps, float lr, bool join_side);
+
 extern "C" {
 
 int arc_nrc_init(arc_ctx* c, uint32_t seed) {
@@ -1108,9 +1113,35 @@ int arc_nrc_train_step_dev(arc_ctx* c, const float* inputs, const float* targets
     return ARC_OK;
 }
 
+int arc_nrc_frame_dev(arc_ctx* c, const uint32_t* list, const uint64_t* n_valid, uint32_t max_n, const float* pos,
+                      const float* normal, const float* nrc_in, const float* albedo, float* out_rgb, uint32_t seed,
+                      uint32_t n_samples, uint32_t steps, float lr) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if (!list || !n_valid || !pos || !normal || !nrc_in || !out_rgb) return nrc_err(c, ARC_E_INVALID_ARG, "null buffer");
+    if (steps == 0 || n_samples < steps || n_samples % steps)
+        return nrc_err(c, ARC_E_INVALID_ARG, "n_samples must be a non-zero multiple of steps");
+    if ((rc = ensure_nrc(c))) return rc;
+    // the query reads the weights the previous frame's last step left; it runs beside the sample
+    // generation and ends before this frame's first Adam step rewrites them
+    if ((rc = arc_ctx_side_begin(c))) return rc;
+    rc = max_n ? launch_infer(c, nrc_in, albedo, max_n, out_rgb, list, reinterpret_cast<const unsigned long long*>(n_valid))
+               : ARC_OK;
+    int rc2 = arc_ctx_side_end(c);
+    if (rc || (rc = rc2)) return rc;
+    return train_frame(c, list, n_valid, pos, normal, nrc_in, seed, n_samples, steps, lr, true);
+}
+
 int arc_nrc_train_frame_dev(arc_ctx* c, const uint32_t* list, const uint64_t* n_valid, const float* pos,
                             const float* normal, const float* nrc_in, uint32_t seed, uint32_t n_samples,
                             uint32_t steps, float lr) {
+    return train_frame(c, list, n_valid, pos, normal, nrc_in, seed, n_samples, steps, lr, false);
+}
+
+}  // extern "C"
+
+static int train_frame(arc_ctx* c, const uint32_t* list, const uint64_t* n_valid, const float* pos, const float* normal,
+                       const float* nrc_in, uint32_t seed, uint32_t n_samples, uint32_t steps, float lr, bool join_side) {
     int rc = arc_ctx_check_ready(c, true);
     if (rc) return rc;
     if (!list || !n_valid || !pos || !normal || !nrc_in) return nrc_err(c, ARC_E_INVALID_ARG, "null buffer");
@@ -1130,6 +1161,7 @@ int arc_nrc_train_frame_dev(arc_ctx* c, const uint32_t* list, const uint64_t* n_
     if ((rc = arc_launch_train_samples_list(c, list, reinterpret_cast<const unsigned long long*>(n_valid), pos, normal,
                                             nrc_in, seed, n_samples, steps, train_in, train_t, c->d_nrc_gate)))
         return rc;
+    if (join_side && (rc = arc_ctx_side_join(c))) return rc;
     const uint32_t per = n_samples / steps;
     for (uint32_t k = 0; k < steps; ++k) {
         if ((rc = launch_grad(c, train_in + 9u * (size_t)k * per, train_t + 3u * (size_t)k * per, per, c->d_nrc_gate)) ||
@@ -1138,5 +1170,3 @@ int arc_nrc_train_frame_dev(arc_ctx* c, const uint32_t* list, const uint64_t* n_
     }
     return ARC_OK;
 }
-
-}  // extern "C"

@@ -604,6 +604,23 @@ int arc_launch_train_samples_list(arc_ctx* c, const uint32_t* list, const unsign
     return launch_check(c, "train_samples_list_kernel");
 }
 
+// One SHARC frame with the query beside the update: the query at the hit list reads the resolved
+// slots of the previous frame's resolve, on the side stream, while the update deposits this frame's
+// radiance; the resolve waits for both.
+int arc_sharc_frame_dev(arc_ctx* c, uint32_t width, uint32_t height, const uint32_t* gdm, const uint32_t* gnm,
+                        const uint32_t* list, const uint64_t* n_dev, uint32_t max_n, const float* pos, const float* normal,
+                        float* out) {
+    if (!c) return ARC_E_INVALID_ARG;
+    int rc = arc_ctx_side_begin(c);
+    if (rc) return rc;
+    rc = arc_sharc_query_list_dev(c, list, n_dev, max_n, pos, normal, out);
+    int rc2 = arc_ctx_side_end(c);
+    if (rc || (rc = rc2)) return rc;
+    if ((rc = arc_sharc_update_dev(c, width, height, gdm, gnm))) return rc;
+    if ((rc = arc_ctx_side_join(c))) return rc;
+    return arc_sharc_resolve(c);
+}
+
 int arc_sharc_query_list_dev(arc_ctx* c, const uint32_t* list, const uint64_t* n_dev, uint32_t max_n, const float* pos,
                              const float* normal, float* out) {
     if (!c) return ARC_E_INVALID_ARG;

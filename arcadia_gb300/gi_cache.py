@@ -94,28 +94,43 @@ class CacheComparison:
         b.synchronize()
         return a.elapsed_time(b)
 
-    def sharc_frame(self):
+    def sharc_frame(self, overlap=False):
+        """SHARC update + resolve + query at every GI hit; with overlap the query runs beside the update
+        against the previous frame's resolve (arc_sharc_frame_dev). Returns its device time in ms."""
         a = self._event()
-        self._ck(self.lib.arc_sharc_update_dev(self.t.ctx, self.w, self.h, self.gdm.data_ptr(), self.gnm.data_ptr()),
-                 "arc_sharc_update_dev")
-        self._ck(self.lib.arc_sharc_resolve(self.t.ctx), "arc_sharc_resolve")
-        self._ck(self.lib.arc_sharc_query_list_dev(self.t.ctx, self.list.data_ptr(), self.n_valid.data_ptr(), self.w * self.h,
-                                                   self.pos.data_ptr(), self.nrm.data_ptr(), self.sharc_out.data_ptr()),
-                 "arc_sharc_query_list_dev")
+        if overlap:
+            self._ck(self.lib.arc_sharc_frame_dev(self.t.ctx, self.w, self.h, self.gdm.data_ptr(), self.gnm.data_ptr(),
+                                                  self.list.data_ptr(), self.n_valid.data_ptr(), self.w * self.h,
+                                                  self.pos.data_ptr(), self.nrm.data_ptr(), self.sharc_out.data_ptr()),
+                     "arc_sharc_frame_dev")
+        else:
+            self._ck(self.lib.arc_sharc_update_dev(self.t.ctx, self.w, self.h, self.gdm.data_ptr(), self.gnm.data_ptr()),
+                     "arc_sharc_update_dev")
+            self._ck(self.lib.arc_sharc_resolve(self.t.ctx), "arc_sharc_resolve")
+            self._ck(self.lib.arc_sharc_query_list_dev(self.t.ctx, self.list.data_ptr(), self.n_valid.data_ptr(),
+                                                       self.w * self.h, self.pos.data_ptr(), self.nrm.data_ptr(),
+                                                       self.sharc_out.data_ptr()), "arc_sharc_query_list_dev")
         b = self._event()
         b.synchronize()
         return a.elapsed_time(b)
 
-    def nrc_frame(self, seed, lr=1e-3, steps=8):
-        """One training frame (TRAIN_SAMPLES samples, `steps` Adam steps on equal slices), then inference at
-        every GI hit; returns its device time in ms."""
+    def nrc_frame(self, seed, lr=1e-3, steps=8, overlap=False):
+        """One training frame (TRAIN_SAMPLES samples, `steps` Adam steps on equal slices) and inference at
+        every GI hit; with overlap the inference runs beside the sample generation with the previous
+        frame's weights (arc_nrc_frame_dev). Returns its device time in ms."""
         a = self._event()
-        self._ck(self.lib.arc_nrc_train_frame_dev(self.t.ctx, self.list.data_ptr(), self.n_valid.data_ptr(),
-                                                  self.pos.data_ptr(), self.nrm.data_ptr(), self.nin.data_ptr(), seed,
-                                                  TRAIN_SAMPLES, steps, C.c_float(lr)), "arc_nrc_train_frame_dev")
-        self._ck(self.lib.arc_nrc_query_list_dev(self.t.ctx, self.list.data_ptr(), self.n_valid.data_ptr(), self.w * self.h,
-                                                 self.nin.data_ptr(), self.alb.data_ptr(), self.nrc_out.data_ptr()),
-                 "arc_nrc_query_list_dev")
+        if overlap:
+            self._ck(self.lib.arc_nrc_frame_dev(self.t.ctx, self.list.data_ptr(), self.n_valid.data_ptr(), self.w * self.h,
+                                                self.pos.data_ptr(), self.nrm.data_ptr(), self.nin.data_ptr(),
+                                                self.alb.data_ptr(), self.nrc_out.data_ptr(), seed, TRAIN_SAMPLES, steps,
+                                                C.c_float(lr)), "arc_nrc_frame_dev")
+        else:
+            self._ck(self.lib.arc_nrc_train_frame_dev(self.t.ctx, self.list.data_ptr(), self.n_valid.data_ptr(),
+                                                      self.pos.data_ptr(), self.nrm.data_ptr(), self.nin.data_ptr(), seed,
+                                                      TRAIN_SAMPLES, steps, C.c_float(lr)), "arc_nrc_train_frame_dev")
+            self._ck(self.lib.arc_nrc_query_list_dev(self.t.ctx, self.list.data_ptr(), self.n_valid.data_ptr(),
+                                                     self.w * self.h, self.nin.data_ptr(), self.alb.data_ptr(),
+                                                     self.nrc_out.data_ptr()), "arc_nrc_query_list_dev")
         b = self._event()
         b.synchronize()
         return a.elapsed_time(b)
@@ -147,9 +162,10 @@ class CacheComparison:
 
 
 def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920, height=1080, frames=300,
-                   eval_points=16384, seed=7, steps_per_frame=8, lr=1e-3, curve=(30, 60, 120)):
+                   eval_points=16384, seed=7, steps_per_frame=8, lr=1e-3, curve=(30, 60, 120), overlap=False):
     """Runs both pipelines for `frames` frames on a static camera and scores them on the last frame;
-    `curve` lists earlier frames at which both are scored as well (8192 points each)."""
+    `curve` lists earlier frames at which both are scored as well (8192 points each). With overlap each
+    cache's query runs beside its own update (one frame behind it), for both caches alike."""
     scene = L.SCENES[scene_name]
     cc = CacheComparison(tracer, scene, width, height)
     lib = cc.lib
@@ -160,8 +176,8 @@ def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920
     conv = []
     for f in range(frames):
         shared_ms.append(cc.shared(f))
-        sharc_ms.append(cc.sharc_frame())
-        nrc_ms.append(cc.nrc_frame(seed * 1000003 + f, lr=lr, steps=steps_per_frame))
+        sharc_ms.append(cc.sharc_frame(overlap=overlap))
+        nrc_ms.append(cc.nrc_frame(seed * 1000003 + f, lr=lr, steps=steps_per_frame, overlap=overlap))
         if f + 1 in curve and f + 1 < frames:
             cand = np.nonzero(cc.valid.cpu().numpy().astype(bool))[0]
             ci = cand[np.linspace(0, len(cand) - 1, min(8192, len(cand))).astype(np.int64)]
@@ -186,6 +202,7 @@ def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920
     steady = slice(frames // 2, None)
     return {
         "frames": frames,
+        "overlap": overlap,
         "train_steps_per_frame": steps_per_frame,
         "lr": lr,
         "width": width,

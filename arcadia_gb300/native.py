@@ -94,6 +94,8 @@ SIGNATURES = {
     "arc_nrc_get_ema_weights": [_vp, _vp],
     "arc_nrc_query_list_dev": [_vp, _vp, _vp, _u32, _vp, _vp, _vp],
     "arc_nrc_train_frame_dev": [_vp, _vp, _vp, _vp, _vp, _vp, _u32, _u32, _u32, _f32],
+    "arc_nrc_frame_dev": [_vp, _vp, _vp, _u32, _vp, _vp, _vp, _vp, _vp, _u32, _u32, _u32, _f32],
+    "arc_sharc_frame_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _u32, _vp, _vp, _vp],
     "arc_sharc_query_list_dev": [_vp, _vp, _vp, _u32, _vp, _vp, _vp],
     "arc_nrc_query_dev": [_vp, _vp, _vp, _u32, _vp],
     "arc_nrc_grad_dev": [_vp, _vp, _vp, _u32, _vp],

@@ -287,6 +287,20 @@ int arc_nrc_query_dev(arc_ctx* ctx, const float* inputs, const float* albedo, ui
 /* arc_nrc_query_dev at the points list[0 .. min(*n_dev, max_n)): out[list[j]] from inputs/albedo[list[j]]. */
 int arc_nrc_query_list_dev(arc_ctx* ctx, const uint32_t* list, const uint64_t* n_dev, uint32_t max_n,
                            const float* inputs, const float* albedo, float* out_rgb);
+/* One NRC frame with the query beside the training: arc_nrc_query_list_dev at the hit list (as above),
+ * on a side stream, with the weights the previous frame's training left, while this frame's training
+ * samples are generated; then this frame's Adam steps (as arc_nrc_train_frame_dev). The query's output
+ * lags the training by one frame; the frame costs about the training alone. No counterpart in the
+ * reference. */
+int arc_nrc_frame_dev(arc_ctx* ctx, const uint32_t* list, const uint64_t* n_valid, uint32_t max_n, const float* pos,
+                      const float* normal, const float* nrc_in, const float* albedo, float* out_rgb, uint32_t seed,
+                      uint32_t n_samples, uint32_t steps, float lr);
+/* One SHARC frame with the query beside the update: query_sharc at the hit list (as
+ * arc_sharc_query_list_dev) against the previous frame's resolved slots, on a side stream, while
+ * arc_sharc_update_dev deposits this frame's radiance; then arc_sharc_resolve. */
+int arc_sharc_frame_dev(arc_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* gbuf_depth_mat,
+                        const uint32_t* gbuf_norm_motion, const uint32_t* list, const uint64_t* n_dev, uint32_t max_n,
+                        const float* pos, const float* normal, float* out);
 /* One frame of online training with no host synchronisation (graph-capturable after the first call,
  * which allocates the batch): n_samples points stratified over list[0 .. *n_valid) with a seeded
  * phase, their demodulated 1-spp one-bounce targets, then `steps` Adam steps on interleaved slices of

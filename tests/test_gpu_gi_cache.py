@@ -166,3 +166,45 @@ def test_gi_points_from_hit_records(native_lib):
         np.testing.assert_allclose(np.linalg.norm(nin[:, 6:9], axis=1), 1.0, atol=1e-5)
     finally:
         t.close()
+
+
+def test_overlapped_cache_frames_query_the_previous_state(native_lib):
+    """arc_nrc_frame_dev / arc_sharc_frame_dev run each cache's query beside its update: the query's
+    output equals a query issued before the update (bit-exact), and the update still happens."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    t, cc = _points(native_lib)
+    lib, n = cc.lib, cc.w * cc.h
+    try:
+        # NRC
+        assert lib.arc_nrc_init(t.ctx, 5) == 0
+        before = torch.zeros_like(cc.nrc_out)
+        assert lib.arc_nrc_query_list_dev(t.ctx, cc.list.data_ptr(), cc.n_valid.data_ptr(), n, cc.nin.data_ptr(),
+                                          cc.alb.data_ptr(), before.data_ptr()) == 0
+        w0 = np.zeros(200000, np.float32)
+        assert lib.arc_nrc_get_weights(t.ctx, w0.ctypes.data) == 0
+        assert lib.arc_nrc_frame_dev(t.ctx, cc.list.data_ptr(), cc.n_valid.data_ptr(), n, cc.pos.data_ptr(), cc.nrm.data_ptr(),
+                                     cc.nin.data_ptr(), cc.alb.data_ptr(), cc.nrc_out.data_ptr(), 77, 8192, 2,
+                                     C.c_float(1e-3)) == 0
+        t.synchronize()
+        assert torch.equal(cc.nrc_out, before)
+        w1 = np.zeros(200000, np.float32)
+        assert lib.arc_nrc_get_weights(t.ctx, w1.ctypes.data) == 0
+        assert not np.array_equal(w0, w1)
+        # SHARC: fill the cache for one frame, then the overlapped frame queries that resolve
+        t.sharc_reset()
+        cc.sharc_frame()
+        before = cc.sharc_out.clone()
+        assert (before[:, 3] > 0.5).any()
+        cc.shared(4)
+        assert lib.arc_sharc_query_list_dev(t.ctx, cc.list.data_ptr(), cc.n_valid.data_ptr(), n, cc.pos.data_ptr(),
+                                            cc.nrm.data_ptr(), before.data_ptr()) == 0
+        res0 = t.sharc_download()[2].copy()
+        cc.sharc_frame(overlap=True)
+        assert torch.equal(cc.sharc_out, before)
+        assert not np.array_equal(t.sharc_download()[2], res0)  # the update and resolve ran
+    finally:
+        t.close()
