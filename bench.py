@@ -59,6 +59,7 @@ def _args():
     p.add_argument("--no-nrc", action="store_true", help="skip the radiance-cache comparison section")
     p.add_argument("--nrc-frames", type=int, default=300)
     p.add_argument("--no-restir", action="store_true", help="skip the ReSTIR GI temporal pass section")
+    p.add_argument("--restir-only", action="store_true", help="run only the ReSTIR GI temporal pass section (profiling runs)")
     p.add_argument("--no-c5", action="store_true", help="skip the 4096^3 edit + trace + NRC pipeline section")
     p.add_argument("--c5-frames", type=int, default=300)
     p.add_argument("--c5-width", type=int, default=3840)
@@ -328,6 +329,13 @@ def run_ours(args):
         t.set_camera(_camera(scene, i, W_, H_))
         t.trace_frame_dev(W_, H_, gdm.data_ptr(), gnm.data_ptr(), gaa.data_ptr(), hits.data_ptr(), gi.data_ptr(),
                           n_gi.data_ptr() + 8 * slot)
+
+    if args.restir_only:
+        r = restir_section(t, scene, W_, H_, dev, (gdm, gnm, gaa, hits, gi), frames=max(args.steps, 3))
+        t.close()
+        if rank == 0:
+            print(json.dumps({"restir_gi_temporal": r}), flush=True)
+        return
 
     tuned_ms = None
     if not knobs and not args.no_autotune:  # untimed setup: pick the launch configuration on this frame
