@@ -114,7 +114,7 @@ class CacheComparison:
         b.synchronize()
         return a.elapsed_time(b)
 
-    def nrc_frame(self, seed, lr=1e-3, steps=8, overlap=False):
+    def nrc_frame(self, seed, lr=1e-3, steps=8, overlap=False, samples=TRAIN_SAMPLES):
         """One training frame (TRAIN_SAMPLES samples, `steps` Adam steps on equal slices) and inference at
         every GI hit; with overlap the inference runs beside the sample generation with the previous
         frame's weights (arc_nrc_frame_dev). Returns its device time in ms."""
@@ -122,12 +122,12 @@ class CacheComparison:
         if overlap:
             self._ck(self.lib.arc_nrc_frame_dev(self.t.ctx, self.list.data_ptr(), self.n_valid.data_ptr(), self.w * self.h,
                                                 self.pos.data_ptr(), self.nrm.data_ptr(), self.nin.data_ptr(),
-                                                self.alb.data_ptr(), self.nrc_out.data_ptr(), seed, TRAIN_SAMPLES, steps,
+                                                self.alb.data_ptr(), self.nrc_out.data_ptr(), seed, samples, steps,
                                                 C.c_float(lr)), "arc_nrc_frame_dev")
         else:
             self._ck(self.lib.arc_nrc_train_frame_dev(self.t.ctx, self.list.data_ptr(), self.n_valid.data_ptr(),
                                                       self.pos.data_ptr(), self.nrm.data_ptr(), self.nin.data_ptr(), seed,
-                                                      TRAIN_SAMPLES, steps, C.c_float(lr)), "arc_nrc_train_frame_dev")
+                                                      samples, steps, C.c_float(lr)), "arc_nrc_train_frame_dev")
             self._ck(self.lib.arc_nrc_query_list_dev(self.t.ctx, self.list.data_ptr(), self.n_valid.data_ptr(),
                                                      self.w * self.h, self.nin.data_ptr(), self.alb.data_ptr(),
                                                      self.nrc_out.data_ptr()), "arc_nrc_query_list_dev")
@@ -162,7 +162,8 @@ class CacheComparison:
 
 
 def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920, height=1080, frames=300,
-                   eval_points=16384, seed=7, steps_per_frame=8, lr=1e-3, curve=(30, 60, 120), overlap=False):
+                   eval_points=16384, seed=7, steps_per_frame=8, lr=1e-3, curve=(30, 60, 120), overlap=False,
+                   train_samples=TRAIN_SAMPLES):
     """Runs both pipelines for `frames` frames on a static camera and scores them on the last frame;
     `curve` lists earlier frames at which both are scored as well (8192 points each). With overlap each
     cache's query runs beside its own update (one frame behind it), for both caches alike."""
@@ -177,7 +178,7 @@ def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920
     for f in range(frames):
         shared_ms.append(cc.shared(f))
         sharc_ms.append(cc.sharc_frame(overlap=overlap))
-        nrc_ms.append(cc.nrc_frame(seed * 1000003 + f, lr=lr, steps=steps_per_frame, overlap=overlap))
+        nrc_ms.append(cc.nrc_frame(seed * 1000003 + f, lr=lr, steps=steps_per_frame, overlap=overlap, samples=train_samples))
         if f + 1 in curve and f + 1 < frames:
             cand = np.nonzero(cc.valid.cpu().numpy().astype(bool))[0]
             ci = cand[np.linspace(0, len(cand) - 1, min(8192, len(cand))).astype(np.int64)]
@@ -203,6 +204,7 @@ def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920
     return {
         "frames": frames,
         "overlap": overlap,
+        "train_samples": train_samples,
         "train_steps_per_frame": steps_per_frame,
         "lr": lr,
         "width": width,
