@@ -24,7 +24,7 @@ from . import layout as L
 from . import native
 from .edits import batch_from_hits, ops_for_brick_budget
 
-TRAIN_SAMPLES = 65536
+TRAIN_SAMPLES = 32768  # the cache comparison's operating point (with 4 Adam steps per frame)
 
 
 def path_camera(scene: L.SceneParams, width: int, height: int, frame: int, n_frames: int, quality=None):
