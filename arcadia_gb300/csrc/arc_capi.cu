@@ -523,6 +523,7 @@ static arc::FrameParams frame_params(arc_ctx* c, uint32_t width, uint32_t height
     P.tile_h = c->cfg.tile_h;
     P.tiles_x = (width + c->cfg.tile_w - 1u) / c->cfg.tile_w;
     P.refill_threshold = c->cfg.refill_threshold;
+    P.gi_mode = arc::kGiRows;  // honoured by the plain kernel; the persistent kernel fuses the GI ray
     frame_rows(c, P, 0u, height);
     return P;
 }

@@ -33,6 +33,12 @@ struct Scratch {
     unsigned long long gi_rays;   // GI rays traced
 };
 
+// Where a frame launch traces its GI rays (for a frame with do_gi).
+enum GiMode : uint32_t {
+    kGiFused = 0u,  // in the frame kernel, after the pixel's primary ray
+    kGiRows = 1u,   // after the frame kernel, gi_rows_kernel traces the GI rays of the launch's rows
+};
+
 struct FrameParams;
 
 }  // namespace arc
@@ -58,6 +64,7 @@ struct FrameParams {
     SurfaceEntry* surf;
     uint32_t* surf_count;
     uint32_t surf_cap;
+    uint32_t gi_mode;  // GiMode of the plain kernel (the persistent kernel always fuses)
 };
 
 // One view of a batched launch: camera block, world slot, resolution, queue offset, outputs.

@@ -20,13 +20,17 @@ def _outputs(torch, npx):
         torch.zeros(1, dtype=torch.int64, device=dev)]
 
 
-def test_noalloc_frame_matches_regular_entry_point(native_lib):
+@pytest.mark.parametrize("variant", [0, 1])
+def test_noalloc_frame_matches_regular_entry_point(native_lib, variant):
+    """variant 0: the plain kernel, whose GI pass runs over the G-buffer rows here (no GI list to
+    allocate) and over the listed hit pixels in arc_trace_frame_dev; variant 1: the persistent kernel."""
     torch = pytest.importorskip("torch")
     scene = L.SCENES["c1_256"]
     roots, nodes, bricks, _ = native_lib.build_world(scene)
     t = native_lib.Tracer(0)
     try:
         t.upload_world(scene.grid, roots, nodes, bricks, native_lib.default_palette())
+        t.set_launch_config(variant=variant)
         w, h = 640, 360
         for frame in (5, 6):  # two calls in a row: the shared static scratch must be cleared each time
             t.set_camera(L.default_camera_for(scene, w, h, quality=L.quality_high(), frame_index=frame))
