@@ -228,13 +228,14 @@ int arc_create(int device, arc_ctx** out) {
     }
     cudaMemset(c->d_scratch, 0, sizeof(Scratch));
     cudaMemset(c->d_status, 0, sizeof(uint32_t));
-    c->cfg.variant = 1;
-    c->cfg.block_threads = 256;
+    // the plain kernel with the GI rays as their own pass (the autotuner's pick on the 1080p caves frame)
+    c->cfg.variant = 0;
+    c->cfg.block_threads = 128;
     c->cfg.blocks_per_sm = 0;
     c->cfg.tile_w = 8;
     c->cfg.tile_h = 4;
     c->cfg.refill_threshold = 24;
-    c->cfg.reg_blocks = 4;
+    c->cfg.reg_blocks = 3;
     *out = c;
     return ARC_OK;
 }
@@ -866,6 +867,7 @@ static int views_enqueue(arc_ctx* c, uint32_t n, uint32_t queue_len, uint64_t* n
     V.tile_h = c->cfg.tile_h;
     V.refill_threshold = c->cfg.refill_threshold;
     V.surf = c->views_surf_cap ? 1u : 0u;
+    V.gi_split = c->cfg.variant == 0u ? 1u : 0u;
     ARC_CK(c, cudaMemsetAsync(c->d_scratch, 0, sizeof(arc::Scratch), c->stream));
     ARC_CK(c, cudaMemcpyAsync(c->d_views, c->h_views, sizeof(arc::ViewDev) * n, cudaMemcpyHostToDevice, c->stream));
     ARC_CK(c, arc::launch_views(V, c->cfg, c->n_sm, c->stream));

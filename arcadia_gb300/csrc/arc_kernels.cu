@@ -644,6 +644,10 @@ __global__ void __launch_bounds__(256, MINB) views_plain_kernel(const ViewsParam
                 if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
                 uint32_t dw, nw;
                 primary_store<SURF>(vd, w.palette, cam, px, py, dir, r == kHit, h, &dw, &nw);
+                if (V.gi_split) {  // views_gi_kernel traces the GI rays
+                    done = true;
+                    continue;
+                }
                 if (!gi_setup(w, cam, px, py, vd.width, vd.height, dw, nw, &go, &gd)) {
                     if (vd.gi_hits) store_no_ray(&vd.gi_hits[k]);
                     done = true;
@@ -652,6 +656,49 @@ __global__ void __launch_bounds__(256, MINB) views_plain_kernel(const ViewsParam
                 gi_ray = true;
                 gi_phase = true;
                 active = ray_begin(s, cam, go, gd, 0.0f, gmax, 2u, true);
+            }
+        }
+    }
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, gi_ray);
+    if ((threadIdx.x & 31u) == 0u && m) atomicAdd(&V.scratch->gi_rays, (unsigned long long)__popc(m));
+}
+
+// GI rays of a batch as their own pass after views_plain_kernel (as gi_rows_kernel for a frame): one
+// thread per queue slot, the GI ray of its pixel from the view's G-buffer.
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) views_gi_kernel(const ViewsParams V) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    bool gi_ray = false;
+    if (q < V.queue_len) {
+        uint32_t lo = 0, hi = V.n_views;  // last view with queue_begin <= q
+        while (hi - lo > 1u) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (V.views[mid].queue_begin <= q) lo = mid; else hi = mid;
+        }
+        const ViewDev& vd = V.views[lo];
+        const uint32_t local = q - vd.queue_begin, tile = local >> 5, within = local & 31u;
+        const uint32_t px = (tile % vd.tiles_x) * V.tile_w + within % V.tile_w;
+        const uint32_t py = (tile / vd.tiles_x) * V.tile_h + within / V.tile_w;
+        if (px < vd.width && py < vd.height) {
+            const arc_camera_uniforms& cam = vd.cam;
+            const World& w = V.worlds[vd.slot];
+            const size_t k = (size_t)py * vd.width + px;
+            f3 go, gd;
+            if (!gi_setup(w, cam, px, py, vd.width, vd.height, vd.gbuf_depth_mat[2u * k], vd.gbuf_norm_motion[2u * k], &go, &gd)) {
+                if (vd.gi_hits) store_no_ray(&vd.gi_hits[k]);
+            } else {
+                gi_ray = true;
+                const float gmax = cam.ray_distances[2];
+                RayState s;
+                HitInfo h;
+                StepResult g = kMiss;
+                if (ray_begin(s, cam, go, gd, 0.0f, gmax, 2u, true)) {
+                    do {
+                        g = ray_advance(s, w, cam, h);
+                    } while (g == kContinue);
+                }
+                if (g != kHit) hit_init_miss(h, go, gd, gmax);
+                if (vd.gi_hits) store_hit(&vd.gi_hits[k], h, g == kHit);
             }
         }
     }
@@ -715,6 +762,7 @@ cudaError_t launch_views_t(const ViewsParams& V, const arc_launch_config& cfg, i
         const uint32_t blocks = (V.queue_len + cfg.block_threads - 1u) / cfg.block_threads;
         if (V.surf) views_plain_kernel<MINB, true><<<blocks, cfg.block_threads, 0, st>>>(V);
         else views_plain_kernel<MINB, false><<<blocks, cfg.block_threads, 0, st>>>(V);
+        if (V.gi_split) views_gi_kernel<MINB><<<blocks, cfg.block_threads, 0, st>>>(V);
         return cudaGetLastError();
     }
     int per_sm = (int)cfg.blocks_per_sm;

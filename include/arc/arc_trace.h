@@ -50,8 +50,10 @@ extern "C" {
 
 typedef struct arc_ctx arc_ctx;
 
-/* Scheduling of the traversal kernels. variant 0 = one thread per pixel/ray on a 2D grid;
- * variant 1 = persistent warps that refill idle lanes from a global ray queue. */
+/* Scheduling of the traversal kernels. variant 0 (the default: 128 threads, reg_blocks 3) = one
+ * thread per pixel on a 2D grid for the primary rays, then the frame's GI rays as a pass of their own
+ * (one thread per pixel, octant-sorted per block); variant 1 = persistent warps that refill idle lanes
+ * from a global ray queue and trace each GI ray right after its primary ray. */
 typedef struct arc_launch_config {
     uint32_t variant;
     uint32_t block_threads;    /* threads per CTA (multiple of 32) */
