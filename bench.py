@@ -156,7 +156,8 @@ def _peaks_all():
 
 
 def _profile_traffic(kernel: str):
-    """DRAM bytes per launch of `kernel` from a committed ncu summary (profiles/*.txt), if any."""
+    """DRAM bytes of `kernel`'s frame (its launch, or its launches: the primary kernel and the GI pass)
+    from a committed ncu summary (profiles/*.txt), if any."""
     d = os.path.join(ROOT, "profiles")
     if not os.path.isdir(d):
         return None
@@ -166,7 +167,7 @@ def _profile_traffic(kernel: str):
         txt = open(os.path.join(d, fn)).read()
         if f"kernel={kernel}" in txt and f"workload={SCENE}" in txt:
             for line in txt.splitlines():
-                if line.startswith("dram_bytes_per_launch="):
+                if line.startswith("dram_bytes_per_frame=") or line.startswith("dram_bytes_per_launch="):
                     return float(line.split("=", 1)[1])
     return None
 
