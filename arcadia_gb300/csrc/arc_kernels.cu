@@ -603,7 +603,8 @@ __global__ void __launch_bounds__(256, MINB) views_persistent_kernel(const Views
 
 // One thread per queue slot over many views: the slot's view by binary search, its pixel by the same
 // 32-pixel tile mapping as the persistent kernel (a warp traces one tile), then the single-view plain
-// kernel's work: one traversal call site for the primary ray and the pixel's GI ray.
+// kernel's work: the primary ray and, unless views_gi_kernel traces the GI rays (gi_split), the pixel's
+// GI ray through the same traversal call site.
 template <int MINB, bool SURF>
 __global__ void __launch_bounds__(256, MINB) views_plain_kernel(const ViewsParams V) {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;

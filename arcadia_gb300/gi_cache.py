@@ -8,8 +8,9 @@ Both caches learn the same quantity, the one-bounce radiance L(x) at the hit of 
                     which also compacts the pixels with a GI hit into a device list
   SHARC pipeline    arc_sharc_update_dev (tile-seeded paths, estimator deposits, mode 1) +
                     arc_sharc_resolve + arc_sharc_query_list_dev at every GI hit
-  NRC pipeline      arc_nrc_train_frame_dev (65,536 one-bounce samples drawn from the list, fused
-                    forward/backward + Adam steps) + arc_nrc_query_list_dev at every GI hit
+  NRC pipeline      arc_nrc_train_frame_dev (one-bounce samples drawn from the list: 32,768 at the
+                    operating point; fused forward/backward + Adam steps) + arc_nrc_query_list_dev at
+                    every GI hit, or both in arc_nrc_frame_dev (the query beside the sample generation)
 
 Neither pipeline reads anything back to the host during a frame.
 
