@@ -80,6 +80,7 @@ class FullPipeline:
         self._ck(self.lib.arc_nrc_init(tracer.ctx, seed), "arc_nrc_init")
         self.last_rewritten = tracer.edit_stats()["bricks_rewritten"]
         self.records = []
+        self.launch = None
 
     def _ck(self, rc, what):
         if rc:
@@ -138,7 +139,17 @@ class FullPipeline:
         self.records.append(rec)
         return rec
 
-    def run(self, warmup: int = 3):
+    def tune(self):
+        """Untimed setup: the frame autotuner picks the launch configuration on the path's first view."""
+        self.t.set_camera(path_camera(self.scene, self.w, self.h, 0, self.n_frames, self.q))
+        best, ms = self.t.autotune_frame_dev(self.w, self.h, self.gdm.data_ptr(), self.gnm.data_ptr(), self.gaa.data_ptr(),
+                                             self.hits.data_ptr(), self.gi.data_ptr(), frames=2)
+        self.launch = {"kernel": "persistent" if best.variant == 1 else "plain", "block_threads": best.block_threads,
+                       "reg_blocks": best.reg_blocks, "tuned_ms": round(ms, 4)}
+
+    def run(self, warmup: int = 3, autotune: bool = True):
+        if autotune:
+            self.tune()
         for f in range(self.n_frames):
             self.frame(f)
         return self.summary(warmup)
@@ -162,5 +173,5 @@ class FullPipeline:
             "gi_hits_per_frame": round(statistics.mean(x["gi_hits"] for x in r), 1),
             "nrc_train_samples": TRAIN_SAMPLES, "nrc_steps": self.nrc_steps,
             "pool_next_node": st["next_node"], "pool_next_brick": st["next_brick"], "overflow": st["overflow"],
-            "device_status": self.t.stats().device_status,
+            "device_status": self.t.stats().device_status, "launch": self.launch,
         }
