@@ -929,7 +929,7 @@ int arc_autotune_views_dev(arc_ctx* c, const arc_view_desc* views, uint32_t n_vi
             for (uint32_t bt : {128u, 256u}) cands.push_back(arc_launch_config{1u, bt, 0u, 8u, 4u, thr, rb});
     cands.push_back(arc_launch_config{1u, 256u, 0u, 4u, 8u, 24u, 4u});
     cands.push_back(arc_launch_config{1u, 256u, 0u, 16u, 2u, 24u, 4u});
-    for (uint32_t rb : {3u, 4u})
+    for (uint32_t rb : {2u, 3u, 4u})
         for (uint32_t bt : {128u, 256u})
             for (uint32_t tw : {8u, 4u, 16u}) cands.push_back(arc_launch_config{0u, bt, 0u, tw, 32u / tw, 8u, rb});
     const arc_launch_config saved = c->cfg;
@@ -977,7 +977,7 @@ int arc_autotune_frame_dev(arc_ctx* c, uint32_t width, uint32_t height, uint32_t
         for (uint32_t thr : {8u, 16u, 24u, 28u})
             for (uint32_t bt : {128u, 256u}) cands.push_back(arc_launch_config{1u, bt, 0u, 8u, 4u, thr, rb});
     for (const auto& t : tiles) cands.push_back(arc_launch_config{1u, 256u, 0u, t[0], t[1], 24u, 4u});
-    for (uint32_t rb : {3u, 4u})
+    for (uint32_t rb : {2u, 3u, 4u})
         for (uint32_t bt : {64u, 128u, 256u}) cands.push_back(arc_launch_config{0u, bt, 0u, 8u, 4u, 8u, rb});
     const arc_launch_config saved = c->cfg;
     float best = 1e30f;

