@@ -1,9 +1,12 @@
 // arc_restir.cu — ReSTIR GI temporal pass (the GI part of temporal_main,
 // shaders/lighting_restir_gi.wgsl:61-336; reservoir helpers shaders/common/types.wgsl:90-190).
 //
-//   restir_gi_temporal_kernel  one thread per pixel: reprojected history validation, sun shadow ray
-//                              with its temporal average (checkerboard half rate in low-tap mode),
-//                              one GI candidate, temporal RIS, the 32 B reservoir.
+//   restir_sun_kernel          one thread per pixel: the sun shadow ray of every hit pixel that is
+//                              not skipped this frame (checkerboard half rate in low-tap mode), its
+//                              visibility parked in the output reservoir's shadow word.
+//   restir_gi_temporal_kernel  one thread per pixel: reprojected history validation, the temporal
+//                              average of the sun visibility, one GI candidate, temporal RIS, the
+//                              32 B reservoir.
 //
 // The GI candidate is the secondary ray the frame kernel already traced (traced again here only
 // when rigid bodies are in the frame, whose hits a record cannot give back): its hit record (hit flag,
@@ -78,6 +81,97 @@ __device__ __forceinline__ void store_reservoir(arc_gi_reservoir* r, f3 pos, uin
     q[1] = make_uint4(lo_rg, lo_b_w, __float_as_uint(depth), shadow);
 }
 
+// Reprojected history of a hit pixel (lighting_restir_gi.wgsl:95-115): the previous reservoir's two
+// halves and whether it is valid here.
+__device__ __forceinline__ bool restir_history(const RestirParams& P, const arc_camera_uniforms& cam, uint32_t x, uint32_t y,
+                                               uint32_t normal_word, f3 hp, float hit_dist, uint4* pr0, uint4* pr1) {
+    const float pu = __fdiv_rn((float)x + 0.5f, (float)P.width), pv = __fdiv_rn((float)y + 0.5f, (float)P.height);
+    const float prev_u = pu + f16_value(normal_word & 0xFFFFu), prev_v = pv + f16_value(normal_word >> 16);
+    *pr0 = make_uint4(0u, 0u, 0u, 0u);
+    *pr1 = make_uint4(0u, 0u, 0u, 0u);
+    if (!(prev_u >= 0.0f && prev_u < 1.0f && prev_v >= 0.0f && prev_v < 1.0f)) return false;
+    const uint32_t ppx = uclamp(f2u(prev_u * (float)P.width), 0u, P.width - 1u);
+    const uint32_t ppy = uclamp(f2u(prev_v * (float)P.height), 0u, P.height - 1u);
+    const uint4* q = reinterpret_cast<const uint4*>(&P.res_in[(size_t)ppy * P.width + ppx]);
+    *pr0 = q[0];
+    *pr1 = q[1];
+    const uint32_t pm = (pr0->w >> 16) & 0xFFu, page = (pr0->w >> 24) & 0x7Fu;
+    const float pdepth = __uint_as_float(pr1->z);
+    if (pm > 0u && page <= 12u && pdepth < 1e4f) {
+        const float pcd = length3(sub3(hp, f3{cam.prev_cam_pos[0], cam.prev_cam_pos[1], cam.prev_cam_pos[2]}));
+        const float tol = fmaxf(0.12f, hit_dist * 0.05f);
+        if (fabsf(pcd - pdepth) < tol) return true;
+    }
+    return false;
+}
+
+// Checkerboard half rate (117-125): a pixel with valid history keeps its previous sample on the
+// frames its slot is off.
+__device__ __forceinline__ bool restir_skip(const arc_camera_uniforms& cam, uint32_t x, uint32_t y, bool prev_valid) {
+    const uint32_t frame = __float_as_uint(cam.cam_up_frame[3]);
+    const bool checker = (cam.quality_flags[3] & 0xFFu) <= 12u;
+    const uint32_t cslot = (x & 1u) ^ ((y & 1u) << 1);
+    return checker && prev_valid && (((cslot ^ (frame & 3u)) & 1u) != 0u);
+}
+
+// Sun shadow ray of a hit pixel (127-150): jittered towards the sun, from the hit lifted off the
+// surface; shadow_mode 0 traces the full ray (visible when it misses and leaves upwards or points
+// down), other modes the any-hit shadow walk.
+template <bool kFullRay>
+__device__ __forceinline__ float restir_sun_vis(const World& w, const arc_camera_uniforms& cam, f3 hp, f3 n, float u1,
+                                                float u2) {
+    const f3 sun{cam.sun_dir_intensity[0], cam.sun_dir_intensity[1], cam.sun_dir_intensity[2]};
+    if (!(fmaxf(dot3(n, sun), 0.0f) > 0.001f && cam.sun_dir_intensity[3] > 0.01f)) return 0.0f;
+    const float j1 = u1 * 2.0f - 1.0f, j2 = u2 * 2.0f - 1.0f;
+    const f3 up = fabsf(sun.y) < 0.9f ? f3{0.0f, 1.0f, 0.0f} : f3{1.0f, 0.0f, 0.0f};
+    const f3 st = normalize3(cross3(up, sun));
+    const f3 sb = cross3(sun, st);
+    const float jr = cam.lod_settings[3];
+    const f3 js = normalize3(f3{sun.x + (st.x * j1 + sb.x * j2) * jr, sun.y + (st.y * j1 + sb.y * j2) * jr,
+                                sun.z + (st.z * j1 + sb.z * j2) * jr});
+    const f3 so = add3(hp, mul3s(n, 0.08f));
+    const float smax = cam.ray_distances[3];
+    if (kFullRay) {
+        RayState s;
+        HitInfo h;
+        StepResult r = kMiss;
+        if (ray_begin(s, cam, so, js, 0.0f, smax, 1u, true)) {
+            do {
+                r = ray_advance(s, w, cam, h);
+            } while (r == kContinue);
+        }
+        return (r != kHit && (so.y + js.y * smax >= 32.0f || js.y < 0.0f)) ? 1.0f : 0.0f;
+    }
+    return shadow_vis(w, cam, so, js, smax);
+}
+
+// Sun shadow rays of the pass, as a pass of their own so that the kernel holds one traversal: every
+// hit pixel that is not skipped this frame parks its visibility in its output reservoir's shadow
+// word, which restir_gi_temporal_kernel reads back before it writes the reservoir.
+template <bool kFullRay>
+__global__ void __launch_bounds__(128) restir_sun_kernel(const RestirParams P, const __grid_constant__ arc_camera_uniforms cam) {
+    const uint32_t x = blockIdx.x * 16u + (threadIdx.x & 15u);
+    const uint32_t y = blockIdx.y * 8u + (threadIdx.x >> 4);
+    if (x >= P.width || y >= P.height) return;
+    const size_t p = (size_t)y * P.width + x;
+    const uint2 gd = P.gdm[p], gn = P.gnm[p];
+    const float hit_dist = __uint_as_float(gd.x);
+    if (hit_dist >= 1e4f) return;
+    const f3 rd = camera_dir(cam, x, y, P.width, P.height);
+    const f3 hp = add3(f3{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]}, mul3s(rd, hit_dist));
+    uint4 pr0, pr1;
+    const bool prev_valid = restir_history(P, cam, x, y, gn.y, hp, hit_dist, &pr0, &pr1);
+    if (restir_skip(cam, x, y, prev_valid)) return;
+    float ox, oy;
+    unpack2x16snorm(gn.x, &ox, &oy);
+    const f3 n = oct_decode(ox, oy);
+    float u1, u2;
+    gradient_noise((float)x, (float)y, __float_as_uint(cam.cam_up_frame[3]), &u1, &u2);
+    reinterpret_cast<float*>(&P.res_out[p])[7] = restir_sun_vis<kFullRay>(P.world, cam, hp, n, u1, u2);
+}
+
+// kRigid: rigid bodies are in the frame, so the GI ray is traced again instead of read from its record.
+template <bool kRigid>
 __global__ void __launch_bounds__(128) restir_gi_temporal_kernel(const RestirParams P,
                                                                  const __grid_constant__ arc_camera_uniforms cam) {
     const uint32_t x = blockIdx.x * 16u + (threadIdx.x & 15u);
@@ -92,42 +186,19 @@ __global__ void __launch_bounds__(128) restir_gi_temporal_kernel(const RestirPar
         store_reservoir(&P.res_out[p], f3{0.0f, 0.0f, 0.0f}, 0u, 0u, 0u, 1e5f, 0u);
         return;
     }
-    const f3 hp = g.hit_pos, n = g.normal;
-    const float pu = __fdiv_rn((float)x + 0.5f, (float)P.width), pv = __fdiv_rn((float)y + 0.5f, (float)P.height);
-    const float prev_u = pu + f16_value(gn.y & 0xFFFFu), prev_v = pv + f16_value(gn.y >> 16);
+    const f3 hp = g.hit_pos;
     const uint32_t frame = __float_as_uint(cam.cam_up_frame[3]);
     const f3 sun{cam.sun_dir_intensity[0], cam.sun_dir_intensity[1], cam.sun_dir_intensity[2]};
     const float sun_power = cam.sun_dir_intensity[3];
-    const float n_dot_l = fmaxf(dot3(n, sun), 0.0f);
 
-    // history validation (lighting_restir_gi.wgsl:95-115)
-    bool prev_valid = false;
-    uint4 pr0 = make_uint4(0u, 0u, 0u, 0u), pr1 = make_uint4(0u, 0u, 0u, 0u);
-    if (prev_u >= 0.0f && prev_u < 1.0f && prev_v >= 0.0f && prev_v < 1.0f) {
-        const uint32_t ppx = uclamp(f2u(prev_u * (float)P.width), 0u, P.width - 1u);
-        const uint32_t ppy = uclamp(f2u(prev_v * (float)P.height), 0u, P.height - 1u);
-        const uint4* q = reinterpret_cast<const uint4*>(&P.res_in[(size_t)ppy * P.width + ppx]);
-        pr0 = q[0];
-        pr1 = q[1];
-        const uint32_t pm = (pr0.w >> 16) & 0xFFu, page = (pr0.w >> 24) & 0x7Fu;
-        const float pdepth = __uint_as_float(pr1.z);
-        if (pm > 0u && page <= 12u && pdepth < 1e4f) {
-            const float pcd = length3(sub3(hp, f3{cam.prev_cam_pos[0], cam.prev_cam_pos[1], cam.prev_cam_pos[2]}));
-            const float tol = fmaxf(0.12f, g.hit_dist * 0.05f);
-            if (fabsf(pcd - pdepth) < tol) prev_valid = true;
-        }
-    }
+    uint4 pr0, pr1;
+    const bool prev_valid = restir_history(P, cam, x, y, gn.y, hp, g.hit_dist, &pr0, &pr1);
     const uint32_t prev_nmf = pr0.w;
 
-    // checkerboard half rate (117-125)
-    const bool checker = (cam.quality_flags[3] & 0xFFu) <= 12u;
-    const uint32_t cslot = (x & 1u) ^ ((y & 1u) << 1);
-    const bool skip = checker && prev_valid && (((cslot ^ (frame & 3u)) & 1u) != 0u);
-
-    // sun shadow ray and its temporal average (127-170)
-    float sun_vis = 0.0f, shadow_m = 1.0f, accum;
+    // temporal average of the sun visibility (151-170); skipped pixels keep their previous sample
+    float sun_vis, shadow_m = 1.0f, accum;
     const float ps_x = f16_value(pr1.w & 0xFFFFu), ps_y = f16_value(pr1.w >> 16);
-    if (skip) {
+    if (restir_skip(cam, x, y, prev_valid)) {
         accum = ps_x;
         shadow_m = fminf(ps_y, 16.0f);
         const f3 pn = unpack_res_normal(prev_nmf);
@@ -137,30 +208,7 @@ __global__ void __launch_bounds__(128) restir_gi_temporal_kernel(const RestirPar
                         pr1.x, pr1.y, g.hit_dist, pack2x16float(accum, shadow_m));
         return;
     }
-    if (n_dot_l > 0.001f && sun_power > 0.01f) {
-        const float j1 = g.u1 * 2.0f - 1.0f, j2 = g.u2 * 2.0f - 1.0f;
-        const f3 up = fabsf(sun.y) < 0.9f ? f3{0.0f, 1.0f, 0.0f} : f3{1.0f, 0.0f, 0.0f};
-        const f3 st = normalize3(cross3(up, sun));
-        const f3 sb = cross3(sun, st);
-        const float jr = cam.lod_settings[3];
-        const f3 js = normalize3(f3{sun.x + (st.x * j1 + sb.x * j2) * jr, sun.y + (st.y * j1 + sb.y * j2) * jr,
-                                    sun.z + (st.z * j1 + sb.z * j2) * jr});
-        const f3 so = add3(hp, mul3s(n, 0.08f));
-        const float smax = cam.ray_distances[3];
-        if (cam.quality_flags[2] == 0u) {
-            RayState s;
-            HitInfo h;
-            StepResult r = kMiss;
-            if (ray_begin(s, cam, so, js, 0.0f, smax, 1u, true)) {
-                do {
-                    r = ray_advance(s, w, cam, h);
-                } while (r == kContinue);
-            }
-            if (r != kHit && (so.y + js.y * smax >= 32.0f || js.y < 0.0f)) sun_vis = 1.0f;
-        } else {
-            sun_vis = shadow_vis(w, cam, so, js, smax);
-        }
-    }
+    sun_vis = reinterpret_cast<const float*>(&P.res_out[p])[7];
     if (prev_valid) {
         const float psm = fminf(ps_y, 16.0f);
         shadow_m = psm + 1.0f;
@@ -176,7 +224,7 @@ __global__ void __launch_bounds__(128) restir_gi_temporal_kernel(const RestirPar
     uint32_t mat = 0u;
     float gd_m = 0.0f;
     f3 gpos{0.0f, 0.0f, 0.0f}, gnrm{0.0f, 1.0f, 0.0f}, lod{0.0f, 0.0f, 0.0f};
-    if (rigid_count(w, cam)) {
+    if (kRigid) {
         HitInfo gh;
         gi_hit = trace_full(w, cam, gi_o, gi_d, cam.ray_distances[2], 2u, true, gh);
         const RigidHit rb = trace_rigid_bodies(w, cam, gi_o, gi_d, gi_hit ? gh.t_voxels * ARC_VOXEL_SIZE : cam.ray_distances[2]);
@@ -342,8 +390,20 @@ extern "C" int arc_restir_gi_temporal_dev(arc_ctx* c, uint32_t width, uint32_t h
     P.sharc = reinterpret_cast<const uint4*>(c->d_sharc_resolved);
     P.radiance = radiance;
     dim3 grid((width + 15u) / 16u, (height + 7u) / 8u);
-    arc::restir_gi_temporal_kernel<<<grid, 128, 0, c->stream>>>(P, c->cam);
+    if (c->cam.quality_flags[2] == 0u)
+        arc::restir_sun_kernel<true><<<grid, 128, 0, c->stream>>>(P, c->cam);
+    else
+        arc::restir_sun_kernel<false><<<grid, 128, 0, c->stream>>>(P, c->cam);
     cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        c->err = std::string("restir_sun_kernel: ") + cudaGetErrorString(e);
+        return ARC_E_CUDA;
+    }
+    if (c->n_bodies && ((c->cam.point_light_count[1] >> 16) & 0xFFFFu))
+        arc::restir_gi_temporal_kernel<true><<<grid, 128, 0, c->stream>>>(P, c->cam);
+    else
+        arc::restir_gi_temporal_kernel<false><<<grid, 128, 0, c->stream>>>(P, c->cam);
+    e = cudaGetLastError();
     if (e != cudaSuccess) {
         c->err = std::string("restir_gi_temporal_kernel: ") + cudaGetErrorString(e);
         return ARC_E_CUDA;
