@@ -43,9 +43,10 @@ __device__ __forceinline__ void rigid_step(f3 vo, f3 d, f3 inv, f3 noi, bool px,
     const bool is_x = tx <= ty && tx <= tz;
     const bool is_y = !is_x && ty <= tz;
     const bool is_z = !is_x && !is_y;
-    const uint32_t ix = uclamp(f2u(fmaxf(vo.x + d.x * nt, 0.0f)), bx, bx + span - 1u);
-    const uint32_t iy = uclamp(f2u(fmaxf(vo.y + d.y * nt, 0.0f)), by, by + span - 1u);
-    const uint32_t iz = uclamp(f2u(fmaxf(vo.z + d.z * nt, 0.0f)), bz, bz + span - 1u);
+    // max(x, 0) before the conversion is implied: cvt.rzi.u32.f32 clamps to [0, 2^32 - 1] and turns NaN into 0
+    const uint32_t ix = uclamp(f2u(vo.x + d.x * nt), bx, bx + span - 1u);
+    const uint32_t iy = uclamp(f2u(vo.y + d.y * nt), by, by + span - 1u);
+    const uint32_t iz = uclamp(f2u(vo.z + d.z * nt), bz, bz + span - 1u);
     t = nt;
     vx = is_x ? (px ? ex : ex - 1u) : ix;
     vy = is_y ? (py ? ey : ey - 1u) : iy;

@@ -84,7 +84,7 @@ struct RayState {
     f3 inv;   // 1 / safe_dir (-vo * inv, the reference's neg_orig_inv, is recomputed where used: same bits)
     float t, t_limit;
     uint32_t vx, vy, vz;
-    uint32_t px, py, pz;      // previous vi
+    uint32_t diff;            // previous vi ^ vi, per axis or-ed (0xFFFFFFFF before the first step)
     uint32_t mtf_c0, mtf_c1;  // packed chunk coords (x | y << 10 | z << 20), 0xFFFFFFFF = none
     uint32_t mtf_root0, mtf_root1;
     uint4 l1, l2, l3;         // ancestor restart cache (levels shift 4, 2, 0)
@@ -159,7 +159,7 @@ __device__ __forceinline__ bool ray_begin(RayState& s, const arc_camera_uniforms
     s.vx = f2u(clampf(s.vo.x + dir.x * st, 0.0f, wx - 1e-3f));
     s.vy = f2u(clampf(s.vo.y + dir.y * st, 0.0f, wy - 1e-3f));
     s.vz = f2u(clampf(s.vo.z + dir.z * st, 0.0f, wz - 1e-3f));
-    s.px = s.py = s.pz = 0xFFFFFFFFu;
+    s.diff = 0xFFFFFFFFu;
     s.mtf_c0 = s.mtf_c1 = 0xFFFFFFFFu;
     s.mtf_root0 = s.mtf_root1 = ARC_EMPTY_CHUNK;
     s.l1 = s.l2 = s.l3 = make_uint4(0u, 0u, 0u, 0u);
@@ -182,13 +182,16 @@ __device__ __forceinline__ void step_box(RayState& s, uint32_t bx, uint32_t by, 
     bool is_y = !is_x && (ty <= tz);
     bool is_z = !is_x && !is_y;
     uint32_t ox = ex - (pxd ? 0u : 1u), oy = ey - (pyd ? 0u : 1u), oz = ez - (pzd ? 0u : 1u);
-    uint32_t ix = uclamp(f2u(fmaxf(s.vo.x + s.dir.x * next_t, 0.0f)), bx, bx + span - 1u);
-    uint32_t iy = uclamp(f2u(fmaxf(s.vo.y + s.dir.y * next_t, 0.0f)), by, by + span - 1u);
-    uint32_t iz = uclamp(f2u(fmaxf(s.vo.z + s.dir.z * next_t, 0.0f)), bz, bz + span - 1u);
+    // max(x, 0) before the conversion is implied: cvt.rzi.u32.f32 clamps to [0, 2^32 - 1] and turns NaN into 0
+    uint32_t ix = uclamp(f2u(s.vo.x + s.dir.x * next_t), bx, bx + span - 1u);
+    uint32_t iy = uclamp(f2u(s.vo.y + s.dir.y * next_t), by, by + span - 1u);
+    uint32_t iz = uclamp(f2u(s.vo.z + s.dir.z * next_t), bz, bz + span - 1u);
+    const uint32_t nx = is_x ? ox : ix, ny = is_y ? oy : iy, nz = is_z ? oz : iz;
     s.t = next_t;
-    s.vx = is_x ? ox : ix;
-    s.vy = is_y ? oy : iy;
-    s.vz = is_z ? oz : iz;
+    s.diff = (s.vx ^ nx) | (s.vy ^ ny) | (s.vz ^ nz);
+    s.vx = nx;
+    s.vy = ny;
+    s.vz = nz;
 }
 
 // eval_leaf_bitwise_ao (traversal64.wgsl:60-131).
@@ -285,10 +288,7 @@ __device__ __forceinline__ StepResult ray_advance(RayState& s, const World& w, c
     const uint32_t gx = cam.world_grid_dims[0], gy = cam.world_grid_dims[1], gz = cam.world_grid_dims[2];
     if (s.vx >= (gx << 8) || s.vy >= (gy << 8) || s.vz >= (gz << 8)) return kMiss;
 
-    const uint32_t diff = (s.px ^ s.vx) | (s.py ^ s.vy) | (s.pz ^ s.vz);
-    s.px = s.vx;
-    s.py = s.vy;
-    s.pz = s.vz;
+    const uint32_t diff = s.diff;  // the voxel changes only in step_box, which records how
     uint32_t root_idx = s.mtf_root0;
     if (diff >= 256u) {
         const uint32_t cxk = s.vx >> 8, cyk = s.vy >> 8, czk = s.vz >> 8;
