@@ -633,11 +633,24 @@ static int ensure_band_streams(arc_ctx* c) {
     return ARC_OK;
 }
 
-// Host-buffer frame in horizontal bands: band b traces rows [b H / n, (b + 1) H / n); the copy stream
-// waits for it and copies that band's rows of every output while later bands trace, so only the last
-// band's copies follow the traversal. The plain kernel's bands are launched together on their own
-// streams (the SMs fill with band b + 1 while band b drains: no tail per band); the persistent kernel's
-// bands share its queue head and run one after another on the context's stream.
+// First row of band b of n (b = n: the height). The bands' heights go 4 : ... : 4 : 2 : 1, so the
+// last band, the only one whose copies follow the traversal, is short (1080 rows in 8 bands: six of
+// 160 rows, then 80 and 40, each a whole number of the kernels' 16- and 8-row blocks).
+static uint32_t band_edge(uint32_t height, uint32_t b, uint32_t n) {
+    auto weight = [n](uint32_t i) -> uint64_t { return i + 2u < n ? 4u : (i + 2u == n ? 2u : 1u); };
+    uint64_t before = 0, total = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (i < b) before += weight(i);
+        total += weight(i);
+    }
+    return (uint32_t)((uint64_t)height * before / total);
+}
+
+// Host-buffer frame in horizontal bands (band_edge): the copy stream waits for each band and copies
+// that band's rows of every output while later bands trace, so only the last band's copies follow the
+// traversal. The plain kernel's bands are launched together on their own streams (the SMs fill with
+// band b + 1 while band b drains: no tail per band); the persistent kernel's bands share its queue
+// head and run one after another on the context's stream.
 int arc_trace_frame(arc_ctx* c, uint32_t width, uint32_t height, uint32_t* gdm, uint32_t* gnm, uint32_t* gaa,
                     arc_hit_record* hits, arc_hit_record* gi_hits, uint64_t* n_gi_out) {
     int rc = arc_ctx_check_ready(c, true);
@@ -676,7 +689,7 @@ int arc_trace_frame(arc_ctx* c, uint32_t width, uint32_t height, uint32_t* gdm, 
     ARC_CK(c, cudaEventRecord(c->ev0, c->stream));
     ARC_CK(c, cudaEventRecord(c->frame_start, c->stream));
     for (uint32_t b = 0; b < n_bands; ++b) {
-        const uint32_t r0 = (uint32_t)((uint64_t)height * b / n_bands), r1 = (uint32_t)((uint64_t)height * (b + 1) / n_bands);
+        const uint32_t r0 = band_edge(height, b, n_bands), r1 = band_edge(height, b + 1u, n_bands);
         frame_rows(c, P, r0, r1);
         cudaStream_t st = c->stream;
         if (concurrent) {
