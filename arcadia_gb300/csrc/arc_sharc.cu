@@ -575,7 +575,9 @@ int arc_gi_points_from_hits_dev(arc_ctx* c, uint32_t width, uint32_t height, con
     if ((c->cam.world_grid_dims[3] & 0xFFFFu) != width || (c->cam.world_grid_dims[3] >> 16) != height)
         return sharc_err(c, ARC_E_INVALID_ARG, "frame size differs from camera world_grid_dims.w");
     cudaMemsetAsync(n_valid, 0, sizeof(uint64_t), c->stream);
-    dim3 block(8, 8), grid((width + 7u) / 8u, (height + 7u) / 8u);
+    // a warp per 32 consecutive pixels of a row: its 20 B records and the 12 B / 36 B outputs are
+    // contiguous runs
+    dim3 block(32, 4), grid((width + 31u) / 32u, (height + 3u) / 4u);
     arc::gi_points_hits_kernel<<<grid, block, 0, c->stream>>>(c->cam, gdm, gnm, gi_hits, width, height, pos, nrm, albedo,
                                                               nrc_in, valid, reinterpret_cast<unsigned long long*>(n_valid),
                                                               list);
