@@ -527,8 +527,9 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
         if (ok) phase ^= 1u;
         tc::fence_after();
     };
-    // inputs of the CTA's first tile; each iteration then fetches the next tile's before its MMA chain
-    float vn[kIn];
+    // inputs (and albedo) of the CTA's first tile; each iteration then fetches the next tile's before
+    // its MMA chain
+    float vn[kIn], an[kOut];
     uint32_t pn = 0u;
     bool valid_n = false;
     auto fetch = [&](uint32_t tile) {
@@ -537,14 +538,18 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
         pn = valid_n ? (list ? __ldg(&list[j]) : j) : 0u;
 #pragma unroll
         for (int i = 0; i < kIn; ++i) vn[i] = valid_n ? __ldg(&in[(size_t)pn * kIn + i]) : 0.0f;
+#pragma unroll
+        for (int c = 0; c < kOut; ++c) an[c] = valid_n && albedo ? __ldg(&albedo[(size_t)pn * 3 + c]) : 1.0f;
     };
     fetch(blockIdx.x);
     for (uint32_t tile = blockIdx.x; !fail && tile < tiles; tile += gridDim.x) {
         const bool valid = valid_n;
         const uint32_t p = pn;
-        float v[kIn];
+        float v[kIn], a[kOut];
 #pragma unroll
         for (int i = 0; i < kIn; ++i) v[i] = vn[i];
+#pragma unroll
+        for (int c = 0; c < kOut; ++c) a[c] = an[c];
         fetch(tile + gridDim.x);
         // layer 1, first half: features 0..111 = inputs 0..3 and the first 16 features of input 4
         uint32_t h[12];
@@ -608,9 +613,8 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
         if (valid) {
 #pragma unroll
             for (int c = 0; c < kOut; ++c) {
-                const size_t o = (size_t)p * 3 + c;
                 const float val = __uint_as_float(y[c]);
-                out[o] = albedo ? val * __ldg(&albedo[o]) : val;
+                out[(size_t)p * 3 + c] = albedo ? val * a[c] : val;
             }
         }
         tc::fence_before();
