@@ -666,12 +666,23 @@ __global__ void __launch_bounds__(256, MINB) views_plain_kernel(const ViewsParam
     if ((threadIdx.x & 31u) == 0u && m) atomicAdd(&V.scratch->gi_rays, (unsigned long long)__popc(m));
 }
 
-// GI rays of a batch as their own pass after views_plain_kernel (as gi_rows_kernel for a frame): one
-// thread per queue slot, the GI ray of its pixel from the view's G-buffer.
+// GI rays of a batch as their own pass after views_plain_kernel (as gi_rows_kernel for a frame). A
+// block sets up the GI rays of its queue slots (up to 256; a block may span two views), sorts them by
+// direction octant in shared memory (a counting sort; slots without a GI ray, such as sky pixels, drop
+// out) and traces them from the sorted slots, so warps are full and step in similar directions. Every
+// ray is computed as before, only by another thread of the block.
 template <int MINB>
 __global__ void __launch_bounds__(256, MINB) views_gi_kernel(const ViewsParams V) {
-    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    bool gi_ray = false;
+    __shared__ float s_ray[6][256];
+    __shared__ uint32_t s_k[256], s_view[256];
+    __shared__ uint32_t s_cnt[9], s_base[10];
+    const uint32_t t = threadIdx.x;
+    if (t < 9u) s_cnt[t] = 0u;
+    __syncthreads();
+    const uint32_t q = blockIdx.x * blockDim.x + t;
+    uint32_t key = 8u, view = 0u;
+    f3 go{0.0f, 0.0f, 0.0f}, gd{0.0f, 0.0f, 1.0f};
+    size_t k = 0;
     if (q < V.queue_len) {
         uint32_t lo = 0, hi = V.n_views;  // last view with queue_begin <= q
         while (hi - lo > 1u) {
@@ -683,30 +694,55 @@ __global__ void __launch_bounds__(256, MINB) views_gi_kernel(const ViewsParams V
         const uint32_t px = (tile % vd.tiles_x) * V.tile_w + within % V.tile_w;
         const uint32_t py = (tile / vd.tiles_x) * V.tile_h + within / V.tile_w;
         if (px < vd.width && py < vd.height) {
-            const arc_camera_uniforms& cam = vd.cam;
-            const World& w = V.worlds[vd.slot];
-            const size_t k = (size_t)py * vd.width + px;
-            f3 go, gd;
-            if (!gi_setup(w, cam, px, py, vd.width, vd.height, vd.gbuf_depth_mat[2u * k], vd.gbuf_norm_motion[2u * k], &go, &gd)) {
-                if (vd.gi_hits) store_no_ray(&vd.gi_hits[k]);
-            } else {
-                gi_ray = true;
-                const float gmax = cam.ray_distances[2];
-                RayState s;
-                HitInfo h;
-                StepResult g = kMiss;
-                if (ray_begin(s, cam, go, gd, 0.0f, gmax, 2u, true)) {
-                    do {
-                        g = ray_advance(s, w, cam, h);
-                    } while (g == kContinue);
-                }
-                if (g != kHit) hit_init_miss(h, go, gd, gmax);
-                if (vd.gi_hits) store_hit(&vd.gi_hits[k], h, g == kHit);
-            }
+            k = (size_t)py * vd.width + px;
+            view = lo;
+            if (gi_setup(V.worlds[vd.slot], vd.cam, px, py, vd.width, vd.height, vd.gbuf_depth_mat[2u * k],
+                         vd.gbuf_norm_motion[2u * k], &go, &gd))
+                key = (gd.x < 0.0f ? 1u : 0u) | (gd.y < 0.0f ? 2u : 0u) | (gd.z < 0.0f ? 4u : 0u);
+            else if (vd.gi_hits)
+                store_no_ray(&vd.gi_hits[k]);
         }
     }
-    const uint32_t m = __ballot_sync(0xFFFFFFFFu, gi_ray);
-    if ((threadIdx.x & 31u) == 0u && m) atomicAdd(&V.scratch->gi_rays, (unsigned long long)__popc(m));
+    const uint32_t rank = atomicAdd(&s_cnt[key], 1u);
+    __syncthreads();
+    if (t == 0u) {
+        uint32_t acc = 0u;
+        for (int i = 0; i < 9; ++i) {
+            s_base[i] = acc;
+            acc += s_cnt[i];
+        }
+        s_base[9] = acc;
+        if (s_base[8]) atomicAdd(&V.scratch->gi_rays, (unsigned long long)s_base[8]);
+    }
+    __syncthreads();
+    if (key < 8u) {
+        const uint32_t slot = s_base[key] + rank;
+        s_ray[0][slot] = go.x;
+        s_ray[1][slot] = go.y;
+        s_ray[2][slot] = go.z;
+        s_ray[3][slot] = gd.x;
+        s_ray[4][slot] = gd.y;
+        s_ray[5][slot] = gd.z;
+        s_k[slot] = (uint32_t)k;
+        s_view[slot] = view;
+    }
+    __syncthreads();
+    if (t >= s_base[8]) return;
+    const f3 o{s_ray[0][t], s_ray[1][t], s_ray[2][t]}, d{s_ray[3][t], s_ray[4][t], s_ray[5][t]};
+    const ViewDev& vd = V.views[s_view[t]];
+    const arc_camera_uniforms& cam = vd.cam;
+    const World& w = V.worlds[vd.slot];
+    const float gmax = cam.ray_distances[2];
+    RayState s;
+    HitInfo h;
+    StepResult g = kMiss;
+    if (ray_begin(s, cam, o, d, 0.0f, gmax, 2u, true)) {
+        do {
+            g = ray_advance(s, w, cam, h);
+        } while (g == kContinue);
+    }
+    if (g != kHit) hit_init_miss(h, o, d, gmax);
+    if (vd.gi_hits) store_hit(&vd.gi_hits[s_k[t]], h, g == kHit);
 }
 
 // ------------------------------------------------------------------------------------------------
