@@ -115,21 +115,26 @@ __device__ __forceinline__ bool restir_skip(const arc_camera_uniforms& cam, uint
 }
 
 // Sun shadow ray of a hit pixel (127-150): jittered towards the sun, from the hit lifted off the
-// surface; shadow_mode 0 traces the full ray (visible when it misses and leaves upwards or points
-// down), other modes the any-hit shadow walk.
-template <bool kFullRay>
-__device__ __forceinline__ float restir_sun_vis(const World& w, const arc_camera_uniforms& cam, f3 hp, f3 n, float u1,
-                                                float u2) {
+// surface. False when the pixel traces none (surface facing away from the sun, or no sun).
+__device__ __forceinline__ bool restir_sun_ray(const arc_camera_uniforms& cam, f3 hp, f3 n, float u1, float u2, f3* so,
+                                               f3* js) {
     const f3 sun{cam.sun_dir_intensity[0], cam.sun_dir_intensity[1], cam.sun_dir_intensity[2]};
-    if (!(fmaxf(dot3(n, sun), 0.0f) > 0.001f && cam.sun_dir_intensity[3] > 0.01f)) return 0.0f;
+    if (!(fmaxf(dot3(n, sun), 0.0f) > 0.001f && cam.sun_dir_intensity[3] > 0.01f)) return false;
     const float j1 = u1 * 2.0f - 1.0f, j2 = u2 * 2.0f - 1.0f;
     const f3 up = fabsf(sun.y) < 0.9f ? f3{0.0f, 1.0f, 0.0f} : f3{1.0f, 0.0f, 0.0f};
     const f3 st = normalize3(cross3(up, sun));
     const f3 sb = cross3(sun, st);
     const float jr = cam.lod_settings[3];
-    const f3 js = normalize3(f3{sun.x + (st.x * j1 + sb.x * j2) * jr, sun.y + (st.y * j1 + sb.y * j2) * jr,
-                                sun.z + (st.z * j1 + sb.z * j2) * jr});
-    const f3 so = add3(hp, mul3s(n, 0.08f));
+    *js = normalize3(f3{sun.x + (st.x * j1 + sb.x * j2) * jr, sun.y + (st.y * j1 + sb.y * j2) * jr,
+                        sun.z + (st.z * j1 + sb.z * j2) * jr});
+    *so = add3(hp, mul3s(n, 0.08f));
+    return true;
+}
+
+// Visibility along a sun ray: shadow_mode 0 traces the full ray (visible when it misses and leaves
+// upwards or points down), other modes the any-hit shadow walk.
+template <bool kFullRay>
+__device__ __forceinline__ float restir_sun_trace(const World& w, const arc_camera_uniforms& cam, f3 so, f3 js) {
     const float smax = cam.ray_distances[3];
     if (kFullRay) {
         RayState s;
@@ -147,27 +152,60 @@ __device__ __forceinline__ float restir_sun_vis(const World& w, const arc_camera
 
 // Sun shadow rays of the pass, as a pass of their own so that the kernel holds one traversal: every
 // hit pixel that is not skipped this frame parks its visibility in its output reservoir's shadow
-// word, which restir_gi_temporal_kernel reads back before it writes the reservoir.
+// word, which restir_gi_temporal_kernel reads back before it writes the reservoir. A block sets up
+// the rays of its 16 x 8 pixels and appends them to shared memory (pixels without a ray, such as
+// the sky, drop out), so the warps that trace are full.
 template <bool kFullRay>
 __global__ void __launch_bounds__(128) restir_sun_kernel(const RestirParams P, const __grid_constant__ arc_camera_uniforms cam) {
-    const uint32_t x = blockIdx.x * 16u + (threadIdx.x & 15u);
-    const uint32_t y = blockIdx.y * 8u + (threadIdx.x >> 4);
-    if (x >= P.width || y >= P.height) return;
-    const size_t p = (size_t)y * P.width + x;
-    const uint2 gd = P.gdm[p], gn = P.gnm[p];
-    const float hit_dist = __uint_as_float(gd.x);
-    if (hit_dist >= 1e4f) return;
-    const f3 rd = camera_dir(cam, x, y, P.width, P.height);
-    const f3 hp = add3(f3{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]}, mul3s(rd, hit_dist));
-    uint4 pr0, pr1;
-    const bool prev_valid = restir_history(P, cam, x, y, gn.y, hp, hit_dist, &pr0, &pr1);
-    if (restir_skip(cam, x, y, prev_valid)) return;
-    float ox, oy;
-    unpack2x16snorm(gn.x, &ox, &oy);
-    const f3 n = oct_decode(ox, oy);
-    float u1, u2;
-    gradient_noise((float)x, (float)y, __float_as_uint(cam.cam_up_frame[3]), &u1, &u2);
-    reinterpret_cast<float*>(&P.res_out[p])[7] = restir_sun_vis<kFullRay>(P.world, cam, hp, n, u1, u2);
+    __shared__ float s_ray[6][128];
+    __shared__ uint32_t s_p[128];
+    __shared__ uint32_t s_n;
+    const uint32_t t = threadIdx.x, lane = t & 31u;
+    if (t == 0u) s_n = 0u;
+    __syncthreads();
+    const uint32_t x = blockIdx.x * 16u + (t & 15u);
+    const uint32_t y = blockIdx.y * 8u + (t >> 4);
+    bool want = false;
+    f3 so{0.0f, 0.0f, 0.0f}, js{0.0f, 1.0f, 0.0f};
+    size_t p = 0;
+    if (x < P.width && y < P.height) {
+        p = (size_t)y * P.width + x;
+        const uint2 gd = P.gdm[p], gn = P.gnm[p];
+        const float hit_dist = __uint_as_float(gd.x);
+        if (hit_dist < 1e4f) {
+            const f3 rd = camera_dir(cam, x, y, P.width, P.height);
+            const f3 hp = add3(f3{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]}, mul3s(rd, hit_dist));
+            uint4 pr0, pr1;
+            const bool prev_valid = restir_history(P, cam, x, y, gn.y, hp, hit_dist, &pr0, &pr1);
+            if (!restir_skip(cam, x, y, prev_valid)) {
+                float ox, oy;
+                unpack2x16snorm(gn.x, &ox, &oy);
+                const f3 n = oct_decode(ox, oy);
+                float u1, u2;
+                gradient_noise((float)x, (float)y, __float_as_uint(cam.cam_up_frame[3]), &u1, &u2);
+                want = restir_sun_ray(cam, hp, n, u1, u2, &so, &js);
+                if (!want) reinterpret_cast<float*>(&P.res_out[p])[7] = 0.0f;
+            }
+        }
+    }
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, want);
+    uint32_t base = 0u;
+    if (lane == 0u && m) base = atomicAdd(&s_n, (uint32_t)__popc(m));
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (want) {
+        const uint32_t slot = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+        s_ray[0][slot] = so.x;
+        s_ray[1][slot] = so.y;
+        s_ray[2][slot] = so.z;
+        s_ray[3][slot] = js.x;
+        s_ray[4][slot] = js.y;
+        s_ray[5][slot] = js.z;
+        s_p[slot] = (uint32_t)p;
+    }
+    __syncthreads();
+    if (t >= s_n) return;
+    const f3 o{s_ray[0][t], s_ray[1][t], s_ray[2][t]}, d{s_ray[3][t], s_ray[4][t], s_ray[5][t]};
+    reinterpret_cast<float*>(&P.res_out[s_p[t]])[7] = restir_sun_trace<kFullRay>(P.world, cam, o, d);
 }
 
 // kRigid: rigid bodies are in the frame, so the GI ray is traced again instead of read from its record.
