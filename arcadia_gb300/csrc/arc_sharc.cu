@@ -275,18 +275,58 @@ __global__ void sharc_deposit_kernel(SharcBuffers S, f3 pos, f3 n, f3 cam, f3 ra
 
 // GI hit points of a frame: per pixel with a primary hit, the Pass-2A GI ray is traced again from the
 // G-buffer and its hit recorded as position, normal, material albedo (cmp_albedo) and the 9 NRC inputs
-// (position / world extent, normal, view direction = -ray direction).
-__global__ void gi_points_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, const uint32_t* __restrict__ gdm,
+// (position / world extent, normal, view direction = -ray direction). A block of 128 threads sets up
+// the GI rays of its 16 x 8 pixels, sorts them by direction octant in shared memory (pixels without a
+// GI ray drop out) and traces them from the sorted slots, as gi_rows_kernel does for a frame.
+__global__ void __launch_bounds__(128) gi_points_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, const uint32_t* __restrict__ gdm,
                                  const uint32_t* __restrict__ gnm, uint32_t W, uint32_t H, float* __restrict__ pos,
                                  float* __restrict__ nrm, float* __restrict__ alb, float* __restrict__ nrc_in,
                                  uint32_t* __restrict__ valid, unsigned long long* __restrict__ n_valid,
                                  uint32_t* __restrict__ list) {
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= W || y >= H) return;
-    const size_t k = (size_t)y * W + x;
-    f3 o, d;
+    __shared__ float s_ray[6][128];
+    __shared__ uint32_t s_k[128];
+    __shared__ uint32_t s_cnt[9], s_base[10];
+    const uint32_t t = threadIdx.x;
+    if (t < 9u) s_cnt[t] = 0u;
+    __syncthreads();
+    const uint32_t x = blockIdx.x * 16u + (t & 15u), y = blockIdx.y * 8u + (t >> 4);
+    uint32_t key = 8u;
+    f3 go{0.0f, 0.0f, 0.0f}, gd{0.0f, 0.0f, 1.0f};
+    size_t gk = 0;
+    if (x < W && y < H) {
+        gk = (size_t)y * W + x;
+        if (gi_setup(w, cam, x, y, W, H, gdm[2 * gk], gnm[2 * gk], &go, &gd))
+            key = (gd.x < 0.0f ? 1u : 0u) | (gd.y < 0.0f ? 2u : 0u) | (gd.z < 0.0f ? 4u : 0u);
+        else
+            valid[gk] = 0u;
+    }
+    const uint32_t rank = atomicAdd(&s_cnt[key], 1u);
+    __syncthreads();
+    if (t == 0u) {
+        uint32_t acc = 0u;
+        for (int i = 0; i < 9; ++i) {
+            s_base[i] = acc;
+            acc += s_cnt[i];
+        }
+        s_base[9] = acc;
+    }
+    __syncthreads();
+    if (key < 8u) {
+        const uint32_t slot = s_base[key] + rank;
+        s_ray[0][slot] = go.x;
+        s_ray[1][slot] = go.y;
+        s_ray[2][slot] = go.z;
+        s_ray[3][slot] = gd.x;
+        s_ray[4][slot] = gd.y;
+        s_ray[5][slot] = gd.z;
+        s_k[slot] = (uint32_t)gk;
+    }
+    __syncthreads();
+    if (t >= s_base[8]) return;
+    const size_t k = s_k[t];
+    const f3 o{s_ray[0][t], s_ray[1][t], s_ray[2][t]}, d{s_ray[3][t], s_ray[4][t], s_ray[5][t]};
     uint32_t ok = 0u;
-    if (gi_setup(w, cam, x, y, W, H, gdm[2 * k], gnm[2 * k], &o, &d)) {
+    {
         RayState s;
         HitInfo h;
         StepResult r = kMiss;
@@ -325,7 +365,7 @@ __global__ void gi_points_kernel(const World w, const __grid_constant__ arc_came
     // warp-aggregated slot in the compacted list (order across warps is arbitrary)
     const uint32_t act = __activemask();
     const uint32_t m = __ballot_sync(act, ok != 0u);
-    const uint32_t lane = (threadIdx.x + threadIdx.y * blockDim.x) & 31u;
+    const uint32_t lane = t & 31u;
     unsigned long long base = 0ull;
     if (m && lane == (uint32_t)(__ffs(m) - 1)) base = atomicAdd(n_valid, (unsigned long long)__popc(m));
     if (m) base = __shfl_sync(act, base, __ffs(m) - 1);
@@ -592,8 +632,8 @@ int arc_gi_points_dev(arc_ctx* c, uint32_t width, uint32_t height, const uint32_
     if ((c->cam.world_grid_dims[3] & 0xFFFFu) != width || (c->cam.world_grid_dims[3] >> 16) != height)
         return sharc_err(c, ARC_E_INVALID_ARG, "frame size differs from camera world_grid_dims.w");
     cudaMemsetAsync(n_valid, 0, sizeof(uint64_t), c->stream);
-    dim3 block(8, 8), grid((width + 7u) / 8u, (height + 7u) / 8u);
-    arc::gi_points_kernel<<<grid, block, 0, c->stream>>>(c->world(), c->cam, gdm, gnm, width, height, pos, nrm, albedo,
+    dim3 grid((width + 15u) / 16u, (height + 7u) / 8u);
+    arc::gi_points_kernel<<<grid, 128, 0, c->stream>>>(c->world(), c->cam, gdm, gnm, width, height, pos, nrm, albedo,
                                                          nrc_in, valid, reinterpret_cast<unsigned long long*>(n_valid), list);
     return launch_check(c, "gi_points_kernel");
 }
