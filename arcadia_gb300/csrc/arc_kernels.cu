@@ -10,8 +10,7 @@
 //                            finishes is refilled with the next pixel between DDA iterations, a primary
 //                            hit turns the lane into its GI ray, so uneven ray lengths do not idle lanes.
 //   gi_rows_kernel           the frame's GI rays as their own pass after frame_plain_kernel (octant-
-//                            sorted per block).
-//   secondary_kernel         GI ray per pixel from an existing G-buffer.
+//                            sorted per block); also the GI rays from an existing G-buffer.
 //   rays_kernel / shadow_kernel  trace_world_64tree / trace_shadow_vis over a ray batch.
 //   sharc_*                  shaders/sharc_update.wgsl, sharc_resolve.wgsl, common/sharc_query.wgsl.
 //
@@ -273,30 +272,6 @@ __global__ void __launch_bounds__(256, MINB) frame_persistent_kernel(const Frame
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) gi_count += __shfl_down_sync(0xFFFFFFFFu, gi_count, o);
     if (lane == 0 && gi_count) atomicAdd(&P.scratch->gi_rays, (unsigned long long)gi_count);
-}
-
-__global__ void secondary_kernel(const FrameParams P, const __grid_constant__ arc_camera_uniforms cam) {
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= P.width || y >= P.height) return;
-    const size_t k = (size_t)y * P.width + x;
-    const uint32_t dw = P.gbuf_depth_mat[2 * k], nw = P.gbuf_norm_motion[2 * k];
-    f3 go, gd;
-    if (!gi_setup(P.world, cam, x, y, P.width, P.height, dw, nw, &go, &gd)) {
-        store_no_ray(&P.gi_hits[k]);
-        return;
-    }
-    const float gmax = cam.ray_distances[2];
-    RayState s;
-    HitInfo h;
-    StepResult g = kMiss;
-    if (ray_begin(s, cam, go, gd, 0.0f, gmax, 2u, true)) {
-        do {
-            g = ray_advance(s, P.world, cam, h);
-        } while (g == kContinue);
-    }
-    if (g != kHit) hit_init_miss(h, go, gd, gmax);
-    store_hit(&P.gi_hits[k], h, g == kHit);
 }
 
 // GI pass over the launch's rows from the G-buffer (lighting_restir_gi.wgsl:195-209). As a pass of its
@@ -914,9 +889,9 @@ cudaError_t launch_surface_views(const ViewsParams& V, const SurfaceEntry* surf,
 }
 
 cudaError_t launch_secondary(const FrameParams& P, const arc_camera_uniforms& cam, cudaStream_t st) {
-    dim3 block(8, 8);
-    dim3 grid((P.width + 7u) / 8u, (P.height + 7u) / 8u);
-    secondary_kernel<<<grid, block, 0, st>>>(P, cam);
+    // the frame's GI pass over the G-buffer's rows: compacted, octant-sorted blocks
+    dim3 grid((P.width + 15u) / 16u, (P.row_end - P.row0 + 7u) / 8u);
+    gi_rows_kernel<3><<<grid, 128, 0, st>>>(P, cam);
     return cudaGetLastError();
 }
 
