@@ -321,6 +321,21 @@ int arc_get_stream(arc_ctx* c, void** stream) {
     return ARC_OK;
 }
 
+int arc_debug_set(arc_ctx* c, int what, long long value) {
+    if (!c) return ARC_E_INVALID_ARG;
+    switch (what) {
+        case ARC_DEBUG_TC_WAIT_BUDGET:
+            if (value < 0) return set_err(c, ARC_E_INVALID_ARG, "wait budget must be >= 0 cycles");
+            c->tc_wait_budget = value;
+            return ARC_OK;
+        case ARC_DEBUG_SKIP_POOL_VALIDATION:
+            c->skip_pool_validation = value != 0;
+            return ARC_OK;
+        default:
+            return set_err(c, ARC_E_INVALID_ARG, "unknown debug hook");
+    }
+}
+
 int arc_set_launch_config(arc_ctx* c, const arc_launch_config* cfg) {
     if (!c || !cfg) return ARC_E_INVALID_ARG;
     if (cfg->variant > 1u) return set_err(c, ARC_E_INVALID_ARG, "variant must be 0 or 1");
@@ -361,14 +376,16 @@ int arc_upload_world(arc_ctx* c, const uint32_t grid[3], const uint32_t* roots, 
     if (nch != n_roots) return set_err(c, ARC_E_INVALID_ARG, "n_roots != grid volume");
     const uint64_t cap_nodes = (uint64_t)n_nodes + node_headroom, cap_bricks = (uint64_t)std::max<uint32_t>(n_bricks, 1u) + brick_headroom;
     if (cap_nodes > ARC_PTR_INDEX_MASK || cap_bricks > ARC_PTR_INDEX_MASK) return set_err(c, ARC_E_CAPACITY, "pool beyond 30-bit index range");
-    for (uint32_t i = 0; i < n_roots; ++i)
-        if (roots[i] != ARC_EMPTY_CHUNK && roots[i] >= n_nodes) {
-            char b[128];
-            snprintf(b, sizeof b, "chunk %u: root %u >= node count %u", i, roots[i], n_nodes);
-            return set_err(c, ARC_E_INVALID_POOL, b);
-        }
-    int rc = validate_nodes(c, nodes, n_nodes, n_nodes, n_bricks, 0);
-    if (rc) return rc;
+    int rc = ARC_OK;
+    if (!c->skip_pool_validation) {  // only a test's fault injection turns this off (arc_debug_set)
+        for (uint32_t i = 0; i < n_roots; ++i)
+            if (roots[i] != ARC_EMPTY_CHUNK && roots[i] >= n_nodes) {
+                char b[128];
+                snprintf(b, sizeof b, "chunk %u: root %u >= node count %u", i, roots[i], n_nodes);
+                return set_err(c, ARC_E_INVALID_POOL, b);
+            }
+        if ((rc = validate_nodes(c, nodes, n_nodes, n_nodes, n_bricks, 0))) return rc;
+    }
     ARC_CK(c, cudaSetDevice(c->device));
     ARC_CK(c, cudaStreamSynchronize(c->stream));
     cudaFree(c->d_roots);
@@ -616,7 +633,9 @@ int arc_trace_secondary_dev(arc_ctx* c, uint32_t width, uint32_t height, const u
     P.gbuf_depth_mat = const_cast<uint32_t*>(gdm);
     P.gbuf_norm_motion = const_cast<uint32_t*>(gnm);
     P.gi_hits = gi_hits;
-    ARC_CK(c, arc::launch_secondary(P, c->cam, c->stream));
+    // the GI pass counts its rays into the context scratch; start that count at zero as a frame does
+    ARC_CK(c, cudaMemsetAsync(c->d_scratch, 0, sizeof(arc::Scratch), c->stream));
+    ARC_CK(c, arc::launch_secondary(P, c->cam, c->cfg, c->stream));
     return ARC_OK;
 }
 

@@ -109,6 +109,11 @@ struct arc_ctx {
     uint32_t graph_surf_cap = 0;                   // ... and of the captured batch graph
     arc::SurfaceEntry* graph_surf_list = nullptr;  // the list the captured graph writes
 
+    // fault-injection hooks (arc_debug_set): the cycle budget of each tensor-core mbarrier wait
+    // (0 = the default of about one second) and an upload that skips the pool range validation
+    long long tc_wait_budget = 0;
+    bool skip_pool_validation = false;
+
     arc_launch_config cfg{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // host-buffer frames: copy stream and per-band events (copies of a band overlap the next band)

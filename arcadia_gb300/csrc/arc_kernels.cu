@@ -888,10 +888,17 @@ cudaError_t launch_surface_views(const ViewsParams& V, const SurfaceEntry* surf,
     return cudaGetLastError();
 }
 
-cudaError_t launch_secondary(const FrameParams& P, const arc_camera_uniforms& cam, cudaStream_t st) {
-    // the frame's GI pass over the G-buffer's rows: compacted, octant-sorted blocks
+cudaError_t launch_secondary(const FrameParams& P, const arc_camera_uniforms& cam, const arc_launch_config& cfg,
+                             cudaStream_t st) {
+    // the frame's GI pass over the G-buffer's rows (compacted, octant-sorted blocks), at the register
+    // budget of the launch configuration as in launch_frame
     dim3 grid((P.width + 15u) / 16u, (P.row_end - P.row0 + 7u) / 8u);
-    gi_rows_kernel<3><<<grid, 128, 0, st>>>(P, cam);
+    switch (cfg.reg_blocks) {
+        case 2: gi_rows_kernel<2><<<grid, 128, 0, st>>>(P, cam); break;
+        case 3: gi_rows_kernel<3><<<grid, 128, 0, st>>>(P, cam); break;
+        case 4: gi_rows_kernel<4><<<grid, 128, 0, st>>>(P, cam); break;
+        default: gi_rows_kernel<1><<<grid, 128, 0, st>>>(P, cam); break;
+    }
     return cudaGetLastError();
 }
 

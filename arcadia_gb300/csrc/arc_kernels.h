@@ -98,7 +98,8 @@ cudaError_t launch_frame(const FrameParams& P, const arc_camera_uniforms& cam, c
 cudaError_t launch_surface(const FrameParams& P, const arc_camera_uniforms& cam, int n_sm, cudaStream_t st);
 cudaError_t launch_surface_views(const ViewsParams& V, const SurfaceEntry* surf, const uint32_t* count, uint32_t cap,
                                  int n_sm, cudaStream_t st);
-cudaError_t launch_secondary(const FrameParams& P, const arc_camera_uniforms& cam, cudaStream_t st);
+cudaError_t launch_secondary(const FrameParams& P, const arc_camera_uniforms& cam, const arc_launch_config& cfg,
+                             cudaStream_t st);
 cudaError_t launch_rays(const World& w, const arc_camera_uniforms& cam, const arc_ray* rays, uint32_t n, float max_dist_m,
                         uint32_t lod_bias, int ignore_water, arc_hit_record* hits, cudaStream_t st);
 cudaError_t launch_rigid_rays(const World& w, const arc_camera_uniforms& cam, const arc_ray* rays, uint32_t n, float max_dist_m,

@@ -16,14 +16,25 @@
 //     the end of the queue, and the limit keeps that far from wrapping; larger frames are rejected
 //     with ARC_E_CAPACITY;
 //   - every call shares the array: the entry point clears it in stream order before each launch,
-//     and calls whose kernels overlap on the GPU (two streams, two contexts on one device) race on
-//     it, so callers must not run two of these calls concurrently on one device;
-//   - the first call on a device looks up the array's device address (cudaGetSymbolAddress) with
-//     that device current; make that first call before any stream capture;
+//     and calls whose kernels overlap on the GPU (on two streams of one CUDA context) race on it, so
+//     callers must not run two of these calls concurrently in one context. Each CUDA context that
+//     loads the library holds its own copy of the array;
+//   - set-up: the first call in a CUDA context (the context of the arc_ctx's stream, normally the
+//     device's primary context) looks up the array's device address with cudaGetSymbolAddress, with
+//     that device current, and then makes the caller's previous device current again. The address is
+//     kept per device together with the context's unique id, so a context created anew (after
+//     cudaDeviceReset, say) is set up again instead of reusing a stale address. Make the first call
+//     before any stream capture;
+//   - with CUDA's lazy module loading (the default), the first launch of each kernel instance can
+//     load its code into device memory. The instance depends on the launch configuration
+//     (arc_set_launch_config: variant, register budget) and on whether the frame needs the surface
+//     list, so make one warm-up call for each such combination before the region that must not
+//     allocate;
 //   - a world with water or mirror voxels, or a camera under water, needs the context's surface
 //     list (the hits that take those shading branches): reserve it beforehand with
 //     arc_reserve_surface_list for at least width x height pixels, else the call fails with
 //     ARC_E_CAPACITY.
+#include <cuda.h>  // driver API types only: the two driver functions used are fetched through the runtime
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -43,27 +54,69 @@ static_assert(sizeof(arc::Scratch) <= kNoAllocScratchBytes, "frame scratch must 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 std::mutex g_setup_mutex;
-void* g_scratch_addr[kMaxDevices] = {};
+struct ScratchAddr {
+    unsigned long long ctx_id = 0;  // unique id of the CUDA context the address belongs to (0 = none yet)
+    void* addr = nullptr;
+};
+ScratchAddr g_scratch_addr[kMaxDevices];
+
+using StreamGetCtxFn = CUresult (*)(CUstream, CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+StreamGetCtxFn g_stream_get_ctx = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
 
 int fail(arc_ctx* c, int code, const std::string& msg) {
     c->err = msg;
     return code;
 }
 
-// Device address of the static array on the context's device (looked up once per device).
+// Unique id of the CUDA context the arc_ctx's stream belongs to (the context its kernels run in).
+// Call with g_setup_mutex held.
+int stream_context_id(arc_ctx* c, unsigned long long* id) {
+    if (!g_stream_get_ctx || !g_ctx_get_id) {
+        void* f0 = nullptr;
+        void* f1 = nullptr;
+        cudaDriverEntryPointQueryResult q0 = cudaDriverEntryPointSymbolNotFound, q1 = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuStreamGetCtx", &f0, 12000, cudaEnableDefault, &q0) != cudaSuccess ||
+            q0 != cudaDriverEntryPointSuccess || !f0 ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess || !f1)
+            return fail(c, ARC_E_CUDA, "driver entry points cuStreamGetCtx / cuCtxGetId not found");
+        g_stream_get_ctx = reinterpret_cast<StreamGetCtxFn>(f0);
+        g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f1);
+    }
+    CUcontext ctx = nullptr;
+    if (g_stream_get_ctx(reinterpret_cast<CUstream>(c->stream), &ctx) != CUDA_SUCCESS || !ctx ||
+        g_ctx_get_id(ctx, id) != CUDA_SUCCESS)
+        return fail(c, ARC_E_CUDA, "context of the library stream not found");
+    return ARC_OK;
+}
+
+// Device address of the static array in the CUDA context of the arc_ctx's stream: looked up once per
+// context (set-up), with the arc_ctx's device current, and the caller's current device restored.
 int scratch_address(arc_ctx* c, void** out) {
     if (c->device < 0 || c->device >= kMaxDevices) return fail(c, ARC_E_INVALID_ARG, "device ordinal out of range");
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[c->device]) {
-        cudaError_t e = cudaSetDevice(c->device);
+    unsigned long long id = 0;
+    int rc = stream_context_id(c, &id);
+    if (rc) return rc;
+    ScratchAddr& s = g_scratch_addr[c->device];
+    if (s.ctx_id != id || !s.addr) {
+        int prev = -1;
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e != cudaSuccess) return fail(c, ARC_E_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+        e = cudaSetDevice(c->device);
         if (e != cudaSuccess) return fail(c, ARC_E_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        const cudaError_t er = prev != c->device ? cudaSetDevice(prev) : cudaSuccess;
         if (e != cudaSuccess || !p)
             return fail(c, ARC_E_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
-        g_scratch_addr[c->device] = p;
+        if (er != cudaSuccess) return fail(c, ARC_E_CUDA, std::string("restoring the current device: ") + cudaGetErrorString(er));
+        s.ctx_id = id;
+        s.addr = p;
     }
-    *out = g_scratch_addr[c->device];
+    *out = s.addr;
     return ARC_OK;
 }
 

@@ -1,17 +1,21 @@
 // arc_nrc.cu — neural radiance cache: fused tensor-core inference and training (sm_103a).
 //
 // No reference counterpart: the NRC stands in for SHARC's hashed lookup (query_sharc,
-// shaders/common/sharc_query.wgsl:138-146) at secondary hits.
+// shaders/common/sharc_query.wgsl:21-29) at secondary hits.
 //
 // Network: 9 inputs (position in [0,1]^3, normal, view direction) -> sin/cos(2^k pi v), k = 0..11
 // (216 features, index = input*24 + 2k + {0 sin, 1 cos}) -> 5 x 64 ReLU -> 3 linear outputs, no
-// biases. FP32 master weights (compact, W[out][in] per layer) with FP16 copies in two padded
-// layouts: forward W[out][in_pad] and transposed WT[in][out_pad] for the backward pass. Activations
-// move between layers in registers: the m16n8k16 accumulator fragment of two adjacent 8-column tiles
-// is exactly the A fragment of the next layer's 16-wide k step, so ReLU + FP16 packing is all the
-// conversion a layer needs. Products run on mma.sync.m16n8k16.f32.f16.f16.f32 (FP32 accumulation).
+// biases. FP32 master weights (compact, W[out][in] per layer) with FP16 copies in padded layouts.
 //
-// Training (one fused kernel per batch): a CTA of 4 warps takes 64 samples at a time; each warp runs
+// The default path runs on the fifth-generation tensor cores: infer_tc_kernel and train_tc_kernel
+// issue tcgen05.mma from one thread into TMEM accumulators, with operands in shared memory (below,
+// "tcgen05 inference" / "tcgen05 training"). The warp-level mma.sync.m16n8k16 kernels (infer_kernel,
+// train_kernel) stay selectable (arc_nrc_set_infer_path / arc_nrc_set_train_path) as the comparison
+// point. In them activations move between layers in registers: the m16n8k16 accumulator fragment of
+// two adjacent 8-column tiles is exactly the A fragment of the next layer's 16-wide k step, so ReLU +
+// FP16 packing is all the conversion a layer needs.
+//
+// mma.sync training (one fused kernel per batch): a CTA of 4 warps takes 64 samples at a time; each warp runs
 // the forward pass for 16 samples and stores the transposed activations in shared memory; the backward
 // pass runs layer by layer (dZ in registers, dZ^T in a double-buffered shared tile), and after each
 // layer all warps compute that layer's weight-gradient tiles dW = dZ^T A over the 64 samples on the
@@ -449,6 +453,10 @@ __global__ void pack_kernel(const float* __restrict__ w, __half* __restrict__ w1
 constexpr int kTcA = 128 * 112;  // halves
 constexpr uint32_t kTcSmem = kUHalves * 2 + kTcA * 2 + 64;
 constexpr long long kTcBudget = 2000000000ll;  // cycles (about one second) per wait
+// A kernel whose wait ran out sets bit 31 of the status word, stops issuing work, and before it frees
+// TMEM and returns waits (with the full budget again) for what it still has in flight: the weight copy
+// into shared memory and, if one was committed and not yet seen to complete, the last MMA batch. The
+// `budget` kernel argument is the per-wait budget in cycles (kTcBudget unless a test shrinks it).
 
 // sin/cos(2^k pi x), k = 0..11, as 12 packed (sin, cos) FP16 pairs: sincospif at k = 0 and k = 6 and
 // five angle doublings after each (s' = 2 s c, c' = (c - s)(c + s)), which add a few ulp of FP32.
@@ -477,7 +485,7 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
                                                           const float* __restrict__ albedo, uint32_t n,
                                                           float* __restrict__ out, const uint32_t* __restrict__ list,
                                                           const unsigned long long* __restrict__ n_dev,
-                                                          uint32_t* __restrict__ status) {
+                                                          uint32_t* __restrict__ status, long long budget) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
     uint8_t* sw = smem_raw;
     uint8_t* sa = smem_raw + kUHalves * 2;
@@ -510,9 +518,10 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
         tc::mbar_expect_tx(bar_w, kUHalves * 2);
         tc::bulk_g2s(sw_u, wu, kUHalves * 2, bar_w);
     }
-    bool ok = tc::mbar_wait(bar_w, 0, kTcBudget);
+    bool ok = tc::mbar_wait(bar_w, 0, budget);
     bool fail = __syncthreads_or(!ok);
     uint32_t phase = 0;
+    bool mma_pending = false;  // thread 0: a committed MMA batch whose completion it has not seen
     constexpr uint32_t kId64 = tc::idesc_f16(128, 64, false, false), kId16 = tc::idesc_f16(128, 16, false, false);
     // one MMA pass: D (+)= A[sa] * W^T, `steps` K-steps; A has a_sbo bytes per 8-row group
     auto issue = [&](uint32_t d, uint32_t w_byte, uint32_t w_sbo, uint32_t a_sbo, int steps, uint32_t idesc, bool acc) {
@@ -522,9 +531,13 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
                 tc::mma_f16(d, tc::sdesc(sa_u + 256u * st, 128u, a_sbo), tc::sdesc(sw_u + w_byte + 256u * st, 128u, w_sbo),
                             idesc, (acc || st) ? 1u : 0u);
             tc::commit(bar_m);
+            mma_pending = true;
         }
-        ok = tc::mbar_wait(bar_m, phase, kTcBudget);
-        if (ok) phase ^= 1u;
+        ok = tc::mbar_wait(bar_m, phase, budget);
+        if (ok) {
+            phase ^= 1u;
+            mma_pending = false;
+        }
         tc::fence_after();
     };
     // inputs (and albedo) of the CTA's first tile; each iteration then fetches the next tile's before
@@ -621,7 +634,9 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
     }
     if (fail && tid == 0) {
         atomicOr(status, 0x80000000u);
-        tc::mbar_wait(bar_m, phase, kTcBudget);  // an MMA still in flight finishes before TMEM is released
+        // the weight copy and an MMA still in flight finish before shared memory and TMEM are released
+        tc::mbar_wait(bar_w, 0, kTcBudget);
+        if (mma_pending) tc::mbar_wait(bar_m, phase, kTcBudget);
     }
     tc::fence_before();
     __syncthreads();
@@ -660,7 +675,8 @@ __device__ __forceinline__ void red_row(float* __restrict__ g, int din, int f, i
 __global__ void __launch_bounds__(128, 1) train_tc_kernel(const __half* __restrict__ wu, const float* __restrict__ in,
                                                           const float* __restrict__ target, uint32_t n, float inv_norm,
                                                           float* __restrict__ grad, float* __restrict__ loss_sum,
-                                                          const uint32_t* __restrict__ gate, uint32_t* __restrict__ status) {
+                                                          const uint32_t* __restrict__ gate, uint32_t* __restrict__ status,
+                                                          long long budget) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
     if (gate && *gate == 0u) return;  // empty frame batch (uniform over the grid)
     const uint32_t tiles = (n + 127u) / 128u;
@@ -689,9 +705,10 @@ __global__ void __launch_bounds__(128, 1) train_tc_kernel(const __half* __restri
         tc::mbar_expect_tx(bar_w, kUHalves * 2);
         tc::bulk_g2s(s0, wu, kUHalves * 2, bar_w);
     }
-    bool ok = tc::mbar_wait(bar_w, 0, kTcBudget);
+    bool ok = tc::mbar_wait(bar_w, 0, budget);
     bool fail = __syncthreads_or(!ok);
     uint32_t phase = 0;
+    bool mma_pending = false;  // thread 0: a committed MMA batch whose completion it has not seen
     float my_loss = 0.0f;
     bool first = true;  // first tile of this CTA: weight-gradient accumulators start from zero
     constexpr uint32_t kF64 = tc::idesc_f16(128, 64, false, false), kF16 = tc::idesc_f16(128, 16, false, false);
@@ -699,9 +716,15 @@ __global__ void __launch_bounds__(128, 1) train_tc_kernel(const __half* __restri
     constexpr uint32_t kG64 = tc::idesc_f16(64, 64, true, true), kG16 = tc::idesc_f16(64, 16, true, true);
     constexpr uint32_t kG1 = tc::idesc_f16(128, 64, true, true);
     auto wait_mma = [&]() {
-        if (tid == 0) tc::commit(bar_m);
-        ok = tc::mbar_wait(bar_m, phase, kTcBudget);
-        if (ok) phase ^= 1u;
+        if (tid == 0) {
+            tc::commit(bar_m);
+            mma_pending = true;
+        }
+        ok = tc::mbar_wait(bar_m, phase, budget);
+        if (ok) {
+            phase ^= 1u;
+            mma_pending = false;
+        }
         tc::fence_after();
     };
     auto fwd_layer = [&](uint32_t d, uint32_t a_off, uint32_t a_sbo, int l, int steps, uint32_t idesc) {
@@ -874,7 +897,9 @@ __global__ void __launch_bounds__(128, 1) train_tc_kernel(const __half* __restri
         if (lane == 0 && loss_sum) atomicAdd(loss_sum, my_loss);
     } else if (tid == 0) {
         atomicOr(status, 0x80000000u);
-        tc::mbar_wait(bar_m, phase, kTcBudget);  // an MMA still in flight finishes before TMEM is released
+        // the weight copy and an MMA still in flight finish before shared memory and TMEM are released
+        tc::mbar_wait(bar_w, 0, kTcBudget);
+        if (mma_pending) tc::mbar_wait(bar_m, phase, kTcBudget);
     }
     tc::fence_before();
     __syncthreads();
@@ -953,12 +978,15 @@ void init_weights(std::vector<float>& w, uint32_t seed) {
     }
 }
 
+long long tc_budget(const arc_ctx* c) { return c->tc_wait_budget > 0 ? c->tc_wait_budget : nrc::kTcBudget; }
+
 int launch_infer(arc_ctx* c, const float* inputs, const float* albedo, uint32_t n, float* out, const uint32_t* list,
                  const unsigned long long* n_dev) {
     if (c->nrc_infer_path == 1) {
         const uint32_t blocks = std::min<uint32_t>((n + 127u) / 128u, (uint32_t)c->n_sm * 2u);
         nrc::infer_tc_kernel<<<blocks, 128, nrc::kTcSmem, c->stream>>>(static_cast<const __half*>(c->d_nrc_wu_ema), inputs,
-                                                                        albedo, n, out, list, n_dev, c->d_status);
+                                                                        albedo, n, out, list, n_dev, c->d_status,
+                                                                        tc_budget(c));
         NRC_CK(cudaGetLastError());
         return ARC_OK;
     }
@@ -980,7 +1008,7 @@ int launch_grad(arc_ctx* c, const float* inputs, const float* targets, uint32_t 
         const uint32_t blocks = std::min<uint32_t>((n + 127u) / 128u, (uint32_t)c->n_sm);
         nrc::train_tc_kernel<<<blocks, 128, nrc::kTtSmem, c->stream>>>(static_cast<const __half*>(c->d_nrc_wu), inputs, targets, n,
                                                                          1.0f / (float)n, c->d_nrc_grad, loss, gate,
-                                                                         c->d_status);
+                                                                         c->d_status, tc_budget(c));
         NRC_CK(cudaGetLastError());
         return ARC_OK;
     }
@@ -1115,6 +1143,40 @@ int arc_nrc_train_step_dev(arc_ctx* c, const float* inputs, const float* targets
         *loss_host = l / (float)n;
     }
     return ARC_OK;
+}
+
+// Host-buffer forms of the query and the training step: inputs staged to the device, results copied
+// back before the call returns.
+int arc_nrc_query(arc_ctx* c, const float* inputs, const float* albedo, uint32_t n, float* out) {
+    if (!c) return ARC_E_INVALID_ARG;
+    if (n == 0) return ARC_OK;
+    if (!inputs || !out) return nrc_err(c, ARC_E_INVALID_ARG, "null buffer");
+    void* stage;
+    int rc = arc_ctx_stage(c, (size_t)n * 60u, &stage);
+    if (rc) return rc;
+    float* d_in = static_cast<float*>(stage);
+    float* d_out = d_in + 9u * (size_t)n;
+    float* d_alb = albedo ? d_out + 3u * (size_t)n : nullptr;
+    NRC_CK(cudaMemcpyAsync(d_in, inputs, (size_t)n * 36u, cudaMemcpyHostToDevice, c->stream));
+    if (albedo) NRC_CK(cudaMemcpyAsync(d_alb, albedo, (size_t)n * 12u, cudaMemcpyHostToDevice, c->stream));
+    if ((rc = arc_nrc_query_dev(c, d_in, d_alb, n, d_out))) return rc;
+    NRC_CK(cudaMemcpyAsync(out, d_out, (size_t)n * 12u, cudaMemcpyDeviceToHost, c->stream));
+    return arc_ctx_finish(c);
+}
+
+int arc_nrc_train_step(arc_ctx* c, const float* inputs, const float* targets, uint32_t n, float lr, float* loss_host) {
+    if (!c) return ARC_E_INVALID_ARG;
+    if (n == 0) return ARC_OK;
+    if (!inputs || !targets) return nrc_err(c, ARC_E_INVALID_ARG, "null buffer");
+    void* stage;
+    int rc = arc_ctx_stage(c, (size_t)n * 48u, &stage);
+    if (rc) return rc;
+    float* d_in = static_cast<float*>(stage);
+    float* d_t = d_in + 9u * (size_t)n;
+    NRC_CK(cudaMemcpyAsync(d_in, inputs, (size_t)n * 36u, cudaMemcpyHostToDevice, c->stream));
+    NRC_CK(cudaMemcpyAsync(d_t, targets, (size_t)n * 12u, cudaMemcpyHostToDevice, c->stream));
+    if ((rc = arc_nrc_train_step_dev(c, d_in, d_t, n, lr, loss_host))) return rc;
+    return arc_ctx_finish(c);
 }
 
 int arc_nrc_frame_dev(arc_ctx* c, const uint32_t* list, const uint64_t* n_valid, uint32_t max_n, const float* pos,

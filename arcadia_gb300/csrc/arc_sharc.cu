@@ -5,7 +5,7 @@
 //                         bounce at x1, then deposits L_o(x1) with a CAS slot claim and fixed-point adds.
 //   sharc_resolve_kernel  sharc_resolve.wgsl main (shaders/sharc_resolve.wgsl:13-70): EMA fold, aging,
 //                         eviction, accumulator clear; one thread per slot.
-//   sharc_query_kernel    query_sharc (shaders/common/sharc_query.wgsl:125-146) on a batch.
+//   sharc_query_kernel    query_sharc (shaders/common/sharc_query.wgsl:21-29) on a batch.
 // Compiled with the canonical arithmetic flags (arc_math.cuh).
 #include <cuda_runtime.h>
 
@@ -707,6 +707,43 @@ int arc_sharc_query_dev(arc_ctx* c, const float* pos, const float* normal, const
     arc::sharc_query_kernel<<<(n + 127u) / 128u, 128, 0, c->stream>>>(reinterpret_cast<const uint4*>(c->d_sharc_resolved), pos,
                                                                       normal, jitter, n, cam, reinterpret_cast<float4*>(out));
     return launch_check(c, "sharc_query_kernel");
+}
+
+// Host-buffer form: the inputs are staged to the device, the results copied back, and the call returns
+// when they are in `out` (the status word is checked as for every host-buffer entry point).
+int arc_sharc_query(arc_ctx* c, const float* pos, const float* normal, const float* jitter, uint32_t n, float* out) {
+    if (!c) return ARC_E_INVALID_ARG;
+    if (n == 0) return ARC_OK;
+    if (!pos || !normal || !out) return sharc_err(c, ARC_E_INVALID_ARG, "null buffer");
+    void* stage;
+    int rc = arc_ctx_stage(c, (size_t)n * 48u, &stage);
+    if (rc) return rc;
+    float* d_pos = static_cast<float*>(stage);
+    float* d_nrm = d_pos + 3u * (size_t)n;
+    float* d_out = d_nrm + 3u * (size_t)n;
+    float* d_jit = jitter ? d_out + 4u * (size_t)n : nullptr;
+    cudaMemcpyAsync(d_pos, pos, (size_t)n * 12u, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(d_nrm, normal, (size_t)n * 12u, cudaMemcpyHostToDevice, c->stream);
+    if (jitter) cudaMemcpyAsync(d_jit, jitter, (size_t)n * 8u, cudaMemcpyHostToDevice, c->stream);
+    if ((rc = arc_sharc_query_dev(c, d_pos, d_nrm, d_jit, n, d_out))) return rc;
+    cudaMemcpyAsync(out, d_out, (size_t)n * 16u, cudaMemcpyDeviceToHost, c->stream);
+    if ((rc = launch_check(c, "arc_sharc_query"))) return rc;
+    return arc_ctx_finish(c);
+}
+
+int arc_nrc_train_samples_dev(arc_ctx* c, const uint32_t* list, const uint64_t* n_valid, const float* pos,
+                              const float* normal, const float* nrc_in, uint32_t seed, uint32_t n_samples, uint32_t steps,
+                              float* train_in, float* train_t) {
+    int rc = arc_ctx_check_ready(c, true);
+    if (rc) return rc;
+    if (!list || !n_valid || !pos || !normal || !nrc_in || !train_in || !train_t)
+        return sharc_err(c, ARC_E_INVALID_ARG, "null buffer");
+    if (steps == 0 || n_samples < steps || n_samples % steps)
+        return sharc_err(c, ARC_E_INVALID_ARG, "n_samples must be a non-zero multiple of steps");
+    if (!c->d_nrc_gate && cudaMalloc((void**)&c->d_nrc_gate, sizeof(uint32_t)) != cudaSuccess)
+        return sharc_err(c, ARC_E_CUDA, "gate word allocation");
+    return arc_launch_train_samples_list(c, list, reinterpret_cast<const unsigned long long*>(n_valid), pos, normal, nrc_in,
+                                         seed, n_samples, steps, train_in, train_t, c->d_nrc_gate);
 }
 
 int arc_sharc_deposit_dev(arc_ctx* c, const float pos[3], const float normal[3], const float cam_pos[3], const float rad[3],

@@ -36,7 +36,7 @@ __device__ __forceinline__ f3 slot_radiance(uint4 s) {
     return f3{f16_value(s.y & 0xFFFFu), f16_value(s.y >> 16), f16_value(s.z & 0xFFFFu)};
 }
 
-// sharc_lookup / query_sharc (shaders/common/sharc_query.wgsl:125-146); w = 1 on hit.
+// sharc_lookup / query_sharc (shaders/common/sharc_query.wgsl:8-29); w = 1 on hit.
 __device__ __forceinline__ float4 sharc_lookup(const uint4* res, uint32_t bucket, uint32_t key) {
     const uint32_t base = bucket * ARC_SHARC_WAYS;
 #pragma unroll

@@ -50,6 +50,7 @@ SIGNATURES = {
     "arc_autotune_frame_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _u32, _vp, _vp],
     "arc_get_launch_config": [_vp, _vp],
     "arc_get_stats": [_vp, _vp],
+    "arc_debug_set": [_vp, _i32, C.c_longlong],
     "arc_upload_world": [_vp, _vp, _vp, _u32, _vp, _u32, _vp, _u32, _vp, _u32, _u32],
     "arc_apply_patch": [_vp, _u32, _u32, _u32, _vp, _u32, _u32, _vp, _u32],
     "arc_set_camera": [_vp, _vp],
@@ -74,6 +75,7 @@ SIGNATURES = {
     "arc_sharc_update_dev": [_vp, _u32, _u32, _vp, _vp],
     "arc_sharc_resolve": [_vp],
     "arc_sharc_query_dev": [_vp, _vp, _vp, _vp, _u32, _vp],
+    "arc_sharc_query": [_vp, _vp, _vp, _vp, _u32, _vp],
     "arc_sharc_download": [_vp, _vp, _vp, _vp],
     "arc_sharc_upload": [_vp, _vp, _vp, _vp],
     "arc_sharc_deposit_dev": [_vp, _vp, _vp, _vp, _vp, _u32],
@@ -98,8 +100,11 @@ SIGNATURES = {
     "arc_sharc_frame_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _u32, _vp, _vp, _vp],
     "arc_sharc_query_list_dev": [_vp, _vp, _vp, _u32, _vp, _vp, _vp],
     "arc_nrc_query_dev": [_vp, _vp, _vp, _u32, _vp],
+    "arc_nrc_query": [_vp, _vp, _vp, _u32, _vp],
+    "arc_nrc_train_samples_dev": [_vp, _vp, _vp, _vp, _vp, _vp, _u32, _u32, _u32, _vp, _vp],
     "arc_nrc_grad_dev": [_vp, _vp, _vp, _u32, _vp],
     "arc_nrc_train_step_dev": [_vp, _vp, _vp, _u32, _f32, _vp],
+    "arc_nrc_train_step": [_vp, _vp, _vp, _u32, _f32, _vp],
     "arc_default_palette": [_vp],
     "arc_world_build": [_vp, _vp, _i32, C.POINTER(_vp)],
     "arc_world_info": [_vp, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u64)],

@@ -13,13 +13,18 @@
  *   arc_trace_primary    record_primary_raymarch_pass (crates/arcadia-render/src/pipeline.rs:150-166)
  *                        -> primary_raymarch (shaders/primary_gbuffer.wgsl:93-312)
  *   arc_trace_secondary  the Pass-2A GI secondary ray (shaders/lighting_restir_gi.wgsl:195-209)
- *   arc_trace_frame      primary + GI secondary in one persistent launch (no reference counterpart:
- *                        the fusion of the two passes above)
+ *   arc_trace_frame      primary + GI secondary of a whole frame (no reference counterpart: the two
+ *                        passes above in one call; by default the primary kernel, then the frame's
+ *                        GI rays as a pass of their own; arc_set_launch_config variant 1 = one
+ *                        persistent launch for both)
  *   arc_trace_rays       trace_world_64tree (shaders/common/traversal64.wgsl:559-567) on a ray batch
  *   arc_sharc_update     record_sharc_update_pass (crates/arcadia-render/src/sharc.rs:225-241)
  *                        -> sharc_update.wgsl main (shaders/sharc_update.wgsl:148-191)
  *   arc_sharc_resolve    record_sharc_resolve_pass (sharc.rs:244-256) -> sharc_resolve.wgsl:13-70
- *   arc_sharc_query      query_sharc (shaders/common/sharc_query.wgsl:138-146) on a batch
+ *   arc_sharc_query      query_sharc (shaders/common/sharc_query.wgsl:21-29) on a batch
+ *   arc_nrc_query        the neural radiance cache in place of query_sharc at secondary hits
+ *                        (lighting_restir_gi.wgsl:249, sharc_update.wgsl:94); no reference counterpart
+ *   arc_nrc_train_step   one Adam step of that cache on a batch of radiance samples (no counterpart)
  *
  * Conventions: library-owned device memory lives behind an opaque arc_ctx; caller-owned host
  * memory is copied in and out inside the call (the *_dev variants take device pointers and
@@ -87,6 +92,25 @@ int arc_autotune_frame_dev(arc_ctx* ctx, uint32_t width, uint32_t height, uint32
 int arc_get_launch_config(const arc_ctx* ctx, arc_launch_config* cfg);
 int arc_get_stats(const arc_ctx* ctx, arc_stats* out);
 
+/* Fault-injection hooks for tests of the library's failure detection; no counterpart in the
+ * reference, whose renderer has no device-side checks. They make a failure happen without faulting
+ * the GPU: the library's own checks must catch it and the context must stay usable.
+ *   ARC_DEBUG_TC_WAIT_BUDGET        value = clock cycles each tensor-core pipeline wait of the NRC
+ *                                   kernels may take before it gives up (0 restores the default of
+ *                                   about one second). A wait that runs out sets bit 31 of the device
+ *                                   status word; the kernel waits for its own copies and MMAs in flight,
+ *                                   frees its TMEM and returns, and the call that reads the status back
+ *                                   (arc_synchronize or a host-buffer entry point) fails with
+ *                                   ARC_E_DEVICE_CHECK ("tensor-core pipeline wait timed out").
+ *   ARC_DEBUG_SKIP_POOL_VALIDATION  value 1 = arc_upload_world uploads the pools without its range
+ *                                   validation, so a corrupt pool reaches the kernels; their range
+ *                                   checks read an out-of-range node as empty and an out-of-range
+ *                                   brick as air, and the status readback fails with
+ *                                   ARC_E_DEVICE_CHECK. 0 restores the validation. */
+#define ARC_DEBUG_TC_WAIT_BUDGET 1
+#define ARC_DEBUG_SKIP_POOL_VALIDATION 2
+int arc_debug_set(arc_ctx* ctx, int what, long long value);
+
 /* Pools as WorldMap packs them. The pools are validated (every child pointer, brick index and root
  * in range) before upload; node/brick capacity reserves headroom for patches. */
 int arc_upload_world(arc_ctx* ctx, const uint32_t grid[3], const uint32_t* roots, uint32_t n_roots,
@@ -146,8 +170,13 @@ int arc_trace_frame_dev(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t*
  * they trace (a renderer whose frame loop runs under a no-allocation rule or its own memory budget).
  * No counterpart in the reference. The kernels' scratch (queue head, GI-ray counter) lives in a
  * 256-byte static device array instead of context memory; frames above 2^26 pixels are rejected with
- * ARC_E_CAPACITY. All calls share that array, so calls overlapping on one device race; the first call
- * on a device looks up the array's address and should come before any stream capture. */
+ * ARC_E_CAPACITY. All calls in one CUDA context share that array, so calls overlapping on the GPU
+ * race. The first call in a CUDA context (again after that context is recreated, e.g. after
+ * cudaDeviceReset) looks up the array's address with the ctx's device current, then restores the
+ * caller's current device; it should come before any stream capture. Under CUDA's lazy module
+ * loading the first launch of each kernel instance may load code into device memory: make one
+ * warm-up call per launch configuration (and with and without the surface list, if both occur)
+ * before the region that must not allocate. */
 int arc_trace_frame_noalloc(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbuf_depth_mat,
                             uint32_t* gbuf_norm_motion, uint32_t* gbuf_albedo_ao, arc_hit_record* hits,
                             arc_hit_record* gi_hits, uint64_t* n_gi_dev);
@@ -184,6 +213,10 @@ int arc_sharc_update_dev(arc_ctx* ctx, uint32_t width, uint32_t height, const ui
 int arc_sharc_resolve(arc_ctx* ctx);
 int arc_sharc_query_dev(arc_ctx* ctx, const float* pos, const float* normal, const float* jitter, uint32_t n,
                         float* out_rgbw);
+/* Host-buffer arc_sharc_query_dev: pos/normal 3 floats, jitter 2 floats (may be NULL = no jitter) and
+ * out_rgbw 4 floats per query, all in caller memory; returns when out_rgbw is filled. */
+int arc_sharc_query(arc_ctx* ctx, const float* pos, const float* normal, const float* jitter, uint32_t n,
+                    float* out_rgbw);
 int arc_sharc_download(arc_ctx* ctx, uint32_t* keys, uint32_t* accum, arc_sharc_slot* resolved);
 int arc_sharc_upload(arc_ctx* ctx, const uint32_t* keys, const uint32_t* accum, const arc_sharc_slot* resolved);
 /* Test hook mirroring the reference's SHARC GPU harness (crates/arcadia-render/tests/sharc_gpu.rs:18-29):
@@ -286,6 +319,9 @@ int arc_nrc_set_train_path(arc_ctx* ctx, int path);
 int arc_nrc_get_ema_weights(arc_ctx* ctx, float* weights);
 /* out_rgb[i] = albedo[i] * network(inputs[i]) per channel; albedo may be NULL (network output only). */
 int arc_nrc_query_dev(arc_ctx* ctx, const float* inputs, const float* albedo, uint32_t n, float* out_rgb);
+/* Host-buffer arc_nrc_query_dev (9 input floats, 3 albedo floats (albedo may be NULL), 3 output floats
+ * per query in caller memory); returns when out_rgb is filled. */
+int arc_nrc_query(arc_ctx* ctx, const float* inputs, const float* albedo, uint32_t n, float* out_rgb);
 /* arc_nrc_query_dev at the points list[0 .. min(*n_dev, max_n)): out[list[j]] from inputs/albedo[list[j]]. */
 int arc_nrc_query_list_dev(arc_ctx* ctx, const uint32_t* list, const uint64_t* n_dev, uint32_t max_n,
                            const float* inputs, const float* albedo, float* out_rgb);
@@ -311,11 +347,21 @@ int arc_sharc_frame_dev(arc_ctx* ctx, uint32_t width, uint32_t height, const uin
 int arc_nrc_train_frame_dev(arc_ctx* ctx, const uint32_t* list, const uint64_t* n_valid, const float* pos,
                             const float* normal, const float* nrc_in, uint32_t seed, uint32_t n_samples,
                             uint32_t steps, float lr);
+/* The training batch arc_nrc_train_frame_dev draws, into caller device buffers: train_in (9 floats per
+ * sample) and train_t (the 1-spp one-bounce target with albedo 1, 3 floats), sample i taken from
+ * list[floor((i + phase) * n_valid / n_samples)] with phase = (pcg_hash(seed) * n_valid) >> 32 and
+ * stored at slot (i mod steps) * (n_samples / steps) + i / steps. Nothing is stored when *n_valid = 0. */
+int arc_nrc_train_samples_dev(arc_ctx* ctx, const uint32_t* list, const uint64_t* n_valid, const float* pos,
+                              const float* normal, const float* nrc_in, uint32_t seed, uint32_t n_samples,
+                              uint32_t steps, float* train_in, float* train_t);
 /* Loss-scaled (x128) weight gradient of the mean relative-L2 loss of one batch (device output). */
 int arc_nrc_grad_dev(arc_ctx* ctx, const float* inputs, const float* targets, uint32_t n, float* grad_out);
 /* One Adam step (lr; beta 0.9/0.99) on a batch; loss_host (optional) receives the batch loss. */
 int arc_nrc_train_step_dev(arc_ctx* ctx, const float* inputs, const float* targets, uint32_t n, float lr,
                            float* loss_host);
+/* Host-buffer arc_nrc_train_step_dev (inputs 9 floats, targets 3 floats per sample in caller memory). */
+int arc_nrc_train_step(arc_ctx* ctx, const float* inputs, const float* targets, uint32_t n, float lr,
+                       float* loss_host);
 
 #ifdef __cplusplus
 }

@@ -192,6 +192,27 @@ void orc_sharc_update(const orc_world* w, const arc_camera_uniforms* cam, const 
                       const uint32_t* gbuf_norm_motion, const arc_sharc_slot* resolved_prev, uint32_t* keys,
                       uint32_t* accum, uint32_t* tile_key, uint32_t* tile_bucket, float* tile_rad, uint32_t* tile_valid);
 
+void orc_sharc_update_mode(const orc_world* w, const arc_camera_uniforms* cam, const uint32_t* gbuf_depth_mat,
+                           const uint32_t* gbuf_norm_motion, const arc_sharc_slot* resolved_prev, uint32_t* keys,
+                           uint32_t* accum, uint32_t* tile_key, uint32_t* tile_bucket, float* tile_rad,
+                           uint32_t* tile_valid, uint32_t mode);
+
+/* one-bounce estimator of the cache comparison and the points / training batch built on it */
+void orc_cmp_albedo(uint32_t mat, float out[3]);
+void orc_onebounce_sun(const orc_world* w, const arc_camera_uniforms* cam, const float pos[3], const float n[3], float out[3]);
+void orc_onebounce_sky(const orc_world* w, const arc_camera_uniforms* cam, const float pos[3], const float n[3],
+                       uint32_t seed, float out[3]);
+void orc_onebounce(const orc_world* w, const arc_camera_uniforms* cam, const uint32_t* idx, uint32_t n, const float* pos,
+                   const float* nrm, const float* alb, uint32_t spp, uint32_t seed, int accumulate, float* out, int threads);
+void orc_train_samples(const orc_world* w, const arc_camera_uniforms* cam, const uint32_t* list, uint64_t n_valid,
+                       const float* pos, const float* nrm, const float* nrc_in, uint32_t seed, uint32_t n_samples,
+                       uint32_t steps, float* train_in, float* train_t, int threads);
+void orc_gi_points(const orc_world* w, const arc_camera_uniforms* cam, uint32_t W, uint32_t H, const uint32_t* gdm,
+                   const uint32_t* gnm, float* pos, float* nrm, float* alb, float* nrc_in, uint32_t* valid, int threads);
+void orc_gi_points_from_hits(const arc_camera_uniforms* cam, uint32_t W, uint32_t H, const uint32_t* gdm, const uint32_t* gnm,
+                             const arc_hit_record* gi_hits, float* pos, float* nrm, float* alb, float* nrc_in,
+                             uint32_t* valid);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,7 +1,7 @@
 /*
  * orc_sharc.c — oracle restatement of the SHARC voxel-surfel radiance cache:
  *   key hashing / packing        shaders/common/sharc.wgsl:36-116
- *   query_sharc                  shaders/common/sharc_query.wgsl:125-146
+ *   query_sharc                  shaders/common/sharc_query.wgsl:8-29
  *   claim / deposit / update     shaders/sharc_update.wgsl:32-191
  *   resolve (EMA, aging, evict)  shaders/sharc_resolve.wgsl:13-70
  *   eval_sky_radiance            shaders/common/types.wgsl:500-523
@@ -180,7 +180,7 @@ static void eval_sky(const float dir[3], const float sun[3], float out[3]) {
 
 void orc_sky_radiance(const float dir[3], const float sun[3], float out[3]) { eval_sky(dir, sun, out); }
 
-typedef struct surf { int hit; float t_m; float pos[3]; float normal[3]; float albedo[3]; float emission[3]; } surf;
+typedef struct surf { int hit; uint32_t mat; float t_m; float pos[3]; float normal[3]; float albedo[3]; float emission[3]; } surf;
 
 static void trace_surface(const orc_world* w, const arc_camera_uniforms* cam, const float o[3], const float d[3],
                           float max_dist, surf* s) {
@@ -190,6 +190,7 @@ static void trace_surface(const orc_world* w, const arc_camera_uniforms* cam, co
     if (!tr.hit) return;
     const arc_material* m = &w->palette[tr.mat_id];
     s->hit = 1;
+    s->mat = tr.mat_id;
     s->t_m = tr.t_voxels * ARC_VOXEL_SIZE;
     memcpy(s->pos, tr.hit_pos_m, sizeof(s->pos));
     memcpy(s->normal, tr.normal, sizeof(s->normal));
@@ -242,9 +243,209 @@ static void oct_decode_packed(uint32_t p, float n[3]) {
     orc_normalize3(v, n);
 }
 
+/* ------------------------------------------------------------------------------------------ */
+/* One-bounce estimator of the cache comparison (no reference counterpart: the light transport the */
+/* NRC and SHARC are judged on). L(x) = albedo * (c_sun max(n.l, 0) V(x, l) + L_sky [a cosine ray  */
+/* from x + 0.10 n escapes within 64 m]); V is trace_shadow_vis (traversal64.wgsl:571-773) from     */
+/* x + 0.10 n over 32 m as in sharc_shade_surface (sharc_update.wgsl:68-105), c_sun = sun_power *    */
+/* (1, 0.9, 0.75) * 0.55, L_sky = (0.30, 0.42, 0.60); the sky ray is a lod_bias 2, water-ignoring   */
+/* trace of the static world with a cosine direction (make_basis + sample_cosine_hemisphere,        */
+/* types.wgsl:531-545) from two PCG draws.                                                        */
+/* ------------------------------------------------------------------------------------------ */
+
+void orc_cmp_albedo(uint32_t mat, float out[3]) {
+    uint32_t h0 = orc_pcg_hash(mat * 3u + 0x2545F491u), h1 = orc_pcg_hash(h0 ^ 0x9E3779B9u), h2 = orc_pcg_hash(h1 ^ 0x85EBCA6Bu);
+    const float s = 0.8f / 16777216.0f;
+    out[0] = 0.1f + (float)(h0 >> 8) * s;
+    out[1] = 0.1f + (float)(h1 >> 8) * s;
+    out[2] = 0.1f + (float)(h2 >> 8) * s;
+}
+
+void orc_onebounce_sun(const orc_world* w, const arc_camera_uniforms* cam, const float pos[3], const float n[3], float out[3]) {
+    const float* sun = cam->sun_dir_intensity;
+    float sun_power = cam->sun_dir_intensity[3];
+    float ndl = orc_max(orc_dot3(n, sun), 0.0f);
+    out[0] = out[1] = out[2] = 0.0f;
+    if (!(ndl > 0.001f && sun_power > 0.01f)) return;
+    float o[3];
+    for (int i = 0; i < 3; ++i) o[i] = pos[i] + n[i] * 0.10f;
+    float k = ((sun_power * ndl) * orc_shadow_vis(w, cam, o, sun, 32.0f, NULL)) * 0.55f;
+    out[0] = 1.0f * k;
+    out[1] = 0.90f * k;
+    out[2] = 0.75f * k;
+}
+
+void orc_onebounce_sky(const orc_world* w, const arc_camera_uniforms* cam, const float pos[3], const float n[3],
+                       uint32_t seed, float out[3]) {
+    uint32_t h1 = orc_pcg_hash(seed), h2 = orc_pcg_hash(h1 ^ 0x68E31DA4u);
+    float u1 = (float)(h1 >> 8) * (1.0f / 16777216.0f), u2 = (float)(h2 >> 8) * (1.0f / 16777216.0f);
+    float d[3], o[3];
+    cos_hemi(u1, u2, n, d);
+    for (int i = 0; i < 3; ++i) o[i] = pos[i] + n[i] * 0.10f;
+    orc_trace_out tr;
+    orc_trace(w, cam, o, d, 0.0f, 64.0f, 2u, 1, &tr);
+    if (tr.hit) {
+        out[0] = out[1] = out[2] = 0.0f;
+    } else {
+        out[0] = 0.30f;
+        out[1] = 0.42f;
+        out[2] = 0.60f;
+    }
+}
+
+static void onebounce(const orc_world* w, const arc_camera_uniforms* cam, const float pos[3], const float n[3],
+                      const float albedo[3], uint32_t seed, float out[3]) {
+    float a[3], c[3];
+    orc_onebounce_sun(w, cam, pos, n, a);
+    orc_onebounce_sky(w, cam, pos, n, seed, c);
+    for (int i = 0; i < 3; ++i) out[i] = albedo[i] * (a[i] + c[i]);
+}
+
+void orc_onebounce(const orc_world* w, const arc_camera_uniforms* cam, const uint32_t* idx, uint32_t n, const float* pos,
+                   const float* nrm, const float* alb, uint32_t spp, uint32_t seed, int accumulate, float* out, int threads) {
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads > 0 ? threads : 1)
+    for (int64_t ii = 0; ii < (int64_t)n; ++ii) {
+        uint32_t i = (uint32_t)ii;
+        uint32_t p = idx ? idx[i] : i;
+        float sum[3] = {0.0f, 0.0f, 0.0f};
+        for (uint32_t k = 0; k < spp; ++k) {
+            float l[3];
+            onebounce(w, cam, &pos[3 * (size_t)p], &nrm[3 * (size_t)p], &alb[3 * (size_t)p],
+                      orc_pcg_hash(p * 0x9E3779B9u ^ orc_pcg_hash(seed + k * 0x632BE5ABu)), l);
+            for (int c = 0; c < 3; ++c) sum[c] += l[c];
+        }
+        float inv = 1.0f / (float)spp;
+        for (int c = 0; c < 3; ++c) {
+            if (accumulate) out[3 * (size_t)i + c] += sum[c] * inv;
+            else out[3 * (size_t)i + c] = sum[c] * inv;
+        }
+    }
+}
+
+/* The NRC training batch of a frame: sample i takes list[floor((i * n_valid + phase) / n_samples)],
+ * phase = (pcg_hash(seed) * n_valid) >> 32; its target is the 1-spp estimator with albedo 1 (sky ray
+ * seeded by pcg_hash(i ^ pcg_hash(seed ^ 0xB5297A4D))), stored with the point's 9 network inputs at
+ * slot (i mod steps) * (n_samples / steps) + i / steps. */
+void orc_train_samples(const orc_world* w, const arc_camera_uniforms* cam, const uint32_t* list, uint64_t n_valid,
+                       const float* pos, const float* nrm, const float* nrc_in, uint32_t seed, uint32_t n_samples,
+                       uint32_t steps, float* train_in, float* train_t, int threads) {
+    if (!n_valid) return;
+    const uint64_t phase = ((uint64_t)orc_pcg_hash(seed) * n_valid) >> 32;
+    const uint32_t per = n_samples / steps;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads > 0 ? threads : 1)
+    for (int64_t ii = 0; ii < (int64_t)n_samples; ++ii) {
+        uint32_t i = (uint32_t)ii;
+        uint32_t j = (uint32_t)(((uint64_t)i * n_valid + phase) / n_samples);
+        uint32_t p = list[j];
+        float sun[3], sky[3];
+        orc_onebounce_sun(w, cam, &pos[3 * (size_t)p], &nrm[3 * (size_t)p], sun);
+        orc_onebounce_sky(w, cam, &pos[3 * (size_t)p], &nrm[3 * (size_t)p], orc_pcg_hash(i ^ orc_pcg_hash(seed ^ 0xB5297A4Du)), sky);
+        size_t slot = (size_t)(i % steps) * per + i / steps;
+        for (int q = 0; q < 9; ++q) train_in[slot * 9 + q] = nrc_in[(size_t)p * 9 + q];
+        for (int c = 0; c < 3; ++c) train_t[3 * slot + c] = sky[c] + sun[c];
+    }
+}
+
+/* GI hit points of a frame (what both caches are queried at): per pixel with a primary hit, the Pass-2A
+ * GI ray from the G-buffer (orc_gi_setup) traced as lod_bias 2, water-ignoring, over ray_distances.z;
+ * at its hit the point, normal, comparison albedo and the 9 network inputs (point / world extent,
+ * normal, -ray direction). valid = 0 where there is no primary hit or the GI ray misses. */
+static void write_point(const arc_camera_uniforms* cam, size_t k, const float p[3], const float n[3], uint32_t mat,
+                        const float view[3], float* pos, float* nrm, float* alb, float* nrc_in) {
+    float a[3];
+    orc_cmp_albedo(mat, a);
+    float ex = (float)cam->world_grid_dims[0] * 16.0f, ey = (float)cam->world_grid_dims[1] * 16.0f,
+          ez = (float)cam->world_grid_dims[2] * 16.0f;
+    for (int i = 0; i < 3; ++i) {
+        pos[3 * k + i] = p[i];
+        nrm[3 * k + i] = n[i];
+        alb[3 * k + i] = a[i];
+    }
+    float* q = nrc_in + 9 * k;
+    q[0] = p[0] / ex;
+    q[1] = p[1] / ey;
+    q[2] = p[2] / ez;
+    q[3] = n[0];
+    q[4] = n[1];
+    q[5] = n[2];
+    q[6] = view[0];
+    q[7] = view[1];
+    q[8] = view[2];
+}
+
+void orc_gi_points(const orc_world* w, const arc_camera_uniforms* cam, uint32_t W, uint32_t H, const uint32_t* gdm,
+                   const uint32_t* gnm, float* pos, float* nrm, float* alb, float* nrc_in, uint32_t* valid, int threads) {
+#pragma omp parallel for schedule(dynamic, 4) num_threads(threads > 0 ? threads : 1)
+    for (int64_t yy = 0; yy < (int64_t)H; ++yy) {
+        for (uint32_t x = 0; x < W; ++x) {
+            uint32_t y = (uint32_t)yy;
+            size_t k = (size_t)y * W + x;
+            uint32_t bytes = 0;
+            orc_gi_ray g;
+            valid[k] = 0u;
+            if (!orc_gi_setup(w, cam, x, y, W, H, gdm[2 * k], gnm[2 * k], &g, &bytes)) continue;
+            orc_trace_out tr;
+            orc_trace(w, cam, g.origin, g.dir, 0.0f, cam->ray_distances[2], 2u, 1, &tr);
+            if (!tr.hit) continue;
+            valid[k] = 1u;
+            float view[3] = {-g.dir[0], -g.dir[1], -g.dir[2]};
+            write_point(cam, k, tr.hit_pos_m, tr.normal, tr.mat_id, view, pos, nrm, alb, nrc_in);
+        }
+    }
+}
+
+/* The same points from the frame's GI hit records, without tracing: the centre of the hit cell's entry
+ * face (LOD cells included), that face's normal, the view direction from the point back to the GI ray's
+ * origin (primary hit + 0.10 m along its G-buffer normal). */
+void orc_gi_points_from_hits(const arc_camera_uniforms* cam, uint32_t W, uint32_t H, const uint32_t* gdm, const uint32_t* gnm,
+                             const arc_hit_record* gi_hits, float* pos, float* nrm, float* alb, float* nrc_in,
+                             uint32_t* valid) {
+    for (uint32_t y = 0; y < H; ++y)
+        for (uint32_t x = 0; x < W; ++x) {
+            size_t k = (size_t)y * W + x;
+            const arc_hit_record* h = &gi_hits[k];
+            float hit_dist = orc_bitsf(gdm[2 * k]);
+            valid[k] = 0u;
+            if (!((h->flags & ARC_HIT_FLAG_HIT) && h->face < 6u && hit_dist < 1e4f)) continue;
+            valid[k] = 1u;
+            int32_t span_i = 1 << (2u * ((h->flags >> 1) & 7u));
+            float span = (float)span_i;
+            float c[3] = {(float)(h->voxel[0] & ~(span_i - 1)), (float)(h->voxel[1] & ~(span_i - 1)),
+                          (float)(h->voxel[2] & ~(span_i - 1))};
+            float axis_sign = (h->face & 1u) ? -1.0f : 1.0f;
+            uint32_t axis = h->face >> 1;
+            float n[3] = {0.0f, 0.0f, 0.0f}, p[3];
+            for (int i = 0; i < 3; ++i) p[i] = c[i] + 0.5f * span;
+            n[axis] = axis_sign;
+            p[axis] = c[axis] + (axis_sign > 0.0f ? span : 0.0f);
+            for (int i = 0; i < 3; ++i) p[i] = p[i] * ARC_VOXEL_SIZE;
+            float rd[3], gn[3], o[3], v[3], view[3];
+            cam_dir(cam, x, y, W, H, rd);
+            oct_decode_packed(gnm[2 * k], gn);
+            for (int i = 0; i < 3; ++i) o[i] = (cam->cam_pos_time[i] + rd[i] * hit_dist) + gn[i] * 0.10f;
+            for (int i = 0; i < 3; ++i) v[i] = o[i] - p[i];
+            float len = orc_length3(v);
+            if (len > 0.0f) {
+                float inv = 1.0f / len;
+                for (int i = 0; i < 3; ++i) view[i] = v[i] * inv;
+            } else {
+                memcpy(view, n, sizeof(view));
+            }
+            write_point(cam, k, p, n, h->mat, view, pos, nrm, alb, nrc_in);
+        }
+}
+
 void orc_sharc_update(const orc_world* w, const arc_camera_uniforms* cam, const uint32_t* gdm, const uint32_t* gnm,
                       const arc_sharc_slot* resolved_prev, uint32_t* keys, uint32_t* accum, uint32_t* tile_key,
                       uint32_t* tile_bucket, float* tile_rad, uint32_t* tile_valid) {
+    orc_sharc_update_mode(w, cam, gdm, gnm, resolved_prev, keys, accum, tile_key, tile_bucket, tile_rad, tile_valid, 0u);
+}
+
+/* mode 0: sharc_shade_surface at the path vertex, as the reference; mode 1: the one-bounce estimator
+ * above with the comparison albedo of the vertex's material. */
+void orc_sharc_update_mode(const orc_world* w, const arc_camera_uniforms* cam, const uint32_t* gdm, const uint32_t* gnm,
+                           const arc_sharc_slot* resolved_prev, uint32_t* keys, uint32_t* accum, uint32_t* tile_key,
+                           uint32_t* tile_bucket, float* tile_rad, uint32_t* tile_valid, uint32_t mode) {
     uint32_t W = cam->world_grid_dims[3] & 0xFFFFu, H = cam->world_grid_dims[3] >> 16;
     uint32_t tile = (cam->quality_flags[3] & 0xFFu) <= 12u ? 16u : 8u;
     uint32_t tx = (W + tile - 1u) / tile, ty = (H + tile - 1u) / tile;
@@ -278,6 +479,19 @@ void orc_sharc_update(const orc_world* w, const arc_camera_uniforms* cam, const 
             surf s1;
             trace_surface(w, cam, o0, d0, bounce_max, &s1);
             if (!s1.hit) continue;
+            if (mode == 1u) {
+                float a1[3], rad[3], zero[2] = {0.0f, 0.0f};
+                orc_cmp_albedo(s1.mat, a1);
+                onebounce(w, cam, s1.pos, s1.normal, a1, h ^ (frame * 0x9E3779B9u), rad);
+                uint32_t b, k;
+                orc_sharc_make_key(s1.pos, s1.normal, cam->cam_pos_time, zero, &b, &k);
+                orc_sharc_deposit(keys, accum, b, k, rad);
+                tile_valid[ti] = 1;
+                tile_key[ti] = k;
+                tile_bucket[ti] = b;
+                memcpy(&tile_rad[3 * ti], rad, sizeof(rad));
+                continue;
+            }
             /* sharc_shade_surface */
             const float* n = s1.normal;
             float direct[3] = {0, 0, 0};

@@ -33,14 +33,22 @@ static inline uint32_t node_child_offset(const arc_node64* n, uint32_t b) {
     return base + orc_popc(n->mask_low & pl) + orc_popc(n->mask_high & ph);
 }
 
+/* Pool reads out of range read zero: the reference validates its traversal shaders with naga's
+ * ReadZeroSkipWrite bounds-check policy (crates/arcadia-render/tests/shader_validation.rs:39-50), so a
+ * corrupt pointer reads an empty node or an air brick word. */
 static inline uint32_t brick_get_material(const orc_world* w, uint32_t brick_idx, uint32_t bit, uint32_t* bytes) {
     *bytes += 4;
+    if (brick_idx >= w->n_bricks) return 0u;
     uint32_t word = w->bricks[brick_idx].packed_materials[bit >> 2];
     return (word >> ((bit & 3u) * 8u)) & 0xFFu;
 }
 
 static inline arc_node64 load_node(const orc_world* w, uint32_t idx, uint32_t* bytes) {
     *bytes += 16;
+    if (idx >= w->n_nodes) {
+        arc_node64 z = {0u, 0u, 0u, 0u};
+        return z;
+    }
     return w->nodes[idx];
 }
 

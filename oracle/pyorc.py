@@ -105,6 +105,12 @@ def lib():
         _lib.orc_sharc_resolve.argtypes = [vp, vp, vp]
         _lib.orc_sharc_query.argtypes = [vp, vp, vp, vp, vp, vp]
         _lib.orc_sharc_update.argtypes = [C.POINTER(_World), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+        _lib.orc_sharc_update_mode.argtypes = [C.POINTER(_World), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32]
+        _lib.orc_cmp_albedo.argtypes = [u32, vp]
+        _lib.orc_onebounce.argtypes = [C.POINTER(_World), vp, vp, u32, vp, vp, vp, u32, u32, i32, vp, i32]
+        _lib.orc_train_samples.argtypes = [C.POINTER(_World), vp, vp, C.c_uint64, vp, vp, vp, u32, u32, u32, vp, vp, i32]
+        _lib.orc_gi_points.argtypes = [C.POINTER(_World), vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, i32]
+        _lib.orc_gi_points_from_hits.argtypes = [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp]
         _lib.orc_shadow_vis.argtypes = [C.POINTER(_World), vp, vp, vp, f32, vp]
         _lib.orc_shadow_vis.restype = f32
         _lib.orc_shadow_vis_di.argtypes = [C.POINTER(_World), vp, vp, vp, f32]
@@ -396,7 +402,7 @@ class Sharc:
         lib().orc_sharc_query(_p(self.resolved), *[_p(a) for a in args], _p(out))
         return out
 
-    def update(self, world: World, cam, gdm, gnm, resolved_prev=None):
+    def update(self, world: World, cam, gdm, gnm, resolved_prev=None, mode: int = 0):
         w = int(cam["world_grid_dims"][0][3] & 0xFFFF)
         h = int(cam["world_grid_dims"][0][3] >> 16)
         tile = 16 if (int(cam["quality_flags"][0][3]) & 0xFF) <= 12 else 8
@@ -404,9 +410,69 @@ class Sharc:
         tk, tb, tv = np.zeros(nt, np.uint32), np.zeros(nt, np.uint32), np.zeros(nt, np.uint32)
         tr = np.zeros((nt, 3), np.float32)
         prev = self.resolved if resolved_prev is None else resolved_prev
-        lib().orc_sharc_update(world.cw, _p(cam), _p(gdm), _p(gnm), _p(prev), _p(self.keys), _p(self.accum), _p(tk),
-                               _p(tb), _p(tr), _p(tv))
+        lib().orc_sharc_update_mode(world.cw, _p(cam), _p(gdm), _p(gnm), _p(prev), _p(self.keys), _p(self.accum), _p(tk),
+                                    _p(tb), _p(tr), _p(tv), mode)
         return tk, tb, tr, tv
+
+
+def _frame_size(cam):
+    return int(cam["world_grid_dims"][0][3] & 0xFFFF), int(cam["world_grid_dims"][0][3] >> 16)
+
+
+def cmp_albedo(mat: int) -> np.ndarray:
+    out = np.zeros(3, np.float32)
+    lib().orc_cmp_albedo(int(mat), _p(out))
+    return out
+
+
+def onebounce(world: World, cam, pos, nrm, alb, spp: int, seed: int, idx=None, accumulate_into=None, threads: int = 8):
+    """Mean of spp one-bounce samples at points idx (or every point): (n, 3) float32, as arc_onebounce_dev."""
+    pos = np.ascontiguousarray(pos, np.float32)
+    nrm = np.ascontiguousarray(nrm, np.float32)
+    alb = np.ascontiguousarray(alb, np.float32)
+    idx_a = None if idx is None else np.ascontiguousarray(idx, np.uint32)
+    n = len(pos) if idx_a is None else len(idx_a)
+    out = np.zeros((n, 3), np.float32) if accumulate_into is None else accumulate_into
+    lib().orc_onebounce(world.cw, _p(cam), _p(idx_a), n, _p(pos), _p(nrm), _p(alb), spp, seed & 0xFFFFFFFF,
+                        int(accumulate_into is not None), _p(out), threads)
+    return out
+
+
+def train_samples(world: World, cam, lst, n_valid: int, pos, nrm, nrc_in, seed: int, n_samples: int, steps: int,
+                  threads: int = 8):
+    """The training batch of arc_nrc_train_samples_dev: (inputs (n, 9), targets (n, 3))."""
+    tin = np.zeros((n_samples, 9), np.float32)
+    tt = np.zeros((n_samples, 3), np.float32)
+    lib().orc_train_samples(world.cw, _p(cam), _p(np.ascontiguousarray(lst, np.uint32)), n_valid,
+                            _p(np.ascontiguousarray(pos, np.float32)), _p(np.ascontiguousarray(nrm, np.float32)),
+                            _p(np.ascontiguousarray(nrc_in, np.float32)), seed & 0xFFFFFFFF, n_samples, steps, _p(tin),
+                            _p(tt), threads)
+    return tin, tt
+
+
+def gi_points(world: World, cam, gdm, gnm, threads: int = 8):
+    """GI hit points traced from the G-buffer: (pos, nrm, alb, nrc_in, valid), as arc_gi_points_dev."""
+    w, h = _frame_size(cam)
+    n = w * h
+    pos, nrm, alb = (np.zeros((n, 3), np.float32) for _ in range(3))
+    nin = np.zeros((n, 9), np.float32)
+    valid = np.zeros(n, np.uint32)
+    lib().orc_gi_points(world.cw, _p(cam), w, h, _p(np.ascontiguousarray(gdm)), _p(np.ascontiguousarray(gnm)), _p(pos),
+                        _p(nrm), _p(alb), _p(nin), _p(valid), threads)
+    return pos, nrm, alb, nin, valid
+
+
+def gi_points_from_hits(cam, gdm, gnm, gi_hits):
+    """GI hit points from GI hit records: (pos, nrm, alb, nrc_in, valid), as arc_gi_points_from_hits_dev."""
+    w, h = _frame_size(cam)
+    n = w * h
+    pos, nrm, alb = (np.zeros((n, 3), np.float32) for _ in range(3))
+    nin = np.zeros((n, 9), np.float32)
+    valid = np.zeros(n, np.uint32)
+    lib().orc_gi_points_from_hits(_p(cam), w, h, _p(np.ascontiguousarray(gdm)), _p(np.ascontiguousarray(gnm)),
+                                  _p(np.ascontiguousarray(gi_hits).view(HIT_DTYPE)), _p(pos), _p(nrm), _p(alb), _p(nin),
+                                  _p(valid))
+    return pos, nrm, alb, nin, valid
 
 
 def sincos(x: np.ndarray):

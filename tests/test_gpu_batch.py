@@ -1,5 +1,7 @@
 """Batched multi-view launch (several worlds, mixed resolutions, one persistent launch, CUDA graph):
 every view's G-buffer and hit records equal a single-view trace of the same camera, bit for bit."""
+import os
+
 import numpy as np
 import pytest
 
@@ -68,5 +70,51 @@ def test_batched_autotune_keeps_results(native_lib):
         for bufs, ref in zip(b.buffers, before):
             for x, y in zip(bufs, ref):
                 assert (x.cpu() == y).all()
+    finally:
+        t.close()
+
+
+def test_bench_batch_matches_oracle(orc, native_lib, world_cache):
+    """The benchmark batch itself (256^3, 512^3, 1024^3 and 1024^3-caves worlds, 16 views each, 320x240 up
+    to 2560x1440, seeded poses), replayed from its CUDA graph with both kernel variants: every view's
+    G-buffer words, primary hit records and GI hit records bit-exact against the oracle's trace of the
+    same camera, and the batch's GI-ray count equal to the oracle's number of primary hits."""
+    torch = pytest.importorskip("torch")
+    from arcadia_gb300.batch import BENCH_SCENES, Batch
+
+    threads = os.cpu_count() or 8
+    worlds = [world_cache(s) for s in BENCH_SCENES]
+    t = native_lib.Tracer(0)
+    try:
+        b = Batch(t, BENCH_SCENES, 16, worlds=[(w.roots, w.nodes, w.bricks) for w in worlds])
+        assert {(v["w"], v["h"]) for v in b.views} >= {(1920, 1080), (2560, 1440)}
+        expect = []
+        for i, v in enumerate(b.views):
+            w = worlds[v["slot"]]
+            cam = b.camera(i, 1)
+            gdm, gnm, gaa, hits, _ = orc.primary(w, cam, threads=threads)
+            _, gi, _ = orc.gi_rays(w, cam, gdm, gnm, threads=threads)
+            expect.append((gdm, gnm, gaa, hits, gi))
+        n_hit = sum(int((e[3]["flags"] & 1).sum()) for e in expect)
+        n_gi = torch.zeros(1, dtype=torch.int64, device="cuda")
+        for variant in (0, 1):
+            t.set_launch_config(variant=variant)
+            for bufs in b.buffers:
+                for x in bufs:
+                    x.fill_(-1)
+            b.set_frame(1)
+            b.trace(n_gi.data_ptr(), use_graph=True)
+            t.synchronize()
+            assert int(n_gi.item()) == n_hit, variant
+            for i, (bufs, e) in enumerate(zip(b.buffers, expect)):
+                for got, want, what in zip(bufs, e, ("depth/material", "normal/motion", "albedo/ao", "hits", "GI hits")):
+                    got = got.cpu().numpy().view(np.uint32)
+                    want = np.ascontiguousarray(want).view(np.uint32).reshape(-1)
+                    if not np.array_equal(got, want):
+                        bad = np.nonzero(got != want)[0]
+                        raise AssertionError(f"variant {variant} view {i} ({b.views[i]['w']}x{b.views[i]['h']}, "
+                                             f"world {BENCH_SCENES[b.views[i]['slot']]}) {what}: {len(bad)} words differ, "
+                                             f"first at {bad[:4]}")
+        t.set_launch_config(variant=0)
     finally:
         t.close()

@@ -22,8 +22,9 @@ def _outputs(torch, npx):
 
 @pytest.mark.parametrize("variant", [0, 1])
 def test_noalloc_frame_matches_regular_entry_point(native_lib, variant):
-    """variant 0: the plain kernel, whose GI pass runs over the G-buffer rows here (no GI list to
-    allocate) and over the listed hit pixels in arc_trace_frame_dev; variant 1: the persistent kernel."""
+    """variant 0: the plain kernel, then the frame's GI pass over the G-buffer rows (both entry points
+    run the same row GI pass, so this compares the scratch placement, not two GI strategies);
+    variant 1: the persistent kernel, whose queue head lives in the scratch."""
     torch = pytest.importorskip("torch")
     scene = L.SCENES["c1_256"]
     roots, nodes, bricks, _ = native_lib.build_world(scene)
@@ -64,5 +65,59 @@ def test_noalloc_rejects_oversize_frames(native_lib):
         with pytest.raises(native_lib.ArcError) as e:
             t.trace_frame_noalloc(9000, 8000, 16, 16, 16)  # rejected before any pointer is used
         assert e.value.code == -8 and "allocation-free limit" in str(e.value)
+    finally:
+        t.close()
+
+
+def test_noalloc_surface_list(native_lib):
+    """A world with water and mirror voxels (recoloured by the library's own edit path) and an underwater
+    camera: both need the surface list of the shading branches. Before it is reserved the allocation-free
+    call fails with ARC_E_CAPACITY (it may not allocate the list itself); after arc_reserve_surface_list
+    it matches arc_trace_frame_dev word for word on consecutive calls, whose surface-entry counter lives
+    in the shared static array."""
+    torch = pytest.importorskip("torch")
+    from arcadia_gb300.layout import EDIT_DTYPE, EDIT_RECOLOR
+
+    scene = L.SCENES["c1_256"]
+    roots, nodes, bricks, _ = native_lib.build_world(scene)
+    t = native_lib.Tracer(0)
+    w, h = 640, 360
+    try:
+        t.upload_world(scene.grid, roots, nodes, bricks, native_lib.default_palette(), node_headroom=4096,
+                       brick_headroom=4096)
+        cam = L.default_camera_for(scene, w, h, quality=L.quality_high(), frame_index=3)
+        t.set_camera(cam)
+        hits = t.trace_frame()[3]
+        vox = hits["voxel"][(hits["flags"] & 1).astype(bool)].astype(np.int64)
+        picked = np.unique(vox >> 2, axis=0)
+        rng = np.random.default_rng(43)
+        picked = picked[rng.choice(len(picked), int(0.4 * len(picked)), replace=False)]
+        ops = np.zeros(len(picked), EDIT_DTYPE)
+        ops["kind"] = EDIT_RECOLOR
+        ops["brick"] = picked.astype(np.uint32)
+        ops["material"] = np.where(rng.random(len(picked)) < 0.75, 18, 28)
+        t.apply_edits(ops)
+        t.synchronize()
+        out = _outputs(torch, w * h)
+        with pytest.raises(native_lib.ArcError) as e:
+            t.trace_frame_noalloc(w, h, *[x.data_ptr() for x in out])
+        assert e.value.code == -8 and "surface list" in str(e.value)
+        assert native_lib.lib().arc_reserve_surface_list(t.ctx, w * h) == 0
+        for frame, underwater in ((5, False), (6, False), (7, True), (8, True)):
+            c = L.default_camera_for(scene, w, h, quality=L.quality_high(), frame_index=frame)
+            if underwater:
+                c[0]["point_light_count"][1] = 1
+            t.set_camera(c)
+            ref = _outputs(torch, w * h)
+            t.trace_frame_dev(w, h, *[x.data_ptr() for x in ref])
+            t.synchronize()
+            out = _outputs(torch, w * h)
+            t.trace_frame_noalloc(w, h, *[x.data_ptr() for x in out])
+            t.synchronize()
+            for a, b in zip(out, ref):
+                assert torch.equal(a, b), (frame, underwater)
+            if frame == 6:
+                mats = ref[0].cpu().numpy().view(np.uint32).reshape(-1, 2)[:, 1] & 0xFF
+                assert ((mats == 18) | (mats == 28)).sum() > 1000  # the branches ran on many pixels
     finally:
         t.close()
