@@ -328,6 +328,9 @@ int arc_debug_set(arc_ctx* c, int what, long long value) {
             if (value < 0) return set_err(c, ARC_E_INVALID_ARG, "wait budget must be >= 0 cycles");
             c->tc_wait_budget = value;
             return ARC_OK;
+        case ARC_DEBUG_TC_STALL:
+            c->tc_stall = value != 0;
+            return ARC_OK;
         case ARC_DEBUG_SKIP_POOL_VALIDATION:
             c->skip_pool_validation = value != 0;
             return ARC_OK;

@@ -110,8 +110,10 @@ struct arc_ctx {
     arc::SurfaceEntry* graph_surf_list = nullptr;  // the list the captured graph writes
 
     // fault-injection hooks (arc_debug_set): the cycle budget of each tensor-core mbarrier wait
-    // (0 = the default of about one second) and an upload that skips the pool range validation
+    // (0 = the default of about one second), NRC kernels whose weight barrier is armed but never fed
+    // (so the wait runs out), and an upload that skips the pool range validation
     long long tc_wait_budget = 0;
+    bool tc_stall = false;
     bool skip_pool_validation = false;
 
     arc_launch_config cfg{};

@@ -456,7 +456,9 @@ constexpr long long kTcBudget = 2000000000ll;  // cycles (about one second) per 
 // A kernel whose wait ran out sets bit 31 of the status word, stops issuing work, and before it frees
 // TMEM and returns waits (with the full budget again) for what it still has in flight: the weight copy
 // into shared memory and, if one was committed and not yet seen to complete, the last MMA batch. The
-// `budget` kernel argument is the per-wait budget in cycles (kTcBudget unless a test shrinks it).
+// `budget` kernel argument is the per-wait budget in cycles (kTcBudget unless a test shrinks it). With
+// `stall` set (a test's fault injection) the weight barrier is armed but the copy is never issued, so
+// the first wait can only run out; nothing is then in flight and the drain waits only `budget`.
 
 // sin/cos(2^k pi x), k = 0..11, as 12 packed (sin, cos) FP16 pairs: sincospif at k = 0 and k = 6 and
 // five angle doublings after each (s' = 2 s c, c' = (c - s)(c + s)), which add a few ulp of FP32.
@@ -485,7 +487,8 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
                                                           const float* __restrict__ albedo, uint32_t n,
                                                           float* __restrict__ out, const uint32_t* __restrict__ list,
                                                           const unsigned long long* __restrict__ n_dev,
-                                                          uint32_t* __restrict__ status, long long budget) {
+                                                          uint32_t* __restrict__ status, long long budget,
+                                                          uint32_t stall) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
     uint8_t* sw = smem_raw;
     uint8_t* sa = smem_raw + kUHalves * 2;
@@ -516,7 +519,7 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
     const uint32_t d_hid = tmem, d_out = tmem + 64u, lane_off = (warp * 32u) << 16;
     if (tid == 0) {
         tc::mbar_expect_tx(bar_w, kUHalves * 2);
-        tc::bulk_g2s(sw_u, wu, kUHalves * 2, bar_w);
+        if (!stall) tc::bulk_g2s(sw_u, wu, kUHalves * 2, bar_w);
     }
     bool ok = tc::mbar_wait(bar_w, 0, budget);
     bool fail = __syncthreads_or(!ok);
@@ -635,7 +638,7 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
     if (fail && tid == 0) {
         atomicOr(status, 0x80000000u);
         // the weight copy and an MMA still in flight finish before shared memory and TMEM are released
-        tc::mbar_wait(bar_w, 0, kTcBudget);
+        tc::mbar_wait(bar_w, 0, stall ? budget : kTcBudget);
         if (mma_pending) tc::mbar_wait(bar_m, phase, kTcBudget);
     }
     tc::fence_before();
@@ -676,7 +679,7 @@ __global__ void __launch_bounds__(128, 1) train_tc_kernel(const __half* __restri
                                                           const float* __restrict__ target, uint32_t n, float inv_norm,
                                                           float* __restrict__ grad, float* __restrict__ loss_sum,
                                                           const uint32_t* __restrict__ gate, uint32_t* __restrict__ status,
-                                                          long long budget) {
+                                                          long long budget, uint32_t stall) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
     if (gate && *gate == 0u) return;  // empty frame batch (uniform over the grid)
     const uint32_t tiles = (n + 127u) / 128u;
@@ -703,7 +706,7 @@ __global__ void __launch_bounds__(128, 1) train_tc_kernel(const __half* __restri
     auto d_wl = [&](int l) { return tmem + 256u + 64u * (uint32_t)(l - 2); };  // dW_l^T, l = 2..5
     if (tid == 0) {
         tc::mbar_expect_tx(bar_w, kUHalves * 2);
-        tc::bulk_g2s(s0, wu, kUHalves * 2, bar_w);
+        if (!stall) tc::bulk_g2s(s0, wu, kUHalves * 2, bar_w);
     }
     bool ok = tc::mbar_wait(bar_w, 0, budget);
     bool fail = __syncthreads_or(!ok);
@@ -898,7 +901,7 @@ __global__ void __launch_bounds__(128, 1) train_tc_kernel(const __half* __restri
     } else if (tid == 0) {
         atomicOr(status, 0x80000000u);
         // the weight copy and an MMA still in flight finish before shared memory and TMEM are released
-        tc::mbar_wait(bar_w, 0, kTcBudget);
+        tc::mbar_wait(bar_w, 0, stall ? budget : kTcBudget);
         if (mma_pending) tc::mbar_wait(bar_m, phase, kTcBudget);
     }
     tc::fence_before();
@@ -986,7 +989,7 @@ int launch_infer(arc_ctx* c, const float* inputs, const float* albedo, uint32_t 
         const uint32_t blocks = std::min<uint32_t>((n + 127u) / 128u, (uint32_t)c->n_sm * 2u);
         nrc::infer_tc_kernel<<<blocks, 128, nrc::kTcSmem, c->stream>>>(static_cast<const __half*>(c->d_nrc_wu_ema), inputs,
                                                                         albedo, n, out, list, n_dev, c->d_status,
-                                                                        tc_budget(c));
+                                                                        tc_budget(c), c->tc_stall ? 1u : 0u);
         NRC_CK(cudaGetLastError());
         return ARC_OK;
     }
@@ -1008,7 +1011,7 @@ int launch_grad(arc_ctx* c, const float* inputs, const float* targets, uint32_t 
         const uint32_t blocks = std::min<uint32_t>((n + 127u) / 128u, (uint32_t)c->n_sm);
         nrc::train_tc_kernel<<<blocks, 128, nrc::kTtSmem, c->stream>>>(static_cast<const __half*>(c->d_nrc_wu), inputs, targets, n,
                                                                          1.0f / (float)n, c->d_nrc_grad, loss, gate,
-                                                                         c->d_status, tc_budget(c));
+                                                                         c->d_status, tc_budget(c), c->tc_stall ? 1u : 0u);
         NRC_CK(cudaGetLastError());
         return ARC_OK;
     }

@@ -513,7 +513,18 @@ def run_ours(args):
         v, frames, dt, world, cam = cpu_leg(SCENE, args.cpu_seconds, threads, reference_query=True, frame=args.warmup)
         cpu = {"value": round(v, 3), "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{frames} full frame(s) ({WIDTH}x{HEIGHT} primary + GI) in {dt:.1f} s through the C "
-                         "restatement of WorldMap::raycast_meters -> raycast_chunk_tree"}
+                         "restatement of WorldMap::raycast_meters -> raycast_chunk_tree",
+               "build": "gcc -O3 -ffp-contract=off -fopenmp (portable flags: the same build on x86-64 and aarch64)"}
+        # the same query on one core, and the line-for-line WGSL transcription on all cores and on one
+        v1, f1, d1 = cpu_leg(SCENE, args.cpu_seconds / 2, 1, reference_query=True, frame=args.warmup)[:3]
+        cpu["single_core"] = {"value": round(v1, 3), "unit": UNIT, "cores": 1, "sample": f"{f1} frame(s) in {d1:.1f} s"}
+        vw, fw, dw = cpu_leg(SCENE, args.cpu_seconds / 2, threads, reference_query=False, frame=args.warmup)[:3]
+        vw1, fw1, dw1 = cpu_leg(SCENE, args.cpu_seconds / 2, 1, reference_query=False, frame=args.warmup)[:3]
+        cpu["wgsl_transcription"] = {
+            "value": round(vw, 3), "unit": UNIT, "cores": threads, "sample": f"{fw} frame(s) in {dw:.1f} s",
+            "single_core": round(vw1, 3),
+            "what": "the oracle's line-for-line C transcription of trace_world_64tree_from (traversal64.wgsl:226-556) "
+                    "and the primary / GI passes, on the same frames"}
         bpp = bytes_per_pixel(world, cam, threads)
     peak, peak_kind = _peaks()
     avg_ms = total_ms / args.steps if ws == 1 else statistics.mean(ms)
@@ -548,6 +559,21 @@ def run_ours(args):
         "c5": c5,
         "clocks": clk,
     }
+    if nrc is not None:
+        # the cache comparison at its operating point in both modes, last so that a tail of the line keeps it
+        ov, se = nrc, nrc["serial"]
+        line["c4"] = {
+            "workload": "NRC vs SHARC at the GI hits of 1920x1080 frames of the 1024^3 caves world, 300 static frames",
+            "operating_point": {"train_samples": 32768, "adam_steps_per_frame": 4},
+            "overlapped": {"nrc_ms": ov["nrc_ms_per_frame"], "sharc_ms": ov["sharc_ms_per_frame"],
+                           "rel_mse_nrc": round(ov["rel_mse_nrc"], 4), "rel_mse_sharc": round(ov["rel_mse_sharc"], 4)},
+            "serial": {"nrc_ms": se["nrc_ms_per_frame"], "sharc_ms": se["sharc_ms_per_frame"],
+                       "rel_mse_nrc": se["rel_mse_nrc"], "rel_mse_sharc": se["rel_mse_sharc"]},
+            "nrc_faster_and_better_in_both": bool(ov["nrc_ms_per_frame"] < ov["sharc_ms_per_frame"]
+                                                  and se["nrc_ms_per_frame"] < se["sharc_ms_per_frame"]
+                                                  and ov["rel_mse_nrc"] <= ov["rel_mse_sharc"]
+                                                  and se["rel_mse_nrc"] <= se["rel_mse_sharc"]),
+            "reference_spp": 4096}
     print(json.dumps(line), flush=True)
 
 

@@ -102,6 +102,9 @@ int arc_get_stats(const arc_ctx* ctx, arc_stats* out);
  *                                   frees its TMEM and returns, and the call that reads the status back
  *                                   (arc_synchronize or a host-buffer entry point) fails with
  *                                   ARC_E_DEVICE_CHECK ("tensor-core pipeline wait timed out").
+ *   ARC_DEBUG_TC_STALL              value 1 = the NRC tensor-core kernels arm the barrier of their weight
+ *                                   copy but never issue the copy, so that wait can only run out (after
+ *                                   the budget above); 0 restores normal operation.
  *   ARC_DEBUG_SKIP_POOL_VALIDATION  value 1 = arc_upload_world uploads the pools without its range
  *                                   validation, so a corrupt pool reaches the kernels; their range
  *                                   checks read an out-of-range node as empty and an out-of-range
@@ -109,6 +112,7 @@ int arc_get_stats(const arc_ctx* ctx, arc_stats* out);
  *                                   ARC_E_DEVICE_CHECK. 0 restores the validation. */
 #define ARC_DEBUG_TC_WAIT_BUDGET 1
 #define ARC_DEBUG_SKIP_POOL_VALIDATION 2
+#define ARC_DEBUG_TC_STALL 3
 int arc_debug_set(arc_ctx* ctx, int what, long long value);
 
 /* Pools as WorldMap packs them. The pools are validated (every child pointer, brick index and root

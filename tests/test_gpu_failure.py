@@ -2,10 +2,11 @@
 
 The reference renderer has no device-side checks (it handles only swapchain loss,
 crates/arcadia-render/src/renderer.rs:368-378); this library's are exercised here:
-  * a tensor-core pipeline wait that runs out of its cycle budget (the budget shrunk through
-    arc_debug_set, so the wait on the kernels' own weight copy gives up): the kernel sets status bit
-    31, waits for what it has in flight, frees TMEM and returns; the call fails with
-    ARC_E_DEVICE_CHECK and the next call on the same context works and gives the earlier results;
+  * a tensor-core pipeline wait that runs out of its cycle budget: through arc_debug_set the NRC
+    kernels arm the barrier of their weight copy without issuing the copy (a flag that nothing sets)
+    and the budget is shrunk to 0.1 ms; the kernel sets status bit 31, frees TMEM and returns, the
+    call fails with ARC_E_DEVICE_CHECK, and the next call on the same context works and gives the
+    earlier results;
   * a corrupt pool that reaches the kernels (upload validation switched off through arc_debug_set):
     the range checks read the bad nodes as empty and the bad bricks as air, exactly as the oracle's
     ReadZeroSkipWrite reads, and the status readback reports ARC_E_DEVICE_CHECK;
@@ -24,6 +25,7 @@ pytestmark = pytest.mark.gpu
 THREADS = os.cpu_count() or 8
 ARC_DEBUG_TC_WAIT_BUDGET = 1
 ARC_DEBUG_SKIP_POOL_VALIDATION = 2
+ARC_DEBUG_TC_STALL = 3
 ARC_E_DEVICE_CHECK = -6
 
 
@@ -50,21 +52,25 @@ def test_tc_wait_timeout_is_reported_and_context_recovers(native_lib, world_cach
         base = np.zeros((n, 3), np.float32)
         assert lib.arc_nrc_query(t.ctx, _fp(x), None, n, _fp(base)) == 0, _err(t)
         assert np.isfinite(base).all() and np.abs(base).max() > 0
-        # every wait gives up after one cycle: the weight copy into shared memory takes longer
-        assert lib.arc_debug_set(t.ctx, ARC_DEBUG_TC_WAIT_BUDGET, 1) == 0
+        # the weight barrier is armed but never fed; its wait gives up after 200,000 cycles
+        assert lib.arc_debug_set(t.ctx, ARC_DEBUG_TC_WAIT_BUDGET, 200000) == 0
+        assert lib.arc_debug_set(t.ctx, ARC_DEBUG_TC_STALL, 1) == 0
         out = np.zeros((n, 3), np.float32)
         assert lib.arc_nrc_query(t.ctx, _fp(x), None, n, _fp(out)) == ARC_E_DEVICE_CHECK
         assert "tensor-core pipeline wait timed out" in _err(t)
-        # the budget restored, the same context answers again with the same results
+        # the hook switched off and the budget restored, the same context answers again with the same results
+        assert lib.arc_debug_set(t.ctx, ARC_DEBUG_TC_STALL, 0) == 0
         assert lib.arc_debug_set(t.ctx, ARC_DEBUG_TC_WAIT_BUDGET, 0) == 0
         again = np.zeros((n, 3), np.float32)
         assert lib.arc_nrc_query(t.ctx, _fp(x), None, n, _fp(again)) == 0, _err(t)
         np.testing.assert_array_equal(again, base)
-        # the training kernel's waits run out the same way
-        assert lib.arc_debug_set(t.ctx, ARC_DEBUG_TC_WAIT_BUDGET, 1) == 0
+        # the training kernel's wait runs out the same way
+        assert lib.arc_debug_set(t.ctx, ARC_DEBUG_TC_WAIT_BUDGET, 200000) == 0
+        assert lib.arc_debug_set(t.ctx, ARC_DEBUG_TC_STALL, 1) == 0
         loss = ctypes.c_float(0.0)
         assert lib.arc_nrc_train_step(t.ctx, _fp(x), _fp(tgt), n, ctypes.c_float(1e-3), ctypes.byref(loss)) == ARC_E_DEVICE_CHECK
         assert "tensor-core pipeline wait timed out" in _err(t)
+        assert lib.arc_debug_set(t.ctx, ARC_DEBUG_TC_STALL, 0) == 0
         assert lib.arc_debug_set(t.ctx, ARC_DEBUG_TC_WAIT_BUDGET, 0) == 0
         assert lib.arc_nrc_init(t.ctx, 5) == 0
         assert lib.arc_nrc_query(t.ctx, _fp(x), None, n, _fp(again)) == 0, _err(t)
