@@ -49,7 +49,7 @@ def test_gi_points_match_oracle(orc, frame):
     gvalid = _np(cc.valid).view(np.uint32)
     np.testing.assert_array_equal(gvalid, valid)
     m = valid.astype(bool)
-    assert m.sum() > 0.2 * W * H
+    assert m.sum() > 0.05 * W * H
     for got, want in ((cc.pos, pos), (cc.nrm, nrm), (cc.alb, alb), (cc.nin, nin)):
         np.testing.assert_array_equal(_np(got)[m].view(np.uint32), want[m].view(np.uint32))
     n = int(cc.n_valid.item())
@@ -79,7 +79,7 @@ def test_gi_points_from_hits_match_oracle(orc, native_lib, frame):
     opos, onrm, oalb, onin, ovalid = orc.gi_points_from_hits(cam, gdm, gnm, ogi)
     np.testing.assert_array_equal(_np(valid).view(np.uint32), ovalid)
     m = ovalid.astype(bool)
-    assert m.sum() > 0.2 * n and int(n_valid.item()) == int(m.sum())
+    assert m.sum() > 0.05 * n and int(n_valid.item()) == int(m.sum())
     for got, want in ((pos, opos), (nrm, onrm), (alb, oalb), (nin, onin)):
         np.testing.assert_array_equal(_np(got)[m].view(np.uint32), want[m].view(np.uint32))
 
