@@ -349,6 +349,8 @@ int arc_set_launch_config(arc_ctx* c, const arc_launch_config* cfg) {
     if (cfg->refill_threshold < 1u || cfg->refill_threshold > 32u) return set_err(c, ARC_E_INVALID_ARG, "refill_threshold in [1, 32]");
     if (cfg->block_threads > 256u) return set_err(c, ARC_E_INVALID_ARG, "block_threads <= 256");
     if (cfg->reg_blocks < 1u || cfg->reg_blocks > 4u) return set_err(c, ARC_E_INVALID_ARG, "reg_blocks in [1, 4]");
+    if (cfg->order > 1u) return set_err(c, ARC_E_INVALID_ARG, "order must be 0 (row-major) or 1 (Morton)");
+    if (cfg->features & ~(ARC_FEAT_WARP_FETCH | ARC_FEAT_NODE_VISIT)) return set_err(c, ARC_E_INVALID_ARG, "unknown feature bits");
     c->cfg = *cfg;
     return ARC_OK;
 }
@@ -545,6 +547,7 @@ static arc::FrameParams frame_params(arc_ctx* c, uint32_t width, uint32_t height
     P.tiles_x = (width + c->cfg.tile_w - 1u) / c->cfg.tile_w;
     P.refill_threshold = c->cfg.refill_threshold;
     P.gi_mode = arc::kGiRows;  // honoured by the plain kernel; the persistent kernel fuses the GI ray
+    P.order = c->cfg.order;
     frame_rows(c, P, 0u, height);
     return P;
 }
@@ -958,15 +961,14 @@ int arc_autotune_views_dev(arc_ctx* c, const arc_view_desc* views, uint32_t n_vi
                            arc_launch_config* best_out, float* best_ms) {
     if (!c) return ARC_E_INVALID_ARG;
     if (frames == 0) frames = 3;
+    // the persistent kernel has lost every measured batch to the plain kernels + GI pass, so it keeps
+    // only its best-measured settings in the space
     std::vector<arc_launch_config> cands;
-    for (uint32_t rb : {2u, 3u, 4u})
-        for (uint32_t thr : {8u, 16u, 24u, 28u})
-            for (uint32_t bt : {128u, 256u}) cands.push_back(arc_launch_config{1u, bt, 0u, 8u, 4u, thr, rb});
-    cands.push_back(arc_launch_config{1u, 256u, 0u, 4u, 8u, 24u, 4u});
-    cands.push_back(arc_launch_config{1u, 256u, 0u, 16u, 2u, 24u, 4u});
+    for (uint32_t rb : {3u, 4u})
+        for (uint32_t thr : {16u, 24u}) cands.push_back(arc_launch_config{1u, 256u, 0u, 8u, 4u, thr, rb, 0u, 0u});
     for (uint32_t rb : {2u, 3u, 4u})
         for (uint32_t bt : {128u, 256u})
-            for (uint32_t tw : {8u, 4u, 16u}) cands.push_back(arc_launch_config{0u, bt, 0u, tw, 32u / tw, 8u, rb});
+            for (uint32_t tw : {8u, 4u, 16u}) cands.push_back(arc_launch_config{0u, bt, 0u, tw, 32u / tw, 8u, rb, 0u, 0u});
     const arc_launch_config saved = c->cfg;
     float best = 1e30f;
     arc_launch_config best_cfg = saved;
@@ -1006,14 +1008,19 @@ int arc_autotune_frame_dev(arc_ctx* c, uint32_t width, uint32_t height, uint32_t
     if ((rc = check_dims(c, width, height))) return rc;
     if (!gdm || !gnm || !gaa) return set_err(c, ARC_E_INVALID_ARG, "null G-buffer");
     if (frames == 0) frames = 3;
+    // candidates: the plain kernel + GI pass over register budget x block size x block order (row-major
+    // or Morton super-tiles) x traversal loop (descent loop or one node per iteration, budgets 2 and 3),
+    // and the persistent queue kernel at its best-measured settings
     std::vector<arc_launch_config> cands;
-    const uint32_t tiles[3][2] = {{8, 4}, {4, 8}, {16, 2}};
+    for (uint32_t rb : {3u, 4u})
+        for (uint32_t thr : {16u, 24u}) cands.push_back(arc_launch_config{1u, 256u, 0u, 8u, 4u, thr, rb, 0u, 0u});
     for (uint32_t rb : {2u, 3u, 4u})
-        for (uint32_t thr : {8u, 16u, 24u, 28u})
-            for (uint32_t bt : {128u, 256u}) cands.push_back(arc_launch_config{1u, bt, 0u, 8u, 4u, thr, rb});
-    for (const auto& t : tiles) cands.push_back(arc_launch_config{1u, 256u, 0u, t[0], t[1], 24u, 4u});
-    for (uint32_t rb : {2u, 3u, 4u})
-        for (uint32_t bt : {64u, 128u, 256u}) cands.push_back(arc_launch_config{0u, bt, 0u, 8u, 4u, 8u, rb});
+        for (uint32_t bt : {64u, 128u, 256u})
+            for (uint32_t order : {0u, 1u})
+                for (uint32_t feat : {0u, ARC_FEAT_NODE_VISIT}) {
+                    if (feat && rb == 4u) continue;
+                    cands.push_back(arc_launch_config{0u, bt, 0u, 8u, 4u, 8u, rb, order, feat});
+                }
     const arc_launch_config saved = c->cfg;
     float best = 1e30f;
     arc_launch_config best_cfg = saved;

@@ -82,6 +82,7 @@ struct arc_ctx {
     int nrc_infer_path = 1;           // 1 = tcgen05 inference, 0 = mma.sync inference
     int nrc_train_path = 1;           // 1 = tcgen05 training, 0 = mma.sync training
     float nrc_ema_decay = 0.99f;
+    uint32_t nrc_ema_warmup = 10;     // EMA warm-up: decay min(nrc_ema_decay, (1 + k) / (warmup + k)); 0 = off
     float* d_nrc_loss = nullptr;
     uint32_t nrc_step = 0;
     // in-place edits: device counters [next node, next brick, bricks rewritten, overflow] and staging

@@ -145,11 +145,36 @@ __device__ __forceinline__ void pixel_of(const FrameParams& P, uint32_t q, uint3
 // Frame kernels
 // ------------------------------------------------------------------------------------------------
 
-template <int MINB, bool SURF, bool FUSED>
+// Block coordinates of block `id` of a 1D launch over an nbx x nby grid of pixel blocks: row-major
+// (order 0), or Morton (Z) order inside super-tiles of 8 x 8 blocks that follow each other row-major
+// (order 1), so the blocks resident on the GPU at a time cover a compact part of the screen. Returns
+// false for the padding blocks of partial super-tiles.
+__device__ __forceinline__ bool block_coords(uint32_t id, uint32_t nbx, uint32_t nby, uint32_t order, uint32_t* bx,
+                                             uint32_t* by) {
+    if (order == 0u) {
+        *bx = id % nbx;
+        *by = id / nbx;
+        return *by < nby;
+    }
+    const uint32_t nsx = (nbx + 7u) >> 3, st = id >> 6, m = id & 63u;
+    *bx = (st % nsx) * 8u + ((m & 1u) | ((m >> 1) & 2u) | ((m >> 2) & 4u));
+    *by = (st / nsx) * 8u + (((m >> 1) & 1u) | ((m >> 2) & 2u) | ((m >> 3) & 4u));
+    return *bx < nbx && *by < nby;
+}
+
+__host__ __device__ __forceinline__ uint32_t blocks_for(uint32_t nbx, uint32_t nby, uint32_t order) {
+    return order == 0u ? nbx * nby : ((nbx + 7u) >> 3) * ((nby + 7u) >> 3) * 64u;
+}
+
+template <int MINB, bool SURF, bool FUSED, int FEAT = 0>
 __global__ void __launch_bounds__(256, MINB) frame_plain_kernel(const FrameParams P,
                                                                    const __grid_constant__ arc_camera_uniforms cam) {
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t y = P.row0 + blockIdx.y * blockDim.y + threadIdx.y;
+    const uint32_t nbx = (P.width + blockDim.x - 1u) / blockDim.x;
+    const uint32_t nby = (P.row_end - P.row0 + blockDim.y - 1u) / blockDim.y;
+    uint32_t bx, by;
+    if (!block_coords(blockIdx.x, nbx, nby, P.order, &bx, &by)) return;
+    const uint32_t x = bx * blockDim.x + threadIdx.x;
+    const uint32_t y = P.row0 + by * blockDim.y + threadIdx.y;
     if (x >= P.width || y >= P.row_end) return;
     const World& w = P.world;
     const f3 eye{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]};
@@ -166,7 +191,7 @@ __global__ void __launch_bounds__(256, MINB) frame_plain_kernel(const FrameParam
     const float gmax = cam.ray_distances[2];
     StepResult r;
     for (;;) {
-        r = active ? ray_advance(s, w, cam, h) : kMiss;
+        r = active ? ray_next<FEAT>(s, w, cam, h) : kMiss;
         if (r == kContinue) continue;
         if (gi_phase) break;
         if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
@@ -281,14 +306,16 @@ __global__ void __launch_bounds__(256, MINB) frame_persistent_kernel(const Frame
 // pixels, sorts them by direction octant in shared memory (a counting sort; the rays without a GI ray
 // drop out) and traces them from the sorted slots, so a warp's rays step in the same directions.
 // Every ray is computed as before, only by another thread of the block.
-template <int MINB>
+template <int MINB, int FEAT = 0>
 __global__ void __launch_bounds__(128, MINB) gi_rows_kernel(const FrameParams P, const __grid_constant__ arc_camera_uniforms cam) {
     __shared__ float s_ray[6][128];
     __shared__ uint32_t s_k[128];
     __shared__ uint32_t s_cnt[9], s_base[10];
     const uint32_t t = threadIdx.x;
-    const uint32_t x = blockIdx.x * 16u + (t & 15u);
-    const uint32_t y = P.row0 + blockIdx.y * 8u + (t >> 4);
+    uint32_t bx, by;
+    if (!block_coords(blockIdx.x, (P.width + 15u) / 16u, (P.row_end - P.row0 + 7u) / 8u, P.order, &bx, &by)) return;
+    const uint32_t x = bx * 16u + (t & 15u);
+    const uint32_t y = P.row0 + by * 8u + (t >> 4);
     if (t < 9u) s_cnt[t] = 0u;
     __syncthreads();
     uint32_t key = 8u;
@@ -333,7 +360,7 @@ __global__ void __launch_bounds__(128, MINB) gi_rows_kernel(const FrameParams P,
     StepResult g = kMiss;
     if (ray_begin(s, cam, o, d, 0.0f, gmax, 2u, true)) {
         do {
-            g = ray_advance(s, P.world, cam, h);
+            g = ray_next<FEAT>(s, P.world, cam, h);
         } while (g == kContinue);
     }
     if (g != kHit) hit_init_miss(h, o, d, gmax);
@@ -735,11 +762,18 @@ cudaError_t launch_frame_t(const FrameParams& P, const arc_camera_uniforms& cam,
     if (cfg.variant == 0u) {
         const uint32_t bw = 8u, bh = cfg.block_threads / 8u;
         dim3 block(bw, bh);
-        dim3 grid((P.width + bw - 1u) / bw, (P.row_end - P.row0 + bh - 1u) / bh);
+        const dim3 grid(blocks_for((P.width + bw - 1u) / bw, (P.row_end - P.row0 + bh - 1u) / bh, P.order));
         const bool fused = P.do_gi && P.gi_mode == kGiFused;
+        // the traversal variants are built for the primary-only instance and the GI pass (no surface list)
+        const int feat = (int)(cfg.features & (uint32_t)(kFeatWarpFetch | kFeatNodeVisit));
+        const bool variant_kernels = feat != 0 && !P.surf && !fused && (MINB == 2 || MINB == 3);
         if (P.surf) {
             if (fused) frame_plain_kernel<MINB, true, true><<<grid, block, 0, st>>>(P, cam);
             else frame_plain_kernel<MINB, true, false><<<grid, block, 0, st>>>(P, cam);
+        } else if (variant_kernels) {
+            if (feat == kFeatWarpFetch) frame_plain_kernel<MINB, false, false, kFeatWarpFetch><<<grid, block, 0, st>>>(P, cam);
+            else if (feat == kFeatNodeVisit) frame_plain_kernel<MINB, false, false, kFeatNodeVisit><<<grid, block, 0, st>>>(P, cam);
+            else frame_plain_kernel<MINB, false, false, kFeatWarpFetch | kFeatNodeVisit><<<grid, block, 0, st>>>(P, cam);
         } else {
             if (fused) frame_plain_kernel<MINB, false, true><<<grid, block, 0, st>>>(P, cam);
             else frame_plain_kernel<MINB, false, false><<<grid, block, 0, st>>>(P, cam);
@@ -747,8 +781,14 @@ cudaError_t launch_frame_t(const FrameParams& P, const arc_camera_uniforms& cam,
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess || !P.do_gi) return e;
         if (P.gi_mode == kGiRows) {
-            dim3 g2((P.width + 15u) / 16u, (P.row_end - P.row0 + 7u) / 8u);
-            gi_rows_kernel<MINB><<<g2, 128, 0, st>>>(P, cam);
+            const dim3 g2(blocks_for((P.width + 15u) / 16u, (P.row_end - P.row0 + 7u) / 8u, P.order));
+            if (variant_kernels || (feat != 0 && P.surf && (MINB == 2 || MINB == 3))) {
+                if (feat == kFeatWarpFetch) gi_rows_kernel<MINB, kFeatWarpFetch><<<g2, 128, 0, st>>>(P, cam);
+                else if (feat == kFeatNodeVisit) gi_rows_kernel<MINB, kFeatNodeVisit><<<g2, 128, 0, st>>>(P, cam);
+                else gi_rows_kernel<MINB, kFeatWarpFetch | kFeatNodeVisit><<<g2, 128, 0, st>>>(P, cam);
+            } else {
+                gi_rows_kernel<MINB><<<g2, 128, 0, st>>>(P, cam);
+            }
         }
         return cudaGetLastError();
     }
@@ -892,7 +932,7 @@ cudaError_t launch_secondary(const FrameParams& P, const arc_camera_uniforms& ca
                              cudaStream_t st) {
     // the frame's GI pass over the G-buffer's rows (compacted, octant-sorted blocks), at the register
     // budget of the launch configuration as in launch_frame
-    dim3 grid((P.width + 15u) / 16u, (P.row_end - P.row0 + 7u) / 8u);
+    const dim3 grid(blocks_for((P.width + 15u) / 16u, (P.row_end - P.row0 + 7u) / 8u, P.order));
     switch (cfg.reg_blocks) {
         case 2: gi_rows_kernel<2><<<grid, 128, 0, st>>>(P, cam); break;
         case 3: gi_rows_kernel<3><<<grid, 128, 0, st>>>(P, cam); break;

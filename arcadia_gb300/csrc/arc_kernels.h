@@ -65,6 +65,7 @@ struct FrameParams {
     uint32_t* surf_count;
     uint32_t surf_cap;
     uint32_t gi_mode;  // GiMode of the plain kernel (the persistent kernel always fuses)
+    uint32_t order;    // block order of the plain kernel and the GI pass: 0 row-major, 1 Morton (block_coords)
 };
 
 // One view of a batched launch: camera block, world slot, resolution, queue offset, outputs.

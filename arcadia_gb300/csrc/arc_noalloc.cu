@@ -161,6 +161,7 @@ extern "C" int arc_trace_frame_noalloc(arc_ctx* c, uint32_t width, uint32_t heig
     P.row0 = 0u;
     P.row_end = height;
     P.gi_mode = arc::kGiRows;
+    P.order = c->cfg.order;
     if (c->surface_mats[0] || (c->cam.point_light_count[1] & 0xFFFFu) != 0u) {
         if (c->surf_cap < (size_t)width * height)
             return fail(c, ARC_E_CAPACITY, "surface list not reserved for this frame size (arc_reserve_surface_list)");

@@ -91,7 +91,17 @@ struct RayState {
     uint32_t cached_shift;
     uint32_t step;
     uint32_t mode;            // lod_bias | ignore_water << 2
+    // node-visit loop (ray_visit) only: the node under evaluation, its level, the LOD floor of the
+    // current voxel, and whether the head of the outer loop still has to run at this voxel
+    uint4 node;
+    uint32_t nshift, min_shift, have_node;
 };
+
+// Traversal variants (the features field of arc_launch_config); every variant makes the same DDA
+// decisions in the same order, so results are identical bit for bit.
+constexpr int kFeatWarpFetch = 1;   // lanes that descend into the same node fetch it once per warp
+constexpr int kFeatNodeVisit = 2;   // one node evaluation per loop iteration instead of a descent loop
+constexpr int kFeatTopTable = 4;    // chunk roots and their level-1 children from a dense table in shared memory
 
 __device__ __forceinline__ float noi_x(const RayState& s) { return -s.vo.x * s.inv.x; }
 __device__ __forceinline__ float noi_y(const RayState& s) { return -s.vo.y * s.inv.y; }
@@ -166,7 +176,34 @@ __device__ __forceinline__ bool ray_begin(RayState& s, const arc_camera_uniforms
     s.cached_shift = 6u;
     s.step = 0u;
     s.mode = lod_bias | (ignore_water ? 4u : 0u);
+    s.have_node = 0u;
     return true;
+}
+
+__device__ __forceinline__ uint32_t lane_id() {
+    uint32_t l;
+    asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
+    return l;
+}
+
+// A child node fetch. With kFeatWarpFetch the lanes of a warp that need the same node index elect one
+// lane to load it and receive it by shuffle (one request per distinct node instead of one per lane).
+template <int FEAT>
+__device__ __forceinline__ uint4 fetch_node(const World& w, uint32_t idx) {
+    if constexpr ((FEAT & kFeatWarpFetch) != 0) {
+        const uint32_t act = __activemask();
+        const uint32_t peers = __match_any_sync(act, idx);
+        const int leader = __ffs(peers) - 1;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if ((int)lane_id() == leader) v = load_node(w, idx);
+        v.x = __shfl_sync(act, v.x, leader);
+        v.y = __shfl_sync(act, v.y, leader);
+        v.z = __shfl_sync(act, v.z, leader);
+        v.w = __shfl_sync(act, v.w, leader);
+        return v;
+    } else {
+        return load_node(w, idx);
+    }
 }
 
 // step_dda_box (traversal64.wgsl:152-179) over the box [bmin, bmin + span)^3.
@@ -281,6 +318,7 @@ __device__ __forceinline__ void resolve_hit(const RayState& s, const arc_camera_
 // cell (451-465) or the air leaf cell (525-537). Here the branches only choose the box's span and one
 // convergent step_box runs after them, so lanes that took different branches step together instead
 // of executing five inlined copies one after another. Decisions and their order are unchanged.
+template <int FEAT = 0>
 __device__ __forceinline__ StepResult ray_advance(RayState& s, const World& w, const arc_camera_uniforms& cam,
                                                   HitInfo& h) {
     if (s.step >= max_steps_of(cam, s.mode)) return kMiss;
@@ -359,7 +397,7 @@ __device__ __forceinline__ StepResult ray_advance(RayState& s, const World& w, c
                 }
                 break;  // air leaf cell
             }
-            node = load_node(w, child_index(node, b));
+            node = fetch_node<FEAT>(w, child_index(node, b));
             shift -= 2u;
             s.cached_shift = shift;
             if (shift == 4u) s.l1 = node;
@@ -370,6 +408,118 @@ __device__ __forceinline__ StepResult ray_advance(RayState& s, const World& w, c
     step_box(s, s.vx & ~(span - 1u), s.vy & ~(span - 1u), s.vz & ~(span - 1u), span);
     s.step++;
     return kContinue;
+}
+
+// ray_advance with the descent loop unrolled across calls (kFeatNodeVisit): every call evaluates one
+// node. A call at a new voxel first runs the head of the reference's outer loop (budget and bounds
+// checks, chunk MTF cache, LOD floor, ancestor restart: traversal64.wgsl:302-387); a call that
+// descends loads the child and returns, and the next call evaluates it; a call that decides the cell
+// steps. Lanes of a warp then spend one short, mostly common iteration per node instead of waiting
+// in the descent loop for the deepest lane. The state changes, their order and the results are
+// those of ray_advance.
+template <int FEAT = 0>
+__device__ __forceinline__ StepResult ray_visit(RayState& s, const World& w, const arc_camera_uniforms& cam,
+                                                HitInfo& h) {
+    uint32_t span = 256u;  // empty chunk: leave the whole chunk
+    bool eval = true;
+    if (!s.have_node) {
+        if (s.step >= max_steps_of(cam, s.mode)) return kMiss;
+        if (s.t >= s.t_limit) return kMiss;
+        const uint32_t gx = cam.world_grid_dims[0], gy = cam.world_grid_dims[1], gz = cam.world_grid_dims[2];
+        if (s.vx >= (gx << 8) || s.vy >= (gy << 8) || s.vz >= (gz << 8)) return kMiss;
+        const uint32_t diff = s.diff;
+        uint32_t root_idx = s.mtf_root0;
+        if (diff >= 256u) {
+            const uint32_t cxk = s.vx >> 8, cyk = s.vy >> 8, czk = s.vz >> 8;
+            const uint32_t c = cxk | (cyk << 10) | (czk << 20);
+            s.cached_shift = 6u;
+            if (c == s.mtf_c1) root_idx = s.mtf_root1;
+            else root_idx = load_root(w, cxk + cyk * gx + czk * gx * gy);
+            s.mtf_c1 = s.mtf_c0;
+            s.mtf_root1 = s.mtf_root0;
+            s.mtf_c0 = c;
+            s.mtf_root0 = root_idx;
+        }
+        if (root_idx == ARC_EMPTY_CHUNK) {
+            eval = false;
+        } else {
+            const uint32_t lod_bias = s.mode & 3u;
+            uint32_t min_shift = 0u;
+            if (lod_bias == 0u) {
+                if (s.t > cam.lod_settings[0] * ARC_VOXELS_PER_METER || s.step > cam.quality_flags[0]) min_shift = 2u;
+            } else if (lod_bias == 1u) {
+                const float sec_t = cam.lod_settings[1] * ARC_VOXELS_PER_METER;
+                if (s.t > sec_t * 2.2857f || s.step > cam.quality_flags[1]) min_shift = 4u;
+                else if (s.t > sec_t) min_shift = 2u;
+            } else {
+                if (s.t > cam.lod_settings[2] * ARC_VOXELS_PER_METER || s.step > ((cam.quality_flags[3] >> 16) & 0xFFu))
+                    min_shift = 2u;
+            }
+            s.min_shift = min_shift;
+            if (diff < 4u && min_shift == 0u && s.cached_shift == 0u) {
+                s.node = s.l3;
+                s.nshift = 0u;
+            } else if (diff < 16u && min_shift <= 2u && s.cached_shift <= 2u) {
+                s.node = s.l2;
+                s.nshift = 2u;
+            } else if (diff < 64u && min_shift <= 4u && s.cached_shift <= 4u) {
+                s.node = s.l1;
+                s.nshift = 4u;
+            } else {
+                s.node = load_node(w, root_idx);
+                s.nshift = 6u;
+            }
+            s.cached_shift = s.nshift;
+            s.have_node = 1u;
+        }
+    }
+    if (eval) {
+        const uint32_t shift = s.nshift;
+        const uint4 node = s.node;
+        const bool ignore_water = (s.mode & 4u) != 0u;
+        const uint32_t lx = s.vx & 255u, ly = s.vy & 255u, lz = s.vz & 255u;
+        const uint32_t b = (((lz >> shift) & 3u) << 4) | (((ly >> shift) & 3u) << 2) | ((lx >> shift) & 3u);
+        if (ignore_water && (node.z & ARC_IS_UNIFORM_FLAG) != 0u && ((node.w >> 24) & 0xFFu) == ARC_MAT_WATER_CRYSTAL) {
+            span = 4u << shift;  // uniform water node
+        } else {
+            span = 1u << shift;
+            if (has_child(node.x, node.y, b)) {
+                const bool is_leaf = (node.z & ARC_IS_LEAF_FLAG) != 0u;
+                if (is_leaf || shift <= s.min_shift) {
+                    uint32_t mat = (node.w >> 24) & 0xFFu;
+                    if (is_leaf && (node.z & ARC_IS_UNIFORM_FLAG) == 0u)
+                        mat = load_brick_mat(w, node.z & ARC_PTR_INDEX_MASK, b);
+                    if (!(ignore_water && mat == ARC_MAT_WATER_CRYSTAL) && mat != ARC_MAT_AIR) {
+                        resolve_hit(s, cam, node, mat, s.vx & ~(span - 1u), s.vy & ~(span - 1u), s.vz & ~(span - 1u),
+                                    span, shift, b, h);
+                        return kHit;
+                    }
+                    // water cell or air leaf cell: step
+                } else {
+                    const uint4 child = fetch_node<FEAT>(w, child_index(node, b));
+                    const uint32_t cs = shift - 2u;
+                    s.node = child;
+                    s.nshift = cs;
+                    s.cached_shift = cs;
+                    if (cs == 4u) s.l1 = child;
+                    else if (cs == 2u) s.l2 = child;
+                    else if (cs == 0u) s.l3 = child;
+                    return kContinue;  // the next call evaluates the child
+                }
+            }
+        }
+    }
+    step_box(s, s.vx & ~(span - 1u), s.vy & ~(span - 1u), s.vz & ~(span - 1u), span);
+    s.step++;
+    s.have_node = 0u;
+    return kContinue;
+}
+
+// The traversal loop body of a kernel instantiated with the feature bits FEAT.
+template <int FEAT>
+__device__ __forceinline__ StepResult ray_next(RayState& s, const World& w, const arc_camera_uniforms& cam, HitInfo& h) {
+    if constexpr ((FEAT & kFeatNodeVisit) != 0) return ray_visit<FEAT>(s, w, cam, h);
+    else return ray_advance<FEAT>(s, w, cam, h);
 }
 
 // is_emissive_mat (traversal64.wgsl:775-777)

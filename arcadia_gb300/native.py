@@ -27,6 +27,8 @@ from .layout import (
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libarc_trace.so")
 
 ARC_OK = 0
+ARC_FEAT_WARP_FETCH = 1
+ARC_FEAT_NODE_VISIT = 2
 ERRORS = {
     -1: "ARC_E_INVALID_ARG",
     -2: "ARC_E_CUDA",
@@ -91,6 +93,7 @@ SIGNATURES = {
     "arc_nrc_set_weights": [_vp, _vp],
     "arc_nrc_get_weights": [_vp, _vp],
     "arc_nrc_set_ema_decay": [_vp, _f32],
+    "arc_nrc_set_ema_warmup": [_vp, _u32],
     "arc_nrc_set_infer_path": [_vp, C.c_int],
     "arc_nrc_set_train_path": [_vp, C.c_int],
     "arc_nrc_get_ema_weights": [_vp, _vp],
@@ -130,6 +133,8 @@ class LaunchConfig(C.Structure):
         ("tile_h", C.c_uint32),
         ("refill_threshold", C.c_uint32),
         ("reg_blocks", C.c_uint32),
+        ("order", C.c_uint32),
+        ("features", C.c_uint32),
     ]
 
 

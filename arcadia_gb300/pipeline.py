@@ -11,6 +11,12 @@ Per frame ``FullPipeline.frame`` runs, in stream order on the tracer's stream:
   nrc      ``arc_nrc_train_frame_dev`` (online training) + ``arc_nrc_query_list_dev`` at every GI hit
 Each stage is timed with CUDA events. The camera follows a seeded circular path above the terrain.
 The edit batches are kept (``ops_log``) so that a test can replay them on the oracle.
+
+With ``compare_every`` > 0 the SHARC pipeline runs beside the NRC on the same frames, after the timed
+stages (update in mode 1 from this frame's G-buffer, resolve, query at the same GI hit list), and every
+``compare_every`` frames both caches are scored against a 4096-spp reference of the one-bounce
+estimator at 4096 of the frame's GI hits (rel-MSE, as in the static cache comparison): how each cache
+keeps up with a moving camera over a world that is edited every frame.
 """
 from __future__ import annotations
 
@@ -42,7 +48,7 @@ def path_camera(scene: L.SceneParams, width: int, height: int, frame: int, n_fra
 class FullPipeline:
     def __init__(self, tracer: native.Tracer, scene: L.SceneParams, width: int, height: int, n_bricks: int,
                  n_frames: int = 300, edit_fraction: float = 0.01, nrc_steps: int = 4, seed: int = 2027, quality=None,
-                 keep_ops: bool = False):
+                 keep_ops: bool = False, compare_every: int = 0, compare_points: int = 4096):
         import torch
 
         self.torch = torch
@@ -81,6 +87,13 @@ class FullPipeline:
         self.last_rewritten = tracer.edit_stats()["bricks_rewritten"]
         self.records = []
         self.launch = None
+        self.compare_every = compare_every
+        self.compare_points = compare_points
+        self.path_scores = []
+        if compare_every:
+            self.sharc_out = torch.zeros((n, 4), dtype=f32, device=dev)
+            self._ck(self.lib.arc_sharc_set_mode(tracer.ctx, 1), "arc_sharc_set_mode")
+            self._ck(self.lib.arc_sharc_reset(tracer.ctx), "arc_sharc_reset")
 
     def _ck(self, rc, what):
         if rc:
@@ -127,6 +140,8 @@ class FullPipeline:
                                                  self.nin.data_ptr(), self.alb.data_ptr(), self.nrc_out.data_ptr()),
                  "arc_nrc_query_list_dev")
         e4 = self._event()
+        if self.compare_every:
+            self._sharc_frame()
         e4.synchronize()
         rewritten = self.t.edit_stats()["bricks_rewritten"]
         dr = rewritten - self.last_rewritten
@@ -137,7 +152,43 @@ class FullPipeline:
                "nrc_ms": e3.elapsed_time(e4), "total_ms": e0.elapsed_time(e4), "ops": int(len(ops)),
                "bricks_rewritten": int(dr), "rays": n_px + int(self.n_gi.item()), "gi_hits": int(self.n_valid.item())}
         self.records.append(rec)
+        if self.compare_every and (f + 1) % self.compare_every == 0:
+            self.path_scores.append(self._score(f))
         return rec
+
+    def _sharc_frame(self):
+        """SHARC beside the NRC (untimed): mode-1 update from this frame's G-buffer, resolve, query at the
+        frame's GI hit list."""
+        n_px = self.w * self.h
+        self._ck(self.lib.arc_sharc_update_dev(self.t.ctx, self.w, self.h, self.gdm.data_ptr(), self.gnm.data_ptr()),
+                 "arc_sharc_update_dev")
+        self._ck(self.lib.arc_sharc_resolve(self.t.ctx), "arc_sharc_resolve")
+        self._ck(self.lib.arc_sharc_query_list_dev(self.t.ctx, self.list.data_ptr(), self.n_valid.data_ptr(), n_px,
+                                                   self.pos.data_ptr(), self.nrm.data_ptr(), self.sharc_out.data_ptr()),
+                 "arc_sharc_query_list_dev")
+
+    def _score(self, f: int):
+        """rel-MSE of both caches at `compare_points` of this frame's GI hits against 64 x 64 spp of the
+        estimator (FP32 launches, FP64 accumulation on the host)."""
+        from .gi_cache import REF_LAUNCHES, REF_SPP_PER_LAUNCH, rel_mse
+
+        torch = self.torch
+        self.t.synchronize()
+        cand = np.nonzero(self.valid.cpu().numpy().astype(bool))[0]
+        idx = cand[np.linspace(0, len(cand) - 1, min(self.compare_points, len(cand))).astype(np.int64)]
+        d_idx = torch.from_numpy(idx.astype(np.int32)).cuda()
+        out = torch.zeros((len(idx), 3), dtype=torch.float32, device="cuda")
+        acc = np.zeros((len(idx), 3), np.float64)
+        for k in range(REF_LAUNCHES):
+            self._ck(self.lib.arc_onebounce_dev(self.t.ctx, d_idx.data_ptr(), len(idx), self.pos.data_ptr(),
+                                                self.nrm.data_ptr(), self.alb.data_ptr(), REF_SPP_PER_LAUNCH,
+                                                777 + 7919 * k + 104729 * f, 0, out.data_ptr()), "arc_onebounce_dev")
+            self.t.synchronize()
+            acc += out.cpu().numpy().astype(np.float64)
+        ref = acc / REF_LAUNCHES
+        nrc = self.nrc_out.cpu().numpy()[idx]
+        sharc = self.sharc_out.cpu().numpy()[idx, :3]
+        return {"frame": f + 1, "rel_mse_nrc": round(rel_mse(nrc, ref), 4), "rel_mse_sharc": round(rel_mse(sharc, ref), 4)}
 
     def tune(self):
         """Untimed setup: the frame autotuner picks the launch configuration on the path's first view."""
@@ -174,4 +225,5 @@ class FullPipeline:
             "nrc_train_samples": TRAIN_SAMPLES, "nrc_steps": self.nrc_steps,
             "pool_next_node": st["next_node"], "pool_next_brick": st["next_brick"], "overflow": st["overflow"],
             "device_status": self.t.stats().device_status, "launch": self.launch,
+            **({"cache_scores_along_path": self.path_scores} if self.compare_every else {}),
         }

@@ -52,6 +52,8 @@ def _args():
     p.add_argument("--variant", type=int, default=None, help="0 plain kernel, 1 persistent kernel (default: tuned)")
     p.add_argument("--reg-blocks", type=int, default=None, help="register budget (CTAs/SM the kernel is built for)")
     p.add_argument("--block-threads", type=int, default=None)
+    p.add_argument("--order", type=int, default=None, help="block order of the plain kernel: 0 row-major, 1 Morton")
+    p.add_argument("--features", type=int, default=None, help="traversal variant bits (ARC_FEAT_*)")
     p.add_argument("--width", type=int, default=WIDTH)
     p.add_argument("--height", type=int, default=HEIGHT)
     p.add_argument("--frame-only", action="store_true", help="time only the frame kernel (profiling runs)")
@@ -311,7 +313,8 @@ def run_ours(args):
     t = native.Tracer(local)
     t.upload_world(scene.grid, roots, nodes, bricks, pal)
     knobs = {k: v for k, v in (("variant", args.variant), ("reg_blocks", args.reg_blocks),
-                               ("block_threads", args.block_threads)) if v is not None}
+                               ("block_threads", args.block_threads), ("order", args.order),
+                               ("features", args.features)) if v is not None}
     if knobs:
         t.set_launch_config(**knobs)
     W_, H_ = args.width, args.height
@@ -428,7 +431,9 @@ def run_ours(args):
         t.set_launch_config(variant=cfg.variant)
         # operating point: 32,768 training samples and 4 Adam steps per frame, queries beside the updates
         nrc = gi_cache.run_comparison(t, SCENE, W_, H_, frames=args.nrc_frames, steps_per_frame=4, overlap=True,
-                                      train_samples=32768)
+                                      train_samples=32768, curve=(10, 20, 30, 60, 120))
+        below = [c["frame"] for c in nrc["convergence"] if c["rel_mse_nrc"] < c["rel_mse_sharc"]]
+        nrc["first_curve_frame_nrc_below_sharc"] = below[0] if below else None
         nrc["unit"] = "ms/frame"
         nrc["network"] = ("216-64x5-3, FP16 weights and activations, FP32 accumulation; tcgen05.mma with TMEM "
                           "accumulators for inference and training")
@@ -494,7 +499,8 @@ def run_ours(args):
         r5, n5, b5, _ = native.build_world(sc5)
         t5 = native.Tracer(local)
         t5.upload_world(sc5.grid, r5, n5, b5, pal, node_headroom=1 << 25, brick_headroom=1 << 22)
-        p5 = FullPipeline(t5, sc5, args.c5_width, args.c5_height, n_bricks=len(b5), n_frames=args.c5_frames)
+        p5 = FullPipeline(t5, sc5, args.c5_width, args.c5_height, n_bricks=len(b5), n_frames=args.c5_frames,
+                          compare_every=30)
         c5 = p5.run(warmup=3)
         c5.update({"workload": "4096^3 sparse world (16^3 chunks: heightfield at 20-35 % of the height, caves in a "
                                "48-voxel band), edits + primary + GI + NRC per frame, camera path",
@@ -545,7 +551,8 @@ def run_ours(args):
                    "autotuned": tuned_ms is not None,
                    "launch": {"block_threads": cfg.block_threads, "blocks_per_sm": cfg.blocks_per_sm,
                               "tile": [cfg.tile_w, cfg.tile_h], "refill_threshold": cfg.refill_threshold,
-                              "reg_blocks": cfg.reg_blocks}},
+                              "reg_blocks": cfg.reg_blocks, "order": "morton" if cfg.order else "row-major",
+                              "features": cfg.features}},
         "plain_kernel": {"value": round(plain_value, 3), "unit": UNIT, "ms_per_step": round(statistics.mean(plain_ms), 4)},
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": 480,
                 "d2h_bytes_per_step": npx * 60 + 8 + 16},
@@ -573,7 +580,10 @@ def run_ours(args):
                                                   and se["nrc_ms_per_frame"] < se["sharc_ms_per_frame"]
                                                   and ov["rel_mse_nrc"] <= ov["rel_mse_sharc"]
                                                   and se["rel_mse_nrc"] <= se["rel_mse_sharc"]),
-            "reference_spp": 4096}
+            "reference_spp": 4096,
+            "static_curve": [[c["frame"], round(c["rel_mse_nrc"], 3), round(c["rel_mse_sharc"], 3)] for c in ov["convergence"]],
+            "moving_c5_path": ([[c["frame"], c["rel_mse_nrc"], c["rel_mse_sharc"]] for c in c5["cache_scores_along_path"]]
+                               if c5 and "cache_scores_along_path" in c5 else None)}
     print(json.dumps(line), flush=True)
 
 

@@ -66,7 +66,14 @@ typedef struct arc_launch_config {
     uint32_t tile_w, tile_h;   /* pixel tile a warp's 32 consecutive queue entries cover (tile_w*tile_h = 32) */
     uint32_t refill_threshold; /* persistent variant: refill when at least this many lanes are idle */
     uint32_t reg_blocks;       /* register budget: kernel built for at least this many 256-thread CTAs per SM (1-4) */
+    uint32_t order;            /* variant 0: order of the pixel blocks (primary kernel and GI pass): 0 row-major,
+                                  1 Morton (Z) order inside super-tiles of 8 x 8 blocks */
+    uint32_t features;         /* traversal variants of variant 0's primary-only kernel and GI pass (register
+                                  budgets 2 and 3), ARC_FEAT_* bits; every variant gives the same results */
 } arc_launch_config;
+
+#define ARC_FEAT_WARP_FETCH 1u  /* lanes of a warp that descend into the same node load it once (match + shuffle) */
+#define ARC_FEAT_NODE_VISIT 2u  /* one node evaluation per loop iteration instead of a per-step descent loop */
 
 typedef struct arc_stats {
     float last_kernel_ms;      /* device time of the last traversal launch (CUDA events) */
@@ -315,6 +322,10 @@ int arc_nrc_get_weights(arc_ctx* ctx, float* weights);
  * after every Adam step (decay 0.99 by default; 0 = the latest weights). set_weights / init restart
  * it from the given weights. */
 int arc_nrc_set_ema_decay(arc_ctx* ctx, float decay);
+/* Warm-up of that average: at Adam step k after init / set_weights the decay is
+ * min(decay, (1 + k) / (steps + k)), so early in training the average follows the weights closely
+ * (default steps = 10; 0 = the fixed decay from the first step). */
+int arc_nrc_set_ema_warmup(arc_ctx* ctx, uint32_t steps);
 /* Inference kernel: 1 = tcgen05 tensor cores with TMEM accumulators (default), 0 = the warp-level
  * mma.sync kernel (kept as the comparison point). */
 int arc_nrc_set_infer_path(arc_ctx* ctx, int path);

@@ -99,11 +99,13 @@ def test_primary_then_secondary_matches_fused(orc, tracer, world_cache):
 
 
 @pytest.mark.parametrize("quality", ["parity", "high"])
-def test_frame_c2_1024_caves_full(orc, tracer, world_cache, quality):
+def test_frame_c2_1024_caves_full(orc, tracer, world_cache, quality, native_lib):
     """1024^3 caves world at 1920x1080 (the headline workload): the whole frame, every G-buffer word,
     primary hit record and GI hit record of all 2,073,600 pixels, bit-exact against the oracle for both
-    kernel variants (plain kernel + GI pass, persistent queue kernel), in parity mode (up to 512 steps,
-    LOD out of reach) and with the high_quality preset (LOD on)."""
+    kernel variants (plain kernel + GI pass, persistent queue kernel) and the plain kernel's traversal
+    variants (Morton block order, one node per loop iteration, warp-shared node fetch), in parity mode
+    (up to 512 steps, LOD out of reach) and with the high_quality preset (LOD on)."""
+    native_lib_feat = native_lib
     w = world_cache("c2_1024_caves")
     q = L.quality_parity(512) if quality == "parity" else L.quality_high()
     cam = L.default_camera_for(L.SCENES["c2_1024_caves"], 1920, 1080, quality=q, frame_index=1)
@@ -112,16 +114,21 @@ def test_frame_c2_1024_caves_full(orc, tracer, world_cache, quality):
     _, ogi, _ = orc.gi_rays(w, cam, ogdm, ognm, threads=THREADS)
     n_hit = int((ohits["flags"] & 1).sum())
     assert n_hit > 0.3 * 1920 * 1080
-    for variant in (0, 1):
-        tracer.set_launch_config(variant=variant)
+    configs = [dict(variant=0), dict(variant=1),
+               dict(variant=0, order=1, features=native_lib_feat.ARC_FEAT_NODE_VISIT, reg_blocks=3),
+               dict(variant=0, order=0, features=native_lib_feat.ARC_FEAT_WARP_FETCH, reg_blocks=2),
+               dict(variant=0, order=1, features=native_lib_feat.ARC_FEAT_WARP_FETCH | native_lib_feat.ARC_FEAT_NODE_VISIT,
+                    reg_blocks=2, block_threads=64)]
+    for cfg in configs:
+        tracer.set_launch_config(**cfg)
         gdm, gnm, gaa, hits, gi, n_gi = tracer.trace_frame()
         np.testing.assert_array_equal(gdm, ogdm)
         np.testing.assert_array_equal(gnm, ognm)
         np.testing.assert_array_equal(gaa, ogaa)
-        _assert_hits_equal(hits, ohits, f"primary variant {variant}")
-        _assert_hits_equal(gi, ogi, f"GI variant {variant}")
+        _assert_hits_equal(hits, ohits, f"primary {cfg}")
+        _assert_hits_equal(gi, ogi, f"GI {cfg}")
         assert n_gi == n_hit
-    tracer.set_launch_config(variant=0)
+    tracer.set_launch_config(variant=0, order=0, features=0, reg_blocks=3, block_threads=128)
     eye = np.broadcast_to(cam[0]["cam_pos_time"][:3], (len(ohits), 3))
     _check_depth_fp64(orc, eye, _camera_rays(cam, 1920, 1080), ohits, stride=401)
 

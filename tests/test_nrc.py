@@ -222,14 +222,16 @@ def test_gpu_weight_ema_feeds_inference(orc, tracer):
     _set(tracer, w)
     d = np.float32(0.9)
     assert lib().arc_nrc_set_ema_decay(tracer.ctx, float(d)) == 0
+    assert lib().arc_nrc_set_ema_warmup(tracer.ctx, 3) == 0
     try:
         dx, dt = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
         ema = w.copy()
-        for _ in range(3):
+        for k in range(1, 4):  # warm-up of 3 steps: decay min(0.9, (1 + k) / (3 + k)) = 0.5, 0.6, 0.6667
             assert lib().arc_nrc_train_step_dev(tracer.ctx, dx.data_ptr(), dt.data_ptr(), len(x), 1e-3, None) == 0
             wk = np.zeros(30400, np.float32)
             assert lib().arc_nrc_get_weights(tracer.ctx, wk.ctypes.data) == 0
-            ema = d * ema + (np.float32(1) - d) * wk
+            dk = min(d, np.float32((1.0 + k) / (3.0 + k)))
+            ema = dk * ema + (np.float32(1) - dk) * wk
         eg = np.zeros(30400, np.float32)
         assert lib().arc_nrc_get_ema_weights(tracer.ctx, eg.ctypes.data) == 0
         np.testing.assert_allclose(eg, ema, atol=1e-6)
@@ -242,6 +244,7 @@ def test_gpu_weight_ema_feeds_inference(orc, tracer):
         assert lib().arc_nrc_set_ema_decay(tracer.ctx, 1.0) != 0  # outside [0, 1)
     finally:
         assert lib().arc_nrc_set_ema_decay(tracer.ctx, 0.99) == 0
+        assert lib().arc_nrc_set_ema_warmup(tracer.ctx, 10) == 0
 
 
 @pytest.mark.gpu
