@@ -60,6 +60,9 @@ struct arc_ctx {
     // staging block of the host-buffer entry points
     void* d_stage = nullptr;
     size_t stage_bytes = 0;
+    // scratch of the globally sorted GI pass (ARC_FEAT_GI_SORT): bins, per-pixel rays, sorted rays
+    unsigned char* d_gisort = nullptr;
+    size_t gisort_bytes = 0;
 
     // SHARC cache
     uint32_t* d_sharc_keys = nullptr;
@@ -83,6 +86,7 @@ struct arc_ctx {
     int nrc_train_path = 1;           // 1 = tcgen05 training, 0 = mma.sync training
     float nrc_ema_decay = 0.99f;
     uint32_t nrc_ema_warmup = 10;     // EMA warm-up: decay min(nrc_ema_decay, (1 + k) / (warmup + k)); 0 = off
+    bool nrc_clamp = false;           // queries return max(output, 0)
     float* d_nrc_loss = nullptr;
     uint32_t nrc_step = 0;
     // in-place edits: device counters [next node, next brick, bricks rewritten, overflow] and staging

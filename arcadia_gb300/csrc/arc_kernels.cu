@@ -369,6 +369,124 @@ __global__ void __launch_bounds__(128, MINB) gi_rows_kernel(const FrameParams P,
     if ((t & 31u) == (uint32_t)(__ffs(m) - 1)) atomicAdd(&P.scratch->gi_rays, (unsigned long long)__popc(m));
 }
 
+// ---- the frame's GI pass with a global sort of its rays (ARC_FEAT_GI_SORT) ----------------------
+// 1. gi_sort_keys_kernel: per pixel of the launch's rows, the GI ray (gi_setup, as gi_rows_kernel) and
+//    its key = octant << 12 | Morton code of the origin's cell (voxel >> cell_shift, 16 cells per axis);
+//    a bin histogram (one atomic per distinct key of a warp).
+// 2. gi_sort_scan_kernel: exclusive scan of the bins (one block).
+// 3. gi_sort_scatter_kernel: each ray to the next slot of its bin.
+// 4. gi_sort_trace_kernel: one thread per sorted slot traces the ray and writes the hit record of its
+//    pixel. The rays and their results are gi_rows_kernel's; only the thread that traces each differs.
+__device__ __forceinline__ uint32_t spread4(uint32_t v) {  // 4 bits -> bits 0, 3, 6, 9
+    return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6);
+}
+
+__global__ void __launch_bounds__(128) gi_sort_keys_kernel(const FrameParams P, const __grid_constant__ arc_camera_uniforms cam) {
+    const uint32_t t = threadIdx.x;
+    uint32_t bx, by;
+    if (!block_coords(blockIdx.x, (P.width + 15u) / 16u, (P.row_end - P.row0 + 7u) / 8u, P.order, &bx, &by)) return;
+    const uint32_t x = bx * 16u + (t & 15u), y = P.row0 + by * 8u + (t >> 4);
+    if (x >= P.width || y >= P.row_end) return;
+    const size_t k = (size_t)y * P.width + x;
+    f3 go, gd;
+    uint32_t key = 0xFFFFFFFFu;
+    if (gi_setup(P.world, cam, x, y, P.width, P.height, P.gbuf_depth_mat[2u * k], P.gbuf_norm_motion[2u * k], &go, &gd)) {
+        const uint32_t sh = P.gisort.cell_shift;
+        const uint32_t cx = umin(f2u(go.x * ARC_VOXELS_PER_METER) >> sh, 15u);
+        const uint32_t cy = umin(f2u(go.y * ARC_VOXELS_PER_METER) >> sh, 15u);
+        const uint32_t cz = umin(f2u(go.z * ARC_VOXELS_PER_METER) >> sh, 15u);
+        const uint32_t oct = (gd.x < 0.0f ? 1u : 0u) | (gd.y < 0.0f ? 2u : 0u) | (gd.z < 0.0f ? 4u : 0u);
+        key = (oct << 12) | spread4(cx) | (spread4(cy) << 1) | (spread4(cz) << 2);
+        P.gisort.ray_dir[k] = make_float4(gd.x, gd.y, gd.z, 0.0f);
+        const uint32_t act = __activemask();
+        const uint32_t peers = __match_any_sync(act, key);
+        if ((int)lane_id() == __ffs(peers) - 1) atomicAdd(&P.gisort.bins[key], (uint32_t)__popc(peers));
+    } else if (P.gi_hits) {
+        store_no_ray(&P.gi_hits[k]);
+    }
+    P.gisort.ray_pix[k] = make_float4(go.x, go.y, go.z, __uint_as_float(key));
+}
+
+__global__ void __launch_bounds__(1024) gi_sort_scan_kernel(uint32_t* __restrict__ bins) {
+    constexpr uint32_t kPer = kGiSortBins / 1024u;  // 32 bins per thread
+    __shared__ uint32_t s_sum[1024];
+    const uint32_t t = threadIdx.x;
+    uint32_t v[kPer], sum = 0u;
+#pragma unroll
+    for (uint32_t i = 0; i < kPer; ++i) {
+        v[i] = bins[t * kPer + i];
+        sum += v[i];
+    }
+    s_sum[t] = sum;
+    __syncthreads();
+    for (uint32_t o = 1; o < 1024u; o <<= 1) {  // inclusive scan of the per-thread sums
+        const uint32_t add = t >= o ? s_sum[t - o] : 0u;
+        __syncthreads();
+        s_sum[t] += add;
+        __syncthreads();
+    }
+    uint32_t run = s_sum[t] - sum;
+#pragma unroll
+    for (uint32_t i = 0; i < kPer; ++i) {
+        bins[t * kPer + i] = run;
+        run += v[i];
+    }
+    if (t == 1023u) bins[kGiSortBins] = s_sum[1023];
+}
+
+__global__ void __launch_bounds__(256) gi_sort_scatter_kernel(const FrameParams P) {
+    const size_t k = (size_t)P.row0 * P.width + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (size_t)P.row_end * P.width) return;
+    const float4 o = P.gisort.ray_pix[k];
+    const uint32_t key = __float_as_uint(o.w);
+    if (key == 0xFFFFFFFFu) return;
+    const float4 d = P.gisort.ray_dir[k];
+    const uint32_t act = __activemask();
+    const uint32_t peers = __match_any_sync(act, key);
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0u;
+    if ((int)lane_id() == leader) base = atomicAdd(&P.gisort.bins[key], (uint32_t)__popc(peers));
+    base = __shfl_sync(act, base, leader);
+    const uint32_t slot = base + __popc(peers & ((1u << lane_id()) - 1u));
+    P.gisort.sorted[2u * slot] = make_float4(o.x, o.y, o.z, __uint_as_float((uint32_t)k));
+    P.gisort.sorted[2u * slot + 1u] = d;
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) gi_sort_trace_kernel(const FrameParams P, const __grid_constant__ arc_camera_uniforms cam) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.gisort.bins[kGiSortBins]) return;
+    const float4 a = P.gisort.sorted[2u * i], b = P.gisort.sorted[2u * i + 1u];
+    const f3 o{a.x, a.y, a.z}, d{b.x, b.y, b.z};
+    const uint32_t kk = __float_as_uint(a.w);
+    const float gmax = cam.ray_distances[2];
+    RayState s;
+    HitInfo h;
+    StepResult g = kMiss;
+    if (ray_begin(s, cam, o, d, 0.0f, gmax, 2u, true)) {
+        do {
+            g = ray_advance(s, P.world, cam, h);
+        } while (g == kContinue);
+    }
+    if (g != kHit) hit_init_miss(h, o, d, gmax);
+    if (P.gi_hits) store_hit(&P.gi_hits[kk], h, g == kHit);
+    const uint32_t m = __activemask();
+    if ((threadIdx.x & 31u) == (uint32_t)(__ffs(m) - 1)) atomicAdd(&P.scratch->gi_rays, (unsigned long long)__popc(m));
+}
+
+template <int MINB>
+cudaError_t launch_gi_sorted(const FrameParams& P, const arc_camera_uniforms& cam, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(P.gisort.bins, 0, sizeof(uint32_t) * (kGiSortBins + 1u), st);
+    if (e != cudaSuccess) return e;
+    const uint32_t rows = P.row_end - P.row0;
+    gi_sort_keys_kernel<<<blocks_for((P.width + 15u) / 16u, (rows + 7u) / 8u, P.order), 128, 0, st>>>(P, cam);
+    gi_sort_scan_kernel<<<1, 1024, 0, st>>>(P.gisort.bins);
+    const uint32_t npx = P.width * rows;
+    gi_sort_scatter_kernel<<<(npx + 255u) / 256u, 256, 0, st>>>(P);
+    gi_sort_trace_kernel<MINB><<<(npx + 127u) / 128u, 128, 0, st>>>(P, cam);
+    return cudaGetLastError();
+}
+
 __global__ void rays_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, const arc_ray* __restrict__ rays,
                             uint32_t n, float max_dist_m, uint32_t lod_bias, uint32_t ignore_water,
                             arc_hit_record* __restrict__ hits) {
@@ -780,6 +898,7 @@ cudaError_t launch_frame_t(const FrameParams& P, const arc_camera_uniforms& cam,
         }
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess || !P.do_gi) return e;
+        if (P.gi_mode == kGiRows && P.gisort.bins) return launch_gi_sorted<MINB>(P, cam, st);
         if (P.gi_mode == kGiRows) {
             const dim3 g2(blocks_for((P.width + 15u) / 16u, (P.row_end - P.row0 + 7u) / 8u, P.order));
             if (variant_kernels || (feat != 0 && P.surf && (MINB == 2 || MINB == 3))) {

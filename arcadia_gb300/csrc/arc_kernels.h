@@ -41,6 +41,17 @@ enum GiMode : uint32_t {
 
 struct FrameParams;
 
+// Scratch of the frame's GI pass with a global sort of its rays (ARC_FEAT_GI_SORT): a counting sort by
+// key = direction octant << 12 | Morton code of the origin's cell on a 16 x 16 x 16 grid over the world.
+constexpr uint32_t kGiSortBins = 1u << 15;
+struct GiSortScratch {
+    uint32_t* bins;    // kGiSortBins counters (then the bins' running slots), and the ray total after them
+    float4* ray_pix;   // per pixel: GI ray origin xyz, w = key bits (0xFFFFFFFF: no GI ray)
+    float4* ray_dir;   // per pixel: GI ray direction xyz
+    float4* sorted;    // per sorted slot, two float4: origin xyz + pixel index bits, direction xyz
+    uint32_t cell_shift;  // voxel coordinate >> cell_shift = cell (0..15 per axis)
+};
+
 }  // namespace arc
 
 #include "arc_traverse.cuh"
@@ -66,6 +77,7 @@ struct FrameParams {
     uint32_t surf_cap;
     uint32_t gi_mode;  // GiMode of the plain kernel (the persistent kernel always fuses)
     uint32_t order;    // block order of the plain kernel and the GI pass: 0 row-major, 1 Morton (block_coords)
+    GiSortScratch gisort;  // bins == nullptr: the GI pass sorts per block (gi_rows_kernel)
 };
 
 // One view of a batched launch: camera block, world slot, resolution, queue offset, outputs.

@@ -201,10 +201,13 @@ __device__ __forceinline__ void load_weights_smem(__half* sw, const __half* __re
 
 // Query rows j < n (n = min(n, *n_dev) when n_dev is given); row j reads and writes point list[j] when a
 // list is given, else point j.
+// Radiance is not negative: with `clamp` set, the queries return max(network output, 0).
+__device__ __forceinline__ float out_clamp(float v, uint32_t clamp) { return clamp ? fmaxf(v, 0.0f) : v; }
+
 __global__ void __launch_bounds__(128) infer_kernel(const __half* __restrict__ w16, const float* __restrict__ in,
                                                     const float* __restrict__ albedo, uint32_t n, float* __restrict__ out,
                                                     const uint32_t* __restrict__ list,
-                                                    const unsigned long long* __restrict__ n_dev) {
+                                                    const unsigned long long* __restrict__ n_dev, uint32_t clamp) {
     extern __shared__ __align__(16) __half smem[];
     if (n_dev) {
         const unsigned long long nd = *n_dev;
@@ -231,13 +234,13 @@ __global__ void __launch_bounds__(128) infer_kernel(const __half* __restrict__ w
             const size_t c = 2u * tig;
             if (ok0) {
                 const size_t o = (size_t)p0 * 3 + c;
-                out[o] = albedo ? y[0] * __ldg(&albedo[o]) : y[0];
-                if (tig == 0) out[o + 1] = albedo ? y[1] * __ldg(&albedo[o + 1]) : y[1];
+                out[o] = albedo ? out_clamp(y[0], clamp) * __ldg(&albedo[o]) : out_clamp(y[0], clamp);
+                if (tig == 0) out[o + 1] = albedo ? out_clamp(y[1], clamp) * __ldg(&albedo[o + 1]) : out_clamp(y[1], clamp);
             }
             if (ok1) {
                 const size_t o = (size_t)p1 * 3 + c;
-                out[o] = albedo ? y[2] * __ldg(&albedo[o]) : y[2];
-                if (tig == 0) out[o + 1] = albedo ? y[3] * __ldg(&albedo[o + 1]) : y[3];
+                out[o] = albedo ? out_clamp(y[2], clamp) * __ldg(&albedo[o]) : out_clamp(y[2], clamp);
+                if (tig == 0) out[o + 1] = albedo ? out_clamp(y[3], clamp) * __ldg(&albedo[o + 1]) : out_clamp(y[3], clamp);
             }
         }
     }
@@ -488,7 +491,7 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
                                                           float* __restrict__ out, const uint32_t* __restrict__ list,
                                                           const unsigned long long* __restrict__ n_dev,
                                                           uint32_t* __restrict__ status, long long budget,
-                                                          uint32_t stall) {
+                                                          uint32_t stall, uint32_t clamp) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
     uint8_t* sw = smem_raw;
     uint8_t* sa = smem_raw + kUHalves * 2;
@@ -629,7 +632,7 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
         if (valid) {
 #pragma unroll
             for (int c = 0; c < kOut; ++c) {
-                const float val = __uint_as_float(y[c]);
+                const float val = out_clamp(__uint_as_float(y[c]), clamp);
                 out[(size_t)p * 3 + c] = albedo ? val * a[c] : val;
             }
         }
@@ -989,14 +992,15 @@ int launch_infer(arc_ctx* c, const float* inputs, const float* albedo, uint32_t 
         const uint32_t blocks = std::min<uint32_t>((n + 127u) / 128u, (uint32_t)c->n_sm * 2u);
         nrc::infer_tc_kernel<<<blocks, 128, nrc::kTcSmem, c->stream>>>(static_cast<const __half*>(c->d_nrc_wu_ema), inputs,
                                                                         albedo, n, out, list, n_dev, c->d_status,
-                                                                        tc_budget(c), c->tc_stall ? 1u : 0u);
+                                                                        tc_budget(c), c->tc_stall ? 1u : 0u,
+                                                                        c->nrc_clamp ? 1u : 0u);
         NRC_CK(cudaGetLastError());
         return ARC_OK;
     }
     const uint32_t tiles = (n + 15u) / 16u;
     const uint32_t blocks = std::min<uint32_t>((tiles + 3u) / 4u, (uint32_t)c->n_sm * 3u);
     nrc::infer_kernel<<<blocks, 128, nrc::kFwdHalves * sizeof(__half), c->stream>>>(
-        static_cast<const __half*>(c->d_nrc_w16_ema), inputs, albedo, n, out, list, n_dev);
+        static_cast<const __half*>(c->d_nrc_w16_ema), inputs, albedo, n, out, list, n_dev, c->nrc_clamp ? 1u : 0u);
     NRC_CK(cudaGetLastError());
     return ARC_OK;
 }
@@ -1112,6 +1116,12 @@ int arc_nrc_set_ema_decay(arc_ctx* c, float decay) {
         return ARC_E_INVALID_ARG;
     }
     c->nrc_ema_decay = decay;
+    return ARC_OK;
+}
+
+int arc_nrc_set_output_clamp(arc_ctx* c, int on) {
+    if (!c) return ARC_E_INVALID_ARG;
+    c->nrc_clamp = on != 0;
     return ARC_OK;
 }
 

@@ -557,7 +557,8 @@ def run_ours(args):
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": 480,
                 "d2h_bytes_per_step": npx * 60 + 8 + 16},
         # per timed frame: the persistent kernel, or the plain kernel's primary instance + the GI pass
-        "gpu_launches": args.steps * (1 if cfg.variant == 1 else 2),
+        # (one kernel, or four with the GI rays sorted over the frame: keys, scan, scatter, trace)
+        "gpu_launches": args.steps * (1 if cfg.variant == 1 else (5 if cfg.features & 4 else 2)),
         "roofline": roofline,
         "cpu_baseline": cpu,
         "nrc": nrc,

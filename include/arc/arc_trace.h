@@ -74,6 +74,9 @@ typedef struct arc_launch_config {
 
 #define ARC_FEAT_WARP_FETCH 1u  /* lanes of a warp that descend into the same node load it once (match + shuffle) */
 #define ARC_FEAT_NODE_VISIT 2u  /* one node evaluation per loop iteration instead of a per-step descent loop */
+#define ARC_FEAT_GI_SORT 4u     /* arc_trace_frame_dev: the frame's GI rays sorted over the whole frame by
+                                   (direction octant, origin cell on a 16^3 grid over the world) before they
+                                   are traced (one thread per sorted ray); other entry points sort per block */
 
 typedef struct arc_stats {
     float last_kernel_ms;      /* device time of the last traversal launch (CUDA events) */
@@ -326,6 +329,9 @@ int arc_nrc_set_ema_decay(arc_ctx* ctx, float decay);
  * min(decay, (1 + k) / (steps + k)), so early in training the average follows the weights closely
  * (default steps = 10; 0 = the fixed decay from the first step). */
 int arc_nrc_set_ema_warmup(arc_ctx* ctx, uint32_t steps);
+/* on = 1: queries return max(network output, 0) per channel (radiance is not negative); 0 (default) =
+ * the network output as it is. Training is unaffected. */
+int arc_nrc_set_output_clamp(arc_ctx* ctx, int on);
 /* Inference kernel: 1 = tcgen05 tensor cores with TMEM accumulators (default), 0 = the warp-level
  * mma.sync kernel (kept as the comparison point). */
 int arc_nrc_set_infer_path(arc_ctx* ctx, int path);
