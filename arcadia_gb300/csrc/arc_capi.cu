@@ -254,6 +254,7 @@ int arc_destroy(arc_ctx* c) {
     cudaFree(c->d_status);
     cudaFree(c->d_stage);
     cudaFree(c->d_gisort);
+    cudaFree(c->d_top);
     cudaFree(c->d_sharc_keys);
     cudaFree(c->d_sharc_accum);
     cudaFree(c->d_sharc_resolved);
@@ -353,7 +354,7 @@ int arc_set_launch_config(arc_ctx* c, const arc_launch_config* cfg) {
     if (cfg->block_threads > 256u) return set_err(c, ARC_E_INVALID_ARG, "block_threads <= 256");
     if (cfg->reg_blocks < 1u || cfg->reg_blocks > 4u) return set_err(c, ARC_E_INVALID_ARG, "reg_blocks in [1, 4]");
     if (cfg->order > 1u) return set_err(c, ARC_E_INVALID_ARG, "order must be 0 (row-major) or 1 (Morton)");
-    if (cfg->features & ~(ARC_FEAT_WARP_FETCH | ARC_FEAT_NODE_VISIT | ARC_FEAT_GI_SORT))
+    if (cfg->features & ~(ARC_FEAT_WARP_FETCH | ARC_FEAT_NODE_VISIT | ARC_FEAT_GI_SORT | ARC_FEAT_TOP_TABLE | ARC_FEAT_GRID_STRIDE))
         return set_err(c, ARC_E_INVALID_ARG, "unknown feature bits");
     c->cfg = *cfg;
     return ARC_OK;
@@ -552,6 +553,14 @@ static arc::FrameParams frame_params(arc_ctx* c, uint32_t width, uint32_t height
     P.refill_threshold = c->cfg.refill_threshold;
     P.gi_mode = arc::kGiRows;  // honoured by the plain kernel; the persistent kernel fuses the GI ray
     P.order = c->cfg.order;
+    if (c->cfg.variant == 0u && (c->cfg.features & (ARC_FEAT_TOP_TABLE | ARC_FEAT_GRID_STRIDE))) {
+        if (!c->d_top && cudaMalloc((void**)&c->d_top, sizeof(uint4) * arc::kTopMaxNodes + 16u) != cudaSuccess)
+            c->d_top = nullptr;  // without the table the plain kernel runs
+        if (c->d_top) {
+            P.top = reinterpret_cast<uint4*>(c->d_top);
+            P.top_info = reinterpret_cast<uint32_t*>(c->d_top + sizeof(uint4) * arc::kTopMaxNodes);
+        }
+    }
     frame_rows(c, P, 0u, height);
     return P;
 }

@@ -63,6 +63,8 @@ struct arc_ctx {
     // scratch of the globally sorted GI pass (ARC_FEAT_GI_SORT): bins, per-pixel rays, sorted rays
     unsigned char* d_gisort = nullptr;
     size_t gisort_bytes = 0;
+    // table of the top two tree levels (ARC_FEAT_TOP_TABLE), rebuilt on the device before every frame
+    unsigned char* d_top = nullptr;
 
     // SHARC cache
     uint32_t* d_sharc_keys = nullptr;
@@ -87,6 +89,7 @@ struct arc_ctx {
     float nrc_ema_decay = 0.99f;
     uint32_t nrc_ema_warmup = 10;     // EMA warm-up: decay min(nrc_ema_decay, (1 + k) / (warmup + k)); 0 = off
     bool nrc_clamp = false;           // queries return max(output, 0)
+    float nrc_beta1 = 0.9f, nrc_beta2 = 0.99f;  // Adam moment decays
     float* d_nrc_loss = nullptr;
     uint32_t nrc_step = 0;
     // in-place edits: device counters [next node, next brick, bricks rewritten, overflow] and staging

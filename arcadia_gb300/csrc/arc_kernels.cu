@@ -213,6 +213,111 @@ __global__ void __launch_bounds__(256, MINB) frame_plain_kernel(const FrameParam
     if (((threadIdx.x + threadIdx.y * blockDim.x) & 31u) == (uint32_t)(__ffs(m) - 1)) atomicAdd(&P.scratch->gi_rays, (unsigned long long)__popc(m));
 }
 
+// ---- primary rays from resident CTAs (ARC_FEAT_TOP_TABLE, ARC_FEAT_GRID_STRIDE) ---------------
+// top_build_kernel (one CTA) writes the table of the top two tree levels from the current pools: entry c
+// is chunk c's root, an internal root's child index rebased into the level-1 part that follows the
+// roots (each root's child slice in order); *info = number of entries, 0 when they exceed kTopMaxNodes.
+__global__ void __launch_bounds__(1024) top_build_kernel(const World w, uint32_t n_chunks, uint4* __restrict__ out,
+                                                         uint32_t* __restrict__ info) {
+    __shared__ uint32_t s_sum[1024];
+    const uint32_t t = threadIdx.x, per = (n_chunks + 1023u) / 1024u;
+    uint32_t cnt = 0u;
+    for (uint32_t i = 0; i < per; ++i) {
+        const uint32_t c = t * per + i;
+        if (c >= n_chunks) break;
+        const uint32_t r = w.roots[c];
+        if (r == ARC_EMPTY_CHUNK || r >= w.n_nodes) continue;
+        const uint4 nd = w.nodes[r];
+        if (!(nd.z & ARC_IS_LEAF_FLAG)) cnt += __popc(nd.x) + __popc(nd.y);
+    }
+    s_sum[t] = cnt;
+    __syncthreads();
+    for (uint32_t o = 1; o < 1024u; o <<= 1) {
+        const uint32_t add = t >= o ? s_sum[t - o] : 0u;
+        __syncthreads();
+        s_sum[t] += add;
+        __syncthreads();
+    }
+    const uint32_t total = s_sum[1023];
+    const bool fits = (uint64_t)n_chunks + total <= kTopMaxNodes;
+    if (t == 0u) *info = fits ? n_chunks + total : 0u;
+    if (!fits) return;
+    uint32_t off = s_sum[t] - cnt;
+    for (uint32_t i = 0; i < per; ++i) {
+        const uint32_t c = t * per + i;
+        if (c >= n_chunks) break;
+        const uint32_t r = w.roots[c];
+        uint4 nd = make_uint4(0u, 0u, 0u, 0u);
+        if (r != ARC_EMPTY_CHUNK && r < w.n_nodes) {
+            nd = w.nodes[r];
+            if (!(nd.z & ARC_IS_LEAF_FLAG)) {
+                const uint32_t k = __popc(nd.x) + __popc(nd.y), src = nd.z & ARC_PTR_INDEX_MASK;
+                for (uint32_t j = 0; j < k; ++j) out[n_chunks + off + j] = load_node(w, src + j);
+                nd.z = off;  // internal node: no flag bits
+                off += k;
+            }
+        }
+        out[c] = nd;
+    }
+}
+
+// Primary rays (no surface list) from resident CTAs that take the pixel blocks of the launch in turn
+// (block order as the plain kernel). With TOP each CTA first copies the top-level table into shared
+// memory, and restarts from a chunk root read it there.
+template <int MINB, bool TOP>
+__global__ void __launch_bounds__(256, MINB) frame_grid_kernel(const FrameParams P, const __grid_constant__ arc_camera_uniforms cam) {
+    extern __shared__ uint4 s_top[];
+    const World& w = P.world;
+    TopView top{nullptr, nullptr};
+    if constexpr (TOP) {
+        const uint32_t n = *P.top_info;  // the same for every thread
+        const uint32_t tid = threadIdx.x + threadIdx.y * blockDim.x, nthr = blockDim.x * blockDim.y;
+        for (uint32_t i = tid; i < n; i += nthr) s_top[i] = P.top[i];
+        __syncthreads();
+        if (n) top = TopView{s_top, s_top + cam.world_grid_dims[0] * cam.world_grid_dims[1] * cam.world_grid_dims[2]};
+    }
+    const uint32_t nbx = (P.width + blockDim.x - 1u) / blockDim.x;
+    const uint32_t nby = (P.row_end - P.row0 + blockDim.y - 1u) / blockDim.y;
+    const uint32_t total = blocks_for(nbx, nby, P.order);
+    const f3 eye{cam.cam_pos_time[0], cam.cam_pos_time[1], cam.cam_pos_time[2]};
+    const bool underwater = (cam.point_light_count[1] & 0xFFFFu) != 0u;
+    for (uint32_t id = blockIdx.x; id < total; id += gridDim.x) {
+        uint32_t bx, by;
+        if (!block_coords(id, nbx, nby, P.order, &bx, &by)) continue;
+        const uint32_t x = bx * blockDim.x + threadIdx.x, y = P.row0 + by * blockDim.y + threadIdx.y;
+        if (x >= P.width || y >= P.row_end) continue;
+        const f3 dir = camera_dir(cam, x, y, P.width, P.height);
+        RayState s;
+        HitInfo h;
+        StepResult r = kMiss;
+        if (ray_begin(s, cam, eye, dir, 0.0f, 250.0f, 0u, underwater)) {
+            do {
+                r = ray_advance<TOP ? kFeatTopTable : 0>(s, w, cam, h, top);
+            } while (r == kContinue);
+        }
+        if (r != kHit) hit_init_miss(h, eye, dir, 250.0f);
+        uint32_t dw, nw;
+        primary_store<false>(P, w.palette, cam, x, y, dir, r == kHit, h, &dw, &nw);
+    }
+}
+
+template <int MINB, bool TOP>
+cudaError_t launch_grid_primary(const FrameParams& P, const arc_camera_uniforms& cam, const arc_launch_config& cfg, int n_sm,
+                                cudaStream_t st) {
+    const size_t smem = TOP ? sizeof(uint4) * kTopMaxNodes : 0u;
+    if (TOP) {
+        const uint32_t n_chunks = cam.world_grid_dims[0] * cam.world_grid_dims[1] * cam.world_grid_dims[2];
+        top_build_kernel<<<1, 1024, 0, st>>>(P.world, n_chunks, P.top, P.top_info);
+    }
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, frame_grid_kernel<MINB, TOP>, (int)cfg.block_threads, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm <= 0) per_sm = 1;
+    const dim3 block(8u, cfg.block_threads / 8u);
+    frame_grid_kernel<MINB, TOP><<<n_sm * per_sm, block, smem, st>>>(P, cam);
+    return cudaGetLastError();
+}
+
 enum : uint32_t { kIdle = 0u, kPrimary = 1u, kGi = 2u };
 
 template <int MINB, bool SURF>
@@ -885,7 +990,13 @@ cudaError_t launch_frame_t(const FrameParams& P, const arc_camera_uniforms& cam,
         // the traversal variants are built for the primary-only instance and the GI pass (no surface list)
         const int feat = (int)(cfg.features & (uint32_t)(kFeatWarpFetch | kFeatNodeVisit));
         const bool variant_kernels = feat != 0 && !P.surf && !fused && (MINB == 2 || MINB == 3);
-        if (P.surf) {
+        const bool grid_primary = (cfg.features & (ARC_FEAT_TOP_TABLE | ARC_FEAT_GRID_STRIDE)) && !P.surf && !fused &&
+                                  P.top && (MINB == 2 || MINB == 3);
+        if (grid_primary) {
+            cudaError_t e = (cfg.features & ARC_FEAT_TOP_TABLE) ? launch_grid_primary<MINB, true>(P, cam, cfg, n_sm, st)
+                                                               : launch_grid_primary<MINB, false>(P, cam, cfg, n_sm, st);
+            if (e != cudaSuccess) return e;
+        } else if (P.surf) {
             if (fused) frame_plain_kernel<MINB, true, true><<<grid, block, 0, st>>>(P, cam);
             else frame_plain_kernel<MINB, true, false><<<grid, block, 0, st>>>(P, cam);
         } else if (variant_kernels) {

@@ -78,7 +78,10 @@ struct FrameParams {
     uint32_t gi_mode;  // GiMode of the plain kernel (the persistent kernel always fuses)
     uint32_t order;    // block order of the plain kernel and the GI pass: 0 row-major, 1 Morton (block_coords)
     GiSortScratch gisort;  // bins == nullptr: the GI pass sorts per block (gi_rows_kernel)
+    uint4* top;            // ARC_FEAT_TOP_TABLE: table of chunk roots + level-1 nodes (kTopMaxNodes entries)
+    uint32_t* top_info;    // its entry count (0: the table did not fit)
 };
+constexpr uint32_t kTopMaxNodes = 3072;  // 48 KB of 16-byte nodes
 
 // One view of a batched launch: camera block, world slot, resolution, queue offset, outputs.
 struct ViewDev {

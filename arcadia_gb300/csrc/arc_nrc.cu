@@ -399,10 +399,11 @@ __global__ void __launch_bounds__(128) train_kernel(const __half* __restrict__ w
 __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
                             float* __restrict__ g, __half* __restrict__ w16, float* __restrict__ ema,
                             __half* __restrict__ w16_ema, __half* __restrict__ wu, __half* __restrict__ wu_ema, float decay,
-                            float lr, float c1, float c2, float inv_scale, const uint32_t* __restrict__ gate) {
+                            float lr, float c1, float c2, float inv_scale, const uint32_t* __restrict__ gate, float b1,
+                            float b2) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams || (gate && *gate == 0u)) return;
-    const float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
+    const float eps = 1e-8f;
     const float gi = g[i] * inv_scale;
     g[i] = 0.0f;  // the gradient starts from zero for the next step (no separate clear)
     const float mi = b1 * m[i] + (1.0f - b1) * gi;
@@ -1039,11 +1040,11 @@ float ema_decay_at(const arc_ctx* c, uint32_t k) {
 // One Adam step from d_nrc_grad; the host step counter sets the bias correction.
 int launch_adam(arc_ctx* c, float lr, const uint32_t* gate) {
     c->nrc_step += 1;
-    const float c1 = 1.0f - std::pow(0.9f, (float)c->nrc_step), c2 = 1.0f - std::pow(0.99f, (float)c->nrc_step);
+    const float c1 = 1.0f - std::pow(c->nrc_beta1, (float)c->nrc_step), c2 = 1.0f - std::pow(c->nrc_beta2, (float)c->nrc_step);
     nrc::adam_kernel<<<(nrc::kParams + 255) / 256, 256, 0, c->stream>>>(
         c->d_nrc_w32, c->d_nrc_m, c->d_nrc_v, c->d_nrc_grad, static_cast<__half*>(c->d_nrc_w16), c->d_nrc_ema,
         static_cast<__half*>(c->d_nrc_w16_ema), static_cast<__half*>(c->d_nrc_wu), static_cast<__half*>(c->d_nrc_wu_ema),
-        ema_decay_at(c, c->nrc_step), lr, c1, c2, 1.0f / nrc::kLossScale, gate);
+        ema_decay_at(c, c->nrc_step), lr, c1, c2, 1.0f / nrc::kLossScale, gate, c->nrc_beta1, c->nrc_beta2);
     NRC_CK(cudaGetLastError());
     return ARC_OK;
 }
@@ -1116,6 +1117,17 @@ int arc_nrc_set_ema_decay(arc_ctx* c, float decay) {
         return ARC_E_INVALID_ARG;
     }
     c->nrc_ema_decay = decay;
+    return ARC_OK;
+}
+
+int arc_nrc_set_adam_betas(arc_ctx* c, float beta1, float beta2) {
+    if (!c) return ARC_E_INVALID_ARG;
+    if (!(beta1 >= 0.0f && beta1 < 1.0f && beta2 >= 0.0f && beta2 < 1.0f)) {
+        c->err = "Adam betas must lie in [0, 1)";
+        return ARC_E_INVALID_ARG;
+    }
+    c->nrc_beta1 = beta1;
+    c->nrc_beta2 = beta2;
     return ARC_OK;
 }
 

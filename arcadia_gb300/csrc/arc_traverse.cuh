@@ -101,7 +101,7 @@ struct RayState {
 // decisions in the same order, so results are identical bit for bit.
 constexpr int kFeatWarpFetch = 1;   // lanes that descend into the same node fetch it once per warp
 constexpr int kFeatNodeVisit = 2;   // one node evaluation per loop iteration instead of a descent loop
-constexpr int kFeatTopTable = 4;    // chunk roots and their level-1 children from a dense table in shared memory
+constexpr int kFeatTopTable = 8;    // chunk roots and their level-1 children from a table staged in shared memory
 
 __device__ __forceinline__ float noi_x(const RayState& s) { return -s.vo.x * s.inv.x; }
 __device__ __forceinline__ float noi_y(const RayState& s) { return -s.vo.y * s.inv.y; }
@@ -318,9 +318,17 @@ __device__ __forceinline__ void resolve_hit(const RayState& s, const arc_camera_
 // cell (451-465) or the air leaf cell (525-537). Here the branches only choose the box's span and one
 // convergent step_box runs after them, so lanes that took different branches step together instead
 // of executing five inlined copies one after another. Decisions and their order are unchanged.
+// The top two tree levels staged in shared memory for kFeatTopTable: roots[c] is chunk c's root node
+// with the child index of an internal root rebased into l1[], which holds every root's level-1 children
+// (each root's child slice, in order). Null roots: the nodes come from the pool as usual.
+struct TopView {
+    const uint4* roots;
+    const uint4* l1;
+};
+
 template <int FEAT = 0>
 __device__ __forceinline__ StepResult ray_advance(RayState& s, const World& w, const arc_camera_uniforms& cam,
-                                                  HitInfo& h) {
+                                                  HitInfo& h, const TopView top = TopView{nullptr, nullptr}) {
     if (s.step >= max_steps_of(cam, s.mode)) return kMiss;
     if (s.t >= s.t_limit) return kMiss;
     const uint32_t gx = cam.world_grid_dims[0], gy = cam.world_grid_dims[1], gz = cam.world_grid_dims[2];
@@ -371,7 +379,11 @@ __device__ __forceinline__ StepResult ray_advance(RayState& s, const World& w, c
             node = s.l1;
             shift = 4u;
         } else {
-            node = load_node(w, root_idx);
+            if constexpr ((FEAT & kFeatTopTable) != 0) {
+                node = top.roots ? top.roots[(s.vx >> 8) + (s.vy >> 8) * gx + (s.vz >> 8) * gx * gy] : load_node(w, root_idx);
+            } else {
+                node = load_node(w, root_idx);
+            }
             shift = 6u;
         }
         s.cached_shift = shift;
@@ -397,7 +409,12 @@ __device__ __forceinline__ StepResult ray_advance(RayState& s, const World& w, c
                 }
                 break;  // air leaf cell
             }
-            node = fetch_node<FEAT>(w, child_index(node, b));
+            if constexpr ((FEAT & kFeatTopTable) != 0) {
+                // at level 6 the node is the chunk root, from the table when it is staged
+                node = (shift == 6u && top.roots) ? top.l1[child_index(node, b)] : fetch_node<FEAT>(w, child_index(node, b));
+            } else {
+                node = fetch_node<FEAT>(w, child_index(node, b));
+            }
             shift -= 2u;
             s.cached_shift = shift;
             if (shift == 4u) s.l1 = node;

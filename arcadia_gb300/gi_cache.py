@@ -164,12 +164,13 @@ class CacheComparison:
 
 def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920, height=1080, frames=300,
                    eval_points=16384, seed=7, steps_per_frame=8, lr=1e-3, curve=(30, 60, 120), overlap=False,
-                   train_samples=TRAIN_SAMPLES, boost_frames=0, boost_steps=16):
+                   train_samples=TRAIN_SAMPLES, boost_frames=0, boost_steps=16, lr_warmup_frames=0):
     """Runs both pipelines for `frames` frames on a static camera and scores them on the last frame;
     `curve` lists earlier frames at which both are scored as well (8192 points each). With overlap each
     cache's query runs beside its own update (one frame behind it), for both caches alike. The first
     `boost_frames` frames train with `boost_steps` Adam steps instead of `steps_per_frame` (a start-up
-    phase; the timings average the second half of the run)."""
+    phase; the timings average the second half of the run). With lr_warmup_frames the learning rate
+    rises linearly to `lr` over that many frames."""
     scene = L.SCENES[scene_name]
     cc = CacheComparison(tracer, scene, width, height)
     lib = cc.lib
@@ -182,7 +183,8 @@ def run_comparison(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920
         shared_ms.append(cc.shared(f))
         sharc_ms.append(cc.sharc_frame(overlap=overlap))
         steps = boost_steps if f < boost_frames else steps_per_frame
-        nrc_ms.append(cc.nrc_frame(seed * 1000003 + f, lr=lr, steps=steps, overlap=overlap, samples=train_samples))
+        lr_f = lr * min(1.0, (f + 1) / lr_warmup_frames) if lr_warmup_frames else lr
+        nrc_ms.append(cc.nrc_frame(seed * 1000003 + f, lr=lr_f, steps=steps, overlap=overlap, samples=train_samples))
         if f + 1 in curve and f + 1 < frames:
             cand = np.nonzero(cc.valid.cpu().numpy().astype(bool))[0]
             ci = cand[np.linspace(0, len(cand) - 1, min(8192, len(cand))).astype(np.int64)]

@@ -30,6 +30,8 @@ ARC_OK = 0
 ARC_FEAT_WARP_FETCH = 1
 ARC_FEAT_NODE_VISIT = 2
 ARC_FEAT_GI_SORT = 4
+ARC_FEAT_TOP_TABLE = 8
+ARC_FEAT_GRID_STRIDE = 16
 ERRORS = {
     -1: "ARC_E_INVALID_ARG",
     -2: "ARC_E_CUDA",
@@ -96,6 +98,7 @@ SIGNATURES = {
     "arc_nrc_set_ema_decay": [_vp, _f32],
     "arc_nrc_set_ema_warmup": [_vp, _u32],
     "arc_nrc_set_output_clamp": [_vp, _i32],
+    "arc_nrc_set_adam_betas": [_vp, _f32, _f32],
     "arc_nrc_set_infer_path": [_vp, C.c_int],
     "arc_nrc_set_train_path": [_vp, C.c_int],
     "arc_nrc_get_ema_weights": [_vp, _vp],

@@ -77,6 +77,11 @@ typedef struct arc_launch_config {
 #define ARC_FEAT_GI_SORT 4u     /* arc_trace_frame_dev: the frame's GI rays sorted over the whole frame by
                                    (direction octant, origin cell on a 16^3 grid over the world) before they
                                    are traced (one thread per sorted ray); other entry points sort per block */
+#define ARC_FEAT_TOP_TABLE 8u   /* the primary kernel as resident CTAs that loop over the pixel blocks, each CTA
+                                   staging every chunk root and its level-1 children (at most 48 KB, else
+                                   read from the pool) in shared memory once */
+#define ARC_FEAT_GRID_STRIDE 16u /* the same resident-CTA primary kernel without the staged table (the
+                                    control of ARC_FEAT_TOP_TABLE) */
 
 typedef struct arc_stats {
     float last_kernel_ms;      /* device time of the last traversal launch (CUDA events) */
@@ -332,6 +337,8 @@ int arc_nrc_set_ema_warmup(arc_ctx* ctx, uint32_t steps);
 /* on = 1: queries return max(network output, 0) per channel (radiance is not negative); 0 (default) =
  * the network output as it is. Training is unaffected. */
 int arc_nrc_set_output_clamp(arc_ctx* ctx, int on);
+/* Adam's moment decays (default beta1 0.9, beta2 0.99; both in [0, 1)). */
+int arc_nrc_set_adam_betas(arc_ctx* ctx, float beta1, float beta2);
 /* Inference kernel: 1 = tcgen05 tensor cores with TMEM accumulators (default), 0 = the warp-level
  * mma.sync kernel (kept as the comparison point). */
 int arc_nrc_set_infer_path(arc_ctx* ctx, int path);
