@@ -87,7 +87,7 @@ struct arc_ctx {
     int nrc_infer_path = 1;           // 1 = tcgen05 inference, 0 = mma.sync inference
     int nrc_train_path = 1;           // 1 = tcgen05 training, 0 = mma.sync training
     float nrc_ema_decay = 0.99f;
-    uint32_t nrc_ema_warmup = 10;     // EMA warm-up: decay min(nrc_ema_decay, (1 + k) / (warmup + k)); 0 = off
+    uint32_t nrc_ema_warmup = 0;      // EMA warm-up: decay min(nrc_ema_decay, (1 + k) / (warmup + k)); 0 = off
     bool nrc_clamp = false;           // queries return max(output, 0)
     float nrc_beta1 = 0.9f, nrc_beta2 = 0.99f;  // Adam moment decays
     float* d_nrc_loss = nullptr;

@@ -185,6 +185,7 @@ __global__ void __launch_bounds__(256, MINB) frame_plain_kernel(const FrameParam
     // One traversal call site for both rays: the primary ray, then (for a hit) the GI ray continues in
     // the same loop, so lanes in either phase run the same instructions together.
     bool active = ray_begin(s, cam, eye, dir, 0.0f, 250.0f, 0u, underwater);
+    if constexpr ((FEAT & kFeatPrecomp) != 0) ray_precompute(s, cam);
     bool gi_phase = false;
     const size_t k = (size_t)y * P.width + x;
     f3 go{0.0f, 0.0f, 0.0f}, gd{0.0f, 0.0f, 1.0f};
@@ -205,6 +206,7 @@ __global__ void __launch_bounds__(256, MINB) frame_plain_kernel(const FrameParam
         }
         gi_phase = true;
         active = ray_begin(s, cam, go, gd, 0.0f, gmax, 2u, true);
+        if constexpr ((FEAT & kFeatPrecomp) != 0) ray_precompute(s, cam);
     }
     if (r != kHit) hit_init_miss(h, go, gd, gmax);
     if (P.gi_hits) store_hit(&P.gi_hits[k], h, r == kHit);
@@ -464,6 +466,7 @@ __global__ void __launch_bounds__(128, MINB) gi_rows_kernel(const FrameParams P,
     HitInfo h;
     StepResult g = kMiss;
     if (ray_begin(s, cam, o, d, 0.0f, gmax, 2u, true)) {
+        if constexpr ((FEAT & kFeatPrecomp) != 0) ray_precompute(s, cam);
         do {
             g = ray_next<FEAT>(s, P.world, cam, h);
         } while (g == kContinue);
@@ -988,7 +991,10 @@ cudaError_t launch_frame_t(const FrameParams& P, const arc_camera_uniforms& cam,
         const dim3 grid(blocks_for((P.width + bw - 1u) / bw, (P.row_end - P.row0 + bh - 1u) / bh, P.order));
         const bool fused = P.do_gi && P.gi_mode == kGiFused;
         // the traversal variants are built for the primary-only instance and the GI pass (no surface list)
-        const int feat = (int)(cfg.features & (uint32_t)(kFeatWarpFetch | kFeatNodeVisit));
+        // the instantiated traversal variants; any other combination of these bits runs the standard kernels
+        const int feat0 = (int)(cfg.features & (uint32_t)(kFeatWarpFetch | kFeatNodeVisit | kFeatPrecomp));
+        const int feat = (feat0 == kFeatWarpFetch || feat0 == kFeatNodeVisit || feat0 == kFeatPrecomp ||
+                          feat0 == (kFeatWarpFetch | kFeatNodeVisit)) ? feat0 : 0;
         const bool variant_kernels = feat != 0 && !P.surf && !fused && (MINB == 2 || MINB == 3);
         const bool grid_primary = (cfg.features & (ARC_FEAT_TOP_TABLE | ARC_FEAT_GRID_STRIDE)) && !P.surf && !fused &&
                                   P.top && (MINB == 2 || MINB == 3);
@@ -1002,6 +1008,7 @@ cudaError_t launch_frame_t(const FrameParams& P, const arc_camera_uniforms& cam,
         } else if (variant_kernels) {
             if (feat == kFeatWarpFetch) frame_plain_kernel<MINB, false, false, kFeatWarpFetch><<<grid, block, 0, st>>>(P, cam);
             else if (feat == kFeatNodeVisit) frame_plain_kernel<MINB, false, false, kFeatNodeVisit><<<grid, block, 0, st>>>(P, cam);
+            else if (feat == kFeatPrecomp) frame_plain_kernel<MINB, false, false, kFeatPrecomp><<<grid, block, 0, st>>>(P, cam);
             else frame_plain_kernel<MINB, false, false, kFeatWarpFetch | kFeatNodeVisit><<<grid, block, 0, st>>>(P, cam);
         } else {
             if (fused) frame_plain_kernel<MINB, false, true><<<grid, block, 0, st>>>(P, cam);
@@ -1015,6 +1022,7 @@ cudaError_t launch_frame_t(const FrameParams& P, const arc_camera_uniforms& cam,
             if (variant_kernels || (feat != 0 && P.surf && (MINB == 2 || MINB == 3))) {
                 if (feat == kFeatWarpFetch) gi_rows_kernel<MINB, kFeatWarpFetch><<<g2, 128, 0, st>>>(P, cam);
                 else if (feat == kFeatNodeVisit) gi_rows_kernel<MINB, kFeatNodeVisit><<<g2, 128, 0, st>>>(P, cam);
+                else if (feat == kFeatPrecomp) gi_rows_kernel<MINB, kFeatPrecomp><<<g2, 128, 0, st>>>(P, cam);
                 else gi_rows_kernel<MINB, kFeatWarpFetch | kFeatNodeVisit><<<g2, 128, 0, st>>>(P, cam);
             } else {
                 gi_rows_kernel<MINB><<<g2, 128, 0, st>>>(P, cam);

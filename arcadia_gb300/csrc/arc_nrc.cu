@@ -1029,9 +1029,9 @@ int launch_grad(arc_ctx* c, const float* inputs, const float* targets, uint32_t 
 }
 
 // Decay of the weight average at Adam step k (counted from the last init / set_weights): the set decay,
-// or during a warm-up of w steps min(decay, (1 + k) / (w + k)), so the average follows the fast early
-// training instead of dragging the initial weights along (at decay 0.99 they would still weigh 30 %
-// after 120 steps).
+// or during a warm-up of w steps min(decay, (1 + k) / (w + k)), so the average follows the early
+// training instead of keeping the initial weights' share (at decay 0.99 they still weigh 30 % after
+// 120 steps). The warm-up is off by default.
 float ema_decay_at(const arc_ctx* c, uint32_t k) {
     if (c->nrc_ema_warmup == 0u) return c->nrc_ema_decay;
     return std::min(c->nrc_ema_decay, (1.0f + (float)k) / ((float)c->nrc_ema_warmup + (float)k));

@@ -95,6 +95,10 @@ struct RayState {
     // current voxel, and whether the head of the outer loop still has to run at this voxel
     uint4 node;
     uint32_t nshift, min_shift, have_node;
+    // kFeatPrecomp only: the ray class's step budget and LOD thresholds, and -vo * inv, computed once per ray
+    uint32_t max_steps, lod_step, lod_shift;
+    float lod_t, lod_t2;
+    f3 noi;
 };
 
 // Traversal variants (the features field of arc_launch_config); every variant makes the same DDA
@@ -102,6 +106,7 @@ struct RayState {
 constexpr int kFeatWarpFetch = 1;   // lanes that descend into the same node fetch it once per warp
 constexpr int kFeatNodeVisit = 2;   // one node evaluation per loop iteration instead of a descent loop
 constexpr int kFeatTopTable = 8;    // chunk roots and their level-1 children from a table staged in shared memory
+constexpr int kFeatPrecomp = 32;    // step budget, LOD thresholds and -origin/dir of the ray computed once per ray
 
 __device__ __forceinline__ float noi_x(const RayState& s) { return -s.vo.x * s.inv.x; }
 __device__ __forceinline__ float noi_y(const RayState& s) { return -s.vo.y * s.inv.y; }
@@ -180,6 +185,33 @@ __device__ __forceinline__ bool ray_begin(RayState& s, const arc_camera_uniforms
     return true;
 }
 
+// The per-step quantities of the ray class that do not change along the ray (kFeatPrecomp): the step
+// budget, the LOD floor's thresholds, min_shift = (t > lod_t || step > lod_step) ? lod_shift
+// : (t > lod_t2 ? 2 : 0), and -vo * inv. The products are the ones ray_advance forms every step, so
+// the decisions are unchanged.
+__device__ __forceinline__ void ray_precompute(RayState& s, const arc_camera_uniforms& cam) {
+    const uint32_t lod_bias = s.mode & 3u;
+    s.max_steps = max_steps_of(cam, s.mode);
+    if (lod_bias == 0u) {
+        s.lod_t = cam.lod_settings[0] * ARC_VOXELS_PER_METER;
+        s.lod_step = cam.quality_flags[0];
+        s.lod_shift = 2u;
+        s.lod_t2 = __uint_as_float(0x7F800000u);  // +inf: no second threshold
+    } else if (lod_bias == 1u) {
+        const float sec_t = cam.lod_settings[1] * ARC_VOXELS_PER_METER;
+        s.lod_t = sec_t * 2.2857f;
+        s.lod_step = cam.quality_flags[1];
+        s.lod_shift = 4u;
+        s.lod_t2 = sec_t;
+    } else {
+        s.lod_t = cam.lod_settings[2] * ARC_VOXELS_PER_METER;
+        s.lod_step = (cam.quality_flags[3] >> 16) & 0xFFu;
+        s.lod_shift = 2u;
+        s.lod_t2 = __uint_as_float(0x7F800000u);
+    }
+    s.noi = f3{noi_x(s), noi_y(s), noi_z(s)};
+}
+
 __device__ __forceinline__ uint32_t lane_id() {
     uint32_t l;
     asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
@@ -206,13 +238,15 @@ __device__ __forceinline__ uint4 fetch_node(const World& w, uint32_t idx) {
     }
 }
 
-// step_dda_box (traversal64.wgsl:152-179) over the box [bmin, bmin + span)^3.
+// step_dda_box (traversal64.wgsl:152-179) over the box [bmin, bmin + span)^3. PRE: -vo * inv from the
+// ray state (ray_precompute) instead of formed here; the same bits either way.
+template <bool PRE = false>
 __device__ __forceinline__ void step_box(RayState& s, uint32_t bx, uint32_t by, uint32_t bz, uint32_t span) {
     const bool pxd = s.inv.x >= 0.0f, pyd = s.inv.y >= 0.0f, pzd = s.inv.z >= 0.0f;
     uint32_t ex = pxd ? bx + span : bx, ey = pyd ? by + span : by, ez = pzd ? bz + span : bz;
-    float tx = (float)ex * s.inv.x + noi_x(s);
-    float ty = (float)ey * s.inv.y + noi_y(s);
-    float tz = (float)ez * s.inv.z + noi_z(s);
+    float tx = (float)ex * s.inv.x + (PRE ? s.noi.x : noi_x(s));
+    float ty = (float)ey * s.inv.y + (PRE ? s.noi.y : noi_y(s));
+    float tz = (float)ez * s.inv.z + (PRE ? s.noi.z : noi_z(s));
     float t_exit = fminf(fminf(tx, ty), tz);
     float next_t = fmaxf(s.t, t_exit);
     bool is_x = tx <= ty && tx <= tz;
@@ -329,7 +363,11 @@ struct TopView {
 template <int FEAT = 0>
 __device__ __forceinline__ StepResult ray_advance(RayState& s, const World& w, const arc_camera_uniforms& cam,
                                                   HitInfo& h, const TopView top = TopView{nullptr, nullptr}) {
-    if (s.step >= max_steps_of(cam, s.mode)) return kMiss;
+    if constexpr ((FEAT & kFeatPrecomp) != 0) {
+        if (s.step >= s.max_steps) return kMiss;
+    } else {
+        if (s.step >= max_steps_of(cam, s.mode)) return kMiss;
+    }
     if (s.t >= s.t_limit) return kMiss;
     const uint32_t gx = cam.world_grid_dims[0], gy = cam.world_grid_dims[1], gz = cam.world_grid_dims[2];
     if (s.vx >= (gx << 8) || s.vy >= (gy << 8) || s.vz >= (gz << 8)) return kMiss;
@@ -356,7 +394,9 @@ __device__ __forceinline__ StepResult ray_advance(RayState& s, const World& w, c
         const uint32_t lod_bias = s.mode & 3u;
         const bool ignore_water = (s.mode & 4u) != 0u;
         uint32_t min_shift = 0u;
-        if (lod_bias == 0u) {
+        if constexpr ((FEAT & kFeatPrecomp) != 0) {
+            min_shift = (s.t > s.lod_t || s.step > s.lod_step) ? s.lod_shift : (s.t > s.lod_t2 ? 2u : 0u);
+        } else if (lod_bias == 0u) {
             if (s.t > cam.lod_settings[0] * ARC_VOXELS_PER_METER || s.step > cam.quality_flags[0]) min_shift = 2u;
         } else if (lod_bias == 1u) {
             const float sec_t = cam.lod_settings[1] * ARC_VOXELS_PER_METER;
@@ -422,7 +462,7 @@ __device__ __forceinline__ StepResult ray_advance(RayState& s, const World& w, c
             else if (shift == 0u) s.l3 = node;
         }
     }
-    step_box(s, s.vx & ~(span - 1u), s.vy & ~(span - 1u), s.vz & ~(span - 1u), span);
+    step_box<(FEAT & kFeatPrecomp) != 0>(s, s.vx & ~(span - 1u), s.vy & ~(span - 1u), s.vz & ~(span - 1u), span);
     s.step++;
     return kContinue;
 }

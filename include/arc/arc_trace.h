@@ -82,6 +82,8 @@ typedef struct arc_launch_config {
                                    read from the pool) in shared memory once */
 #define ARC_FEAT_GRID_STRIDE 16u /* the same resident-CTA primary kernel without the staged table (the
                                     control of ARC_FEAT_TOP_TABLE) */
+#define ARC_FEAT_PRECOMP 32u     /* the ray class's step budget, LOD thresholds and -origin/dir computed once per
+                                    ray instead of every DDA step (alone, not combined with other bits) */
 
 typedef struct arc_stats {
     float last_kernel_ms;      /* device time of the last traversal launch (CUDA events) */
@@ -332,7 +334,9 @@ int arc_nrc_get_weights(arc_ctx* ctx, float* weights);
 int arc_nrc_set_ema_decay(arc_ctx* ctx, float decay);
 /* Warm-up of that average: at Adam step k after init / set_weights the decay is
  * min(decay, (1 + k) / (steps + k)), so early in training the average follows the weights closely
- * (default steps = 10; 0 = the fixed decay from the first step). */
+ * (default 0 = the fixed decay from the first step: on the cache comparison, the average that starts
+ * from the initial weights scores better over the first 30 frames than one that follows the early
+ * weights). */
 int arc_nrc_set_ema_warmup(arc_ctx* ctx, uint32_t steps);
 /* on = 1: queries return max(network output, 0) per channel (radiance is not negative); 0 (default) =
  * the network output as it is. Training is unaffected. */

@@ -104,8 +104,8 @@ def test_frame_c2_1024_caves_full(orc, tracer, world_cache, quality, native_lib)
     primary hit record and GI hit record of all 2,073,600 pixels, bit-exact against the oracle for both
     kernel variants (plain kernel + GI pass, persistent queue kernel) and the plain kernel's traversal
     variants (Morton block order, one node per loop iteration, warp-shared node fetch, GI rays sorted over
-    the whole frame, resident CTAs with and without the top tree levels staged in shared memory), in
-    parity mode
+    the whole frame, resident CTAs with and without the top tree levels staged in shared memory,
+    per-ray constants computed once), in parity mode
     (up to 512 steps, LOD out of reach) and with the high_quality preset (LOD on)."""
     native_lib_feat = native_lib
     w = world_cache("c2_1024_caves")
@@ -123,7 +123,8 @@ def test_frame_c2_1024_caves_full(orc, tracer, world_cache, quality, native_lib)
                     reg_blocks=2, block_threads=64),
                dict(variant=0, order=1, features=native_lib_feat.ARC_FEAT_GI_SORT, reg_blocks=3, block_threads=128),
                dict(variant=0, order=1, features=native_lib_feat.ARC_FEAT_TOP_TABLE, reg_blocks=3, block_threads=256),
-               dict(variant=0, order=0, features=native_lib_feat.ARC_FEAT_GRID_STRIDE, reg_blocks=2, block_threads=128)]
+               dict(variant=0, order=0, features=native_lib_feat.ARC_FEAT_GRID_STRIDE, reg_blocks=2, block_threads=128),
+               dict(variant=0, order=1, features=native_lib_feat.ARC_FEAT_PRECOMP, reg_blocks=3, block_threads=64)]
     for cfg in configs:
         tracer.set_launch_config(**cfg)
         gdm, gnm, gaa, hits, gi, n_gi = tracer.trace_frame()

@@ -244,7 +244,7 @@ def test_gpu_weight_ema_feeds_inference(orc, tracer):
         assert lib().arc_nrc_set_ema_decay(tracer.ctx, 1.0) != 0  # outside [0, 1)
     finally:
         assert lib().arc_nrc_set_ema_decay(tracer.ctx, 0.99) == 0
-        assert lib().arc_nrc_set_ema_warmup(tracer.ctx, 10) == 0
+        assert lib().arc_nrc_set_ema_warmup(tracer.ctx, 0) == 0
 
 
 @pytest.mark.gpu
