@@ -455,7 +455,9 @@ __global__ void pack_kernel(const float* __restrict__ w, __half* __restrict__ w1
 // CTA through one bulk copy. The A buffer (28 KB) holds half of the 224 encoded features or one hidden
 // layer, so layer 1 runs as two accumulating passes; two CTAs fit on an SM.
 constexpr int kTcA = 128 * 112;  // halves
-constexpr uint32_t kTcSmem = kUHalves * 2 + kTcA * 2 + 64;
+constexpr uint32_t kTcSmem = kUHalves * 2 + kTcA * 2 + 64;          // one tile group
+constexpr int kTcGroups = 4;                                       // tile groups of the default kernel
+constexpr uint32_t kTcSmemG = kUHalves * 2 + kTcGroups * kTcA * 2 + 64;
 constexpr long long kTcBudget = 2000000000ll;  // cycles (about one second) per wait
 // A kernel whose wait ran out sets bit 31 of the status word, stops issuing work, and before it frees
 // TMEM and returns waits (with the full budget again) for what it still has in flight: the weight copy
@@ -487,48 +489,64 @@ __device__ __forceinline__ void st_chunk(uint8_t* sa, int kbc, int m, int lc, ui
     *reinterpret_cast<uint4*>(sa + 2 * ((m >> 3) * kbc * 64 + lc * 64 + (m & 7) * 8)) = v;
 }
 
-__global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restrict__ wu, const float* __restrict__ in,
-                                                          const float* __restrict__ albedo, uint32_t n,
-                                                          float* __restrict__ out, const uint32_t* __restrict__ list,
-                                                          const unsigned long long* __restrict__ n_dev,
-                                                          uint32_t* __restrict__ status, long long budget,
-                                                          uint32_t stall, uint32_t clamp) {
+// OR of `v` over the 128 threads of tile group `id - 1` (named barrier `id`; id 0 is __syncthreads).
+__device__ __forceinline__ bool group_sync_or(uint32_t id, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, %2, 128, p;\n\tselp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(id)
+        : "memory");
+    return r != 0u;
+}
+
+// Tensor-core inference with G tile groups per CTA: the CTA holds the weights once and G groups of
+// four warps each run their own 128-query tiles (own A buffer, TMEM columns 128 g .. 128 g + 79,
+// mbarrier and named barrier), so while one group waits on its MMA chain or its input loads another
+// encodes or stores. G = 4 keeps four tiles in flight per SM (weights 63.5 KB + 4 x 28 KB of A
+// buffers); G = 1 is the single-tile kernel, two CTAs per SM.
+template <int G>
+__global__ void __launch_bounds__(128 * G, G == 1 ? 2 : 1) infer_tc_kernel(
+    const __half* __restrict__ wu, const float* __restrict__ in, const float* __restrict__ albedo, uint32_t n,
+    float* __restrict__ out, const uint32_t* __restrict__ list, const unsigned long long* __restrict__ n_dev,
+    uint32_t* __restrict__ status, long long budget, uint32_t stall, uint32_t clamp) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
+    const uint32_t g = threadIdx.x >> 7, tid = threadIdx.x & 127u, warp = tid >> 5;
     uint8_t* sw = smem_raw;
-    uint8_t* sa = smem_raw + kUHalves * 2;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + kUHalves * 2 + kTcA * 2);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
+    uint8_t* sa = smem_raw + kUHalves * 2 + (size_t)g * kTcA * 2;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + kUHalves * 2 + (size_t)G * kTcA * 2);  // bar_w, bar_m[G]
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 1 + G);
     if (n_dev) {
         const unsigned long long nd = *n_dev;
         n = nd < n ? (uint32_t)nd : n;
     }
     const uint32_t tiles = (n + 127u) / 128u;
-    if (blockIdx.x >= tiles) return;  // uniform over the CTA, before any TMEM allocation
-    const uint32_t tid = threadIdx.x, warp = tid >> 5;
-    const uint32_t bar_w = tc::smem_u32(&bars[0]), bar_m = tc::smem_u32(&bars[1]);
+    if (blockIdx.x * G >= tiles) return;  // uniform over the CTA, before any TMEM allocation
+    const uint32_t bar_w = tc::smem_u32(&bars[0]), bar_m = tc::smem_u32(&bars[1 + g]);
     const uint32_t sa_u = tc::smem_u32(sa), sw_u = tc::smem_u32(sw);
-    if (tid == 0) {
+    if (threadIdx.x == 0) {
         tc::mbar_init(bar_w, 1);
-        tc::mbar_init(bar_m, 1);
+        for (int i = 0; i < G; ++i) tc::mbar_init(tc::smem_u32(&bars[1 + i]), 1);
         tc::fence_mbar_init();
     }
-    if (warp == 0) {
-        tc::tmem_alloc(tc::smem_u32(tslot), 128);
+    if (threadIdx.x < 32) {
+        tc::tmem_alloc(tc::smem_u32(tslot), G == 1 ? 128u : (G == 2 ? 256u : 512u));
         tc::tmem_relinquish();
     }
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = *tslot;
-    const uint32_t d_hid = tmem, d_out = tmem + 64u, lane_off = (warp * 32u) << 16;
-    if (tid == 0) {
+    const uint32_t d_hid = tmem + 128u * g, d_out = d_hid + 64u, lane_off = (warp * 32u) << 16;
+    if (threadIdx.x == 0) {
         tc::mbar_expect_tx(bar_w, kUHalves * 2);
         if (!stall) tc::bulk_g2s(sw_u, wu, kUHalves * 2, bar_w);
     }
     bool ok = tc::mbar_wait(bar_w, 0, budget);
     bool fail = __syncthreads_or(!ok);
     uint32_t phase = 0;
-    bool mma_pending = false;  // thread 0: a committed MMA batch whose completion it has not seen
+    bool mma_pending = false;  // group leader: a committed MMA batch whose completion it has not seen
+    auto gsync = [&](bool v) { return G == 1 ? (__syncthreads_or(v) != 0) : group_sync_or(1u + g, v); };
     constexpr uint32_t kId64 = tc::idesc_f16(128, 64, false, false), kId16 = tc::idesc_f16(128, 16, false, false);
     // one MMA pass: D (+)= A[sa] * W^T, `steps` K-steps; A has a_sbo bytes per 8-row group
     auto issue = [&](uint32_t d, uint32_t w_byte, uint32_t w_sbo, uint32_t a_sbo, int steps, uint32_t idesc, bool acc) {
@@ -547,7 +565,7 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
         }
         tc::fence_after();
     };
-    // inputs (and albedo) of the CTA's first tile; each iteration then fetches the next tile's before
+    // inputs (and albedo) of the group's first tile; each iteration then fetches the next tile's before
     // its MMA chain
     float vn[kIn], an[kOut];
     uint32_t pn = 0u;
@@ -561,8 +579,9 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
 #pragma unroll
         for (int c = 0; c < kOut; ++c) an[c] = valid_n && albedo ? __ldg(&albedo[(size_t)pn * 3 + c]) : 1.0f;
     };
-    fetch(blockIdx.x);
-    for (uint32_t tile = blockIdx.x; !fail && tile < tiles; tile += gridDim.x) {
+    const uint32_t first = blockIdx.x * G + g, stride = gridDim.x * G;
+    fetch(first);
+    for (uint32_t tile = first; !fail && tile < tiles; tile += stride) {
         const bool valid = valid_n;
         const uint32_t p = pn;
         float v[kIn], a[kOut];
@@ -570,7 +589,7 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
         for (int i = 0; i < kIn; ++i) v[i] = vn[i];
 #pragma unroll
         for (int c = 0; c < kOut; ++c) a[c] = an[c];
-        fetch(tile + gridDim.x);
+        fetch(tile + stride);
         // layer 1, first half: features 0..111 = inputs 0..3 and the first 16 features of input 4
         uint32_t h[12];
         uint4 keep;
@@ -586,10 +605,10 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
         }
         tc::fence_async_smem();
         tc::fence_before();
-        if ((fail = __syncthreads_or(!ok))) break;
+        if ((fail = gsync(!ok))) break;
         issue(d_hid, 2u * u_off(1), 3584u, 1792u, 7, kId64, false);
         // second half: features 112..223 (the rest of input 4, inputs 5..8, 8 zero features)
-        if ((fail = __syncthreads_or(!ok))) break;
+        if ((fail = gsync(!ok))) break;
         st_chunk(sa, 14, tid, 0, keep);
 #pragma unroll
         for (int i = 5; i < kIn; ++i) {
@@ -601,7 +620,7 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
         st_chunk(sa, 14, tid, 13, make_uint4(0u, 0u, 0u, 0u));
         tc::fence_async_smem();
         tc::fence_before();
-        if ((fail = __syncthreads_or(!ok))) break;
+        if ((fail = gsync(!ok))) break;
         issue(d_hid, 2u * u_off(1) + 14u * 128u, 3584u, 1792u, 7, kId64, true);
         // layers 2..6: ReLU of the accumulator -> FP16 A operand -> next MMA
         for (int l = 2; l <= 6 && !fail; ++l) {
@@ -623,10 +642,10 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
             }
             tc::fence_async_smem();
             tc::fence_before();
-            if ((fail = __syncthreads_or(!ok))) break;
+            if ((fail = gsync(!ok))) break;
             issue(l < 6 ? d_hid : d_out, 2u * u_off(l), 1024u, 1024u, 4, l < 6 ? kId64 : kId16, false);
         }
-        if ((fail = __syncthreads_or(!ok))) break;
+        if ((fail = gsync(!ok))) break;
         uint32_t y[16];
         tc::tmem_ld16(d_out + lane_off, y);
         tc::tmem_wait_ld();
@@ -648,7 +667,7 @@ __global__ void __launch_bounds__(128, 2) infer_tc_kernel(const __half* __restri
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
-    if (warp == 0) tc::tmem_dealloc(tmem, 128);
+    if (threadIdx.x < 32) tc::tmem_dealloc(tmem, G == 1 ? 128u : (G == 2 ? 256u : 512u));
 }
 
 // ---- tcgen05 training -----------------------------------------------------------------------------
@@ -955,7 +974,9 @@ int ensure_nrc(arc_ctx* c) {
     NRC_CK(cudaMemsetAsync(c->d_nrc_wu_ema, 0, sizeof(__half) * nrc::kUHalves, c->stream));
     NRC_CK(cudaMemsetAsync(c->d_nrc_wu, 0, sizeof(__half) * nrc::kUHalves, c->stream));
     NRC_CK(cudaFuncSetAttribute(nrc::train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nrc::kTtSmem));
-    NRC_CK(cudaFuncSetAttribute(nrc::infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nrc::kTcSmem));
+    NRC_CK(cudaFuncSetAttribute(nrc::infer_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nrc::kTcSmem));
+    NRC_CK(cudaFuncSetAttribute(nrc::infer_tc_kernel<nrc::kTcGroups>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)nrc::kTcSmemG));
     NRC_CK(cudaFuncSetAttribute(nrc::infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 nrc::kFwdHalves * (int)sizeof(__half)));
     NRC_CK(cudaFuncSetAttribute(nrc::train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -989,12 +1010,20 @@ long long tc_budget(const arc_ctx* c) { return c->tc_wait_budget > 0 ? c->tc_wai
 
 int launch_infer(arc_ctx* c, const float* inputs, const float* albedo, uint32_t n, float* out, const uint32_t* list,
                  const unsigned long long* n_dev) {
-    if (c->nrc_infer_path == 1) {
+    const __half* wu = static_cast<const __half*>(c->d_nrc_wu_ema);
+    if (c->nrc_infer_path == 1) {  // four tile groups per CTA, one CTA per SM
+        const uint32_t tiles = (n + 127u) / 128u;
+        const uint32_t blocks = std::min<uint32_t>((tiles + nrc::kTcGroups - 1u) / nrc::kTcGroups, (uint32_t)c->n_sm);
+        nrc::infer_tc_kernel<nrc::kTcGroups><<<blocks, 128 * nrc::kTcGroups, nrc::kTcSmemG, c->stream>>>(
+            wu, inputs, albedo, n, out, list, n_dev, c->d_status, tc_budget(c), c->tc_stall ? 1u : 0u, c->nrc_clamp ? 1u : 0u);
+        NRC_CK(cudaGetLastError());
+        return ARC_OK;
+    }
+    if (c->nrc_infer_path == 2) {  // one tile group per CTA, two CTAs per SM
         const uint32_t blocks = std::min<uint32_t>((n + 127u) / 128u, (uint32_t)c->n_sm * 2u);
-        nrc::infer_tc_kernel<<<blocks, 128, nrc::kTcSmem, c->stream>>>(static_cast<const __half*>(c->d_nrc_wu_ema), inputs,
-                                                                        albedo, n, out, list, n_dev, c->d_status,
-                                                                        tc_budget(c), c->tc_stall ? 1u : 0u,
-                                                                        c->nrc_clamp ? 1u : 0u);
+        nrc::infer_tc_kernel<1><<<blocks, 128, nrc::kTcSmem, c->stream>>>(wu, inputs, albedo, n, out, list, n_dev, c->d_status,
+                                                                           tc_budget(c), c->tc_stall ? 1u : 0u,
+                                                                           c->nrc_clamp ? 1u : 0u);
         NRC_CK(cudaGetLastError());
         return ARC_OK;
     }
@@ -1099,7 +1128,7 @@ int arc_nrc_get_ema_weights(arc_ctx* c, float* w) {
 }
 
 int arc_nrc_set_infer_path(arc_ctx* c, int path) {
-    if (!c || (path != 0 && path != 1)) return ARC_E_INVALID_ARG;
+    if (!c || path < 0 || path > 2) return ARC_E_INVALID_ARG;
     c->nrc_infer_path = path;
     return ARC_OK;
 }

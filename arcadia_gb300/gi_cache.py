@@ -271,9 +271,11 @@ def kernel_timing(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920,
                                                           TRAIN_SAMPLES, steps, C.c_float(1e-3)), "train")
 
     out = {"gi_hits": n_hits, "train_samples": TRAIN_SAMPLES, "flops_per_query": NRC_FLOPS_PER_QUERY}
-    for name, path in (("tcgen05", 1), ("mma_sync", 0)):
+    # tcgen05 inference with four tile groups per CTA (the default), with one group (two CTAs per SM),
+    # and the mma.sync kernels
+    for name, path in (("tcgen05", 1), ("tcgen05_one_group", 2), ("mma_sync", 0)):
         cc._ck(lib.arc_nrc_set_infer_path(tracer.ctx, path), "path")
-        cc._ck(lib.arc_nrc_set_train_path(tracer.ctx, path), "path")
+        cc._ck(lib.arc_nrc_set_train_path(tracer.ctx, min(path, 1)), "path")
         q = timed(query)
         t1, t8 = timed(train(1)), timed(train(8))
         out[name] = {"query_ms": round(q, 4), "query_tflops": round(n_hits * NRC_FLOPS_PER_QUERY / (q * 1e-3) / 1e12, 1),

@@ -260,7 +260,7 @@ def test_gpu_tcgen05_and_mma_sync_inference_agree(orc, tracer):
     dx = torch.from_numpy(x).cuda()
     outs = []
     try:
-        for path in (1, 0):
+        for path in (1, 0, 2):  # tcgen05 with four tile groups per CTA, mma.sync, tcgen05 with one group
             assert lib().arc_nrc_set_infer_path(tracer.ctx, path) == 0
             dy = torch.zeros((len(x), 3), dtype=torch.float32, device="cuda")
             assert lib().arc_nrc_query_dev(tracer.ctx, dx.data_ptr(), None, len(x), dy.data_ptr()) == 0
@@ -270,6 +270,7 @@ def test_gpu_tcgen05_and_mma_sync_inference_agree(orc, tracer):
         for y in outs:
             assert np.all(np.abs(y[:4096] - ref) <= 2e-2 * np.abs(ref) + 2e-3), np.max(np.abs(y[:4096] - ref))
         assert np.max(np.abs(outs[0] - outs[1])) <= 1e-2 * np.max(np.abs(outs[1])) + 1e-3
+        np.testing.assert_array_equal(outs[0], outs[2])  # the same MMAs per tile: identical bits
         # compacted list on the tcgen05 path: every third point, in reverse order
         assert lib().arc_nrc_set_infer_path(tracer.ctx, 1) == 0
         idx = np.arange(len(x) - 1, -1, -3, dtype=np.int32)
