@@ -502,9 +502,10 @@ __device__ __forceinline__ bool group_sync_or(uint32_t id, bool v) {
 
 // Tensor-core inference with G tile groups per CTA: the CTA holds the weights once and G groups of
 // four warps each run their own 128-query tiles (own A buffer, TMEM columns 128 g .. 128 g + 79,
-// mbarrier and named barrier), so while one group waits on its MMA chain or its input loads another
-// encodes or stores. G = 4 keeps four tiles in flight per SM (weights 63.5 KB + 4 x 28 KB of A
-// buffers); G = 1 is the single-tile kernel, two CTAs per SM.
+// mbarrier and named barrier). G = 1 (the default) is the single-tile kernel, two CTAs per SM. G = 4
+// keeps four tiles in flight per SM (weights 63.5 KB + 4 x 28 KB of A buffers) but measured 7 %
+// slower on a 1080p hit list (0.0547 against 0.0513 ms), and its one CTA per SM no longer shares the
+// SMs with the training-sample kernel when the query runs beside it.
 template <int G>
 __global__ void __launch_bounds__(128 * G, G == 1 ? 2 : 1) infer_tc_kernel(
     const __half* __restrict__ wu, const float* __restrict__ in, const float* __restrict__ albedo, uint32_t n,
@@ -1011,7 +1012,7 @@ long long tc_budget(const arc_ctx* c) { return c->tc_wait_budget > 0 ? c->tc_wai
 int launch_infer(arc_ctx* c, const float* inputs, const float* albedo, uint32_t n, float* out, const uint32_t* list,
                  const unsigned long long* n_dev) {
     const __half* wu = static_cast<const __half*>(c->d_nrc_wu_ema);
-    if (c->nrc_infer_path == 1) {  // four tile groups per CTA, one CTA per SM
+    if (c->nrc_infer_path == 2) {  // four tile groups per CTA, one CTA per SM
         const uint32_t tiles = (n + 127u) / 128u;
         const uint32_t blocks = std::min<uint32_t>((tiles + nrc::kTcGroups - 1u) / nrc::kTcGroups, (uint32_t)c->n_sm);
         nrc::infer_tc_kernel<nrc::kTcGroups><<<blocks, 128 * nrc::kTcGroups, nrc::kTcSmemG, c->stream>>>(
@@ -1019,7 +1020,7 @@ int launch_infer(arc_ctx* c, const float* inputs, const float* albedo, uint32_t 
         NRC_CK(cudaGetLastError());
         return ARC_OK;
     }
-    if (c->nrc_infer_path == 2) {  // one tile group per CTA, two CTAs per SM
+    if (c->nrc_infer_path == 1) {  // one tile group per CTA, two CTAs per SM
         const uint32_t blocks = std::min<uint32_t>((n + 127u) / 128u, (uint32_t)c->n_sm * 2u);
         nrc::infer_tc_kernel<1><<<blocks, 128, nrc::kTcSmem, c->stream>>>(wu, inputs, albedo, n, out, list, n_dev, c->d_status,
                                                                            tc_budget(c), c->tc_stall ? 1u : 0u,

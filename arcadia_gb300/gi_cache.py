@@ -271,9 +271,9 @@ def kernel_timing(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920,
                                                           TRAIN_SAMPLES, steps, C.c_float(1e-3)), "train")
 
     out = {"gi_hits": n_hits, "train_samples": TRAIN_SAMPLES, "flops_per_query": NRC_FLOPS_PER_QUERY}
-    # tcgen05 inference with four tile groups per CTA (the default), with one group (two CTAs per SM),
-    # and the mma.sync kernels
-    for name, path in (("tcgen05", 1), ("tcgen05_one_group", 2), ("mma_sync", 0)):
+    # tcgen05 inference with one tile group per CTA (the default, two CTAs per SM), with four groups in
+    # one CTA per SM, and the mma.sync kernels
+    for name, path in (("tcgen05", 1), ("tcgen05_four_groups", 2), ("mma_sync", 0)):
         cc._ck(lib.arc_nrc_set_infer_path(tracer.ctx, path), "path")
         cc._ck(lib.arc_nrc_set_train_path(tracer.ctx, min(path, 1)), "path")
         q = timed(query)

@@ -343,9 +343,9 @@ int arc_nrc_set_ema_warmup(arc_ctx* ctx, uint32_t steps);
 int arc_nrc_set_output_clamp(arc_ctx* ctx, int on);
 /* Adam's moment decays (default beta1 0.9, beta2 0.99; both in [0, 1)). */
 int arc_nrc_set_adam_betas(arc_ctx* ctx, float beta1, float beta2);
-/* Inference kernel: 1 = tcgen05 tensor cores with TMEM accumulators, four 128-query tile groups per
- * CTA (default); 2 = the same with one tile group per CTA (two CTAs per SM); 0 = the warp-level
- * mma.sync kernel (kept as the comparison point). */
+/* Inference kernel: 1 = tcgen05 tensor cores with TMEM accumulators, one 128-query tile per CTA and
+ * two CTAs per SM (default); 2 = the same with four tile groups in one CTA per SM (measured slower);
+ * 0 = the warp-level mma.sync kernel (kept as the comparison point). */
 int arc_nrc_set_infer_path(arc_ctx* ctx, int path);
 /* Training kernel (gradients): 1 = tcgen05 (default), 0 = the mma.sync kernel. */
 int arc_nrc_set_train_path(arc_ctx* ctx, int path);

@@ -260,7 +260,7 @@ def test_gpu_tcgen05_and_mma_sync_inference_agree(orc, tracer):
     dx = torch.from_numpy(x).cuda()
     outs = []
     try:
-        for path in (1, 0, 2):  # tcgen05 with four tile groups per CTA, mma.sync, tcgen05 with one group
+        for path in (1, 0, 2):  # tcgen05 one tile group per CTA, mma.sync, tcgen05 four groups per CTA
             assert lib().arc_nrc_set_infer_path(tracer.ctx, path) == 0
             dy = torch.zeros((len(x), 3), dtype=torch.float32, device="cuda")
             assert lib().arc_nrc_query_dev(tracer.ctx, dx.data_ptr(), None, len(x), dy.data_ptr()) == 0
