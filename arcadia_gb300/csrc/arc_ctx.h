@@ -90,6 +90,7 @@ struct arc_ctx {
     uint32_t nrc_ema_warmup = 0;      // EMA warm-up: decay min(nrc_ema_decay, (1 + k) / (warmup + k)); 0 = off
     bool nrc_clamp = false;           // queries return max(output, 0)
     float nrc_beta1 = 0.9f, nrc_beta2 = 0.99f;  // Adam moment decays
+    bool nrc_pdl = true;              // NRC kernels launched with programmatic dependent launch
     float* d_nrc_loss = nullptr;
     uint32_t nrc_step = 0;
     // in-place edits: device counters [next node, next brick, bricks rewritten, overflow] and staging

@@ -29,6 +29,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "arc_ctx.h"
@@ -401,6 +402,8 @@ __global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float*
                             __half* __restrict__ w16_ema, __half* __restrict__ wu, __half* __restrict__ wu_ema, float decay,
                             float lr, float c1, float c2, float inv_scale, const uint32_t* __restrict__ gate, float b1,
                             float b2) {
+    tc::pdl_wait();  // the gradient of the training kernel ahead
+    tc::pdl_trigger();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams || (gate && *gate == 0u)) return;
     const float eps = 1e-8f;
@@ -517,6 +520,7 @@ __global__ void __launch_bounds__(128 * G, G == 1 ? 2 : 1) infer_tc_kernel(
     uint8_t* sa = smem_raw + kUHalves * 2 + (size_t)g * kTcA * 2;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + kUHalves * 2 + (size_t)G * kTcA * 2);  // bar_w, bar_m[G]
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 1 + G);
+    tc::pdl_wait();  // the weight average of the Adam step ahead, the hit list of the kernel ahead
     if (n_dev) {
         const unsigned long long nd = *n_dev;
         n = nd < n ? (uint32_t)nd : n;
@@ -705,6 +709,7 @@ __global__ void __launch_bounds__(128, 1) train_tc_kernel(const __half* __restri
                                                           const uint32_t* __restrict__ gate, uint32_t* __restrict__ status,
                                                           long long budget, uint32_t stall) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
+    tc::pdl_wait();  // the samples (or the weights of the Adam step) of the kernel ahead
     if (gate && *gate == 0u) return;  // empty frame batch (uniform over the grid)
     const uint32_t tiles = (n + 127u) / 128u;
     if (blockIdx.x >= tiles) return;
@@ -897,6 +902,7 @@ __global__ void __launch_bounds__(128, 1) train_tc_kernel(const __half* __restri
         }
         first = false;
     }
+    tc::pdl_trigger();  // the Adam step behind may be scheduled (it waits for this grid to finish)
     if (!fail) fail = __syncthreads_or(!ok);
     if (!fail) {
         // weight gradients out of TMEM (every warp runs the collective loads; lanes pick their rows)
@@ -1007,6 +1013,23 @@ void init_weights(std::vector<float>& w, uint32_t seed) {
     }
 }
 
+// Launch with programmatic stream serialization when the context allows it (the kernel then starts
+// while the one ahead of it finishes, and waits for it with pdl_wait before reading its results).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_k(const arc_ctx* c, void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = c->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = c->nrc_pdl ? 1 : 0;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
+
 long long tc_budget(const arc_ctx* c) { return c->tc_wait_budget > 0 ? c->tc_wait_budget : nrc::kTcBudget; }
 
 int launch_infer(arc_ctx* c, const float* inputs, const float* albedo, uint32_t n, float* out, const uint32_t* list,
@@ -1015,17 +1038,15 @@ int launch_infer(arc_ctx* c, const float* inputs, const float* albedo, uint32_t 
     if (c->nrc_infer_path == 2) {  // four tile groups per CTA, one CTA per SM
         const uint32_t tiles = (n + 127u) / 128u;
         const uint32_t blocks = std::min<uint32_t>((tiles + nrc::kTcGroups - 1u) / nrc::kTcGroups, (uint32_t)c->n_sm);
-        nrc::infer_tc_kernel<nrc::kTcGroups><<<blocks, 128 * nrc::kTcGroups, nrc::kTcSmemG, c->stream>>>(
-            wu, inputs, albedo, n, out, list, n_dev, c->d_status, tc_budget(c), c->tc_stall ? 1u : 0u, c->nrc_clamp ? 1u : 0u);
-        NRC_CK(cudaGetLastError());
+        NRC_CK(launch_k(c, nrc::infer_tc_kernel<nrc::kTcGroups>, dim3(blocks), dim3(128 * nrc::kTcGroups), nrc::kTcSmemG, wu,
+                        inputs, albedo, n, out, list, n_dev, c->d_status, tc_budget(c), c->tc_stall ? 1u : 0u,
+                        c->nrc_clamp ? 1u : 0u));
         return ARC_OK;
     }
     if (c->nrc_infer_path == 1) {  // one tile group per CTA, two CTAs per SM
         const uint32_t blocks = std::min<uint32_t>((n + 127u) / 128u, (uint32_t)c->n_sm * 2u);
-        nrc::infer_tc_kernel<1><<<blocks, 128, nrc::kTcSmem, c->stream>>>(wu, inputs, albedo, n, out, list, n_dev, c->d_status,
-                                                                           tc_budget(c), c->tc_stall ? 1u : 0u,
-                                                                           c->nrc_clamp ? 1u : 0u);
-        NRC_CK(cudaGetLastError());
+        NRC_CK(launch_k(c, nrc::infer_tc_kernel<1>, dim3(blocks), dim3(128), nrc::kTcSmem, wu, inputs, albedo, n, out, list,
+                        n_dev, c->d_status, tc_budget(c), c->tc_stall ? 1u : 0u, c->nrc_clamp ? 1u : 0u));
         return ARC_OK;
     }
     const uint32_t tiles = (n + 15u) / 16u;
@@ -1044,10 +1065,9 @@ int launch_grad(arc_ctx* c, const float* inputs, const float* targets, uint32_t 
     if (want_loss) NRC_CK(cudaMemsetAsync(c->d_nrc_loss, 0, sizeof(float), c->stream));
     if (c->nrc_train_path == 1) {
         const uint32_t blocks = std::min<uint32_t>((n + 127u) / 128u, (uint32_t)c->n_sm);
-        nrc::train_tc_kernel<<<blocks, 128, nrc::kTtSmem, c->stream>>>(static_cast<const __half*>(c->d_nrc_wu), inputs, targets, n,
-                                                                         1.0f / (float)n, c->d_nrc_grad, loss, gate,
-                                                                         c->d_status, tc_budget(c), c->tc_stall ? 1u : 0u);
-        NRC_CK(cudaGetLastError());
+        NRC_CK(launch_k(c, nrc::train_tc_kernel, dim3(blocks), dim3(128), nrc::kTtSmem, static_cast<const __half*>(c->d_nrc_wu),
+                        inputs, targets, n, 1.0f / (float)n, c->d_nrc_grad, loss, gate, c->d_status, tc_budget(c),
+                        c->tc_stall ? 1u : 0u));
         return ARC_OK;
     }
     const uint32_t tiles = (n + 63u) / 64u;
@@ -1071,11 +1091,11 @@ float ema_decay_at(const arc_ctx* c, uint32_t k) {
 int launch_adam(arc_ctx* c, float lr, const uint32_t* gate) {
     c->nrc_step += 1;
     const float c1 = 1.0f - std::pow(c->nrc_beta1, (float)c->nrc_step), c2 = 1.0f - std::pow(c->nrc_beta2, (float)c->nrc_step);
-    nrc::adam_kernel<<<(nrc::kParams + 255) / 256, 256, 0, c->stream>>>(
-        c->d_nrc_w32, c->d_nrc_m, c->d_nrc_v, c->d_nrc_grad, static_cast<__half*>(c->d_nrc_w16), c->d_nrc_ema,
-        static_cast<__half*>(c->d_nrc_w16_ema), static_cast<__half*>(c->d_nrc_wu), static_cast<__half*>(c->d_nrc_wu_ema),
-        ema_decay_at(c, c->nrc_step), lr, c1, c2, 1.0f / nrc::kLossScale, gate, c->nrc_beta1, c->nrc_beta2);
-    NRC_CK(cudaGetLastError());
+    NRC_CK(launch_k(c, nrc::adam_kernel, dim3((nrc::kParams + 255) / 256), dim3(256), 0, c->d_nrc_w32, c->d_nrc_m,
+                    c->d_nrc_v, c->d_nrc_grad, static_cast<__half*>(c->d_nrc_w16), c->d_nrc_ema,
+                    static_cast<__half*>(c->d_nrc_w16_ema), static_cast<__half*>(c->d_nrc_wu),
+                    static_cast<__half*>(c->d_nrc_wu_ema), ema_decay_at(c, c->nrc_step), lr, c1, c2,
+                    1.0f / nrc::kLossScale, gate, c->nrc_beta1, c->nrc_beta2));
     return ARC_OK;
 }
 
@@ -1158,6 +1178,12 @@ int arc_nrc_set_adam_betas(arc_ctx* c, float beta1, float beta2) {
     }
     c->nrc_beta1 = beta1;
     c->nrc_beta2 = beta2;
+    return ARC_OK;
+}
+
+int arc_nrc_set_launch_overlap(arc_ctx* c, int on) {
+    if (!c) return ARC_E_INVALID_ARG;
+    c->nrc_pdl = on != 0;
     return ARC_OK;
 }
 

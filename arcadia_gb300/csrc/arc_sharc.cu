@@ -505,6 +505,7 @@ __global__ void __launch_bounds__(128) train_samples_list_kernel(
         const f3 x{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]}, n{nrm[3 * p], nrm[3 * p + 1], nrm[3 * p + 2]};
         l = part ? onebounce_sky(w, cam, x, n, pcg_hash(i ^ pcg_hash(seed ^ 0xB5297A4Du))) : onebounce_sun(w, cam, x, n);
     }
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");  // the training kernel behind may be scheduled
     const uint32_t k = pair * 32u + lane;
     if (part == 0u) {
         s_sun[k][0] = l.x;

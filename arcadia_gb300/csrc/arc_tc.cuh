@@ -99,4 +99,11 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst_smem, const void* src, uin
                  : "memory");
 }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream serialization may start
+// before the kernel ahead of it in the stream has finished; pdl_wait blocks (in hardware, not a spin)
+// until that kernel has completed and its memory operations are visible, and is a no-op for a kernel
+// launched without the attribute. pdl_trigger lets the kernel behind this one be scheduled early.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 }  // namespace tc
