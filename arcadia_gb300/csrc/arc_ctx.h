@@ -90,7 +90,7 @@ struct arc_ctx {
     uint32_t nrc_ema_warmup = 0;      // EMA warm-up: decay min(nrc_ema_decay, (1 + k) / (warmup + k)); 0 = off
     bool nrc_clamp = false;           // queries return max(output, 0)
     float nrc_beta1 = 0.9f, nrc_beta2 = 0.99f;  // Adam moment decays
-    bool nrc_pdl = true;              // NRC kernels launched with programmatic dependent launch
+    bool cache_pdl = true;            // radiance-cache kernels launched with programmatic dependent launch
     float* d_nrc_loss = nullptr;
     uint32_t nrc_step = 0;
     // in-place edits: device counters [next node, next brick, bricks rewritten, overflow] and staging
@@ -144,6 +144,25 @@ struct arc_ctx {
 
     arc::World world() const;
 };
+
+// Launch on the context's stream with programmatic stream serialization when c->cache_pdl is set: the
+// kernel is scheduled while the kernel ahead of it finishes and waits for it (griddepcontrol.wait,
+// a hardware wait) before it reads that kernel's results.
+template <typename... KArgs, typename... Args>
+cudaError_t arc_launch_overlapped(const arc_ctx* c, void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                                  Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = c->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = c->cache_pdl ? 1 : 0;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, static_cast<Args&&>(args)...);
+}
 
 int arc_ctx_check_ready(arc_ctx* c, bool need_cam);
 int arc_ctx_finish(arc_ctx* c);

@@ -1013,23 +1013,6 @@ void init_weights(std::vector<float>& w, uint32_t seed) {
     }
 }
 
-// Launch with programmatic stream serialization when the context allows it (the kernel then starts
-// while the one ahead of it finishes, and waits for it with pdl_wait before reading its results).
-template <typename... KArgs, typename... Args>
-cudaError_t launch_k(const arc_ctx* c, void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, Args&&... args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = c->stream;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = c->nrc_pdl ? 1 : 0;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
-}
-
 long long tc_budget(const arc_ctx* c) { return c->tc_wait_budget > 0 ? c->tc_wait_budget : nrc::kTcBudget; }
 
 int launch_infer(arc_ctx* c, const float* inputs, const float* albedo, uint32_t n, float* out, const uint32_t* list,
@@ -1038,14 +1021,14 @@ int launch_infer(arc_ctx* c, const float* inputs, const float* albedo, uint32_t 
     if (c->nrc_infer_path == 2) {  // four tile groups per CTA, one CTA per SM
         const uint32_t tiles = (n + 127u) / 128u;
         const uint32_t blocks = std::min<uint32_t>((tiles + nrc::kTcGroups - 1u) / nrc::kTcGroups, (uint32_t)c->n_sm);
-        NRC_CK(launch_k(c, nrc::infer_tc_kernel<nrc::kTcGroups>, dim3(blocks), dim3(128 * nrc::kTcGroups), nrc::kTcSmemG, wu,
+        NRC_CK(arc_launch_overlapped(c, nrc::infer_tc_kernel<nrc::kTcGroups>, dim3(blocks), dim3(128 * nrc::kTcGroups), nrc::kTcSmemG, wu,
                         inputs, albedo, n, out, list, n_dev, c->d_status, tc_budget(c), c->tc_stall ? 1u : 0u,
                         c->nrc_clamp ? 1u : 0u));
         return ARC_OK;
     }
     if (c->nrc_infer_path == 1) {  // one tile group per CTA, two CTAs per SM
         const uint32_t blocks = std::min<uint32_t>((n + 127u) / 128u, (uint32_t)c->n_sm * 2u);
-        NRC_CK(launch_k(c, nrc::infer_tc_kernel<1>, dim3(blocks), dim3(128), nrc::kTcSmem, wu, inputs, albedo, n, out, list,
+        NRC_CK(arc_launch_overlapped(c, nrc::infer_tc_kernel<1>, dim3(blocks), dim3(128), nrc::kTcSmem, wu, inputs, albedo, n, out, list,
                         n_dev, c->d_status, tc_budget(c), c->tc_stall ? 1u : 0u, c->nrc_clamp ? 1u : 0u));
         return ARC_OK;
     }
@@ -1065,7 +1048,7 @@ int launch_grad(arc_ctx* c, const float* inputs, const float* targets, uint32_t 
     if (want_loss) NRC_CK(cudaMemsetAsync(c->d_nrc_loss, 0, sizeof(float), c->stream));
     if (c->nrc_train_path == 1) {
         const uint32_t blocks = std::min<uint32_t>((n + 127u) / 128u, (uint32_t)c->n_sm);
-        NRC_CK(launch_k(c, nrc::train_tc_kernel, dim3(blocks), dim3(128), nrc::kTtSmem, static_cast<const __half*>(c->d_nrc_wu),
+        NRC_CK(arc_launch_overlapped(c, nrc::train_tc_kernel, dim3(blocks), dim3(128), nrc::kTtSmem, static_cast<const __half*>(c->d_nrc_wu),
                         inputs, targets, n, 1.0f / (float)n, c->d_nrc_grad, loss, gate, c->d_status, tc_budget(c),
                         c->tc_stall ? 1u : 0u));
         return ARC_OK;
@@ -1091,7 +1074,7 @@ float ema_decay_at(const arc_ctx* c, uint32_t k) {
 int launch_adam(arc_ctx* c, float lr, const uint32_t* gate) {
     c->nrc_step += 1;
     const float c1 = 1.0f - std::pow(c->nrc_beta1, (float)c->nrc_step), c2 = 1.0f - std::pow(c->nrc_beta2, (float)c->nrc_step);
-    NRC_CK(launch_k(c, nrc::adam_kernel, dim3((nrc::kParams + 255) / 256), dim3(256), 0, c->d_nrc_w32, c->d_nrc_m,
+    NRC_CK(arc_launch_overlapped(c, nrc::adam_kernel, dim3((nrc::kParams + 255) / 256), dim3(256), 0, c->d_nrc_w32, c->d_nrc_m,
                     c->d_nrc_v, c->d_nrc_grad, static_cast<__half*>(c->d_nrc_w16), c->d_nrc_ema,
                     static_cast<__half*>(c->d_nrc_w16_ema), static_cast<__half*>(c->d_nrc_wu),
                     static_cast<__half*>(c->d_nrc_wu_ema), ema_decay_at(c, c->nrc_step), lr, c1, c2,
@@ -1181,9 +1164,9 @@ int arc_nrc_set_adam_betas(arc_ctx* c, float beta1, float beta2) {
     return ARC_OK;
 }
 
-int arc_nrc_set_launch_overlap(arc_ctx* c, int on) {
+int arc_set_cache_launch_overlap(arc_ctx* c, int on) {
     if (!c) return ARC_E_INVALID_ARG;
-    c->nrc_pdl = on != 0;
+    c->cache_pdl = on != 0;
     return ARC_OK;
 }
 

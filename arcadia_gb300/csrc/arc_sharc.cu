@@ -142,6 +142,8 @@ __device__ __forceinline__ f3 onebounce(const World& w, const arc_camera_uniform
 __global__ void sharc_update_kernel(const World w, const __grid_constant__ arc_camera_uniforms cam, const SharcBuffers S,
                                     const uint32_t* __restrict__ gdm, const uint32_t* __restrict__ gnm, uint32_t W,
                                     uint32_t H, uint32_t mode) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // the G-buffer / slots of the kernel ahead
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const uint32_t tile = (cam.quality_flags[3] & 0xFFu) <= 12u ? 16u : 8u;
     const uint32_t tiles_x = (W + tile - 1u) / tile, tiles_y = (H + tile - 1u) / tile;
     const uint32_t gx = blockIdx.x * blockDim.x + threadIdx.x, gy = blockIdx.y * blockDim.y + threadIdx.y;
@@ -217,6 +219,8 @@ __global__ void sharc_update_kernel(const World w, const __grid_constant__ arc_c
 }
 
 __global__ void sharc_resolve_kernel(SharcBuffers S) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // the deposits of the update ahead
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= ARC_SHARC_SLOTS) return;
     const uint32_t key = S.keys[slot];
@@ -530,6 +534,7 @@ __global__ void sharc_query_list_kernel(const uint4* __restrict__ res, const uin
                                         const unsigned long long* __restrict__ n_dev, uint32_t max_n,
                                         const float* __restrict__ pos, const float* __restrict__ nrm, f3 cam,
                                         float4* __restrict__ out) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // the resolved slots / hit list of the kernel ahead
     const unsigned long long nd = *n_dev;
     const uint32_t n = nd < max_n ? (uint32_t)nd : max_n;
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
@@ -595,8 +600,9 @@ int arc_sharc_update_dev(arc_ctx* c, uint32_t width, uint32_t height, const uint
     const uint32_t tile = (c->cam.quality_flags[3] & 0xFFu) <= 12u ? 16u : 8u;
     const uint32_t tx = (width + tile - 1u) / tile, ty = (height + tile - 1u) / tile;
     dim3 block(8, 8), grid((tx + 7u) / 8u, (ty + 7u) / 8u);
-    arc::sharc_update_kernel<<<grid, block, 0, c->stream>>>(c->world(), c->cam, bufs(c), gdm, gnm, width, height,
-                                                            c->sharc_mode);
+    cudaError_t e = arc_launch_overlapped(c, arc::sharc_update_kernel, grid, block, 0, c->world(), c->cam, bufs(c), gdm, gnm,
+                                          width, height, c->sharc_mode);
+    if (e != cudaSuccess) return sharc_err(c, ARC_E_CUDA, std::string("sharc_update_kernel: ") + cudaGetErrorString(e));
     return launch_check(c, "sharc_update_kernel");
 }
 
@@ -673,9 +679,10 @@ int arc_sharc_query_list_dev(arc_ctx* c, const uint32_t* list, const uint64_t* n
     if (rc || max_n == 0) return rc;
     const arc::f3 cam{c->cam.cam_pos_time[0], c->cam.cam_pos_time[1], c->cam.cam_pos_time[2]};
     const uint32_t blocks = std::min<uint32_t>((max_n + 255u) / 256u, (uint32_t)c->n_sm * 8u);
-    arc::sharc_query_list_kernel<<<blocks, 256, 0, c->stream>>>(reinterpret_cast<const uint4*>(c->d_sharc_resolved), list,
+    cudaError_t e = arc_launch_overlapped(c, arc::sharc_query_list_kernel, dim3(blocks), dim3(256), 0, reinterpret_cast<const uint4*>(c->d_sharc_resolved), list,
                                                                 reinterpret_cast<const unsigned long long*>(n_dev), max_n,
                                                                 pos, normal, cam, reinterpret_cast<float4*>(out));
+    if (e != cudaSuccess) return sharc_err(c, ARC_E_CUDA, std::string("sharc_query_list_kernel: ") + cudaGetErrorString(e));
     return launch_check(c, "sharc_query_list_kernel");
 }
 
@@ -694,7 +701,8 @@ int arc_sharc_resolve(arc_ctx* c) {
     if (!c) return ARC_E_INVALID_ARG;
     int rc = ensure_sharc(c);
     if (rc) return rc;
-    arc::sharc_resolve_kernel<<<ARC_SHARC_SLOTS / 256u, 256, 0, c->stream>>>(bufs(c));
+    cudaError_t e = arc_launch_overlapped(c, arc::sharc_resolve_kernel, dim3(ARC_SHARC_SLOTS / 256u), dim3(256), 0, bufs(c));
+    if (e != cudaSuccess) return sharc_err(c, ARC_E_CUDA, std::string("sharc_resolve_kernel: ") + cudaGetErrorString(e));
     return launch_check(c, "sharc_resolve_kernel");
 }
 

@@ -341,10 +341,12 @@ int arc_nrc_set_ema_warmup(arc_ctx* ctx, uint32_t steps);
 /* on = 1: queries return max(network output, 0) per channel (radiance is not negative); 0 (default) =
  * the network output as it is. Training is unaffected. */
 int arc_nrc_set_output_clamp(arc_ctx* ctx, int on);
-/* on = 1 (default): the tcgen05 training kernel, the Adam step and the tcgen05 query are launched with
- * programmatic dependent launch, so each is scheduled while the kernel ahead of it finishes and waits
- * for it in hardware before reading its results; 0 = plain stream order. Results are the same. */
-int arc_nrc_set_launch_overlap(arc_ctx* ctx, int on);
+/* on = 1 (default): the radiance-cache kernels of both caches (NRC tcgen05 training, Adam step and
+ * tcgen05 query; SHARC update, resolve and list query) are launched with programmatic dependent launch,
+ * so each is scheduled while the kernel ahead of it finishes and waits for it in hardware before it
+ * reads that kernel's results; 0 = plain stream order. Results are the same. No counterpart in the
+ * reference. */
+int arc_set_cache_launch_overlap(arc_ctx* ctx, int on);
 /* Adam's moment decays (default beta1 0.9, beta2 0.99; both in [0, 1)). */
 int arc_nrc_set_adam_betas(arc_ctx* ctx, float beta1, float beta2);
 /* Inference kernel: 1 = tcgen05 tensor cores with TMEM accumulators, one 128-query tile per CTA and
