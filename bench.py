@@ -463,7 +463,7 @@ def run_ours(args):
         t.set_launch_config(variant=cfg.variant)
         restir = restir_section(t, scene, W_, H_, dev, (gdm, gnm, gaa, hits, gi))
 
-    # many views over several worlds in one persistent launch replayed from a CUDA graph
+    # many views over several worlds in one call replayed from a CUDA graph (autotuned kernel form)
     batched = None
     if not args.no_batched:
         from arcadia_gb300.batch import BENCH_SCENES, Batch

@@ -206,8 +206,10 @@ int arc_trace_frame_noalloc(arc_ctx* ctx, uint32_t width, uint32_t height, uint3
  * arc_trace_frame_noalloc requires it when the world holds water or mirror voxels or the camera is
  * under water. No counterpart in the reference. */
 int arc_reserve_surface_list(arc_ctx* ctx, uint64_t max_pixels);
-/* Primary + GI rays of many views (several worlds, mixed resolutions) in one persistent launch; with
- * use_graph the launch is captured once into a CUDA graph and replayed (re-captured when the view
+/* Primary + GI rays of many views (several worlds, mixed resolutions) in one call: with the default
+ * launch configuration (variant 0) the batch's primary kernel and its GI pass over every view; with
+ * variant 1 one persistent launch for both (slower in every batch measured, kept for the autotuner).
+ * With use_graph the batch is captured once into a CUDA graph and replayed (re-captured when the view
  * count, n_gi_dev or the launch configuration changes). Outputs per view as arc_trace_frame_dev.
  * No counterpart in the reference (one view per frame there). */
 int arc_trace_views_dev(arc_ctx* ctx, const arc_view_desc* views, uint32_t n_views, uint64_t* n_gi_dev, int use_graph);
