@@ -91,6 +91,7 @@ struct arc_ctx {
     bool nrc_clamp = false;           // queries return max(output, 0)
     float nrc_beta1 = 0.9f, nrc_beta2 = 0.99f;  // Adam moment decays
     bool cache_pdl = true;            // radiance-cache kernels launched with programmatic dependent launch
+    uint32_t nrc_sample_cluster = 1;  // training samples in runs of this many consecutive hit-list entries
     float* d_nrc_loss = nullptr;
     uint32_t nrc_step = 0;
     // in-place edits: device counters [next node, next brick, bricks rewritten, overflow] and staging

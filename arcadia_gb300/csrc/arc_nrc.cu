@@ -1170,6 +1170,16 @@ int arc_set_cache_launch_overlap(arc_ctx* c, int on) {
     return ARC_OK;
 }
 
+int arc_nrc_set_sample_cluster(arc_ctx* c, uint32_t k) {
+    if (!c) return ARC_E_INVALID_ARG;
+    if (k == 0u || k > 32u || (k & (k - 1u))) {
+        c->err = "sample cluster must be 1, 2, 4, 8, 16 or 32";
+        return ARC_E_INVALID_ARG;
+    }
+    c->nrc_sample_cluster = k;
+    return ARC_OK;
+}
+
 int arc_nrc_set_output_clamp(arc_ctx* c, int on) {
     if (!c) return ARC_E_INVALID_ARG;
     c->nrc_clamp = on != 0;

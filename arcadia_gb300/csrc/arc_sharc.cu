@@ -480,9 +480,11 @@ __global__ void onebounce_kernel(const World w, const __grid_constant__ arc_came
     }
 }
 
-// NRC training samples from the compacted GI hit list, stratified: sample i takes list entry
-// floor((i + phase) n_valid / n_samples) (phase in [0, 1) from the seed), so neighbouring samples are
-// neighbouring points (the list is in screen-tile order) and every point is covered evenly. A block of
+// NRC training samples from the compacted GI hit list, stratified: with cluster size 1, sample i takes
+// list entry floor((i n_valid + phase) / n_samples) (phase in [0, n_valid) from the seed), so every
+// point is covered evenly; with cluster size k, samples come in runs of k consecutive list entries
+// (a warp's rays then start from neighbouring points: one warp-aggregated append of the GI-points
+// pass) whose starts are stratified the same way over n_samples / k runs. A block of
 // 4 warps takes 64 samples: warps 0 and 2 trace the sun term of samples 0..31 and 32..63, warps 1 and 3
 // the sky term of the same samples (each warp follows one traversal path), and shared memory sums
 // them. Sample i is stored at slot (i mod steps) * (n_samples / steps) + i / steps, so each of the
@@ -490,8 +492,8 @@ __global__ void onebounce_kernel(const World w, const __grid_constant__ arc_came
 __global__ void __launch_bounds__(128) train_samples_list_kernel(
     const World w, const __grid_constant__ arc_camera_uniforms cam, const uint32_t* __restrict__ list,
     const unsigned long long* __restrict__ n_valid, const float* __restrict__ pos, const float* __restrict__ nrm,
-    const float* __restrict__ nrc_in, uint32_t seed, uint32_t n_samples, uint32_t steps, float* __restrict__ train_in,
-    float* __restrict__ train_t, uint32_t* __restrict__ gate) {
+    const float* __restrict__ nrc_in, uint32_t seed, uint32_t n_samples, uint32_t steps, uint32_t cluster,
+    float* __restrict__ train_in, float* __restrict__ train_t, uint32_t* __restrict__ gate) {
     __shared__ float s_sun[64][3];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t pair = warp >> 1, part = warp & 1u;  // part 0: sun, 1: sky
@@ -504,7 +506,10 @@ __global__ void __launch_bounds__(128) train_samples_list_kernel(
     uint32_t p = 0;
     if (valid) {
         const unsigned long long phase = ((unsigned long long)pcg_hash(seed) * nv) >> 32;  // < nv
-        const uint32_t j = (uint32_t)(((unsigned long long)i * nv + phase) / n_samples);  // < nv
+        // clusters of `cluster` consecutive list entries, the clusters stratified over the list
+        const uint32_t c = i / cluster, r = i % cluster, n_cl = n_samples / cluster;
+        const unsigned long long start = ((unsigned long long)c * nv + phase) / n_cl;  // < nv
+        const uint32_t j = (uint32_t)(start + r < nv ? start + r : nv - 1ull);
         p = __ldg(&list[j]);
         const f3 x{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]}, n{nrm[3 * p], nrm[3 * p + 1], nrm[3 * p + 2]};
         l = part ? onebounce_sky(w, cam, x, n, pcg_hash(i ^ pcg_hash(seed ^ 0xB5297A4Du))) : onebounce_sun(w, cam, x, n);
@@ -648,8 +653,9 @@ int arc_gi_points_dev(arc_ctx* c, uint32_t width, uint32_t height, const uint32_
 int arc_launch_train_samples_list(arc_ctx* c, const uint32_t* list, const unsigned long long* n_valid, const float* pos,
                                   const float* nrm, const float* nrc_in, uint32_t seed, uint32_t n_samples, uint32_t steps,
                                   float* train_in, float* train_t, uint32_t* gate) {
+    const uint32_t cluster = (n_samples % c->nrc_sample_cluster) ? 1u : c->nrc_sample_cluster;
     arc::train_samples_list_kernel<<<(n_samples + 63u) / 64u, 128, 0, c->stream>>>(
-        c->world(), c->cam, list, n_valid, pos, nrm, nrc_in, seed, n_samples, steps, train_in, train_t, gate);
+        c->world(), c->cam, list, n_valid, pos, nrm, nrc_in, seed, n_samples, steps, cluster, train_in, train_t, gate);
     return launch_check(c, "train_samples_list_kernel");
 }
 

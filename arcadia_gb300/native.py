@@ -99,6 +99,7 @@ SIGNATURES = {
     "arc_nrc_set_ema_decay": [_vp, _f32],
     "arc_nrc_set_ema_warmup": [_vp, _u32],
     "arc_nrc_set_output_clamp": [_vp, _i32],
+    "arc_nrc_set_sample_cluster": [_vp, _u32],
     "arc_nrc_set_adam_betas": [_vp, _f32, _f32],
     "arc_set_cache_launch_overlap": [_vp, _i32],
     "arc_nrc_set_infer_path": [_vp, C.c_int],

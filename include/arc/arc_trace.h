@@ -343,6 +343,9 @@ int arc_nrc_set_ema_warmup(arc_ctx* ctx, uint32_t steps);
 /* on = 1: queries return max(network output, 0) per channel (radiance is not negative); 0 (default) =
  * the network output as it is. Training is unaffected. */
 int arc_nrc_set_output_clamp(arc_ctx* ctx, int on);
+/* Training samples in runs of k consecutive hit-list entries (k = 1, 2, 4, 8, 16 or 32; default 1 =
+ * every sample from its own stratum); used when n_samples is a multiple of k. */
+int arc_nrc_set_sample_cluster(arc_ctx* ctx, uint32_t k);
 /* on = 1 (default): the radiance-cache kernels of both caches (NRC tcgen05 training, Adam step and
  * tcgen05 query; SHARC update, resolve and list query) are launched with programmatic dependent launch,
  * so each is scheduled while the kernel ahead of it finishes and waits for it in hardware before it
@@ -389,9 +392,11 @@ int arc_nrc_train_frame_dev(arc_ctx* ctx, const uint32_t* list, const uint64_t* 
                             const float* normal, const float* nrc_in, uint32_t seed, uint32_t n_samples,
                             uint32_t steps, float lr);
 /* The training batch arc_nrc_train_frame_dev draws, into caller device buffers: train_in (9 floats per
- * sample) and train_t (the 1-spp one-bounce target with albedo 1, 3 floats), sample i taken from
- * list[floor((i + phase) * n_valid / n_samples)] with phase = (pcg_hash(seed) * n_valid) >> 32 and
- * stored at slot (i mod steps) * (n_samples / steps) + i / steps. Nothing is stored when *n_valid = 0. */
+ * sample) and train_t (the 1-spp one-bounce target with albedo 1, 3 floats). With sample cluster k
+ * (arc_nrc_set_sample_cluster, default 1), sample i is taken from list[min(s + i mod k, n_valid - 1)],
+ * s = floor((floor(i / k) * n_valid + phase) / (n_samples / k)), phase = (pcg_hash(seed) * n_valid) >> 32,
+ * and stored at slot (i mod steps) * (n_samples / steps) + i / steps. Nothing is stored when
+ * *n_valid = 0. */
 int arc_nrc_train_samples_dev(arc_ctx* ctx, const uint32_t* list, const uint64_t* n_valid, const float* pos,
                               const float* normal, const float* nrc_in, uint32_t seed, uint32_t n_samples,
                               uint32_t steps, float* train_in, float* train_t);

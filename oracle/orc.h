@@ -206,7 +206,7 @@ void orc_onebounce(const orc_world* w, const arc_camera_uniforms* cam, const uin
                    const float* nrm, const float* alb, uint32_t spp, uint32_t seed, int accumulate, float* out, int threads);
 void orc_train_samples(const orc_world* w, const arc_camera_uniforms* cam, const uint32_t* list, uint64_t n_valid,
                        const float* pos, const float* nrm, const float* nrc_in, uint32_t seed, uint32_t n_samples,
-                       uint32_t steps, float* train_in, float* train_t, int threads);
+                       uint32_t steps, uint32_t cluster, float* train_in, float* train_t, int threads);
 void orc_gi_points(const orc_world* w, const arc_camera_uniforms* cam, uint32_t W, uint32_t H, const uint32_t* gdm,
                    const uint32_t* gnm, float* pos, float* nrm, float* alb, float* nrc_in, uint32_t* valid, int threads);
 void orc_gi_points_from_hits(const arc_camera_uniforms* cam, uint32_t W, uint32_t H, const uint32_t* gdm, const uint32_t* gnm,

@@ -322,20 +322,26 @@ void orc_onebounce(const orc_world* w, const arc_camera_uniforms* cam, const uin
     }
 }
 
-/* The NRC training batch of a frame: sample i takes list[floor((i * n_valid + phase) / n_samples)],
- * phase = (pcg_hash(seed) * n_valid) >> 32; its target is the 1-spp estimator with albedo 1 (sky ray
- * seeded by pcg_hash(i ^ pcg_hash(seed ^ 0xB5297A4D))), stored with the point's 9 network inputs at
- * slot (i mod steps) * (n_samples / steps) + i / steps. */
+/* The NRC training batch of a frame: sample i takes list[min(s + i mod k, n_valid - 1)] with
+ * s = floor((floor(i / k) * n_valid + phase) / (n_samples / k)), k the cluster size (1: every sample its
+ * own stratum), phase = (pcg_hash(seed) * n_valid) >> 32; its target is the 1-spp estimator with albedo
+ * 1 (sky ray seeded by pcg_hash(i ^ pcg_hash(seed ^ 0xB5297A4D))), stored with the point's 9 network
+ * inputs at slot (i mod steps) * (n_samples / steps) + i / steps. */
 void orc_train_samples(const orc_world* w, const arc_camera_uniforms* cam, const uint32_t* list, uint64_t n_valid,
                        const float* pos, const float* nrm, const float* nrc_in, uint32_t seed, uint32_t n_samples,
-                       uint32_t steps, float* train_in, float* train_t, int threads) {
+                       uint32_t steps, uint32_t cluster, float* train_in, float* train_t, int threads) {
     if (!n_valid) return;
     const uint64_t phase = ((uint64_t)orc_pcg_hash(seed) * n_valid) >> 32;
     const uint32_t per = n_samples / steps;
+    if (cluster == 0u || n_samples % cluster) cluster = 1u;
+    const uint32_t n_cl = n_samples / cluster;
 #pragma omp parallel for schedule(dynamic, 64) num_threads(threads > 0 ? threads : 1)
     for (int64_t ii = 0; ii < (int64_t)n_samples; ++ii) {
         uint32_t i = (uint32_t)ii;
-        uint32_t j = (uint32_t)(((uint64_t)i * n_valid + phase) / n_samples);
+        /* runs of `cluster` consecutive list entries whose starts are stratified over the list */
+        uint64_t start = ((uint64_t)(i / cluster) * n_valid + phase) / n_cl;
+        uint64_t jj = start + i % cluster;
+        uint32_t j = (uint32_t)(jj < n_valid ? jj : n_valid - 1u);
         uint32_t p = list[j];
         float sun[3], sky[3];
         orc_onebounce_sun(w, cam, &pos[3 * (size_t)p], &nrm[3 * (size_t)p], sun);

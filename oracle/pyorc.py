@@ -108,7 +108,7 @@ def lib():
         _lib.orc_sharc_update_mode.argtypes = [C.POINTER(_World), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32]
         _lib.orc_cmp_albedo.argtypes = [u32, vp]
         _lib.orc_onebounce.argtypes = [C.POINTER(_World), vp, vp, u32, vp, vp, vp, u32, u32, i32, vp, i32]
-        _lib.orc_train_samples.argtypes = [C.POINTER(_World), vp, vp, C.c_uint64, vp, vp, vp, u32, u32, u32, vp, vp, i32]
+        _lib.orc_train_samples.argtypes = [C.POINTER(_World), vp, vp, C.c_uint64, vp, vp, vp, u32, u32, u32, u32, vp, vp, i32]
         _lib.orc_gi_points.argtypes = [C.POINTER(_World), vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, i32]
         _lib.orc_gi_points_from_hits.argtypes = [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp]
         _lib.orc_shadow_vis.argtypes = [C.POINTER(_World), vp, vp, vp, f32, vp]
@@ -439,14 +439,14 @@ def onebounce(world: World, cam, pos, nrm, alb, spp: int, seed: int, idx=None, a
 
 
 def train_samples(world: World, cam, lst, n_valid: int, pos, nrm, nrc_in, seed: int, n_samples: int, steps: int,
-                  threads: int = 8):
+                  threads: int = 8, cluster: int = 1):
     """The training batch of arc_nrc_train_samples_dev: (inputs (n, 9), targets (n, 3))."""
     tin = np.zeros((n_samples, 9), np.float32)
     tt = np.zeros((n_samples, 3), np.float32)
     lib().orc_train_samples(world.cw, _p(cam), _p(np.ascontiguousarray(lst, np.uint32)), n_valid,
                             _p(np.ascontiguousarray(pos, np.float32)), _p(np.ascontiguousarray(nrm, np.float32)),
-                            _p(np.ascontiguousarray(nrc_in, np.float32)), seed & 0xFFFFFFFF, n_samples, steps, _p(tin),
-                            _p(tt), threads)
+                            _p(np.ascontiguousarray(nrc_in, np.float32)), seed & 0xFFFFFFFF, n_samples, steps, cluster,
+                            _p(tin), _p(tt), threads)
     return tin, tt
 
 

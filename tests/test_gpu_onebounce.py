@@ -112,14 +112,17 @@ def test_onebounce_matches_oracle(orc, native_lib, frame, spp):
     np.testing.assert_array_equal(_np(out).view(np.uint32), want.view(np.uint32))
 
 
-def test_training_batch_matches_oracle(orc, native_lib, frame):
+@pytest.mark.parametrize("cluster", [1, 32])
+def test_training_batch_matches_oracle(orc, native_lib, frame, cluster):
     """arc_nrc_train_samples_dev, the batch arc_nrc_train_frame_dev trains on: 32,768 samples in 4
-    interleaved slices, inputs and 1-spp targets bit-exact (the oracle draws from the same compacted
-    list, whose order the GPU's warp-aggregated appends decide)."""
+    interleaved slices, each its own stratum or in runs of 32 list entries, inputs and 1-spp targets
+    bit-exact (the oracle draws from the same compacted list, whose order the GPU's warp-aggregated
+    appends decide)."""
     import torch
 
     w, t, cc = frame
     t.set_camera(cc.camera(4))
+    assert native_lib.lib().arc_nrc_set_sample_cluster(t.ctx, cluster) == 0
     n_samples, steps, seed = 32768, 4, 0xC0FFEE
     tin = torch.zeros((n_samples, 9), dtype=torch.float32, device="cuda")
     tt = torch.zeros((n_samples, 3), dtype=torch.float32, device="cuda")
@@ -129,8 +132,9 @@ def test_training_batch_matches_oracle(orc, native_lib, frame):
     t.synchronize()
     n_valid = int(cc.n_valid.item())
     lst = _np(cc.list).view(np.uint32)[:n_valid]
+    assert native_lib.lib().arc_nrc_set_sample_cluster(t.ctx, 1) == 0
     oin, ot = orc.train_samples(w, cc.camera(4), lst, n_valid, _np(cc.pos), _np(cc.nrm), _np(cc.nin), seed, n_samples,
-                                steps, threads=THREADS)
+                                steps, threads=THREADS, cluster=cluster)
     np.testing.assert_array_equal(_np(tin).view(np.uint32), oin.view(np.uint32))
     np.testing.assert_array_equal(_np(tt).view(np.uint32), ot.view(np.uint32))
     assert (ot > 0).any(axis=1).mean() > 0.3
