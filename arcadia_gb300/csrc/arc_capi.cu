@@ -914,7 +914,12 @@ static int views_prepare(arc_ctx* c, const arc_view_desc* views, uint32_t n, uin
             v.surf_count = &c->d_scratch->surf_count;
             v.surf_cap = (uint32_t)n_px;
         }
-        q += (uint64_t)v.tiles_x * ((d.height + c->cfg.tile_h - 1u) / c->cfg.tile_h) * 32u;
+        uint64_t tx = v.tiles_x, ty = (d.height + c->cfg.tile_h - 1u) / c->cfg.tile_h;
+        if (c->cfg.order == 1u) {  // whole super-tiles of 8 x 8 tiles; the padding tiles map off the view
+            tx = (tx + 7u) & ~7ull;
+            ty = (ty + 7u) & ~7ull;
+        }
+        q += tx * ty * 32u;
         if (q > (1ull << 31)) return set_err(c, ARC_E_CAPACITY, "batch exceeds 2^31 queue entries");
     }
     *queue_len = (uint32_t)q;
@@ -933,6 +938,7 @@ static int views_enqueue(arc_ctx* c, uint32_t n, uint32_t queue_len, uint64_t* n
     V.refill_threshold = c->cfg.refill_threshold;
     V.surf = c->views_surf_cap ? 1u : 0u;
     V.gi_split = c->cfg.variant == 0u ? 1u : 0u;
+    V.order = c->cfg.order;
     ARC_CK(c, cudaMemsetAsync(c->d_scratch, 0, sizeof(arc::Scratch), c->stream));
     ARC_CK(c, cudaMemcpyAsync(c->d_views, c->h_views, sizeof(arc::ViewDev) * n, cudaMemcpyHostToDevice, c->stream));
     ARC_CK(c, arc::launch_views(V, c->cfg, c->n_sm, c->stream));
@@ -988,14 +994,14 @@ int arc_autotune_views_dev(arc_ctx* c, const arc_view_desc* views, uint32_t n_vi
                            arc_launch_config* best_out, float* best_ms) {
     if (!c) return ARC_E_INVALID_ARG;
     if (frames == 0) frames = 3;
-    // the persistent kernel has lost every measured batch to the plain kernels + GI pass, so it keeps
-    // only its best-measured settings in the space
+    // the plain kernel + GI pass over register budget x block size x tile shape x tile order; the
+    // persistent kernel (variant 1) lost every measured batch by 1.6x or more and stays out of the
+    // space (arc_set_launch_config still selects it)
     std::vector<arc_launch_config> cands;
-    for (uint32_t rb : {3u, 4u})
-        for (uint32_t thr : {16u, 24u}) cands.push_back(arc_launch_config{1u, 256u, 0u, 8u, 4u, thr, rb, 0u, 0u});
     for (uint32_t rb : {2u, 3u, 4u})
         for (uint32_t bt : {128u, 256u})
-            for (uint32_t tw : {8u, 4u, 16u}) cands.push_back(arc_launch_config{0u, bt, 0u, tw, 32u / tw, 8u, rb, 0u, 0u});
+            for (uint32_t tw : {8u, 4u, 16u})
+                for (uint32_t order : {0u, 1u}) cands.push_back(arc_launch_config{0u, bt, 0u, tw, 32u / tw, 8u, rb, order, 0u});
     const arc_launch_config saved = c->cfg;
     float best = 1e30f;
     arc_launch_config best_cfg = saved;

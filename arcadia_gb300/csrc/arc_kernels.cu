@@ -162,6 +162,13 @@ __device__ __forceinline__ bool block_coords(uint32_t id, uint32_t nbx, uint32_t
     return *bx < nbx && *by < nby;
 }
 
+// Tile of a view's queue (32 pixels each): row-major over the view's tiles, or (order 1) Morton order
+// within super-tiles of 8 x 8 tiles, so that a block's consecutive tiles form a square patch and the
+// blocks resident together cover a compact screen area. Tiles past the view's edge map outside it.
+__device__ __forceinline__ void view_tile(uint32_t tile, uint32_t tiles_x, uint32_t order, uint32_t* tx, uint32_t* ty) {
+    block_coords(tile, tiles_x, 0xFFFFFFFFu, order, tx, ty);
+}
+
 __host__ __device__ __forceinline__ uint32_t blocks_for(uint32_t nbx, uint32_t nby, uint32_t order) {
     return order == 0u ? nbx * nby : ((nbx + 7u) >> 3) * ((nby + 7u) >> 3) * 64u;
 }
@@ -768,8 +775,9 @@ __global__ void __launch_bounds__(256, MINB) views_persistent_kernel(const Views
                     v = lo;
                     const ViewDev& vd = V.views[v];
                     const uint32_t local = q - vd.queue_begin, tile = local >> 5, within = local & 31u;
-                    const uint32_t px = (tile % vd.tiles_x) * V.tile_w + within % V.tile_w;
-                    const uint32_t py = (tile / vd.tiles_x) * V.tile_h + within / V.tile_w;
+                    uint32_t tx, ty;
+                    view_tile(tile, vd.tiles_x, V.order, &tx, &ty);
+                    const uint32_t px = tx * V.tile_w + within % V.tile_w, py = ty * V.tile_h + within / V.tile_w;
                     pxy = px | (py << 16);
                     if (px < vd.width && py < vd.height) {
                         const arc_camera_uniforms& cam = vd.cam;
@@ -847,8 +855,9 @@ __global__ void __launch_bounds__(256, MINB) views_plain_kernel(const ViewsParam
         }
         const ViewDev& vd = V.views[lo];
         const uint32_t local = q - vd.queue_begin, tile = local >> 5, within = local & 31u;
-        const uint32_t px = (tile % vd.tiles_x) * V.tile_w + within % V.tile_w;
-        const uint32_t py = (tile / vd.tiles_x) * V.tile_h + within / V.tile_w;
+        uint32_t tx, ty;
+        view_tile(tile, vd.tiles_x, V.order, &tx, &ty);
+        const uint32_t px = tx * V.tile_w + within % V.tile_w, py = ty * V.tile_h + within / V.tile_w;
         if (px < vd.width && py < vd.height) {
             const arc_camera_uniforms& cam = vd.cam;
             const World& w = V.worlds[vd.slot];
@@ -919,8 +928,9 @@ __global__ void __launch_bounds__(256, MINB) views_gi_kernel(const ViewsParams V
         }
         const ViewDev& vd = V.views[lo];
         const uint32_t local = q - vd.queue_begin, tile = local >> 5, within = local & 31u;
-        const uint32_t px = (tile % vd.tiles_x) * V.tile_w + within % V.tile_w;
-        const uint32_t py = (tile / vd.tiles_x) * V.tile_h + within / V.tile_w;
+        uint32_t tx, ty;
+        view_tile(tile, vd.tiles_x, V.order, &tx, &ty);
+        const uint32_t px = tx * V.tile_w + within % V.tile_w, py = ty * V.tile_h + within / V.tile_w;
         if (px < vd.width && py < vd.height) {
             k = (size_t)py * vd.width + px;
             view = lo;

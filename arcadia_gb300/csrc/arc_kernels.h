@@ -105,6 +105,7 @@ struct ViewsParams {
     uint32_t queue_len, tile_w, tile_h, refill_threshold;
     uint32_t surf;      // 1 when the views carry a surface list (the kernels list surface-branch hits)
     uint32_t gi_split;  // 1: views_plain_kernel stops after the primary ray and views_gi_kernel traces the GI rays
+    uint32_t order;     // tile order within a view: 0 row-major, 1 Morton super-tiles of 8 x 8 tiles
 };
 
 cudaError_t launch_views(const ViewsParams& V, const arc_launch_config& cfg, int n_sm, cudaStream_t st);

@@ -67,7 +67,8 @@ typedef struct arc_launch_config {
     uint32_t refill_threshold; /* persistent variant: refill when at least this many lanes are idle */
     uint32_t reg_blocks;       /* register budget: kernel built for at least this many 256-thread CTAs per SM (1-4) */
     uint32_t order;            /* variant 0: order of the pixel blocks (primary kernel and GI pass): 0 row-major,
-                                  1 Morton (Z) order inside super-tiles of 8 x 8 blocks */
+                                  1 Morton (Z) order inside super-tiles of 8 x 8 blocks; batched views (both
+                                  variants): the same two orders of each view's 32-pixel tiles */
     uint32_t features;         /* traversal variants of variant 0's primary-only kernel and GI pass (register
                                   budgets 2 and 3), ARC_FEAT_* bits; every variant gives the same results */
 } arc_launch_config;
@@ -208,12 +209,13 @@ int arc_trace_frame_noalloc(arc_ctx* ctx, uint32_t width, uint32_t height, uint3
 int arc_reserve_surface_list(arc_ctx* ctx, uint64_t max_pixels);
 /* Primary + GI rays of many views (several worlds, mixed resolutions) in one call: with the default
  * launch configuration (variant 0) the batch's primary kernel and its GI pass over every view; with
- * variant 1 one persistent launch for both (slower in every batch measured, kept for the autotuner).
+ * variant 1 one persistent launch for both (slower in every batch measured; selectable, not tuned).
  * With use_graph the batch is captured once into a CUDA graph and replayed (re-captured when the view
  * count, n_gi_dev or the launch configuration changes). Outputs per view as arc_trace_frame_dev.
  * No counterpart in the reference (one view per frame there). */
 int arc_trace_views_dev(arc_ctx* ctx, const arc_view_desc* views, uint32_t n_views, uint64_t* n_gi_dev, int use_graph);
-/* Autotuner of the batched launch (block size x register budget x refill threshold x tile shape). */
+/* Autotuner of the batched launch: variant 0 over block size x register budget x tile shape x tile
+ * order (row-major or Morton super-tiles); installs the fastest and returns it with its median time. */
 int arc_autotune_views_dev(arc_ctx* ctx, const arc_view_desc* views, uint32_t n_views, uint32_t frames,
                            arc_launch_config* best, float* best_ms);
 /* trace_world_64tree on a batch of rays (origin m, unit dir). */

@@ -36,8 +36,10 @@ def test_batched_views_match_single_view(native_lib):
     try:
         b = Batch(t, scenes, 3, resolutions=[(96, 64), (160, 90), (200, 120)], worlds=worlds, seed=5)
         n_gi = torch.zeros(1, dtype=torch.int64, device="cuda")
-        for frame, use_graph, variant in ((0, False, 1), (1, True, 1), (2, True, 1), (3, False, 0), (4, True, 0)):
-            t.set_launch_config(variant=variant)  # persistent, then plain (one thread per queue slot)
+        runs = ((0, False, 1, 1), (1, True, 1, 0), (2, True, 1, 1), (3, False, 0, 1), (4, True, 0, 0))
+        for frame, use_graph, variant, order in runs:
+            # persistent, then plain (one thread per queue slot); Morton or row-major tile order
+            t.set_launch_config(variant=variant, order=order)
             b.set_frame(frame)
             b.trace(n_gi.data_ptr(), use_graph=use_graph)
             t.synchronize()
@@ -49,6 +51,7 @@ def test_batched_views_match_single_view(native_lib):
                 hits = ref[3].numpy().view(L.HIT_DTYPE)
                 total_gi += int((hits["flags"] & 1).sum())
             assert int(n_gi.item()) == total_gi
+        t.set_launch_config(variant=0, order=1)
     finally:
         t.close()
 
@@ -76,9 +79,10 @@ def test_batched_autotune_keeps_results(native_lib):
 
 def test_bench_batch_matches_oracle(orc, native_lib, world_cache):
     """The benchmark batch itself (256^3, 512^3, 1024^3 and 1024^3-caves worlds, 16 views each, 320x240 up
-    to 2560x1440, seeded poses), replayed from its CUDA graph with both kernel variants: every view's
-    G-buffer words, primary hit records and GI hit records bit-exact against the oracle's trace of the
-    same camera, and the batch's GI-ray count equal to the oracle's number of primary hits."""
+    to 2560x1440, seeded poses), replayed from its CUDA graph with both kernel variants and both tile
+    orders (Morton super-tiles, row-major): every view's G-buffer words, primary hit records and GI hit
+    records bit-exact against the oracle's trace of the same camera, and the batch's GI-ray count equal
+    to the oracle's number of primary hits."""
     torch = pytest.importorskip("torch")
     from arcadia_gb300.batch import BENCH_SCENES, Batch
 
@@ -97,24 +101,24 @@ def test_bench_batch_matches_oracle(orc, native_lib, world_cache):
             expect.append((gdm, gnm, gaa, hits, gi))
         n_hit = sum(int((e[3]["flags"] & 1).sum()) for e in expect)
         n_gi = torch.zeros(1, dtype=torch.int64, device="cuda")
-        for variant in (0, 1):
-            t.set_launch_config(variant=variant)
+        for variant, order in ((0, 1), (1, 1), (0, 0)):  # Morton tile order (default) and row-major
+            t.set_launch_config(variant=variant, order=order)
             for bufs in b.buffers:
                 for x in bufs:
                     x.fill_(-1)
             b.set_frame(1)
             b.trace(n_gi.data_ptr(), use_graph=True)
             t.synchronize()
-            assert int(n_gi.item()) == n_hit, variant
+            assert int(n_gi.item()) == n_hit, (variant, order)
             for i, (bufs, e) in enumerate(zip(b.buffers, expect)):
                 for got, want, what in zip(bufs, e, ("depth/material", "normal/motion", "albedo/ao", "hits", "GI hits")):
                     got = got.cpu().numpy().view(np.uint32)
                     want = np.ascontiguousarray(want).view(np.uint32).reshape(-1)
                     if not np.array_equal(got, want):
                         bad = np.nonzero(got != want)[0]
-                        raise AssertionError(f"variant {variant} view {i} ({b.views[i]['w']}x{b.views[i]['h']}, "
+                        raise AssertionError(f"variant {variant} order {order} view {i} ({b.views[i]['w']}x{b.views[i]['h']}, "
                                              f"world {BENCH_SCENES[b.views[i]['slot']]}) {what}: {len(bad)} words differ, "
                                              f"first at {bad[:4]}")
-        t.set_launch_config(variant=0)
+        t.set_launch_config(variant=0, order=1)
     finally:
         t.close()
