@@ -355,7 +355,7 @@ int arc_set_launch_config(arc_ctx* c, const arc_launch_config* cfg) {
     if (cfg->reg_blocks < 1u || cfg->reg_blocks > 4u) return set_err(c, ARC_E_INVALID_ARG, "reg_blocks in [1, 4]");
     if (cfg->order > 1u) return set_err(c, ARC_E_INVALID_ARG, "order must be 0 (row-major) or 1 (Morton)");
     if (cfg->features & ~(ARC_FEAT_WARP_FETCH | ARC_FEAT_NODE_VISIT | ARC_FEAT_GI_SORT | ARC_FEAT_TOP_TABLE | ARC_FEAT_GRID_STRIDE |
-                          ARC_FEAT_PRECOMP))
+                          ARC_FEAT_PRECOMP | ARC_FEAT_GI_REPACK))
         return set_err(c, ARC_E_INVALID_ARG, "unknown feature bits");
     c->cfg = *cfg;
     return ARC_OK;

@@ -420,7 +420,17 @@ __global__ void __launch_bounds__(256, MINB) frame_persistent_kernel(const Frame
 // pixels, sorts them by direction octant in shared memory (a counting sort; the rays without a GI ray
 // drop out) and traces them from the sorted slots, so a warp's rays step in the same directions.
 // Every ray is computed as before, only by another thread of the block.
-template <int MINB, int FEAT = 0>
+//
+// With REPACK (ARC_FEAT_GI_REPACK) the block also regroups its rays while they run: every
+// P.refill_threshold DDA steps the rays still running are packed into the block's first threads, so
+// the warps that keep tracing are full and the others idle. A GI ray's length varies about tenfold
+// within a block (7 to 77 steps, 10th to 99th percentile, on the 1024^3 caves frame); without the
+// repack a warp runs as long as its longest ray. A ray moves with t, t_limit, its voxel and its step
+// count; vo, dir and 1/dir are rebuilt from its sorted slot as ray_begin forms them, and the chunk and
+// ancestor caches restart empty. Those caches only save node loads (a descent from the chunk root
+// meets the same nodes, and the step is taken at the same level), so every decision and result is
+// unchanged.
+template <int MINB, int FEAT = 0, bool REPACK = false>
 __global__ void __launch_bounds__(128, MINB) gi_rows_kernel(const FrameParams P, const __grid_constant__ arc_camera_uniforms cam) {
     __shared__ float s_ray[6][128];
     __shared__ uint32_t s_k[128];
@@ -465,6 +475,85 @@ __global__ void __launch_bounds__(128, MINB) gi_rows_kernel(const FrameParams P,
     }
     __syncthreads();
     const uint32_t n = s_base[8];
+    if constexpr (REPACK) {
+        static_assert((FEAT & ~kFeatPrecomp) == 0, "the repacked GI pass moves the descent-loop ray state only");
+        __shared__ uint32_t s_st[7][128];  // t, t_limit, vx, vy, vz, step, slot of the running rays
+        __shared__ uint32_t s_wc[4];
+        const uint32_t lane = t & 31u, warp = t >> 5;
+        const float gmax = cam.ray_distances[2];
+        const uint32_t K = P.refill_threshold;
+        if (t == 0u && n) atomicAdd(&P.scratch->gi_rays, (unsigned long long)n);
+        uint32_t slot = t;
+        bool live = false;
+        RayState s;
+        HitInfo h;
+        if (t < n) {
+            live = ray_begin(s, cam, f3{s_ray[0][t], s_ray[1][t], s_ray[2][t]}, f3{s_ray[3][t], s_ray[4][t], s_ray[5][t]},
+                             0.0f, gmax, 2u, true);
+            if constexpr ((FEAT & kFeatPrecomp) != 0) {
+                if (live) ray_precompute(s, cam);
+            }
+            if (!live) {
+                hit_init_miss(h, f3{s_ray[0][t], s_ray[1][t], s_ray[2][t]}, f3{s_ray[3][t], s_ray[4][t], s_ray[5][t]}, gmax);
+                if (P.gi_hits) store_hit(&P.gi_hits[s_k[t]], h, false);
+            }
+        }
+        for (;;) {
+            if (live) {
+                StepResult g = kContinue;
+                for (uint32_t i = 0; i < K && g == kContinue; ++i) g = ray_next<FEAT>(s, P.world, cam, h);
+                if (g != kContinue) {
+                    live = false;
+                    if (g != kHit)
+                        hit_init_miss(h, f3{s_ray[0][slot], s_ray[1][slot], s_ray[2][slot]},
+                                      f3{s_ray[3][slot], s_ray[4][slot], s_ray[5][slot]}, gmax);
+                    if (P.gi_hits) store_hit(&P.gi_hits[s_k[slot]], h, g == kHit);
+                }
+            }
+            const uint32_t ball = __ballot_sync(0xFFFFFFFFu, live);
+            if (lane == 0u) s_wc[warp] = (uint32_t)__popc(ball);
+            __syncthreads();
+            const uint32_t c0 = s_wc[0], c1 = s_wc[1], c2 = s_wc[2], c3 = s_wc[3];
+            const uint32_t total = c0 + c1 + c2 + c3;
+            if (total == 0u) break;  // the same value in every thread of the block
+            if (live) {
+                const uint32_t r = (warp > 0u ? c0 : 0u) + (warp > 1u ? c1 : 0u) + (warp > 2u ? c2 : 0u) +
+                                   (uint32_t)__popc(ball & ((1u << lane) - 1u));
+                s_st[0][r] = __float_as_uint(s.t);
+                s_st[1][r] = __float_as_uint(s.t_limit);
+                s_st[2][r] = s.vx;
+                s_st[3][r] = s.vy;
+                s_st[4][r] = s.vz;
+                s_st[5][r] = s.step;
+                s_st[6][r] = slot;
+            }
+            __syncthreads();
+            live = t < total;
+            if (live) {
+                slot = s_st[6][t];
+                const f3 o{s_ray[0][slot], s_ray[1][slot], s_ray[2][slot]}, d{s_ray[3][slot], s_ray[4][slot], s_ray[5][slot]};
+                s.vo = mul3s(o, ARC_VOXELS_PER_METER);
+                s.dir = d;
+                s.inv = f3{__fdiv_rn(1.0f, safe_component(d.x)), __fdiv_rn(1.0f, safe_component(d.y)),
+                           __fdiv_rn(1.0f, safe_component(d.z))};
+                s.t = __uint_as_float(s_st[0][t]);
+                s.t_limit = __uint_as_float(s_st[1][t]);
+                s.vx = s_st[2][t];
+                s.vy = s_st[3][t];
+                s.vz = s_st[4][t];
+                s.step = s_st[5][t];
+                s.diff = 0xFFFFFFFFu;  // next step: chunk root from the pool, descent from the root
+                s.mtf_c0 = s.mtf_c1 = 0xFFFFFFFFu;
+                s.mtf_root0 = s.mtf_root1 = ARC_EMPTY_CHUNK;
+                s.cached_shift = 6u;
+                s.mode = 2u | 4u;  // lod_bias 2, water ignored (as ray_begin above)
+                s.have_node = 0u;
+                if constexpr ((FEAT & kFeatPrecomp) != 0) ray_precompute(s, cam);
+            }
+            __syncthreads();  // s_st and s_wc are written again in the next round
+        }
+        return;
+    }
     if (t >= n) return;
     const f3 o{s_ray[0][t], s_ray[1][t], s_ray[2][t]}, d{s_ray[3][t], s_ray[4][t], s_ray[5][t]};
     const uint32_t kk = s_k[t];
@@ -1029,7 +1118,12 @@ cudaError_t launch_frame_t(const FrameParams& P, const arc_camera_uniforms& cam,
         if (P.gi_mode == kGiRows && P.gisort.bins) return launch_gi_sorted<MINB>(P, cam, st);
         if (P.gi_mode == kGiRows) {
             const dim3 g2(blocks_for((P.width + 15u) / 16u, (P.row_end - P.row0 + 7u) / 8u, P.order));
-            if (variant_kernels || (feat != 0 && P.surf && (MINB == 2 || MINB == 3))) {
+            if ((cfg.features & ARC_FEAT_GI_REPACK) && (feat == 0 || feat == kFeatPrecomp)) {
+                if (feat == kFeatPrecomp && (MINB == 2 || MINB == 3))
+                    gi_rows_kernel<MINB, kFeatPrecomp, true><<<g2, 128, 0, st>>>(P, cam);
+                else
+                    gi_rows_kernel<MINB, 0, true><<<g2, 128, 0, st>>>(P, cam);
+            } else if (variant_kernels || (feat != 0 && P.surf && (MINB == 2 || MINB == 3))) {
                 if (feat == kFeatWarpFetch) gi_rows_kernel<MINB, kFeatWarpFetch><<<g2, 128, 0, st>>>(P, cam);
                 else if (feat == kFeatNodeVisit) gi_rows_kernel<MINB, kFeatNodeVisit><<<g2, 128, 0, st>>>(P, cam);
                 else if (feat == kFeatPrecomp) gi_rows_kernel<MINB, kFeatPrecomp><<<g2, 128, 0, st>>>(P, cam);
@@ -1181,11 +1275,24 @@ cudaError_t launch_secondary(const FrameParams& P, const arc_camera_uniforms& ca
     // the frame's GI pass over the G-buffer's rows (compacted, octant-sorted blocks), at the register
     // budget of the launch configuration as in launch_frame
     const dim3 grid(blocks_for((P.width + 15u) / 16u, (P.row_end - P.row0 + 7u) / 8u, P.order));
+    const bool repack = (cfg.features & ARC_FEAT_GI_REPACK) != 0u;
     switch (cfg.reg_blocks) {
-        case 2: gi_rows_kernel<2><<<grid, 128, 0, st>>>(P, cam); break;
-        case 3: gi_rows_kernel<3><<<grid, 128, 0, st>>>(P, cam); break;
-        case 4: gi_rows_kernel<4><<<grid, 128, 0, st>>>(P, cam); break;
-        default: gi_rows_kernel<1><<<grid, 128, 0, st>>>(P, cam); break;
+        case 2:
+            if (repack) gi_rows_kernel<2, 0, true><<<grid, 128, 0, st>>>(P, cam);
+            else gi_rows_kernel<2><<<grid, 128, 0, st>>>(P, cam);
+            break;
+        case 3:
+            if (repack) gi_rows_kernel<3, 0, true><<<grid, 128, 0, st>>>(P, cam);
+            else gi_rows_kernel<3><<<grid, 128, 0, st>>>(P, cam);
+            break;
+        case 4:
+            if (repack) gi_rows_kernel<4, 0, true><<<grid, 128, 0, st>>>(P, cam);
+            else gi_rows_kernel<4><<<grid, 128, 0, st>>>(P, cam);
+            break;
+        default:
+            if (repack) gi_rows_kernel<1, 0, true><<<grid, 128, 0, st>>>(P, cam);
+            else gi_rows_kernel<1><<<grid, 128, 0, st>>>(P, cam);
+            break;
     }
     return cudaGetLastError();
 }

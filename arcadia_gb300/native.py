@@ -33,6 +33,7 @@ ARC_FEAT_GI_SORT = 4
 ARC_FEAT_TOP_TABLE = 8
 ARC_FEAT_GRID_STRIDE = 16
 ARC_FEAT_PRECOMP = 32
+ARC_FEAT_GI_REPACK = 64
 ERRORS = {
     -1: "ARC_E_INVALID_ARG",
     -2: "ARC_E_CUDA",

@@ -29,6 +29,7 @@ import numpy as np
 from . import layout as L
 from . import native
 from .edits import batch_from_hits, ops_for_brick_budget
+from .gi_cache import LEARNING_RATE
 
 TRAIN_SAMPLES = 32768  # the cache comparison's operating point (with 4 Adam steps per frame)
 
@@ -49,7 +50,7 @@ class FullPipeline:
     def __init__(self, tracer: native.Tracer, scene: L.SceneParams, width: int, height: int, n_bricks: int,
                  n_frames: int = 300, edit_fraction: float = 0.01, nrc_steps: int = 4, seed: int = 2027, quality=None,
                  keep_ops: bool = False, compare_every: int = 0, compare_points: int = 4096, boost_frames: int = 0,
-                 boost_steps: int = 16, lr_warmup_frames: int = 0):
+                 boost_steps: int = 16, lr_warmup_frames: int = 0, lr: float | None = None):
         import torch
 
         self.torch = torch
@@ -61,6 +62,7 @@ class FullPipeline:
         self.nrc_steps = nrc_steps
         self.boost_frames, self.boost_steps = boost_frames, boost_steps
         self.lr_warmup_frames = lr_warmup_frames
+        self.lr = LEARNING_RATE if lr is None else lr
         self.rng = np.random.default_rng(seed)
         self.seed = seed
         self.brick_target = max(1, int(round(edit_fraction * n_bricks)))
@@ -139,8 +141,8 @@ class FullPipeline:
                                                   self.pos.data_ptr(), self.nrm.data_ptr(), self.nin.data_ptr(),
                                                   self.seed * 7919 + f, TRAIN_SAMPLES,
                                                   self.boost_steps if f < self.boost_frames else self.nrc_steps,
-                                                  C.c_float(1e-3 * min(1.0, (f + 1) / self.lr_warmup_frames)
-                                                            if self.lr_warmup_frames else 1e-3)),
+                                                  C.c_float(self.lr * min(1.0, (f + 1) / self.lr_warmup_frames)
+                                                            if self.lr_warmup_frames else self.lr)),
                  "arc_nrc_train_frame_dev")
         self._ck(self.lib.arc_nrc_query_list_dev(self.t.ctx, self.list.data_ptr(), self.n_valid.data_ptr(), n_px,
                                                  self.nin.data_ptr(), self.alb.data_ptr(), self.nrc_out.data_ptr()),

@@ -54,6 +54,9 @@ def _args():
     p.add_argument("--block-threads", type=int, default=None)
     p.add_argument("--order", type=int, default=None, help="block order of the plain kernel: 0 row-major, 1 Morton")
     p.add_argument("--features", type=int, default=None, help="traversal variant bits (ARC_FEAT_*)")
+    p.add_argument("--refill-threshold", type=int, default=None,
+                   help="variant 1: idle lanes before a refill; ARC_FEAT_GI_REPACK: DDA steps between repacks")
+    p.add_argument("--flush-l2", action="store_true", help="with --frame-only, still flush L2 before every timed frame")
     p.add_argument("--width", type=int, default=WIDTH)
     p.add_argument("--height", type=int, default=HEIGHT)
     p.add_argument("--frame-only", action="store_true", help="time only the frame kernel (profiling runs)")
@@ -314,7 +317,7 @@ def run_ours(args):
     t.upload_world(scene.grid, roots, nodes, bricks, pal)
     knobs = {k: v for k, v in (("variant", args.variant), ("reg_blocks", args.reg_blocks),
                                ("block_threads", args.block_threads), ("order", args.order),
-                               ("features", args.features)) if v is not None}
+                               ("features", args.features), ("refill_threshold", args.refill_threshold)) if v is not None}
     if knobs:
         t.set_launch_config(**knobs)
     W_, H_ = args.width, args.height
@@ -328,7 +331,7 @@ def run_ours(args):
     gi = torch.empty(npx * 5, dtype=torch.int32, device=dev)
     n_gi = torch.zeros(max(args.steps, 1), dtype=torch.int64, device=dev)
     # L2 flush buffer (2x the 126 MB L2); profiling runs skip it so ncu has less memory to save/restore
-    flush = torch.empty(16 if args.frame_only else 256 << 20, dtype=torch.uint8, device=dev)
+    flush = torch.empty(16 if args.frame_only and not args.flush_l2 else 256 << 20, dtype=torch.uint8, device=dev)
 
     def frame(i, slot):
         t.set_camera(_camera(scene, i, W_, H_))
@@ -438,10 +441,13 @@ def run_ours(args):
         nrc["network"] = ("216-64x5-3, FP16 weights and activations, FP32 accumulation; tcgen05.mma with TMEM "
                           "accumulators for inference and training")
         nrc["pareto"] = []
-        for samples, steps in ((16384, 4), (32768, 2), (65536, 2), (65536, 4), (65536, 8), (65536, 16)):
+        lr0 = gi_cache.LEARNING_RATE
+        # the last two rows: the Adam rate the workload names (1e-3), at the operating point and at 65,536 samples
+        for samples, steps, lr in ((16384, 4, lr0), (32768, 2, lr0), (65536, 2, lr0), (65536, 4, lr0), (65536, 8, lr0),
+                                   (65536, 16, lr0), (32768, 4, 1e-3), (65536, 4, 1e-3)):
             r = gi_cache.run_comparison(t, SCENE, W_, H_, frames=args.nrc_frames, steps_per_frame=steps, curve=(),
-                                        overlap=True, train_samples=samples)
-            nrc["pareto"].append({"train_samples": samples, "train_steps_per_frame": steps,
+                                        overlap=True, train_samples=samples, lr=lr)
+            nrc["pareto"].append({"train_samples": samples, "train_steps_per_frame": steps, "lr": lr,
                                   "nrc_ms_per_frame": r["nrc_ms_per_frame"], "sharc_ms_per_frame": r["sharc_ms_per_frame"],
                                   "rel_mse_nrc": round(r["rel_mse_nrc"], 4), "rel_mse_sharc": round(r["rel_mse_sharc"], 4)})
         # the operating point with each query after its cache's update (no overlap)
@@ -572,7 +578,7 @@ def run_ours(args):
         ov, se = nrc, nrc["serial"]
         line["c4"] = {
             "workload": "NRC vs SHARC at the GI hits of 1920x1080 frames of the 1024^3 caves world, 300 static frames",
-            "operating_point": {"train_samples": 32768, "adam_steps_per_frame": 4},
+            "operating_point": {"train_samples": 32768, "adam_steps_per_frame": 4, "lr": ov["lr"]},
             "overlapped": {"nrc_ms": ov["nrc_ms_per_frame"], "sharc_ms": ov["sharc_ms_per_frame"],
                            "rel_mse_nrc": round(ov["rel_mse_nrc"], 4), "rel_mse_sharc": round(ov["rel_mse_sharc"], 4)},
             "serial": {"nrc_ms": se["nrc_ms_per_frame"], "sharc_ms": se["sharc_ms_per_frame"],

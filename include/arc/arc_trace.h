@@ -85,6 +85,9 @@ typedef struct arc_launch_config {
                                     control of ARC_FEAT_TOP_TABLE) */
 #define ARC_FEAT_PRECOMP 32u     /* the ray class's step budget, LOD thresholds and -origin/dir computed once per
                                     ray instead of every DDA step (alone, not combined with other bits) */
+#define ARC_FEAT_GI_REPACK 64u   /* the GI pass packs its still-running rays into the block's first warps every
+                                    refill_threshold DDA steps (with the default traversal or ARC_FEAT_PRECOMP;
+                                    also arc_trace_secondary_dev) */
 
 typedef struct arc_stats {
     float last_kernel_ms;      /* device time of the last traversal launch (CUDA events) */

@@ -96,6 +96,14 @@ def test_primary_then_secondary_matches_fused(orc, tracer, world_cache):
     np.testing.assert_array_equal(gdm, fgdm)
     _assert_hits_equal(hits, fhits, "primary")
     _assert_hits_equal(gi, fgi, "GI")
+    # the GI pass repacking its running rays every 4 steps
+    from arcadia_gb300 import native
+
+    tracer.set_launch_config(features=native.ARC_FEAT_GI_REPACK, refill_threshold=4)
+    try:
+        _assert_hits_equal(tracer.trace_secondary(gdm, gnm), fgi, "GI repacked")
+    finally:
+        tracer.set_launch_config(features=0, refill_threshold=24)
 
 
 @pytest.mark.parametrize("quality", ["parity", "high"])
@@ -105,7 +113,8 @@ def test_frame_c2_1024_caves_full(orc, tracer, world_cache, quality, native_lib)
     kernel variants (plain kernel + GI pass, persistent queue kernel) and the plain kernel's traversal
     variants (Morton block order, one node per loop iteration, warp-shared node fetch, GI rays sorted over
     the whole frame, resident CTAs with and without the top tree levels staged in shared memory,
-    per-ray constants computed once), in parity mode
+    per-ray constants computed once, the GI pass repacking its running rays every 1, 8 or 32 steps),
+    in parity mode
     (up to 512 steps, LOD out of reach) and with the high_quality preset (LOD on)."""
     native_lib_feat = native_lib
     w = world_cache("c2_1024_caves")
@@ -124,7 +133,11 @@ def test_frame_c2_1024_caves_full(orc, tracer, world_cache, quality, native_lib)
                dict(variant=0, order=1, features=native_lib_feat.ARC_FEAT_GI_SORT, reg_blocks=3, block_threads=128),
                dict(variant=0, order=1, features=native_lib_feat.ARC_FEAT_TOP_TABLE, reg_blocks=3, block_threads=256),
                dict(variant=0, order=0, features=native_lib_feat.ARC_FEAT_GRID_STRIDE, reg_blocks=2, block_threads=128),
-               dict(variant=0, order=1, features=native_lib_feat.ARC_FEAT_PRECOMP, reg_blocks=3, block_threads=64)]
+               dict(variant=0, order=1, features=native_lib_feat.ARC_FEAT_PRECOMP, reg_blocks=3, block_threads=64),
+               dict(variant=0, order=1, features=native_lib_feat.ARC_FEAT_GI_REPACK, reg_blocks=3, refill_threshold=8),
+               dict(variant=0, order=0, features=native_lib_feat.ARC_FEAT_GI_REPACK, reg_blocks=4, refill_threshold=1),
+               dict(variant=0, order=1, features=native_lib_feat.ARC_FEAT_GI_REPACK | native_lib_feat.ARC_FEAT_PRECOMP,
+                    reg_blocks=2, refill_threshold=32, block_threads=64)]
     for cfg in configs:
         tracer.set_launch_config(**cfg)
         gdm, gnm, gaa, hits, gi, n_gi = tracer.trace_frame()
@@ -134,7 +147,7 @@ def test_frame_c2_1024_caves_full(orc, tracer, world_cache, quality, native_lib)
         _assert_hits_equal(hits, ohits, f"primary {cfg}")
         _assert_hits_equal(gi, ogi, f"GI {cfg}")
         assert n_gi == n_hit
-    tracer.set_launch_config(variant=0, order=0, features=0, reg_blocks=3, block_threads=128)
+    tracer.set_launch_config(variant=0, order=0, features=0, reg_blocks=3, block_threads=128, refill_threshold=24)
     eye = np.broadcast_to(cam[0]["cam_pos_time"][:3], (len(ohits), 3))
     _check_depth_fp64(orc, eye, _camera_rays(cam, 1920, 1080), ohits, stride=401)
 
