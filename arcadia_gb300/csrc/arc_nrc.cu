@@ -547,8 +547,10 @@ __global__ void __launch_bounds__(128 * G, G == 1 ? 2 : 1) infer_tc_kernel(
         tc::mbar_expect_tx(bar_w, kUHalves * 2);
         if (!stall) tc::bulk_g2s(sw_u, wu, kUHalves * 2, bar_w);
     }
-    bool ok = tc::mbar_wait(bar_w, 0, budget);
-    bool fail = __syncthreads_or(!ok);
+    // the weights are waited for after the group's first tile is fetched and half encoded (the operand
+    // buffer and the weights are disjoint), so the copy runs under that work
+    bool ok = true, weights_pending = true;
+    bool fail = false;
     uint32_t phase = 0;
     bool mma_pending = false;  // group leader: a committed MMA batch whose completion it has not seen
     auto gsync = [&](bool v) { return G == 1 ? (__syncthreads_or(v) != 0) : group_sync_or(1u + g, v); };
@@ -610,6 +612,10 @@ __global__ void __launch_bounds__(128 * G, G == 1 ? 2 : 1) infer_tc_kernel(
         }
         tc::fence_async_smem();
         tc::fence_before();
+        if (weights_pending) {
+            ok = tc::mbar_wait(bar_w, 0, budget);
+            weights_pending = false;
+        }
         if ((fail = gsync(!ok))) break;
         issue(d_hid, 2u * u_off(1), 3584u, 1792u, 7, kId64, false);
         // second half: features 112..223 (the rest of input 4, inputs 5..8, 8 zero features)
@@ -737,8 +743,10 @@ __global__ void __launch_bounds__(128, 1) train_tc_kernel(const __half* __restri
         tc::mbar_expect_tx(bar_w, kUHalves * 2);
         if (!stall) tc::bulk_g2s(s0, wu, kUHalves * 2, bar_w);
     }
-    bool ok = tc::mbar_wait(bar_w, 0, budget);
-    bool fail = __syncthreads_or(!ok);
+    // the weights are waited for after the first tile's inputs are loaded and encoded (their regions
+    // are disjoint), so the copy runs under that work
+    bool ok = true, weights_pending = true;
+    bool fail = false;
     uint32_t phase = 0;
     bool mma_pending = false;  // thread 0: a committed MMA batch whose completion it has not seen
     float my_loss = 0.0f;
@@ -815,6 +823,10 @@ __global__ void __launch_bounds__(128, 1) train_tc_kernel(const __half* __restri
         encode_a0(v);
         tc::fence_async_smem();
         tc::fence_before();
+        if (weights_pending) {
+            ok = tc::mbar_wait(bar_w, 0, budget);
+            weights_pending = false;
+        }
         if ((fail = __syncthreads_or(!ok))) break;
         fwd_layer(d_hid, kTtR, 4096u, 1, 14, kF64);
         uint32_t r[4][16];
