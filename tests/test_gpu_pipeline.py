@@ -46,9 +46,9 @@ def test_pipeline_4096_matches_oracle(orc, native_lib, world_cache):
     """The 4096^3 world of the full pipeline (16^3 chunks, 16.6M nodes, 1.56M bricks), at a reduced
     960x540 resolution so the oracle replay stays short: 8 pipeline frames (edits rewriting 1 % of the
     bricks per frame, trace, GI points, NRC) on the GPU, then the oracle replays the same edit batches.
-    Every chunk's tree equals the oracle's node for node, and a frame traced on the edited world (primary
-    G-buffer, primary and GI hit records, high_quality preset with LOD on) is bit-exact against the
-    oracle's trace of its own edited world."""
+    Every chunk's tree equals the oracle's node for node, and frames traced on the edited world at
+    960x540 and at the workload's 3840x2160 (primary G-buffer, primary and GI hit records, high_quality
+    preset with LOD on) are bit-exact against the oracle's trace of its own edited world."""
     from arcadia_gb300.pipeline import FullPipeline, path_camera
 
     scene = L.SCENES["c5_4096"]
@@ -80,5 +80,17 @@ def test_pipeline_4096_matches_oracle(orc, native_lib, world_cache):
         assert hits.tobytes() == ohits.tobytes()
         assert gi.tobytes() == ogi.tobytes()
         assert n_gi == int((ohits["flags"] & 1).sum()) > 0.2 * W * H
+        # the same edited world at the workload's own 3840x2160
+        cam4 = path_camera(scene, 3840, 2160, F - 1, F, L.quality_high())
+        t.set_camera(cam4)
+        gdm, gnm, gaa, hits, gi, n_gi = t.trace_frame()
+        ogdm, ognm, ogaa, ohits, _ = orc.primary(ow, cam4, threads=THREADS)
+        _, ogi, _ = orc.gi_rays(ow, cam4, ogdm, ognm, threads=THREADS)
+        np.testing.assert_array_equal(gdm, ogdm)
+        np.testing.assert_array_equal(gnm, ognm)
+        np.testing.assert_array_equal(gaa, ogaa)
+        assert hits.tobytes() == ohits.tobytes()
+        assert gi.tobytes() == ogi.tobytes()
+        assert n_gi == int((ohits["flags"] & 1).sum())
     finally:
         t.close()
