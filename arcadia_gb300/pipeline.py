@@ -50,7 +50,8 @@ class FullPipeline:
     def __init__(self, tracer: native.Tracer, scene: L.SceneParams, width: int, height: int, n_bricks: int,
                  n_frames: int = 300, edit_fraction: float = 0.01, nrc_steps: int = 4, seed: int = 2027, quality=None,
                  keep_ops: bool = False, compare_every: int = 0, compare_points: int = 4096, boost_frames: int = 0,
-                 boost_steps: int = 16, lr_warmup_frames: int = 0, lr: float | None = None):
+                 boost_steps: int = 16, lr_warmup_frames: int = 0, lr: float | None = None,
+                 train_samples: int = TRAIN_SAMPLES):
         import torch
 
         self.torch = torch
@@ -63,6 +64,7 @@ class FullPipeline:
         self.boost_frames, self.boost_steps = boost_frames, boost_steps
         self.lr_warmup_frames = lr_warmup_frames
         self.lr = LEARNING_RATE if lr is None else lr
+        self.train_samples = train_samples
         self.rng = np.random.default_rng(seed)
         self.seed = seed
         self.brick_target = max(1, int(round(edit_fraction * n_bricks)))
@@ -139,7 +141,7 @@ class FullPipeline:
         n_px = self.w * self.h
         self._ck(self.lib.arc_nrc_train_frame_dev(self.t.ctx, self.list.data_ptr(), self.n_valid.data_ptr(),
                                                   self.pos.data_ptr(), self.nrm.data_ptr(), self.nin.data_ptr(),
-                                                  self.seed * 7919 + f, TRAIN_SAMPLES,
+                                                  self.seed * 7919 + f, self.train_samples,
                                                   self.boost_steps if f < self.boost_frames else self.nrc_steps,
                                                   C.c_float(self.lr * min(1.0, (f + 1) / self.lr_warmup_frames)
                                                             if self.lr_warmup_frames else self.lr)),
@@ -148,9 +150,11 @@ class FullPipeline:
                                                  self.nin.data_ptr(), self.alb.data_ptr(), self.nrc_out.data_ptr()),
                  "arc_nrc_query_list_dev")
         e4 = self._event()
-        if self.compare_every:
+        e5 = None
+        if self.compare_every:  # SHARC beside the NRC, timed on its own after the frame's NRC work
             self._sharc_frame()
-        e4.synchronize()
+            e5 = self._event()
+        (e5 or e4).synchronize()
         rewritten = self.t.edit_stats()["bricks_rewritten"]
         dr = rewritten - self.last_rewritten
         self.last_rewritten = rewritten
@@ -158,6 +162,7 @@ class FullPipeline:
             self.bricks_per_op = 0.7 * self.bricks_per_op + 0.3 * (dr / len(ops))
         rec = {"edit_ms": e0.elapsed_time(e1), "trace_ms": e1.elapsed_time(e2), "points_ms": e2.elapsed_time(e3),
                "nrc_ms": e3.elapsed_time(e4), "total_ms": e0.elapsed_time(e4), "ops": int(len(ops)),
+               "sharc_ms": e4.elapsed_time(e5) if e5 is not None else None,
                "bricks_rewritten": int(dr), "rays": n_px + int(self.n_gi.item()), "gi_hits": int(self.n_valid.item())}
         self.records.append(rec)
         if self.compare_every and (f + 1) % self.compare_every == 0:
@@ -165,8 +170,8 @@ class FullPipeline:
         return rec
 
     def _sharc_frame(self):
-        """SHARC beside the NRC (untimed): mode-1 update from this frame's G-buffer, resolve, query at the
-        frame's GI hit list."""
+        """SHARC beside the NRC (timed on its own, outside the frame's total): mode-1 update from this
+        frame's G-buffer, resolve, query at the frame's GI hit list."""
         n_px = self.w * self.h
         self._ck(self.lib.arc_sharc_update_dev(self.t.ctx, self.w, self.h, self.gdm.data_ptr(), self.gnm.data_ptr()),
                  "arc_sharc_update_dev")
@@ -224,13 +229,14 @@ class FullPipeline:
             "frames": len(self.records), "frames_summarised": len(r), "width": self.w, "height": self.h,
             "ms_per_frame": round(total_ms / len(r), 4), "median_ms": {k: med(k) for k in
                                                                       ("edit_ms", "trace_ms", "points_ms", "nrc_ms", "total_ms")},
+            **({"sharc_ms_median": med("sharc_ms")} if self.compare_every else {}),
             "trace_mrays_per_s": round(rays / (trace_ms * 1e-3) / 1e6, 2),
             "pipeline_mrays_per_s": round(rays / (total_ms * 1e-3) / 1e6, 2),
             "edit_ops_per_frame": round(statistics.mean(x["ops"] for x in r), 1),
             "bricks_rewritten_per_frame": round(statistics.mean(x["bricks_rewritten"] for x in r), 1),
             "brick_target_per_frame": self.brick_target,
             "gi_hits_per_frame": round(statistics.mean(x["gi_hits"] for x in r), 1),
-            "nrc_train_samples": TRAIN_SAMPLES, "nrc_steps": self.nrc_steps,
+            "nrc_train_samples": self.train_samples, "nrc_steps": self.nrc_steps,
             "pool_next_node": st["next_node"], "pool_next_brick": st["next_brick"], "overflow": st["overflow"],
             "device_status": self.t.stats().device_status, "launch": self.launch,
             **({"cache_scores_along_path": self.path_scores} if self.compare_every else {}),

@@ -590,7 +590,8 @@ def run_ours(args):
             "reference_spp": 4096,
             "static_curve": [[c["frame"], round(c["rel_mse_nrc"], 3), round(c["rel_mse_sharc"], 3)] for c in ov["convergence"]],
             "moving_c5_path": ([[c["frame"], c["rel_mse_nrc"], c["rel_mse_sharc"]] for c in c5["cache_scores_along_path"]]
-                               if c5 and "cache_scores_along_path" in c5 else None)}
+                               if c5 and "cache_scores_along_path" in c5 else None),
+            "c5_cache_ms_4k": ({"nrc": c5["median_ms"]["nrc_ms"], "sharc": c5.get("sharc_ms_median")} if c5 else None)}
     print(json.dumps(line), flush=True)
 
 
