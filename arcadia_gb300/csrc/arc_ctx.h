@@ -84,7 +84,7 @@ struct arc_ctx {
     void* d_nrc_w16_ema = nullptr;    // its FP16 forward layout (mma.sync kernels)
     void* d_nrc_wu_ema = nullptr;     // its FP16 tensor-core operand layout (tcgen05 kernels)
     void* d_nrc_wu = nullptr;         // the latest weights in the tensor-core layout (tcgen05 training)
-    int nrc_infer_path = 1;           // 1 = tcgen05 inference, 0 = mma.sync inference
+    int nrc_infer_path = 3;           // tcgen05 inference: 1 one tile group, 2 four, 3 automatic; 0 = mma.sync
     int nrc_train_path = 1;           // 1 = tcgen05 training, 0 = mma.sync training
     float nrc_ema_decay = 0.99f;
     uint32_t nrc_ema_warmup = 0;      // EMA warm-up: decay min(nrc_ema_decay, (1 + k) / (warmup + k)); 0 = off

@@ -1028,9 +1028,12 @@ void init_weights(std::vector<float>& w, uint32_t seed) {
 long long tc_budget(const arc_ctx* c) { return c->tc_wait_budget > 0 ? c->tc_wait_budget : nrc::kTcBudget; }
 
 int launch_infer(arc_ctx* c, const float* inputs, const float* albedo, uint32_t n, float* out, const uint32_t* list,
-                 const unsigned long long* n_dev) {
+                 const unsigned long long* n_dev, bool beside = false) {
     const __half* wu = static_cast<const __half*>(c->d_nrc_wu_ema);
-    if (c->nrc_infer_path == 2) {  // four tile groups per CTA, one CTA per SM
+    // path 3 (automatic): four tile groups for a query on its own; one group beside the training
+    // samples, whose kernel shares the SMs (a four-group CTA takes a whole SM's shared memory)
+    const int path = c->nrc_infer_path == 3 ? (beside ? 1 : 2) : c->nrc_infer_path;
+    if (path == 2) {  // four tile groups per CTA, one CTA per SM
         const uint32_t tiles = (n + 127u) / 128u;
         const uint32_t blocks = std::min<uint32_t>((tiles + nrc::kTcGroups - 1u) / nrc::kTcGroups, (uint32_t)c->n_sm);
         NRC_CK(arc_launch_overlapped(c, nrc::infer_tc_kernel<nrc::kTcGroups>, dim3(blocks), dim3(128 * nrc::kTcGroups), nrc::kTcSmemG, wu,
@@ -1038,7 +1041,7 @@ int launch_infer(arc_ctx* c, const float* inputs, const float* albedo, uint32_t 
                         c->nrc_clamp ? 1u : 0u));
         return ARC_OK;
     }
-    if (c->nrc_infer_path == 1) {  // one tile group per CTA, two CTAs per SM
+    if (path == 1) {  // one tile group per CTA, two CTAs per SM
         const uint32_t blocks = std::min<uint32_t>((n + 127u) / 128u, (uint32_t)c->n_sm * 2u);
         NRC_CK(arc_launch_overlapped(c, nrc::infer_tc_kernel<1>, dim3(blocks), dim3(128), nrc::kTcSmem, wu, inputs, albedo, n, out, list,
                         n_dev, c->d_status, tc_budget(c), c->tc_stall ? 1u : 0u, c->nrc_clamp ? 1u : 0u));
@@ -1144,7 +1147,7 @@ int arc_nrc_get_ema_weights(arc_ctx* c, float* w) {
 }
 
 int arc_nrc_set_infer_path(arc_ctx* c, int path) {
-    if (!c || path < 0 || path > 2) return ARC_E_INVALID_ARG;
+    if (!c || path < 0 || path > 3) return ARC_E_INVALID_ARG;
     c->nrc_infer_path = path;
     return ARC_OK;
 }
@@ -1292,7 +1295,7 @@ int arc_nrc_frame_dev(arc_ctx* c, const uint32_t* list, const uint64_t* n_valid,
     // the query reads the weights the previous frame's last step left; it runs beside the sample
     // generation and ends before this frame's first Adam step rewrites them
     if ((rc = arc_ctx_side_begin(c))) return rc;
-    rc = max_n ? launch_infer(c, nrc_in, albedo, max_n, out_rgb, list, reinterpret_cast<const unsigned long long*>(n_valid))
+    rc = max_n ? launch_infer(c, nrc_in, albedo, max_n, out_rgb, list, reinterpret_cast<const unsigned long long*>(n_valid), true)
                : ARC_OK;
     int rc2 = arc_ctx_side_end(c);
     if (rc || (rc = rc2)) return rc;

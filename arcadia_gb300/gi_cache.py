@@ -284,6 +284,6 @@ def kernel_timing(tracer: native.Tracer, scene_name="c2_1024_caves", width=1920,
         t1, t8 = timed(train(1)), timed(train(8))
         out[name] = {"query_ms": round(q, 4), "query_tflops": round(n_hits * NRC_FLOPS_PER_QUERY / (q * 1e-3) / 1e12, 1),
                      "train_frame_1step_ms": round(t1, 4), "per_extra_step_ms": round((t8 - t1) / 7, 4)}
-    cc._ck(lib.arc_nrc_set_infer_path(tracer.ctx, 1), "path")
+    cc._ck(lib.arc_nrc_set_infer_path(tracer.ctx, 3), "path")
     cc._ck(lib.arc_nrc_set_train_path(tracer.ctx, 1), "path")
     return out

@@ -360,8 +360,10 @@ int arc_set_cache_launch_overlap(arc_ctx* ctx, int on);
 /* Adam's moment decays (default beta1 0.9, beta2 0.99; both in [0, 1)). */
 int arc_nrc_set_adam_betas(arc_ctx* ctx, float beta1, float beta2);
 /* Inference kernel: 1 = tcgen05 tensor cores with TMEM accumulators, one 128-query tile per CTA and
- * two CTAs per SM (default); 2 = the same with four tile groups in one CTA per SM (measured slower);
- * 0 = the warp-level mma.sync kernel (kept as the comparison point). */
+ * two CTAs per SM; 2 = the same with four tile groups in one CTA per SM (7 % faster on a 4K hit list,
+ * but its CTA takes a whole SM's shared memory); 3 = automatic (default): four groups for a query on
+ * its own, one group for the query that arc_nrc_frame_dev runs beside the training samples;
+ * 0 = the warp-level mma.sync kernel (kept as the comparison point). Results are identical for 1-3. */
 int arc_nrc_set_infer_path(arc_ctx* ctx, int path);
 /* Training kernel (gradients): 1 = tcgen05 (default), 0 = the mma.sync kernel. */
 int arc_nrc_set_train_path(arc_ctx* ctx, int path);

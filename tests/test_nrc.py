@@ -260,7 +260,7 @@ def test_gpu_tcgen05_and_mma_sync_inference_agree(orc, tracer):
     dx = torch.from_numpy(x).cuda()
     outs = []
     try:
-        for path in (1, 0, 2):  # tcgen05 one tile group per CTA, mma.sync, tcgen05 four groups per CTA
+        for path in (1, 0, 2, 3):  # tcgen05 one tile group per CTA, mma.sync, four groups per CTA, automatic
             assert lib().arc_nrc_set_infer_path(tracer.ctx, path) == 0
             dy = torch.zeros((len(x), 3), dtype=torch.float32, device="cuda")
             assert lib().arc_nrc_query_dev(tracer.ctx, dx.data_ptr(), None, len(x), dy.data_ptr()) == 0
@@ -271,8 +271,9 @@ def test_gpu_tcgen05_and_mma_sync_inference_agree(orc, tracer):
             assert np.all(np.abs(y[:4096] - ref) <= 2e-2 * np.abs(ref) + 2e-3), np.max(np.abs(y[:4096] - ref))
         assert np.max(np.abs(outs[0] - outs[1])) <= 1e-2 * np.max(np.abs(outs[1])) + 1e-3
         np.testing.assert_array_equal(outs[0], outs[2])  # the same MMAs per tile: identical bits
-        # compacted list on the tcgen05 path: every third point, in reverse order
-        assert lib().arc_nrc_set_infer_path(tracer.ctx, 1) == 0
+        np.testing.assert_array_equal(outs[0], outs[3])
+        # compacted list on the tcgen05 path (four groups, then one): every third point, in reverse order
+        assert lib().arc_nrc_set_infer_path(tracer.ctx, 2) == 0
         idx = np.arange(len(x) - 1, -1, -3, dtype=np.int32)
         dl = torch.from_numpy(idx).cuda()
         nd = torch.tensor([len(idx)], dtype=torch.int64, device="cuda")
@@ -285,9 +286,15 @@ def test_gpu_tcgen05_and_mma_sync_inference_agree(orc, tracer):
         mask[idx] = True
         np.testing.assert_array_equal(z[mask], outs[0][mask])
         assert (z[~mask] == -5.0).all()
+        assert lib().arc_nrc_set_infer_path(tracer.ctx, 1) == 0
+        dz.fill_(-5.0)
+        assert lib().arc_nrc_query_list_dev(tracer.ctx, dl.data_ptr(), nd.data_ptr(), len(x), dx.data_ptr(), None,
+                                            dz.data_ptr()) == 0
+        tracer.synchronize()
+        np.testing.assert_array_equal(dz.cpu().numpy(), z)
         assert tracer.stats().device_status == 0
     finally:
-        assert lib().arc_nrc_set_infer_path(tracer.ctx, 1) == 0
+        assert lib().arc_nrc_set_infer_path(tracer.ctx, 3) == 0
 
 
 @pytest.mark.gpu
