@@ -361,6 +361,13 @@ int arc_set_launch_config(arc_ctx* c, const arc_launch_config* cfg) {
     return ARC_OK;
 }
 
+int arc_set_frame_bands(arc_ctx* c, uint32_t n) {
+    if (!c) return ARC_E_INVALID_ARG;
+    if (n > (uint32_t)arc_ctx::kMaxBands) return set_err(c, ARC_E_INVALID_ARG, "frame bands in [0, 8]");
+    c->frame_bands = n;
+    return ARC_OK;
+}
+
 int arc_get_launch_config(const arc_ctx* c, arc_launch_config* cfg) {
     if (!c || !cfg) return ARC_E_INVALID_ARG;
     *cfg = c->cfg;
@@ -584,7 +591,55 @@ static int surface_prepare(arc_ctx* c, arc::FrameParams& P, uint32_t* count) {
     return ARC_OK;
 }
 
+static int ensure_band_streams(arc_ctx* c);
+
+// Bands of a device frame: the plain kernel's launches over the whole frame, or (frame_bands > 1)
+// over horizontal bands on the band streams, forked from and joined back to the context stream, so
+// that one band's tail runs beside another band's work. The variants with frame-wide scratch (the GI
+// rays sorted over the frame, the resident-CTA primary with its staged table) and the persistent
+// kernel (one queue) keep one launch. Every pixel is computed by the same code either way.
+static uint32_t device_bands(const arc_ctx* c, const arc::FrameParams& P) {
+    if (c->cfg.variant != 0u || (c->cfg.features & (ARC_FEAT_GI_SORT | ARC_FEAT_TOP_TABLE | ARC_FEAT_GRID_STRIDE)))
+        return 1u;
+    const uint32_t want = c->frame_bands ? c->frame_bands : arc_ctx::kDefaultFrameBands;
+    return std::max<uint32_t>(1u, std::min<uint32_t>(want, (P.row_end - P.row0) / 64u));
+}
+
+// First row of band b of n: equal bands, edges on multiples of 32 rows (whole blocks of every kernel).
+static uint32_t device_band_edge(uint32_t row0, uint32_t row_end, uint32_t b, uint32_t n) {
+    if (b >= n) return row_end;
+    return row0 + (uint32_t)(((uint64_t)(row_end - row0) * b / n) & ~(uint64_t)31);
+}
+
 static int run_frame(arc_ctx* c, arc::FrameParams& P) {
+    const uint32_t nb = device_bands(c, P);
+    if (nb > 1u) {
+        int rc = ensure_band_streams(c);
+        if (rc) return rc;
+        const bool surf = c->surface_mats[0] || cam_underwater(c->cam);
+        ARC_CK(c, cudaMemsetAsync(c->d_scratch, 0, sizeof(Scratch), c->stream));
+        if (surf) {
+            if ((rc = arc_ctx_reserve_surface(c, (size_t)P.width * P.height))) return rc;
+            ARC_CK(c, cudaMemsetAsync(c->d_surf_count, 0, sizeof(uint32_t) * arc_ctx::kMaxBands, c->stream));
+        }
+        ARC_CK(c, cudaEventRecord(c->ev0, c->stream));
+        ARC_CK(c, cudaEventRecord(c->frame_start, c->stream));
+        const uint32_t r0 = P.row0, r1 = P.row_end;
+        for (uint32_t b = 0; b < nb; ++b) {
+            arc::FrameParams Pb = P;
+            frame_rows(c, Pb, device_band_edge(r0, r1, b, nb), device_band_edge(r0, r1, b + 1u, nb));
+            cudaStream_t st = c->band_stream[b];
+            ARC_CK(c, cudaStreamWaitEvent(st, c->frame_start, 0));
+            if ((rc = surface_prepare(c, Pb, c->d_surf_count + b))) return rc;
+            ARC_CK(c, arc::launch_frame(Pb, c->cam, c->cfg, c->n_sm, st));
+            ARC_CK(c, arc::launch_surface(Pb, c->cam, c->n_sm, st));
+            ARC_CK(c, cudaEventRecord(c->band_ev[b], st));
+        }
+        for (uint32_t b = 0; b < nb; ++b) ARC_CK(c, cudaStreamWaitEvent(c->stream, c->band_ev[b], 0));
+        ARC_CK(c, cudaEventRecord(c->ev1, c->stream));
+        c->timing_pending = true;
+        return ARC_OK;
+    }
     int rc = surface_prepare(c, P, &c->d_scratch->surf_count);
     if (rc) return rc;
     ARC_CK(c, cudaMemsetAsync(c->d_scratch, 0, sizeof(Scratch), c->stream));

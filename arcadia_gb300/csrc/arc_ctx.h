@@ -130,6 +130,8 @@ struct arc_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // host-buffer frames: copy stream and per-band events (copies of a band overlap the next band)
     static constexpr int kMaxBands = 8;
+    static constexpr uint32_t kDefaultFrameBands = 4;  // device frames (arc_set_frame_bands 0)
+    uint32_t frame_bands = 0;                           // arc_set_frame_bands; 0 = kDefaultFrameBands
     cudaStream_t copy_stream = nullptr;
     cudaStream_t band_stream[kMaxBands] = {};  // the plain kernel's bands run concurrently, one per stream
     cudaEvent_t band_ev[kMaxBands] = {};

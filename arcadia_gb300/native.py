@@ -54,6 +54,7 @@ SIGNATURES = {
     "arc_synchronize": [_vp],
     "arc_get_stream": [_vp, C.POINTER(_vp)],
     "arc_set_launch_config": [_vp, _vp],
+    "arc_set_frame_bands": [_vp, _u32],
     "arc_autotune_frame_dev": [_vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp, _u32, _vp, _vp],
     "arc_get_launch_config": [_vp, _vp],
     "arc_get_stats": [_vp, _vp],

@@ -57,6 +57,8 @@ def _args():
     p.add_argument("--refill-threshold", type=int, default=None,
                    help="variant 1: idle lanes before a refill; ARC_FEAT_GI_REPACK: DDA steps between repacks")
     p.add_argument("--flush-l2", action="store_true", help="with --frame-only, still flush L2 before every timed frame")
+    p.add_argument("--frame-bands", type=int, default=None,
+                   help="device frames in this many concurrent row bands (library default: 4; 1 = one launch)")
     p.add_argument("--width", type=int, default=WIDTH)
     p.add_argument("--height", type=int, default=HEIGHT)
     p.add_argument("--frame-only", action="store_true", help="time only the frame kernel (profiling runs)")
@@ -320,6 +322,10 @@ def run_ours(args):
                                ("features", args.features), ("refill_threshold", args.refill_threshold)) if v is not None}
     if knobs:
         t.set_launch_config(**knobs)
+    if args.frame_bands is not None:
+        rc = native.lib().arc_set_frame_bands(t.ctx, args.frame_bands)
+        if rc:
+            raise native.ArcError(rc, t.last_error())
     W_, H_ = args.width, args.height
     stream = torch.cuda.ExternalStream(t.stream(), device=torch.device("cuda", local))
     npx = W_ * H_
@@ -547,6 +553,11 @@ def run_ours(args):
         roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
                     "algorithmic_bytes_per_pixel": round(bpp, 2)}
+    # row bands of a device frame (arc_set_frame_bands; the library's rule: default 4, at most one per
+    # 64 rows, one launch for the persistent kernel and the frame-wide variants)
+    bands = 1
+    if cfg.variant == 0 and not (cfg.features & (4 | 8 | 16)):
+        bands = max(1, min(args.frame_bands if args.frame_bands else 4, H_ // 64))
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(avg_ms, 4), "higher_is_better": True, "scaling": "weak",
@@ -558,13 +569,14 @@ def run_ours(args):
                    "launch": {"block_threads": cfg.block_threads, "blocks_per_sm": cfg.blocks_per_sm,
                               "tile": [cfg.tile_w, cfg.tile_h], "refill_threshold": cfg.refill_threshold,
                               "reg_blocks": cfg.reg_blocks, "order": "morton" if cfg.order else "row-major",
-                              "features": cfg.features}},
+                              "features": cfg.features, "row_bands": bands}},
         "plain_kernel": {"value": round(plain_value, 3), "unit": UNIT, "ms_per_step": round(statistics.mean(plain_ms), 4)},
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": 480,
                 "d2h_bytes_per_step": npx * 60 + 8 + 16},
         # per timed frame: the persistent kernel, or the plain kernel's primary instance + the GI pass
-        # (one kernel, or four with the GI rays sorted over the frame: keys, scan, scatter, trace)
-        "gpu_launches": args.steps * (1 if cfg.variant == 1 else (5 if cfg.features & 4 else 2)),
+        # (one kernel, or four with the GI rays sorted over the frame: keys, scan, scatter, trace),
+        # once per concurrent row band
+        "gpu_launches": args.steps * (1 if cfg.variant == 1 else (5 if cfg.features & 4 else 2 * bands)),
         "roofline": roofline,
         "cpu_baseline": cpu,
         "nrc": nrc,

@@ -114,6 +114,7 @@ def test_frame_c2_1024_caves_full(orc, tracer, world_cache, quality, native_lib)
     variants (Morton block order, one node per loop iteration, warp-shared node fetch, GI rays sorted over
     the whole frame, resident CTAs with and without the top tree levels staged in shared memory,
     per-ray constants computed once, the GI pass repacking its running rays every 1, 8 or 32 steps),
+    through the host-buffer entry point and the device-buffer one (one launch, or concurrent row bands),
     in parity mode
     (up to 512 steps, LOD out of reach) and with the high_quality preset (LOD on)."""
     native_lib_feat = native_lib
@@ -148,6 +149,30 @@ def test_frame_c2_1024_caves_full(orc, tracer, world_cache, quality, native_lib)
         _assert_hits_equal(gi, ogi, f"GI {cfg}")
         assert n_gi == n_hit
     tracer.set_launch_config(variant=0, order=0, features=0, reg_blocks=3, block_threads=128, refill_threshold=24)
+    # the device-buffer entry point, in one launch and in concurrent row bands (default 4)
+    import torch
+
+    n = 1920 * 1080
+    bufs = [torch.zeros(m, dtype=torch.int32, device="cuda") for m in (2 * n, 2 * n, n, 5 * n, 5 * n)]
+    n_gi_dev = torch.zeros(1, dtype=torch.int64, device="cuda")
+    try:
+        for bands, order in ((1, 1), (2, 0), (0, 1), (8, 1)):
+            assert native_lib.lib().arc_set_frame_bands(tracer.ctx, bands) == 0
+            tracer.set_launch_config(order=order)
+            for x in bufs:
+                x.fill_(-1)
+            tracer.trace_frame_dev(1920, 1080, *[x.data_ptr() for x in bufs], n_gi_dev.data_ptr())
+            tracer.synchronize()
+            got = [x.cpu().numpy().view(np.uint32) for x in bufs]
+            np.testing.assert_array_equal(got[0].reshape(-1, 2), ogdm)
+            np.testing.assert_array_equal(got[1].reshape(-1, 2), ognm)
+            np.testing.assert_array_equal(got[2], ogaa)
+            _assert_hits_equal(got[3].view(L.HIT_DTYPE), ohits, f"primary, device frame in {bands} bands")
+            _assert_hits_equal(got[4].view(L.HIT_DTYPE), ogi, f"GI, device frame in {bands} bands")
+            assert int(n_gi_dev.item()) == n_hit
+    finally:
+        native_lib.lib().arc_set_frame_bands(tracer.ctx, 0)
+        tracer.set_launch_config(order=0)
     eye = np.broadcast_to(cam[0]["cam_pos_time"][:3], (len(ohits), 3))
     _check_depth_fp64(orc, eye, _camera_rays(cam, 1920, 1080), ohits, stride=401)
 
