@@ -595,11 +595,13 @@ static int ensure_band_streams(arc_ctx* c);
 
 // Bands of a device frame: the plain kernel's launches over the whole frame, or (frame_bands > 1)
 // over horizontal bands on the band streams, forked from and joined back to the context stream, so
-// that one band's tail runs beside another band's work. The variants with frame-wide scratch (the GI
-// rays sorted over the frame, the resident-CTA primary with its staged table) and the persistent
-// kernel (one queue) keep one launch. Every pixel is computed by the same code either way.
+// that one band's GI pass runs in another band's primary-kernel tail. The variants with frame-wide
+// scratch (the GI rays sorted over the frame, the resident-CTA primary with its staged table), the
+// persistent kernel (one queue) and primary-only frames (no GI pass to fill the tails: 0.479 against
+// 0.464 ms at 1080p in four bands) keep one launch. Every pixel is computed by the same code either way.
 static uint32_t device_bands(const arc_ctx* c, const arc::FrameParams& P) {
-    if (c->cfg.variant != 0u || (c->cfg.features & (ARC_FEAT_GI_SORT | ARC_FEAT_TOP_TABLE | ARC_FEAT_GRID_STRIDE)))
+    if (c->cfg.variant != 0u || !P.do_gi ||
+        (c->cfg.features & (ARC_FEAT_GI_SORT | ARC_FEAT_TOP_TABLE | ARC_FEAT_GRID_STRIDE)))
         return 1u;
     const uint32_t want = c->frame_bands ? c->frame_bands : arc_ctx::kDefaultFrameBands;
     return std::max<uint32_t>(1u, std::min<uint32_t>(want, (P.row_end - P.row0) / 64u));

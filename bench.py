@@ -163,6 +163,36 @@ def _peaks_all():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 
 
+def _l2_copy_gbs(dev, mib=32, iters=50):
+    """Copy bandwidth of a working set resident in L2 (two buffers of `mib` MiB, read + write bytes):
+    `iters` copies replayed from one CUDA graph (no launch gaps), best of 5 replays, CUDA events. The
+    L2 ceiling of a traversal whose node fetches are mostly cache hits."""
+    import torch
+
+    a = torch.empty(mib << 20, dtype=torch.uint8, device=dev)
+    b = torch.empty_like(a)
+    a.fill_(1)
+    side = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(side):
+        for _ in range(3):
+            b.copy_(a)
+    torch.cuda.synchronize(dev)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        for _ in range(iters):
+            b.copy_(a)
+    best = 0.0
+    for _ in range(5):
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        g.replay()
+        s1.record()
+        s1.synchronize()
+        best = max(best, 2.0 * a.numel() * iters / (s0.elapsed_time(s1) * 1e-3) / 1e9)
+    del g, a, b
+    return best
+
+
 def _profile_traffic(kernel: str):
     """DRAM bytes of `kernel`'s frame (its launch, or its launches: the primary kernel and the GI pass)
     from a committed ncu summary (profiles/*.txt), if any."""
@@ -389,8 +419,11 @@ def run_ours(args):
                               "variant": cfg.variant, "reg_blocks": cfg.reg_blocks}), flush=True)
         return
 
-    # plain one-thread-per-pixel kernel, same frames (the "vs plain kernel" comparison)
-    t.set_launch_config(variant=0)
+    # the library's default launch configuration (arc_create's: plain kernel + GI pass, 128 threads,
+    # register budget 3, Morton block order, 4 row bands), same frames, against the tuned one above
+    tuned_cfg = t.launch_config()
+    t.set_launch_config(variant=0, block_threads=128, blocks_per_sm=0, tile_w=8, tile_h=4, refill_threshold=24,
+                        reg_blocks=3, order=1, features=0)
     np_frames = min(args.steps, 20)
     with torch.cuda.stream(stream):
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(np_frames)]
@@ -403,7 +436,7 @@ def run_ours(args):
     plain_ms = [a.elapsed_time(b) for a, b in ev]
     plain_rays = np_frames * npx + int(n_gi[:np_frames].sum().item())
     plain_value = plain_rays / (sum(plain_ms) * 1e-3) / 1e6
-    t.set_launch_config(variant=cfg.variant)
+    t.set_launch_config(**{k: getattr(tuned_cfg, k) for k, _ in type(tuned_cfg)._fields_})
 
     # end to end through the C ABI with host (pinned) buffers
     pin = {k: torch.empty(n, dtype=torch.int32).pin_memory().numpy() for k, n in
@@ -521,6 +554,7 @@ def run_ours(args):
         t5.close()
         del r5, n5, b5
     clk = clocks.stop() if clocks else None
+    l2_gbs = _l2_copy_gbs(dev) if not args.frame_only else None  # untimed, after every timed section
 
     if rank != 0:
         return
@@ -553,6 +587,9 @@ def run_ours(args):
         roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
                     "algorithmic_bytes_per_pixel": round(bpp, 2)}
+        if l2_gbs:
+            roofline["l2"] = {"peak": round(l2_gbs, 1), "frac": round(achieved / l2_gbs, 4),
+                              "peak_kind": "measured by this run: 50 copies of 32 MiB resident in L2, one CUDA graph"}
     # row bands of a device frame (arc_set_frame_bands; the library's rule: default 4, at most one per
     # 64 rows, one launch for the persistent kernel and the frame-wide variants)
     bands = 1
@@ -570,7 +607,8 @@ def run_ours(args):
                               "tile": [cfg.tile_w, cfg.tile_h], "refill_threshold": cfg.refill_threshold,
                               "reg_blocks": cfg.reg_blocks, "order": "morton" if cfg.order else "row-major",
                               "features": cfg.features, "row_bands": bands}},
-        "plain_kernel": {"value": round(plain_value, 3), "unit": UNIT, "ms_per_step": round(statistics.mean(plain_ms), 4)},
+        "default_config": {"value": round(plain_value, 3), "unit": UNIT, "ms_per_step": round(statistics.mean(plain_ms), 4),
+                           "frames": np_frames},
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": 480,
                 "d2h_bytes_per_step": npx * 60 + 8 + 16},
         # per timed frame: the persistent kernel, or the plain kernel's primary instance + the GI pass

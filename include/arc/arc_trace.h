@@ -104,11 +104,12 @@ int arc_synchronize(arc_ctx* ctx);
 /* cudaStream_t of the context, for callers that order their own work after it */
 int arc_get_stream(arc_ctx* ctx, void** stream);
 int arc_set_launch_config(arc_ctx* ctx, const arc_launch_config* cfg);
-/* Device frames (arc_trace_frame_dev, arc_trace_primary_dev) with the plain kernel run in n horizontal
- * bands, each band's kernels on a stream of their own, forked from and joined back to the context's
- * stream, so one band's tail overlaps another band's work. 0 = automatic (4 bands; default), 1 = one
- * launch over the frame, at most 8. The global GI sort, the resident-CTA primary and the persistent
- * kernel always run as one launch. Results are identical. No counterpart in the reference. */
+/* Device frames (arc_trace_frame_dev) with the plain kernel run in n horizontal bands, each band's
+ * primary kernel and GI pass on a stream of their own, forked from and joined back to the context's
+ * stream, so one band's GI pass runs in another band's primary tail. 0 = automatic (4 bands; default),
+ * 1 = one launch over the frame, at most 8. Primary-only frames, the global GI sort, the resident-CTA
+ * primary and the persistent kernel always run as one launch. Results are identical. No counterpart
+ * in the reference. */
 int arc_set_frame_bands(arc_ctx* ctx, uint32_t n);
 /* Times candidate launch configurations (variant x block size x register budget x refill threshold x
  * tile shape) on the caller's frame, installs the fastest and returns it with its median frame time.
