@@ -278,12 +278,16 @@ int arc_destroy(arc_ctx* c) {
     if (c->copy_stream) {
         cudaStreamSynchronize(c->copy_stream);
         cudaStreamDestroy(c->copy_stream);
+        cudaStreamSynchronize(c->gi_copy_stream);
+        cudaStreamDestroy(c->gi_copy_stream);
         for (int i = 0; i < arc_ctx::kMaxBands; ++i) {
             cudaStreamSynchronize(c->band_stream[i]);
             cudaStreamDestroy(c->band_stream[i]);
             cudaEventDestroy(c->band_ev[i]);
+            cudaEventDestroy(c->band_gev[i]);
         }
         cudaEventDestroy(c->copies_done);
+        cudaEventDestroy(c->gi_copies_done);
         cudaEventDestroy(c->frame_start);
     }
     cudaFree(c->d_surf);
@@ -732,6 +736,10 @@ int arc_trace_secondary_dev(arc_ctx* c, uint32_t width, uint32_t height, const u
 // Host-buffer variants: stage outputs in one context-owned device block.
 static int ensure_band_streams(arc_ctx* c) {
     if (c->copy_stream) return ARC_OK;
+    ARC_CK(c, cudaStreamCreateWithFlags(&c->gi_copy_stream, cudaStreamNonBlocking));
+    ARC_CK(c, cudaEventCreateWithFlags(&c->gi_copies_done, cudaEventDisableTiming));
+    for (int i = 0; i < arc_ctx::kMaxBands; ++i)
+        ARC_CK(c, cudaEventCreateWithFlags(&c->band_gev[i], cudaEventDisableTiming));
     ARC_CK(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
     for (int i = 0; i < arc_ctx::kMaxBands; ++i) {
         ARC_CK(c, cudaStreamCreateWithFlags(&c->band_stream[i], cudaStreamNonBlocking));
@@ -808,15 +816,18 @@ int arc_trace_frame(arc_ctx* c, uint32_t width, uint32_t height, uint32_t* gdm, 
             ARC_CK(c, cudaMemsetAsync(&c->d_scratch->queue_head, 0, sizeof(uint32_t), c->stream));
         }
         if ((rc = surface_prepare(c, P, c->d_surf_count + b))) return rc;
-        ARC_CK(c, arc::launch_frame(P, c->cam, c->cfg, c->n_sm, st));
-        ARC_CK(c, arc::launch_surface(P, c->cam, c->n_sm, st));
+        // the surface branches run between the primary kernel and the GI pass, so the band's G-buffer and
+        // primary hit records are final (band_gev) and copied while its GI pass runs
+        const arc::FrameHooks hooks{true, c->band_gev[b]};
+        ARC_CK(c, arc::launch_frame(P, c->cam, c->cfg, c->n_sm, st, &hooks));
         ARC_CK(c, cudaEventRecord(c->band_ev[b], st));
-        ARC_CK(c, cudaStreamWaitEvent(c->copy_stream, c->band_ev[b], 0));
+        ARC_CK(c, cudaStreamWaitEvent(c->copy_stream, c->band_gev[b], 0));
+        ARC_CK(c, cudaStreamWaitEvent(c->gi_copy_stream, c->band_ev[b], 0));
         for (int i = 0; i < 5; ++i) {
             if (!host[i]) continue;
             const size_t o = (size_t)r0 * width * px_bytes[i], len = (size_t)(r1 - r0) * width * px_bytes[i];
             ARC_CK(c, cudaMemcpyAsync(static_cast<unsigned char*>(host[i]) + o, dev[i] + o, len, cudaMemcpyDeviceToHost,
-                                      c->copy_stream));
+                                      i == 4 ? c->gi_copy_stream : c->copy_stream));
         }
     }
     if (concurrent)
@@ -824,7 +835,9 @@ int arc_trace_frame(arc_ctx* c, uint32_t width, uint32_t height, uint32_t* gdm, 
     ARC_CK(c, cudaEventRecord(c->ev1, c->stream));
     c->timing_pending = true;
     ARC_CK(c, cudaEventRecord(c->copies_done, c->copy_stream));
+    ARC_CK(c, cudaEventRecord(c->gi_copies_done, c->gi_copy_stream));
     ARC_CK(c, cudaStreamWaitEvent(c->stream, c->copies_done, 0));
+    ARC_CK(c, cudaStreamWaitEvent(c->stream, c->gi_copies_done, 0));
     return collect_frame(c, np, n_gi_out);
 }
 

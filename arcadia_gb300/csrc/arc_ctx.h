@@ -132,10 +132,12 @@ struct arc_ctx {
     static constexpr int kMaxBands = 8;
     static constexpr uint32_t kDefaultFrameBands = 4;  // device frames (arc_set_frame_bands 0)
     uint32_t frame_bands = 0;                           // arc_set_frame_bands; 0 = kDefaultFrameBands
-    cudaStream_t copy_stream = nullptr;
+    cudaStream_t copy_stream = nullptr;        // G-buffer and primary hit record copies, band by band
+    cudaStream_t gi_copy_stream = nullptr;     // GI hit record copies, band by band
     cudaStream_t band_stream[kMaxBands] = {};  // the plain kernel's bands run concurrently, one per stream
-    cudaEvent_t band_ev[kMaxBands] = {};
-    cudaEvent_t copies_done = nullptr, frame_start = nullptr;
+    cudaEvent_t band_ev[kMaxBands] = {};       // a band's kernels done
+    cudaEvent_t band_gev[kMaxBands] = {};      // a band's G-buffer and primary hit records final
+    cudaEvent_t copies_done = nullptr, gi_copies_done = nullptr, frame_start = nullptr;
     // side stream for a cache query that overlaps the cache's own update (arc_nrc_frame_dev,
     // arc_sharc_frame_dev): forked from and joined back into `stream` with two events
     cudaStream_t side_stream = nullptr;

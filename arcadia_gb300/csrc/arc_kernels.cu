@@ -1078,11 +1078,17 @@ __global__ void __launch_bounds__(256, MINB) views_gi_kernel(const ViewsParams V
 
 template <int MINB>
 cudaError_t launch_frame_t(const FrameParams& P, const arc_camera_uniforms& cam, const arc_launch_config& cfg, int n_sm,
-                           cudaStream_t st) {
+                           cudaStream_t st, const FrameHooks* hooks) {
+    auto mid = [&]() -> cudaError_t {  // FrameHooks: after the primary rays, before the GI pass
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess || !hooks) return e;
+        if (hooks->surface && (e = launch_surface(P, cam, n_sm, st)) != cudaSuccess) return e;
+        return hooks->primary_done ? cudaEventRecord(hooks->primary_done, st) : cudaSuccess;
+    };
     if (P.world.n_bodies && ((cam.point_light_count[1] >> 16) & 0xFFFFu)) {
         dim3 grid((P.width + 15u) / 16u, (P.row_end - P.row0 + 7u) / 8u);
         frame_rigid_kernel<<<grid, 128, 0, st>>>(P, cam);
-        return cudaGetLastError();
+        return mid();
     }
     if (cfg.variant == 0u) {
         const uint32_t bw = 8u, bh = cfg.block_threads / 8u;
@@ -1113,7 +1119,7 @@ cudaError_t launch_frame_t(const FrameParams& P, const arc_camera_uniforms& cam,
             if (fused) frame_plain_kernel<MINB, false, true><<<grid, block, 0, st>>>(P, cam);
             else frame_plain_kernel<MINB, false, false><<<grid, block, 0, st>>>(P, cam);
         }
-        cudaError_t e = cudaGetLastError();
+        cudaError_t e = mid();
         if (e != cudaSuccess || !P.do_gi) return e;
         if (P.gi_mode == kGiRows && P.gisort.bins) return launch_gi_sorted<MINB>(P, cam, st);
         if (P.gi_mode == kGiRows) {
@@ -1145,16 +1151,16 @@ cudaError_t launch_frame_t(const FrameParams& P, const arc_camera_uniforms& cam,
     }
     if (P.surf) frame_persistent_kernel<MINB, true><<<n_sm * per_sm, cfg.block_threads, 0, st>>>(P, cam);
     else frame_persistent_kernel<MINB, false><<<n_sm * per_sm, cfg.block_threads, 0, st>>>(P, cam);
-    return cudaGetLastError();
+    return mid();
 }
 
 cudaError_t launch_frame(const FrameParams& P, const arc_camera_uniforms& cam, const arc_launch_config& cfg, int n_sm,
-                         cudaStream_t st) {
+                         cudaStream_t st, const FrameHooks* hooks) {
     switch (cfg.reg_blocks) {
-        case 2: return launch_frame_t<2>(P, cam, cfg, n_sm, st);
-        case 3: return launch_frame_t<3>(P, cam, cfg, n_sm, st);
-        case 4: return launch_frame_t<4>(P, cam, cfg, n_sm, st);
-        default: return launch_frame_t<1>(P, cam, cfg, n_sm, st);
+        case 2: return launch_frame_t<2>(P, cam, cfg, n_sm, st, hooks);
+        case 3: return launch_frame_t<3>(P, cam, cfg, n_sm, st, hooks);
+        case 4: return launch_frame_t<4>(P, cam, cfg, n_sm, st, hooks);
+        default: return launch_frame_t<1>(P, cam, cfg, n_sm, st, hooks);
     }
 }
 

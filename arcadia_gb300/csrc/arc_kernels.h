@@ -109,8 +109,16 @@ struct ViewsParams {
 };
 
 cudaError_t launch_views(const ViewsParams& V, const arc_launch_config& cfg, int n_sm, cudaStream_t st);
+// Work between a frame's primary kernel and its GI pass: the surface branches (they rewrite only the
+// albedo bytes, and the GI pass reads only depth and normal) and an event that marks the G-buffer and
+// the primary hit records final, so their copies can start under the GI pass. The forms without a
+// separate GI pass (persistent, fused, rigid bodies) do both after their kernel.
+struct FrameHooks {
+    bool surface;              // launch_surface here; the caller does not launch it again
+    cudaEvent_t primary_done;  // recorded once the G-buffer and primary hit records are final (or null)
+};
 cudaError_t launch_frame(const FrameParams& P, const arc_camera_uniforms& cam, const arc_launch_config& cfg, int n_sm,
-                         cudaStream_t st);
+                         cudaStream_t st, const FrameHooks* hooks = nullptr);
 // Surface branches of the hits a frame launch listed (one thread per entry, grid-stride).
 cudaError_t launch_surface(const FrameParams& P, const arc_camera_uniforms& cam, int n_sm, cudaStream_t st);
 cudaError_t launch_surface_views(const ViewsParams& V, const SurfaceEntry* surf, const uint32_t* count, uint32_t cap,
