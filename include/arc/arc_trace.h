@@ -189,10 +189,12 @@ int arc_trace_secondary(arc_ctx* ctx, uint32_t width, uint32_t height, const uin
                         const uint32_t* gbuf_norm_motion, arc_hit_record* gi_hits);
 int arc_trace_secondary_dev(arc_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* gbuf_depth_mat,
                             const uint32_t* gbuf_norm_motion, arc_hit_record* gi_hits);
-/* Both passes in one launch: writes the G-buffer, primary hits and GI hits (any output may be NULL
- * except the G-buffer). n_gi_out (optional) receives the number of GI rays traced. The host-buffer
- * form traces the frame in horizontal bands and copies each band back while the next one traces
- * (page-locked host buffers make those copies asynchronous). */
+/* Primary rays and GI rays of a frame: writes the G-buffer, primary hits and GI hits (any output may
+ * be NULL except the G-buffer). n_gi_out (optional) receives the number of GI rays traced. The
+ * host-buffer form traces the frame in horizontal bands on concurrent streams and copies each band's
+ * G-buffer and primary hits back while its GI rays trace, and its GI hits once they are done
+ * (page-locked host buffers make those copies asynchronous). The device form runs in row bands as
+ * arc_set_frame_bands sets. */
 int arc_trace_frame(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbuf_depth_mat, uint32_t* gbuf_norm_motion,
                     uint32_t* gbuf_albedo_ao, arc_hit_record* hits, arc_hit_record* gi_hits, uint64_t* n_gi_out);
 int arc_trace_frame_dev(arc_ctx* ctx, uint32_t width, uint32_t height, uint32_t* gbuf_depth_mat,
