@@ -245,7 +245,7 @@ static void oct_decode_packed(uint32_t p, float n[3]) {
 
 /* ------------------------------------------------------------------------------------------ */
 /* One-bounce estimator of the cache comparison (no reference counterpart: the light transport the */
-/* NRC and SHARC are judged on). L(x) = albedo * (c_sun max(n.l, 0) V(x, l) + L_sky [a cosine ray  */
+/* NRC and SHARC are scored on). L(x) = albedo * (c_sun max(n.l, 0) V(x, l) + L_sky [a cosine ray  */
 /* from x + 0.10 n escapes within 64 m]); V is trace_shadow_vis (traversal64.wgsl:571-773) from     */
 /* x + 0.10 n over 32 m as in sharc_shade_surface (sharc_update.wgsl:68-105), c_sun = sun_power *    */
 /* (1, 0.9, 0.75) * 0.55, L_sky = (0.30, 0.42, 0.60); the sky ray is a lod_bias 2, water-ignoring   */

@@ -4,7 +4,7 @@ Every radiance number the cache comparison reports is built on this estimator (s
 trace_shadow_vis, shaders/common/traversal64.wgsl:571-773, from x + 0.10 n as in sharc_shade_surface,
 shaders/sharc_update.wgsl:68-105; sky term through one cosine ray, types.wgsl:531-545): the GI hit points
 the caches are queried at, the NRC's training targets, SHARC's mode-1 deposits and the 4096-spp
-reference that judges both caches. Each is checked here bit for bit against the oracle on the 1024^3
+reference that scores both caches. Each is checked here bit for bit against the oracle on the 1024^3
 caves world (high_quality preset).
 """
 import os
@@ -140,9 +140,9 @@ def test_training_batch_matches_oracle(orc, native_lib, frame, cluster):
     assert (ot > 0).any(axis=1).mean() > 0.3
 
 
-def test_reference_judge_matches_oracle(orc, frame):
+def test_reference_scores_match_oracle(orc, frame):
     """The 4096-spp reference that scores both caches (64 launches of 64 spp, accumulated in FP64 on the
-    host): at 64 points every launch is bit-exact against the oracle's, so the judge equals the oracle's
+    host): at 64 points every launch is bit-exact against the oracle's, so the reference equals the oracle's
     FP64 accumulation exactly."""
     from arcadia_gb300 import gi_cache
 
