@@ -87,6 +87,13 @@ __device__ __forceinline__ uint32_t pack_h2(float lo, float hi) {
     __half2 h = __floats2half2_rn(lo, hi);
     return *reinterpret_cast<uint32_t*>(&h);
 }
+// ReLU of an FP16-rounded pair, one packed max after the conversion: the same values as
+// pack_h2(fmaxf(lo, 0), fmaxf(hi, 0)) (rounding keeps the sign), except that an input rounding to -0
+// may stay -0, which no product or mask downstream tells from +0.
+__device__ __forceinline__ uint32_t relu_pack_h2(float lo, float hi) {
+    __half2 h = __hmax2(__floats2half2_rn(lo, hi), __float2half2_rn(0.0f));
+    return *reinterpret_cast<uint32_t*>(&h);
+}
 __device__ __forceinline__ uint32_t lds32(const __half* p) { return *reinterpret_cast<const uint32_t*>(p); }
 
 __device__ __forceinline__ void red_add2(float* p, float a, float b) {
@@ -646,8 +653,7 @@ __global__ void __launch_bounds__(128 * G, G == 1 ? 2 : 1) infer_tc_kernel(
                     uint32_t pk[4];
 #pragma unroll
                     for (int e = 0; e < 4; ++e)
-                        pk[e] = pack_h2(fmaxf(__uint_as_float(r[q][8 * c2 + 2 * e]), 0.0f),
-                                        fmaxf(__uint_as_float(r[q][8 * c2 + 2 * e + 1]), 0.0f));
+                        pk[e] = relu_pack_h2(__uint_as_float(r[q][8 * c2 + 2 * e]), __uint_as_float(r[q][8 * c2 + 2 * e + 1]));
                     st_chunk(sa, 8, tid, 2 * q + c2, make_uint4(pk[0], pk[1], pk[2], pk[3]));
                 }
             }
@@ -784,12 +790,8 @@ __global__ void __launch_bounds__(128, 1) train_tc_kernel(const __half* __restri
             uint32_t pk[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
-                float a = __uint_as_float(r[c >> 1][8 * (c & 1) + 2 * e]), b = __uint_as_float(r[c >> 1][8 * (c & 1) + 2 * e + 1]);
-                if (relu) {
-                    a = fmaxf(a, 0.0f);
-                    b = fmaxf(b, 0.0f);
-                }
-                pk[e] = pack_h2(a, b);
+                const float a = __uint_as_float(r[c >> 1][8 * (c & 1) + 2 * e]), b = __uint_as_float(r[c >> 1][8 * (c & 1) + 2 * e + 1]);
+                pk[e] = relu ? relu_pack_h2(a, b) : pack_h2(a, b);
             }
             st_chunk(smem_raw + buf, 8, tid, c, make_uint4(pk[0], pk[1], pk[2], pk[3]));
         }
