@@ -500,9 +500,11 @@ def run_ours(args):
                          "rel_mse_sharc": round(r["rel_mse_sharc"], 4)}
         kt = gi_cache.kernel_timing(t, SCENE, W_, H_)
         bf16_peak = _peaks_all().get("bf16_tflops")
-        kt["roofline_query"] = {"bound": "tensor", "achieved": kt["tcgen05"]["query_tflops"], "peak": bf16_peak,
+        # the default form of a query on its own (four tile groups per CTA)
+        q_tf = kt["tcgen05_four_groups"]["query_tflops"]
+        kt["roofline_query"] = {"bound": "tensor", "achieved": q_tf, "peak": bf16_peak, "kernel": "infer_tc_kernel<4>",
                                 "unit": "TFLOP/s", "peak_kind": "measured cuBLAS bf16 burst",
-                                "frac": round(kt["tcgen05"]["query_tflops"] / bf16_peak, 4) if bf16_peak else None}
+                                "frac": round(q_tf / bf16_peak, 4) if bf16_peak else None}
         nrc["kernels"] = kt
 
     # ReSTIR GI temporal pass on this world's frames (before the batch replaces world slot 0)
