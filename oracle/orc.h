@@ -137,6 +137,10 @@ int orc_gi_setup(const orc_world* w, const arc_camera_uniforms* cam, uint32_t x,
                  uint32_t gd0, uint32_t gn0, orc_gi_ray* g, uint32_t* bytes);
 void orc_ign(float px, float py, uint32_t frame, float out[2]);
 void orc_oct_decode_packed(uint32_t packed, float n[3]);
+/* test hooks of the G-buffer packing (orc_test.c, orc_trace.c) */
+void orc_test_pack4x8unorm(const float* x, uint32_t n, uint32_t* out);
+void orc_test_pack2x16snorm(const float* x, uint32_t n, uint32_t* out);
+void orc_test_oct_encode(const float* nrm, uint32_t n, float* out);
 void orc_sky_radiance(const float dir[3], const float sun[3], float out[3]);
 
 /* ReSTIR GI temporal pass (orc_restir.c): res_in is the previous frame's reservoirs, res_out this

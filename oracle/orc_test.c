@@ -42,3 +42,13 @@ void orc_test_scene_volume(const orc_scene_params* p, uint32_t cx, uint32_t cy, 
                     (uint8_t)orc_scene_voxel(p, hm, cx * 256u + x, cy * 256u + y, cz * 256u + (uint32_t)z);
     free(hm);
 }
+
+/* WGSL pack4x8unorm / pack2x16snorm as the oracle's G-buffer writer applies them (orc_math.h). */
+void orc_test_pack4x8unorm(const float* x, uint32_t n, uint32_t* out) {
+    for (uint32_t i = 0; i < n; ++i) out[i] = orc_pack4x8unorm(x[4 * i], x[4 * i + 1], x[4 * i + 2], x[4 * i + 3]);
+}
+
+void orc_test_pack2x16snorm(const float* x, uint32_t n, uint32_t* out) {
+    for (uint32_t i = 0; i < n; ++i) out[i] = orc_pack2x16snorm(x[2 * i], x[2 * i + 1]);
+}
+

@@ -718,6 +718,11 @@ static void oct_encode(const float n[3], float p[2]) {
     }
 }
 
+/* test hook: the octahedral encoding of n unit normals (3 floats each) into 2 floats each */
+void orc_test_oct_encode(const float* nrm, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) oct_encode(nrm + 3 * i, out + 2 * i);
+}
+
 static void oct_decode(const float p[2], float out[3]) {
     float n[3] = {p[0], p[1], (1.0f - fabsf(p[0])) - fabsf(p[1])};
     if (n[2] < 0.0f) {

@@ -117,6 +117,9 @@ def lib():
         _lib.orc_shadow_vis_di.restype = f32
         _lib.orc_test_sincos.argtypes = [vp, u32, vp, vp]
         _lib.orc_test_f16.argtypes = [vp, u32, vp]
+        _lib.orc_test_pack4x8unorm.argtypes = [vp, u32, vp]
+        _lib.orc_test_pack2x16snorm.argtypes = [vp, u32, vp]
+        _lib.orc_test_oct_encode.argtypes = [vp, u32, vp]
         _lib.orc_test_powi.argtypes = [vp, u32, u32, vp]
         _lib.orc_test_exp2_log2.argtypes = [vp, u32, vp, vp]
         _lib.orc_test_pow.argtypes = [vp, u32, C.c_float, vp]
@@ -480,6 +483,30 @@ def sincos(x: np.ndarray):
     s, c = np.zeros_like(x), np.zeros_like(x)
     lib().orc_test_sincos(_p(x), len(x), _p(s), _p(c))
     return s, c
+
+
+def pack4x8unorm(x: np.ndarray) -> np.ndarray:
+    """The oracle's WGSL pack4x8unorm over rows of 4 floats."""
+    x = np.ascontiguousarray(x, np.float32).reshape(-1, 4)
+    out = np.zeros(len(x), np.uint32)
+    lib().orc_test_pack4x8unorm(_p(x), len(x), _p(out))
+    return out
+
+
+def pack2x16snorm(x: np.ndarray) -> np.ndarray:
+    """The oracle's WGSL pack2x16snorm over rows of 2 floats."""
+    x = np.ascontiguousarray(x, np.float32).reshape(-1, 2)
+    out = np.zeros(len(x), np.uint32)
+    lib().orc_test_pack2x16snorm(_p(x), len(x), _p(out))
+    return out
+
+
+def oct_encode(n: np.ndarray) -> np.ndarray:
+    """The oracle's octahedral encoding of unit normals (rows of 3 floats) into rows of 2 floats."""
+    n = np.ascontiguousarray(n, np.float32).reshape(-1, 3)
+    out = np.zeros((len(n), 2), np.float32)
+    lib().orc_test_oct_encode(_p(n), len(n), _p(out))
+    return out
 
 
 def f16_bits(x: np.ndarray) -> np.ndarray:

@@ -244,3 +244,56 @@ def test_powi_exact_small(orc):
     x = np.float32([0.0, 0.5, 1.0, 0.75, 0.999])
     np.testing.assert_allclose(orc.powi(x, 14), x.astype(np.float64) ** 14, rtol=2e-6, atol=1e-30)
     np.testing.assert_allclose(orc.powi(x, 3), x.astype(np.float64) ** 3, rtol=1e-6, atol=1e-30)
+
+
+def _pack4x8unorm_wgsl(x):
+    """WGSL pack4x8unorm by the specification's definition: byte i = floor(0.5 + 255 * min(1, max(0, e[i])))."""
+    f = np.float32
+    x = np.asarray(x, np.float32).reshape(-1, 4)
+    v = np.floor(f(0.5) + f(255.0) * np.minimum(f(1.0), np.maximum(f(0.0), x))).astype(np.uint32)
+    return v[:, 0] | (v[:, 1] << 8) | (v[:, 2] << 16) | (v[:, 3] << 24)
+
+
+def _pack2x16snorm_wgsl(x):
+    """WGSL pack2x16snorm by the specification's definition: half i = floor(0.5 + 32767 * min(1, max(-1, e[i])))
+    as a 16-bit two's complement integer."""
+    f = np.float32
+    x = np.asarray(x, np.float32).reshape(-1, 2)
+    v = np.floor(f(0.5) + f(32767.0) * np.minimum(f(1.0), np.maximum(f(-1.0), x))).astype(np.int64) & 0xFFFF
+    return (v[:, 0] | (v[:, 1] << 16)).astype(np.uint32)
+
+
+def _oct_encode_wgsl(n):
+    """oct_encode / oct_wrap (shaders/common/types.wgsl:108-119) in float32."""
+    f = np.float32
+    n = np.asarray(n, np.float32).reshape(-1, 3)
+    l1 = (np.abs(n[:, 0]) + np.abs(n[:, 1])) + np.abs(n[:, 2])
+    p = n[:, :2] * (f(1.0) / np.maximum(l1, f(1e-6)))[:, None]
+    wrapped = (f(1.0) - np.abs(p[:, ::-1])) * np.where(p >= 0, f(1.0), f(-1.0))
+    return np.where((n[:, 2] < 0)[:, None], wrapped, p).astype(np.float32)
+
+
+def test_gbuffer_packing_matches_wgsl_definitions(orc):
+    """The G-buffer words (normal and albedo/AO packing) pinned to the WGSL definitions: the oracle's
+    pack4x8unorm and pack2x16snorm equal the specification's formulas bit for bit, including the clamps
+    and the values on rounding midpoints, and its octahedral encoding equals types.wgsl's in float32.
+    The GPU writes the same words as the oracle (every frame parity test), so both sides are pinned."""
+    rng = np.random.default_rng(11)
+    mids = ((np.arange(256, dtype=np.float64) + 0.5) / 255.0).astype(np.float32)
+    u = np.concatenate([rng.uniform(-0.5, 1.5, 400000).astype(np.float32), mids, np.nextafter(mids, np.float32(0)),
+                        np.nextafter(mids, np.float32(2)), np.float32([0.0, -0.0, 1.0, -1.0, 2.0, 1e-30, 1e30, -1e30])])
+    u = u[: len(u) // 4 * 4]
+    np.testing.assert_array_equal(orc.pack4x8unorm(u), _pack4x8unorm_wgsl(u))
+    smid = ((np.arange(-32767, 32767, 7, dtype=np.float64) + 0.5) / 32767.0).astype(np.float32)
+    s = np.concatenate([rng.uniform(-1.5, 1.5, 400000).astype(np.float32), smid, np.nextafter(smid, np.float32(-2)),
+                        np.float32([0.0, -0.0, 1.0, -1.0, 3.0, -3.0])])
+    s = s[: len(s) // 2 * 2]
+    np.testing.assert_array_equal(orc.pack2x16snorm(s), _pack2x16snorm_wgsl(s))
+    d = rng.standard_normal((200000, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    axes = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1], [0.0, -0.0, -1.0],
+                     [-0.0, 0.0, -1.0]], np.float64)
+    n = np.concatenate([d, axes]).astype(np.float32)
+    got = orc.oct_encode(n)
+    np.testing.assert_array_equal(got.view(np.uint32), _oct_encode_wgsl(n).view(np.uint32))
+    np.testing.assert_array_equal(got[-8:-2], np.float32([[1, 0], [-1, 0], [0, 1], [0, -1], [0, 0], [1, 1]]))
