@@ -108,8 +108,9 @@ int arc_set_launch_config(arc_ctx* ctx, const arc_launch_config* cfg);
  * primary kernel and GI pass on a stream of their own, forked from and joined back to the context's
  * stream, so one band's GI pass runs in another band's primary tail. 0 = automatic (4 bands; default),
  * 1 = one launch over the frame, at most 8. Primary-only frames, the global GI sort, the resident-CTA
- * primary and the persistent kernel always run as one launch. Results are identical. No counterpart
- * in the reference. */
+ * primary and the persistent kernel always run as one launch. Results are identical. The band streams
+ * are created by the first banded call (or host-buffer frame), so make one such call before capturing
+ * a banded frame into a CUDA graph. No counterpart in the reference. */
 int arc_set_frame_bands(arc_ctx* ctx, uint32_t n);
 /* Times candidate launch configurations (variant x block size x register budget x refill threshold x
  * tile shape) on the caller's frame, installs the fastest and returns it with its median frame time.
