@@ -411,3 +411,49 @@ def test_host_frame_into_pinned_buffers(tracer, world_cache):
         a = np.ascontiguousarray(a).view(np.int32).reshape(-1)
         assert np.array_equal(a, b.numpy()) and np.array_equal(a, c.cpu().numpy())
     assert n.value == pageable[5]
+
+
+def test_banded_device_frame_in_cuda_graph(orc, tracer, world_cache, native_lib):
+    """arc_trace_frame_dev in four concurrent row bands, captured into a CUDA graph on the library's
+    stream after one direct call (which creates the band streams): the replay writes the same words as
+    the direct call, and those equal the oracle's."""
+    torch = pytest.importorskip("torch")
+    w = world_cache("c1_256")
+    W, H = 1280, 720
+    cam = L.default_camera_for(L.SCENES["c1_256"], W, H, quality=L.quality_high(), frame_index=5)
+    _load(tracer, w, cam)
+    n = W * H
+    bufs = [torch.zeros(m, dtype=torch.int32, device="cuda") for m in (2 * n, 2 * n, n, 5 * n, 5 * n)]
+    n_gi = torch.zeros(1, dtype=torch.int64, device="cuda")
+    ptrs = [x.data_ptr() for x in bufs] + [n_gi.data_ptr()]
+    assert native_lib.lib().arc_set_frame_bands(tracer.ctx, 4) == 0
+    try:
+        tracer.trace_frame_dev(W, H, *ptrs)
+        tracer.synchronize()
+        direct = [x.clone() for x in bufs]
+        n_direct = int(n_gi.item())
+        for x in bufs:
+            x.fill_(-1)
+        n_gi.zero_()
+        stream = torch.cuda.ExternalStream(tracer.stream())
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(stream):
+            g.capture_begin(capture_error_mode="thread_local")
+            tracer.trace_frame_dev(W, H, *ptrs)
+            g.capture_end()
+        for x in bufs:  # nothing ran during the capture
+            assert (x == -1).all()
+        g.replay()
+        torch.cuda.synchronize()
+        for got, want in zip(bufs, direct):
+            assert torch.equal(got, want)
+        assert int(n_gi.item()) == n_direct
+    finally:
+        native_lib.lib().arc_set_frame_bands(tracer.ctx, 0)
+    ogdm, ognm, ogaa, ohits, _ = orc.primary(w, cam, threads=THREADS)
+    _, ogi, _ = orc.gi_rays(w, cam, ogdm, ognm, threads=THREADS)
+    got = [x.cpu().numpy().view(np.uint32) for x in bufs]
+    np.testing.assert_array_equal(got[0].reshape(-1, 2), ogdm)
+    np.testing.assert_array_equal(got[2], ogaa)
+    _assert_hits_equal(got[3].view(L.HIT_DTYPE), ohits, "primary, graph replay")
+    _assert_hits_equal(got[4].view(L.HIT_DTYPE), ogi, "GI, graph replay")
